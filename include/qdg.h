@@ -1,0 +1,200 @@
+/*
+ * qdg.h -- C ABI of the GB300 propagation engine (libqdg.so).
+ *
+ * This is the drop-in boundary for QDng's time-stepping hot path. A QDng
+ * operator module (a C++ OPropagator subclass built against the QDng
+ * headers) walks its Hamiltonian tree once in
+ * Init(WaveFunction*), fills a qdg_hplan_desc and then calls the entry
+ * points below once per time step from Apply(WaveFunction*).
+ *
+ * Plain C: fixed-width integers, doubles and opaque handles, no exceptions,
+ * integer status codes.  Complex arrays are interleaved (re, im) doubles,
+ * the layout of QDng's dcomplex/cVec (src/math/dcomplex.h); a multistate
+ * wave function is stored state after state, each state contiguous with
+ * grid dimension 0 fastest (src/qdlib/WFMultistate.cpp:89-140,
+ * src/qdlib/GridSystem.h:23-27).
+ *
+ * Reference files are cited relative to the QDng source tree.
+ */
+#ifndef QDG_H
+#define QDG_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QDG_ABI_VERSION 1
+
+/* Limits of the reference: MAX_DIMS (src/math/typedefs.h:28),
+ * QD_MAX_STATES (src/qdlib/WFMultistate.h:10). */
+#define QDG_MAX_DIMS 4
+#define QDG_MAX_STATES 64
+#define QDG_MAX_GROUPS 8   /* GSPO split members A, B, C ... (MAX_OPS) */
+
+/* Status codes. The QDng module maps them onto the reference exceptions
+ * (src/tools/Exception.h): EINVAL -> EParamProblem, EUNSUPPORTED ->
+ * EIncompatible, ENONFINITE -> EOverflow, ECUDA/ENOMEM/ETIMEOUT -> EIOError. */
+typedef enum qdg_status {
+  QDG_OK = 0,
+  QDG_EINVAL = 1,        /* bad argument or parameter */
+  QDG_ENONFINITE = 2,    /* NaN/Inf norm (Reporter.cpp:112-113) */
+  QDG_ETIMEOUT = 3,      /* bounded device wait ran out */
+  QDG_ECUDA = 4,         /* CUDA runtime error */
+  QDG_ENOMEM = 5,        /* device allocation failed */
+  QDG_EUNSUPPORTED = 6,  /* operator tree or grid the engine does not cover */
+  QDG_ENOTCONVERGED = 7  /* informational: series not converged (warning in the reference) */
+} qdg_status;
+
+/* Hamiltonian term kinds (one per QDng operator class on the path). */
+typedef enum qdg_term_kind {
+  QDG_TERM_KINETIC = 1,    /* OGridNablaSq: -1/(2m) Laplacian via FFT (src/qdlib/OGridNablaSq.cpp:28-111) */
+  QDG_TERM_POTENTIAL = 2,  /* OGridPotential: V(x) psi (src/qdlib/OGridPotential.cpp:134-142) */
+  QDG_TERM_DIPOLE = 3      /* OGridDipole: -mu(x) E(t) psi (src/qdlib/OGridDipole.cpp:46-60) */
+} qdg_term_kind;
+
+typedef enum qdg_precision {
+  QDG_PREC_FP64 = 0,       /* IEEE binary64 everywhere (the drop-in path) */
+  QDG_PREC_MIXED = 1       /* FP32 H*phi bulk, FP64 coefficients, psi accumulator and reductions */
+} qdg_precision;
+
+/* Grid description: QDng GridSystem (src/qdlib/GridSystem.cpp:195-215).
+ * dx = (xmax - xmin)/(n - 1); dk = 2 pi/(xmax - xmin + dx) (src/qdlib/Kspace.h:20-23). */
+typedef struct qdg_grid {
+  int32_t ndims;
+  int32_t n[QDG_MAX_DIMS];
+  double xmin[QDG_MAX_DIMS];
+  double xmax[QDG_MAX_DIMS];
+} qdg_grid;
+
+/* One operator of the Hamiltonian matrix H_{row,col}.
+ * The matrix is a QDng "Multistate" of "Sum"s (src/qdlib/OMultistate.cpp:206-231,
+ * src/qdlib/OSum.cpp:53-60); an off-diagonal term given at (row, col) is also
+ * applied at (col, row) (hermitian pointer copy, OMultistate.cpp:122-132).
+ * A single-state Hamiltonian is a plain Sum (nstates = 1). */
+typedef struct qdg_hterm {
+  int32_t kind;                  /* qdg_term_kind */
+  int32_t row, col;              /* matrix element; KINETIC must be diagonal */
+  int32_t grid;                  /* POTENTIAL/DIPOLE: index of the grid array in grid_data */
+  int32_t laser;                 /* DIPOLE: index of the field in laser_data */
+  int32_t group;                 /* GSPO split member: 0 = "A" (full step), 1 = "B", ... (OGSPO.cpp:71-85) */
+  double mass[QDG_MAX_DIMS];     /* KINETIC: masses per dimension, all > 0 */
+} qdg_hterm;
+
+typedef struct qdg_hplan_desc {
+  qdg_grid grid;
+  int32_t nstates;
+  int32_t nterms;
+  const qdg_hterm *terms;
+  int32_t ngrids;
+  const double *grid_data;       /* ngrids * npoints doubles, dim 0 fastest */
+  int32_t nlasers;
+  int32_t laser_nt;              /* samples per field; E(step) = laser[step] (Laser.cpp:125-128) */
+  const double *laser_data;      /* nlasers * laser_nt doubles */
+} qdg_hplan_desc;
+
+/* Per-step observables of QDng's Reporter (src/Reporter.cpp:65-154). */
+typedef struct qdg_observables {
+  double norm2;                  /* <psi|psi> with dx weights (Norm()^2) */
+  double pops[QDG_MAX_STATES];   /* per-state <psi_i|psi_i> */
+  double energy;                 /* Re <psi|H|psi> (Operator::Expec) */
+  double autocorr_re;            /* <psi(t)|psi0> (Reporter.cpp:137) */
+  double autocorr_im;
+} qdg_observables;
+
+/* Propagator information after Init (the values the reference stores in its
+ * ParamContainer, OCheby.cpp:470-491). */
+typedef struct qdg_prop_info {
+  int32_t kind;                  /* 1 Cheby, 2 GSPO, 3 SIL, 4 Arnoldi */
+  int32_t order;                 /* Cheby recursion order / Krylov max order */
+  double scaling;                /* Cheby Delta E (scaling) */
+  double offset_re, offset_im;   /* Cheby energy offset */
+  double exponent_re, exponent_im; /* OPropagator::Exponent() = c0 */
+} qdg_prop_info;
+
+typedef struct qdg_plan qdg_plan;  /* device H-plan: grids, fields, kinetic tables */
+typedef struct qdg_wf qdg_wf;      /* device wave function (all states) */
+typedef struct qdg_prop qdg_prop;  /* a propagator bound to a plan */
+
+/* ---- errors ---------------------------------------------------------- */
+
+/* Text of the last error on the calling thread ("" if none). */
+const char *qdg_last_error(void);
+int32_t qdg_abi_version(void);
+
+/* ---- plan: replaces the operator tree's Init(WaveFunction*) ------------ */
+
+/* Builds the device H-plan: copies grid arrays and fields to HBM, checks the
+ * tree (OGridNablaSq::Init masses > 0, OGridPotential::Init grid match,
+ * Laser::Clock dt), computes Emax/Emin host-side (OSum.cpp:28-51,
+ * OMultistate.cpp:163-203, OGridNablaSq.cpp:89-106, OGridPotential.cpp:124-132,
+ * OGridDipole.cpp:36-44). precision is a qdg_precision. */
+qdg_status qdg_plan_create(const qdg_hplan_desc *desc, int32_t precision, qdg_plan **out);
+qdg_status qdg_plan_destroy(qdg_plan *plan);
+/* Operator::Emax()/Emin() of the whole Hamiltonian (complex). */
+qdg_status qdg_plan_erange(const qdg_plan *plan, double emax[2], double emin[2]);
+/* Run the plan's work on a caller CUDA stream (cudaStream_t passed as void*;
+ * NULL = the plan's own stream). */
+qdg_status qdg_plan_set_stream(qdg_plan *plan, void *cuda_stream);
+qdg_status qdg_plan_synchronize(qdg_plan *plan);
+
+/* ---- wave functions ---------------------------------------------------- */
+
+qdg_status qdg_wf_create(qdg_plan *plan, qdg_wf **out);
+qdg_status qdg_wf_destroy(qdg_wf *wf);
+/* Host <-> device copies of nstates*npoints complex128 values. */
+qdg_status qdg_wf_upload(qdg_wf *wf, const double *host_psi);
+qdg_status qdg_wf_download(const qdg_wf *wf, double *host_psi);
+qdg_status qdg_wf_copy(qdg_wf *dst, const qdg_wf *src);
+
+/* ---- Hamiltonian application ------------------------------------------ */
+
+/* out = H(step) in (Operator::Apply(dest, src), src/qdlib/Operator.h:276). */
+qdg_status qdg_h_apply(qdg_plan *plan, const qdg_wf *in, qdg_wf *out, int64_t step);
+
+/* Reporter::Analyze values of psi at clock step `step` (psi0 may be NULL). */
+qdg_status qdg_observables_compute(qdg_plan *plan, const qdg_wf *psi, const qdg_wf *psi0,
+                                   int64_t step, qdg_observables *out);
+
+/* ---- propagators: replace OCheby / OGSPO / OSIL / OArnoldi ------------- */
+
+/* name: "Cheby", "GSPO", "SIL" or "Arnoldi"; params: the XML attributes of
+ * the <propagator> node as "key=value" pairs separated by ';' or spaces
+ * (Cheby: order, prec, scaling, Emax, Emax_im, Emin, Emin_im -- OCheby.cpp:53-61,386-401;
+ * SIL: order, err -- OSIL.cpp:38-52; Arnoldi: order, conv -- OArnoldi.cpp:39-59).
+ * dt is the clock's time step; direction flags mirror OPropagator::Forward/
+ * Backward/ImaginaryTime (src/qdlib/OPropagator.h:62-131). */
+qdg_status qdg_prop_create(qdg_plan *plan, const char *name, const char *params,
+                           double dt, int32_t imaginary_time, int32_t backward,
+                           qdg_prop **out);
+qdg_status qdg_prop_destroy(qdg_prop *prop);
+/* OPropagator::Init(WaveFunction*): coefficients, order, scratch buffers. */
+qdg_status qdg_prop_init(qdg_prop *prop);
+qdg_status qdg_prop_get_info(const qdg_prop *prop, qdg_prop_info *info);
+/* Cheby coefficients after Init (complex, `order` entries) including the
+ * exp(c0*offset) phase used in the sum (OCheby.cpp:107,122). */
+qdg_status qdg_prop_get_coeffs(const qdg_prop *prop, double *coeffs, int32_t capacity);
+
+/* One time step psi <- U(step) psi on device (OPropagator::Apply(Psi)).
+ * `step` is QDClock::TimeStep() at the call, used by time-dependent terms.
+ * terms_used (may be NULL) receives the Chebyshev terms / Krylov basis size
+ * actually used. */
+qdg_status qdg_prop_apply(qdg_prop *prop, qdg_wf *psi, int64_t step, int32_t *terms_used);
+
+/* The same step with the wave function in host memory (the drop-in call:
+ * host psi stays authoritative, upload before and download after). */
+qdg_status qdg_prop_apply_host(qdg_prop *prop, qdg_wf *scratch, double *host_psi,
+                               int64_t step, int32_t *terms_used);
+
+/* `nsteps` consecutive steps on device starting at clock step `step0`
+ * (ProgPropa.cpp:317-327 without the per-step report). */
+qdg_status qdg_prop_run(qdg_prop *prop, qdg_wf *psi, int64_t step0, int32_t nsteps,
+                        int64_t *terms_total);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QDG_H */

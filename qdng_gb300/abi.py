@@ -1,0 +1,126 @@
+"""ctypes mirror of include/qdg.h (data layouts only; loading libqdg.so lives in _lib.py).
+
+Every structure here matches the C declaration field for field; the
+reference classes each one replaces are cited in include/qdg.h.
+"""
+import ctypes as C
+
+QDG_MAX_DIMS = 4
+QDG_MAX_STATES = 64
+
+QDG_OK = 0
+QDG_EINVAL = 1
+QDG_ENONFINITE = 2
+QDG_ETIMEOUT = 3
+QDG_ECUDA = 4
+QDG_ENOMEM = 5
+QDG_EUNSUPPORTED = 6
+QDG_ENOTCONVERGED = 7
+
+STATUS_NAMES = {
+    0: "QDG_OK", 1: "QDG_EINVAL", 2: "QDG_ENONFINITE", 3: "QDG_ETIMEOUT",
+    4: "QDG_ECUDA", 5: "QDG_ENOMEM", 6: "QDG_EUNSUPPORTED", 7: "QDG_ENOTCONVERGED",
+}
+
+TERM_KINETIC = 1
+TERM_POTENTIAL = 2
+TERM_DIPOLE = 3
+
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+
+class Grid(C.Structure):
+    _fields_ = [
+        ("ndims", C.c_int32),
+        ("n", C.c_int32 * QDG_MAX_DIMS),
+        ("xmin", C.c_double * QDG_MAX_DIMS),
+        ("xmax", C.c_double * QDG_MAX_DIMS),
+    ]
+
+
+class HTerm(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32),
+        ("row", C.c_int32),
+        ("col", C.c_int32),
+        ("grid", C.c_int32),
+        ("laser", C.c_int32),
+        ("group", C.c_int32),
+        ("mass", C.c_double * QDG_MAX_DIMS),
+    ]
+
+
+class HPlanDesc(C.Structure):
+    _fields_ = [
+        ("grid", Grid),
+        ("nstates", C.c_int32),
+        ("nterms", C.c_int32),
+        ("terms", C.POINTER(HTerm)),
+        ("ngrids", C.c_int32),
+        ("grid_data", C.POINTER(C.c_double)),
+        ("nlasers", C.c_int32),
+        ("laser_nt", C.c_int32),
+        ("laser_data", C.POINTER(C.c_double)),
+    ]
+
+
+class Observables(C.Structure):
+    _fields_ = [
+        ("norm2", C.c_double),
+        ("pops", C.c_double * QDG_MAX_STATES),
+        ("energy", C.c_double),
+        ("autocorr_re", C.c_double),
+        ("autocorr_im", C.c_double),
+    ]
+
+
+class PropInfo(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32),
+        ("order", C.c_int32),
+        ("scaling", C.c_double),
+        ("offset_re", C.c_double),
+        ("offset_im", C.c_double),
+        ("exponent_re", C.c_double),
+        ("exponent_im", C.c_double),
+    ]
+
+
+# Every symbol include/qdg.h declares: (name, restype, argtypes).
+_vp = C.c_void_p
+_i32 = C.c_int32
+_i64 = C.c_int64
+_dp = C.POINTER(C.c_double)
+SIGNATURES = [
+    ("qdg_last_error", C.c_char_p, []),
+    ("qdg_abi_version", _i32, []),
+    ("qdg_plan_create", _i32, [C.POINTER(HPlanDesc), _i32, C.POINTER(_vp)]),
+    ("qdg_plan_destroy", _i32, [_vp]),
+    ("qdg_plan_erange", _i32, [_vp, _dp, _dp]),
+    ("qdg_plan_set_stream", _i32, [_vp, _vp]),
+    ("qdg_plan_synchronize", _i32, [_vp]),
+    ("qdg_wf_create", _i32, [_vp, C.POINTER(_vp)]),
+    ("qdg_wf_destroy", _i32, [_vp]),
+    ("qdg_wf_upload", _i32, [_vp, _dp]),
+    ("qdg_wf_download", _i32, [_vp, _dp]),
+    ("qdg_wf_copy", _i32, [_vp, _vp]),
+    ("qdg_h_apply", _i32, [_vp, _vp, _vp, _i64]),
+    ("qdg_observables_compute", _i32, [_vp, _vp, _vp, _i64, C.POINTER(Observables)]),
+    ("qdg_prop_create", _i32, [_vp, C.c_char_p, C.c_char_p, C.c_double, _i32, _i32, C.POINTER(_vp)]),
+    ("qdg_prop_destroy", _i32, [_vp]),
+    ("qdg_prop_init", _i32, [_vp]),
+    ("qdg_prop_get_info", _i32, [_vp, C.POINTER(PropInfo)]),
+    ("qdg_prop_get_coeffs", _i32, [_vp, _dp, _i32]),
+    ("qdg_prop_apply", _i32, [_vp, _vp, _i64, C.POINTER(_i32)]),
+    ("qdg_prop_apply_host", _i32, [_vp, _vp, _dp, _i64, C.POINTER(_i32)]),
+    ("qdg_prop_run", _i32, [_vp, _vp, _i64, _i32, C.POINTER(_i64)]),
+]
+
+
+def header_symbols(path):
+    """Names of the functions declared in a qdg header (for the export test)."""
+    import re
+    text = open(path).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(qdg_[a-z0-9_]+)\s*\(", text)))

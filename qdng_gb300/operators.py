@@ -1,0 +1,279 @@
+"""Host-side mirror of the QDng operator tree on the propagation path.
+
+The classes keep the reference's names and the meaning of their XML
+attributes, and flatten the tree into the qdg_hplan_desc the C ABI takes:
+
+* ``GridNablaSq(mass=[...])``   -- src/qdlib/OGridNablaSq.cpp:28-58
+* ``GridPotential(values)``     -- src/qdlib/OGridPotential.cpp:26-109 (setzero/offset/scale)
+* ``GridDipole(mu, laser)``     -- src/qdlib/OGridDipole.cpp:18-60, Laser.cpp:125-128
+* ``Sum([...])``                -- src/qdlib/OSum.cpp:28-72
+* ``Multistate({(i, j): op})``  -- src/qdlib/OMultistate.cpp:100-241 (hermitian: (i,j) also acts at (j,i))
+* ``DMultistate({(i, j): op})`` -- src/qdlib/ODMultistate.cpp:35-182 (GSPO members)
+
+Errors follow the reference's exceptions: ``EParamProblem`` for bad
+parameters, ``EIncompatible`` for operator/wave-function mismatches.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+
+
+class EParamProblem(ValueError):
+    """src/tools/Exception.h EParamProblem."""
+
+
+class EIncompatible(TypeError):
+    """src/tools/Exception.h EIncompatible."""
+
+
+class EOverflow(ArithmeticError):
+    """src/tools/Exception.h EOverflow."""
+
+
+class EIOError(IOError):
+    """src/tools/Exception.h EIOError."""
+
+
+class GridSystem:
+    """QDng GridSystem: dim 0 fastest, dx = (xmax - xmin)/(N - 1) (GridSystem.cpp:207-211)."""
+
+    def __init__(self, n, xmin, xmax):
+        n = [int(v) for v in np.atleast_1d(n)]
+        xmin = [float(v) for v in np.atleast_1d(xmin)]
+        xmax = [float(v) for v in np.atleast_1d(xmax)]
+        if not (1 <= len(n) <= abi.QDG_MAX_DIMS) or len(xmin) != len(n) or len(xmax) != len(n):
+            raise EParamProblem("invalid grid dimensions")
+        for i in range(len(n)):
+            if n[i] < 1:
+                raise EParamProblem("Zero points grid defined")
+            if xmax[i] - xmin[i] <= 0:
+                raise EParamProblem("Zero length grid defined")
+        self.n, self.xmin, self.xmax = n, xmin, xmax
+
+    @property
+    def ndims(self):
+        return len(self.n)
+
+    @property
+    def npts(self):
+        return int(np.prod(self.n))
+
+    @property
+    def dx(self):
+        return [(self.xmax[i] - self.xmin[i]) / (self.n[i] - 1) for i in range(self.ndims)]
+
+    def axes(self):
+        """Coordinate axes, x_i = xmin + i*dx."""
+        return [self.xmin[i] + np.arange(self.n[i]) * self.dx[i] for i in range(self.ndims)]
+
+    def mesh(self):
+        """Coordinate arrays shaped (n[D-1], ..., n[0]) -- C order with dim 0 fastest."""
+        ax = self.axes()
+        grids = np.meshgrid(*ax[::-1], indexing="ij")
+        return grids[::-1]
+
+    def to_c(self):
+        g = abi.Grid()
+        g.ndims = self.ndims
+        for i in range(self.ndims):
+            g.n[i] = self.n[i]
+            g.xmin[i] = self.xmin[i]
+            g.xmax[i] = self.xmax[i]
+        return g
+
+    def __eq__(self, other):
+        return (isinstance(other, GridSystem) and self.n == other.n
+                and np.allclose(self.xmin, other.xmin, rtol=0, atol=0)
+                and np.allclose(self.xmax, other.xmax, rtol=0, atol=0))
+
+
+class Operator:
+    def terms(self, row, col, group, ctx):
+        raise NotImplementedError
+
+
+class GridNablaSq(Operator):
+    """Kinetic energy -1/(2m) d^2/dx^2 per dimension via FFT."""
+
+    def __init__(self, mass):
+        mass = [float(m) for m in np.atleast_1d(mass)]
+        if len(mass) < 1:
+            raise EParamProblem("Nabla operator needs at least one dimension")
+        for m in mass:
+            if m == 0:
+                raise EParamProblem("Zero mass defined")
+            if m < 0:
+                raise EIncompatible("negative masses (excluded dimensions) are not supported")
+        self.mass = mass
+
+    def terms(self, row, col, group, ctx):
+        if row != col:
+            raise EIncompatible("GridNablaSq must sit on the diagonal")
+        if len(self.mass) != ctx.grid.ndims:
+            raise EIncompatible("OGridNablaSq: Number of dims doesn't match WF")
+        t = abi.HTerm()
+        t.kind, t.row, t.col, t.grid, t.laser, t.group = abi.TERM_KINETIC, row, col, -1, -1, group
+        for i, m in enumerate(self.mass):
+            t.mass[i] = m
+        return [t]
+
+
+class GridPotential(Operator):
+    """V(x) psi. ``values`` has grid shape or npts entries (dim 0 fastest)."""
+
+    def __init__(self, values, setzero=False, offset=0.0, scale=1.0):
+        v = np.array(values, dtype=np.float64).reshape(-1)
+        if setzero:
+            v = v - v.min()
+        if offset != 0:
+            v = v + offset
+        if scale != 1:
+            v = v * scale
+        self.values = v
+
+    def terms(self, row, col, group, ctx):
+        if self.values.size != ctx.grid.npts:
+            raise EIncompatible("GridPotential parameters are not compatible with wave function")
+        t = abi.HTerm()
+        t.kind, t.row, t.col, t.laser, t.group = abi.TERM_POTENTIAL, row, col, -1, group
+        t.grid = ctx.add_grid(self.values)
+        return [t]
+
+
+class GridDipole(Operator):
+    """-mu(x) E(t) psi with E(step) = laser[step]."""
+
+    def __init__(self, mu, laser):
+        self.mu = np.array(mu, dtype=np.float64).reshape(-1)
+        self.laser = np.array(laser, dtype=np.float64).reshape(-1)
+
+    def terms(self, row, col, group, ctx):
+        if self.mu.size != ctx.grid.npts:
+            raise EIncompatible("GridDipole parameters are not compatible with wave function")
+        t = abi.HTerm()
+        t.kind, t.row, t.col, t.group = abi.TERM_DIPOLE, row, col, group
+        t.grid = ctx.add_grid(self.mu)
+        t.laser = ctx.add_laser(self.laser)
+        return [t]
+
+
+class Sum(Operator):
+    def __init__(self, ops):
+        if len(ops) == 0:
+            raise EParamProblem("Sum Operator is empty")
+        self.ops = list(ops)
+
+    def terms(self, row, col, group, ctx):
+        out = []
+        for o in self.ops:
+            out += o.terms(row, col, group, ctx)
+        return out
+
+
+class Multistate(Operator):
+    """Operator matrix; an element given at (i, j), i != j, also acts at (j, i)."""
+
+    def __init__(self, elements, nstates=None):
+        self.elements = dict(elements)
+        n = 1 + max(max(i, j) for (i, j) in self.elements)
+        self.nstates = nstates or n
+        if self.nstates < 1:
+            raise EParamProblem("Multistate operator is empty")
+
+    def terms(self, row, col, group, ctx):
+        out = []
+        seen = set()
+        for (i, j), o in sorted(self.elements.items()):
+            key = (min(i, j), max(i, j))
+            if key in seen and i != j:
+                raise EParamProblem("off-diagonal element given twice")
+            seen.add(key)
+            out += o.terms(i, j, group, ctx)
+        return out
+
+
+class DMultistate(Multistate):
+    """Multistate member of a GSPO split (diagonalisable per grid point or by FFT)."""
+
+
+class _Ctx:
+    def __init__(self, grid):
+        self.grid = grid
+        self.grids = []
+        self.lasers = []
+
+    def add_grid(self, v):
+        for i, g in enumerate(self.grids):
+            if g is v:
+                return i
+        self.grids.append(v)
+        return len(self.grids) - 1
+
+    def add_laser(self, v):
+        for i, g in enumerate(self.lasers):
+            if g is v:
+                return i
+        self.lasers.append(v)
+        return len(self.lasers) - 1
+
+
+class HPlan:
+    """A flattened Hamiltonian (qdg_hplan_desc) plus the arrays it points to."""
+
+    def __init__(self, grid, hamiltonian=None, nstates=1, members=None):
+        """hamiltonian: Sum/Multistate/single operator (Cheby, SIL, Arnoldi);
+        members: [A, B, C, ...] GSPO split operators (OGSPO.cpp:71-85).
+        Exactly one of them is given; a GSPO plan's H is the sum of its members."""
+        self.grid = grid
+        ctx = _Ctx(grid)
+        terms = []
+        if members is not None:
+            for g, m in enumerate(members):
+                if isinstance(m, Multistate):
+                    nstates = max(nstates, m.nstates)
+                terms += m.terms(0, 0, g, ctx)
+        else:
+            if isinstance(hamiltonian, Multistate):
+                nstates = max(nstates, hamiltonian.nstates)
+            terms += hamiltonian.terms(0, 0, 0, ctx)
+        for t in terms:
+            if t.row >= nstates or t.col >= nstates:
+                raise EParamProblem("Multistate operator can only use WFs with same number of states")
+        self.nstates = nstates
+        self.terms = terms
+        npts = grid.npts
+        self.grid_data = (np.concatenate(ctx.grids) if ctx.grids else np.zeros(1)).astype(np.float64)
+        if ctx.lasers:
+            nt = max(len(l) for l in ctx.lasers)
+            lz = np.zeros((len(ctx.lasers), nt))
+            for i, l in enumerate(ctx.lasers):
+                lz[i, :len(l)] = l
+            self.laser_data = lz.reshape(-1)
+            self.laser_nt = nt
+        else:
+            self.laser_data = np.zeros(1)
+            self.laser_nt = 0
+        self.ngrids = len(ctx.grids)
+        self.nlasers = len(ctx.lasers)
+        self._terms_c = (abi.HTerm * max(1, len(terms)))(*terms)
+        d = abi.HPlanDesc()
+        d.grid = grid.to_c()
+        d.nstates = nstates
+        d.nterms = len(terms)
+        d.terms = C.cast(self._terms_c, C.POINTER(abi.HTerm))
+        d.ngrids = self.ngrids
+        self._gd = np.ascontiguousarray(self.grid_data)
+        d.grid_data = self._gd.ctypes.data_as(C.POINTER(C.c_double))
+        d.nlasers = self.nlasers
+        d.laser_nt = self.laser_nt
+        self._ld = np.ascontiguousarray(self.laser_data)
+        d.laser_data = self._ld.ctypes.data_as(C.POINTER(C.c_double))
+        self.desc = d
+        self.npts = npts
+
+    @property
+    def size(self):
+        """Complex values of one wave function (all states)."""
+        return self.npts * self.nstates

@@ -1,0 +1,150 @@
+"""Test systems: QDng's own integration-test inputs (tests/*.qdi.in) rebuilt
+from the committed fixtures, and the seeded synthetic workloads.
+
+Each builder returns (HPlan, psi0 [normalised, complex128], dict of run settings).
+"""
+import numpy as np
+
+from qdng_gb300 import operators as op
+
+
+def mgh_grid(fx):
+    n, xmin, xmax = fx["GridPot0_grid"]
+    return op.GridSystem([int(n)], [xmin], [xmax])
+
+
+def _normalize(hp, psi):
+    dx = np.prod(hp.grid.dx)
+    return psi / np.sqrt((np.abs(psi) ** 2).sum() * dx)
+
+
+def tgp_expec(fx):
+    """tests/TGP-Expec.qdi.in: Cheby, Sum(T, V0), ef_0, dt=20, 1000 steps."""
+    g = mgh_grid(fx)
+    hp = op.HPlan(g, op.Sum([op.GridNablaSq([1763.2]), op.GridPotential(fx["GridPot0"])]))
+    psi = _normalize(hp, fx["GridPot0_ef_0"].astype(np.complex128))
+    return hp, psi, dict(name="Cheby", params="prec=1e-12", dt=20.0, steps=1000)
+
+
+def tgpms(fx, gspo=False):
+    """tests/TGPMS-Cheby.qdi.in / TGPMS-GSPO.qdi.in: two uncoupled states."""
+    g = mgh_grid(fx)
+    T = op.GridNablaSq([1763.2])
+    V0, V1 = op.GridPotential(fx["GridPot0"]), op.GridPotential(fx["GridPot1"])
+    if gspo:
+        hp = op.HPlan(g, members=[op.DMultistate({(0, 0): T, (1, 1): op.GridNablaSq([1763.2])}),
+                                  op.DMultistate({(0, 0): V0, (1, 1): V1})])
+        run = dict(name="GSPO", params="", dt=2.0, steps=3000)
+    else:
+        hp = op.HPlan(g, op.Multistate({(0, 0): op.Sum([T, V0]), (1, 1): op.Sum([T, V1])}))
+        run = dict(name="Cheby", params="prec=1e-12", dt=10.0, steps=1000)
+    ef = fx["GridPot0_ef_0"].astype(np.complex128)
+    psi = _normalize(hp, np.concatenate([ef, ef]))
+    return hp, psi, run
+
+
+def tgpl_ir_pulse(fx, gspo=False):
+    """tests/TGPL-IR-Pulse-{Cheby,GSPO}.qdi.in: laser-driven single state."""
+    g = mgh_grid(fx)
+    T = op.GridNablaSq([1763.2])
+    V = op.GridPotential(fx["GridPot0"])
+    D = op.GridDipole(fx["GridDip0"], fx["GridLaser_w0p00713"])
+    if gspo:
+        hp = op.HPlan(g, members=[T, V, D])
+        run = dict(name="GSPO", params="", dt=10.0, steps=6750)
+    else:
+        hp = op.HPlan(g, op.Sum([T, V, D]))
+        run = dict(name="Cheby", params="prec=1e-12", dt=10.0, steps=6750)
+    psi = _normalize(hp, fx["GridPot0_ef_0"].astype(np.complex128))
+    return hp, psi, run
+
+
+def tgplms(fx, sil=False):
+    """tests/TGPLMS-{Cheby,SIL}.qdi.in: two states coupled by a dipole x field."""
+    g = mgh_grid(fx)
+    T = op.GridNablaSq([1763.2])
+    H = op.Multistate({(0, 0): op.Sum([T, op.GridPotential(fx["GridPot0"])]),
+                       (1, 1): op.Sum([T, op.GridPotential(fx["GridPot1"])]),
+                       (1, 0): op.GridDipole(fx["GridDip01"], fx["GridLaser_w0p176"])})
+    hp = op.HPlan(g, H)
+    ef = fx["GridPot0_ef_0"].astype(np.complex128)
+    psi = _normalize(hp, np.concatenate([ef, np.zeros_like(ef)]))
+    run = dict(name="SIL", params="order=20", dt=1.0, steps=400) if sil else \
+        dict(name="Cheby", params="prec=1e-12", dt=1.0, steps=400)
+    return hp, psi, run
+
+
+def tge(fx, method):
+    """tests/TGE-<method>.qdi.in imaginary-time part: Sum(T, V0) on GridGauss, dt=5."""
+    g = mgh_grid(fx)
+    T, V = op.GridNablaSq([1763.2]), op.GridPotential(fx["GridPot0"])
+    if method == "GSPO":
+        hp = op.HPlan(g, members=[T, V])
+        params = ""
+    else:
+        hp = op.HPlan(g, op.Sum([T, V]))
+        params = {"Cheby": "", "SIL": "order=25", "Arnoldi": "order=15"}[method]
+    psi = _normalize(hp, fx["GridGauss"].astype(np.complex128))
+    return hp, psi, dict(name=method, params=params, dt=5.0, steps=1000, nef=10, conv=1e-5)
+
+
+# ---------------------------------------------------------------- synthetic
+def cfg1_morse(n=1024):
+    """1-D Morse, 1024 points on [1,10], m=1728, D=0.1, a=1, re=2, Gaussian at 2.3 (sigma 0.2), dt=10."""
+    g = op.GridSystem([n], [1.0], [10.0])
+    x = g.axes()[0]
+    V = 0.1 * (1 - np.exp(-(x - 2.0))) ** 2
+    hp = op.HPlan(g, op.Sum([op.GridNablaSq([1728.0]), op.GridPotential(V)]))
+    psi = _normalize(hp, np.exp(-(x - 2.3) ** 2 / (2 * 0.2 ** 2)).astype(np.complex128))
+    return hp, psi, dict(name="Cheby", params="", dt=10.0, steps=2000)
+
+
+def cfg2_two_state(n=256, gspo=False):
+    """2-D two-state diabatic model on [-4,4]^2, masses (1836, 3672), k=0.02, dt=5."""
+    g = op.GridSystem([n, n], [-4.0, -4.0], [4.0, 4.0])
+    X, Y = g.mesh()
+    k = 0.02
+    V1 = 0.5 * k * (X ** 2 + Y ** 2)
+    V2 = 0.5 * k * ((X - 1.0) ** 2 + Y ** 2) + 0.05
+    V12 = 0.01 * np.exp(-(X - 0.5) ** 2 - Y ** 2)
+    m = [1836.0, 3672.0]
+    if gspo:
+        hp = op.HPlan(g, members=[
+            op.DMultistate({(0, 0): op.GridNablaSq(m), (1, 1): op.GridNablaSq(m)}),
+            op.DMultistate({(0, 0): op.GridPotential(V1), (1, 1): op.GridPotential(V2),
+                            (0, 1): op.GridPotential(V12)})])
+        run = dict(name="GSPO", params="", dt=5.0, steps=4000)
+    else:
+        T = op.GridNablaSq(m)
+        hp = op.HPlan(g, op.Multistate({(0, 0): op.Sum([T, op.GridPotential(V1)]),
+                                        (1, 1): op.Sum([T, op.GridPotential(V2)]),
+                                        (0, 1): op.GridPotential(V12)}))
+        run = dict(name="Cheby", params="", dt=5.0, steps=4000)
+    sig = [(mm * np.sqrt(k)) ** -0.5 for mm in m]
+    g1 = np.exp(-(X - 0.3) ** 2 / (2 * sig[0] ** 2) - Y ** 2 / (2 * sig[1] ** 2))
+    psi = np.concatenate([g1.reshape(-1), np.zeros(g.npts)]).astype(np.complex128)
+    return hp, _normalize(hp, psi), run
+
+
+def cfg3_anharmonic(n=128, seed=3):
+    """3-D anharmonic oscillator on [-6,6]^3, m=1836, k=(0.01,0.015,0.02), +0.001 q0 q1 q2, dt=10."""
+    g = op.GridSystem([n] * 3, [-6.0] * 3, [6.0] * 3)
+    Q = g.mesh()
+    kk = [0.01, 0.015, 0.02]
+    V = sum(0.5 * kk[i] * Q[i] ** 2 for i in range(3)) + 0.001 * Q[0] * Q[1] * Q[2]
+    hp = op.HPlan(g, op.Sum([op.GridNablaSq([1836.0] * 3), op.GridPotential(V)]))
+    off = np.random.default_rng(seed).uniform(-0.5, 0.5, size=3)
+    sig = [(1836.0 * np.sqrt(k)) ** -0.5 for k in kk]
+    psi = np.exp(-sum((Q[i] - off[i]) ** 2 / (2 * sig[i] ** 2) for i in range(3)))
+    return hp, _normalize(hp, psi.reshape(-1).astype(np.complex128)), dict(name="Cheby", params="", dt=10.0,
+                                                                          steps=1000)
+
+
+def cfg5_double_well(n=128):
+    """2-D double well V=0.002(x^2-4)^2+0.01y^2 on [-5,5]^2, m=1836."""
+    g = op.GridSystem([n, n], [-5.0, -5.0], [5.0, 5.0])
+    X, Y = g.mesh()
+    V = 0.002 * (X ** 2 - 4) ** 2 + 0.01 * Y ** 2
+    hp = op.HPlan(g, op.Sum([op.GridNablaSq([1836.0, 1836.0]), op.GridPotential(V)]))
+    psi = np.exp(-((X - 2.0) ** 2 + Y ** 2) / 0.5).reshape(-1).astype(np.complex128)
+    return hp, _normalize(hp, psi), dict(name="Cheby", params="", dt=20.0, steps=2000)

@@ -1,0 +1,164 @@
+"""Pin the CPU oracle against QDng's own goldens (tests/checktests.sh).
+
+The reference prints the last propagation line as
+    step  time  norm  [pop_i ...]  energy  <psi(t)|psi0>
+with 6 decimals for populations and 8 for energy and autocorrelation
+(Reporter.cpp:96-141); the eigen tests grep the leading digits of
+energy.dat.  Agreement here is to the printed digits (half a unit in the
+last printed place), which is all the reference's goldens carry.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests import cases
+
+
+def _last_line(hp, psi, run, step_count=None):
+    S = O.System(hp)
+    P = O.Propagator(S, run["name"], run["params"], dt=run["dt"])
+    psi0 = psi.copy()
+    x = psi.copy()
+    n = step_count or run["steps"]
+    obs, terms = P.propagate(x, psi0, n)
+    return obs[-1], terms
+
+
+def _check(golden_line, obs_row, nstates):
+    vals = golden_line["values"]
+    # vals: step, time, norm, [pops], energy, autocorr
+    norm = obs_row[0]
+    assert abs(norm - vals[2]) <= 0.5e-6
+    k = 3
+    if nstates > 1:
+        for s in range(nstates):
+            assert abs(obs_row[1 + s] - vals[k]) <= 0.5e-6, (s, obs_row[1 + s], vals[k])
+            k += 1
+    e = obs_row[1 + nstates]
+    assert abs(e - vals[k]) <= 0.5e-8 + 1e-12, (e, vals[k])
+    ac = complex(obs_row[2 + nstates], obs_row[3 + nstates])
+    gre, gim = vals[k + 1]
+    assert abs(ac.real - gre) <= 0.5e-8 + 1e-12 and abs(ac.imag - gim) <= 0.5e-8 + 1e-12, (ac, gre, gim)
+
+
+def test_fft_matches_numpy():
+    rng = np.random.default_rng(1)
+    for n in [1, 2, 3, 5, 8, 9, 12, 64, 96, 128, 384, 1024, 1536, 3072, 4096]:
+        x = rng.normal(size=n) + 1j * rng.normal(size=n)
+        ref = np.fft.fft(x)
+        sc = np.abs(ref).max()
+        assert np.abs(O.fft1(x, -1) - ref).max() <= 1e-14 * sc
+        assert np.abs(O.fft1(x, +1) - np.fft.ifft(x) * n).max() <= 1e-14 * sc
+
+
+def test_fftn_matches_numpy():
+    from qdng_gb300 import operators as op
+    rng = np.random.default_rng(2)
+    g = op.GridSystem([8, 6, 4], [0, 0, 0], [1, 1, 1])
+    x = rng.normal(size=g.npts) + 1j * rng.normal(size=g.npts)
+    ref = np.fft.fftn(x.reshape(4, 6, 8)).reshape(-1)
+    assert np.abs(O.fftn(g, x, -1) - ref).max() <= 1e-13 * np.abs(ref).max()
+
+
+def test_fft_sine_analytic():
+    """FFTnTest-style known answer (src/tests/FFTnTest.cpp:27-125): a pure
+    sine of k cycles has |F| = N/2 at bins k and N-k and 0 elsewhere."""
+    for n, k in [(4, 1), (6, 2), (8, 3), (9, 2)]:
+        x = np.sin(2 * np.pi * k * np.arange(n) / n).astype(np.complex128)
+        F = np.abs(O.fft1(x, -1))
+        expect = np.zeros(n)
+        expect[k] = expect[n - k] = n / 2
+        assert np.abs(F - expect).max() < 1e-10   # LOOSE_EPS (src/tests/defs.h)
+
+
+def test_bessel_against_amos():
+    """Cheby coefficients: J_n (ZBESJ) and e^-x I_n (ZBESI) vs SciPy's AMOS."""
+    special = pytest.importorskip("scipy.special")
+    for x in [0.5, 9.65, 11.39, 41.98, 185.96]:
+        N = int(20 * x) + 50
+        j, _ = O.bessel(0, N, x)
+        i, _ = O.bessel(1, N, x)
+        rj = special.jv(np.arange(N), x)
+        ri = special.ive(np.arange(N), x)
+        assert np.abs(j - rj).max() <= 5e-15 * max(1.0, np.abs(rj).max() * 10)
+        m = ri > 1e-250
+        assert (np.abs(i[m] - ri[m]) / ri[m]).max() < 1e-12
+
+
+def test_nablasq_sine_eigenvalue():
+    """OGridNablaSqTest-style known answer (src/tests/OGridNablaSqTest.cpp:76-139):
+    on a periodic grid, sin(2 pi x/(L+dx)) is an eigenfunction of -1/(2m) d2/dx2
+    with eigenvalue (2 pi/(L+dx))^2/(2m)."""
+    from qdng_gb300 import operators as op
+    for n in [8, 9]:
+        g = op.GridSystem([n], [0.0], [1.0])
+        dx = g.dx[0]
+        x = g.axes()[0]
+        kk = 2 * np.pi / (1.0 + dx)
+        psi = np.sin(kk * x).astype(np.complex128)
+        hp = op.HPlan(g, op.GridNablaSq([1.0]))
+        Hpsi = O.System(hp).h_apply(psi)
+        assert np.abs(Hpsi - 0.5 * kk ** 2 * psi).max() < 1e-10
+
+
+def test_tgp_expec(fixtures, golden):
+    hp, psi, run = cases.tgp_expec(fixtures)
+    obs, terms = _last_line(hp, psi, run)
+    _check(golden["propagation"]["TGP-Expec"], obs, 1)
+
+
+def test_tgpms_cheby(fixtures, golden):
+    hp, psi, run = cases.tgpms(fixtures)
+    obs, _ = _last_line(hp, psi, run)
+    _check(golden["propagation"]["TGPMS-Cheby"], obs, 2)
+
+
+def test_tgpms_gspo(fixtures, golden):
+    hp, psi, run = cases.tgpms(fixtures, gspo=True)
+    obs, _ = _last_line(hp, psi, run)
+    _check(golden["propagation"]["TGPMS-GSPO"], obs, 2)
+
+
+def test_tgplms_cheby(fixtures, golden):
+    hp, psi, run = cases.tgplms(fixtures)
+    obs, _ = _last_line(hp, psi, run)
+    _check(golden["propagation"]["TGPLMS-Cheby"], obs, 2)
+
+
+def test_tgplms_sil(fixtures, golden):
+    hp, psi, run = cases.tgplms(fixtures, sil=True)
+    obs, _ = _last_line(hp, psi, run)
+    _check(golden["propagation"]["TGPLMS-SIL"], obs, 2)
+
+
+def test_tgpl_ir_pulse_cheby(fixtures, golden):
+    hp, psi, run = cases.tgpl_ir_pulse(fixtures)
+    obs, _ = _last_line(hp, psi, run)
+    _check(golden["propagation"]["TGPL-IR-Pulse-Cheby"], obs, 1)
+
+
+def test_tgpl_ir_pulse_gspo(fixtures, golden):
+    hp, psi, run = cases.tgpl_ir_pulse(fixtures, gspo=True)
+    obs, _ = _last_line(hp, psi, run)
+    _check(golden["propagation"]["TGPL-IR-Pulse-GSPO"], obs, 1)
+
+
+def test_tge_initial(fixtures, golden):
+    hp, psi, run = cases.tge(fixtures, "Cheby")
+    o = O.System(hp).observables(psi)
+    n0, e0 = golden["tge_initial"]
+    assert f"{np.sqrt(o['norm2']):.6e}" == n0
+    assert f"{o['energy']:.6e}" == e0
+
+
+@pytest.mark.parametrize("method", ["Cheby", "GSPO", "SIL", "Arnoldi"])
+def test_tge_imag(fixtures, golden, method):
+    hp, psi, run = cases.tge(fixtures, method)
+    S = O.System(hp)
+    P = O.Propagator(S, run["name"], run["params"], dt=run["dt"], imaginary_time=True, backward=True)
+    _, e_raw, e_diag, steps = P.eigen_imag(psi, run["nef"], run["steps"], run["conv"], diag=True)
+    for i, txt in golden["tge_imag"]:
+        # energy.dat lines start with the grepped digits (ProgEigen WriteEnergyFile)
+        dec = len(txt.split(".")[1])
+        got = f"{e_diag[i]:.{dec + 3}f}"
+        assert got.startswith(txt) or abs(e_diag[i] - float(txt)) < 1.5 * 10 ** (-dec), (method, i, e_diag[i], txt)
