@@ -1,0 +1,1144 @@
+// qdg_api.cu -- the C ABI of include/qdg.h.
+//
+// Host-side orchestration of the engine: plans (device copy of the QDng
+// Hamiltonian tree), wave functions, and the four propagators that replace
+// OCheby, OGSPO, OSIL and OArnoldi.  All numerics run on the device except
+// the small problems of qdg_host.cpp.  No exception leaves this file; every
+// entry point returns a qdg_status and leaves a message for qdg_last_error().
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/qdg.h"
+#include "qdg_host.h"
+#include "qdg_kernels.cuh"
+
+using qdg::cplx;
+typedef std::complex<double> cd;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+qdg_status fail(qdg_status s, const std::string &msg) {
+  g_last_error = msg;
+  return s;
+}
+
+#define CK(...)                                                                           \
+  do {                                                                                    \
+    cudaError_t e_ = (__VA_ARGS__);                                                       \
+    if (e_ != cudaSuccess) return fail(QDG_ECUDA, std::string(#__VA_ARGS__) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+cplx<double> C(cd z) { cplx<double> c; c.re = z.real(); c.im = z.imag(); return c; }
+
+// Per-dimension line geometry and FFT tables.
+struct DimInfo {
+  int n;
+  long long stride;   // prod of n[k], k < d
+  qdg::RadixPlan rp;
+  void *tw;           // n twiddles (cplx<T>)
+  double *kfac;       // [S] dk^2/(2m)/n for H passes
+  int TW_k, TW_e;     // lines per tile: kinetic-only passes, coupled epilogue pass
+};
+
+bool radix_plan(int n, qdg::RadixPlan &rp) {
+  rp.n = n; rp.nstages = 0;
+  int m = n;
+  while (m % 4 == 0) { rp.radix[rp.nstages++] = 4; m /= 4; }
+  while (m % 2 == 0) { rp.radix[rp.nstages++] = 2; m /= 2; }
+  while (m % 3 == 0) { rp.radix[rp.nstages++] = 3; m /= 3; }
+  while (m % 5 == 0) { rp.radix[rp.nstages++] = 5; m /= 5; }
+  if (rp.nstages > 16) return false;
+  return m == 1;
+}
+
+}  // namespace
+
+struct qdg_plan {
+  qdg_grid grid;
+  int S = 1;
+  int nd = 1;
+  long long npts = 1;
+  int precision = QDG_PREC_FP64;
+  size_t csize = 16;  // bytes per complex of the bulk type
+  double dx[QDG_MAX_DIMS], dk[QDG_MAX_DIMS];
+  std::vector<qdg_hterm> terms;
+  std::vector<double> grids_h, lasers_h;
+  int ngrids = 0, nlasers = 0, laser_nt = 0;
+  cd emax = 0, emin = 0;
+  // device
+  void *d_grids = nullptr;      // bulk type
+  double *d_lasers = nullptr;
+  DimInfo dim[QDG_MAX_DIMS];
+  qdg::Couplings cp_h;           // all potential/dipole entries of H
+  qdg::Couplings *d_cp = nullptr;
+  double *d_coef = nullptr;
+  void *d_P = nullptr;           // kinetic partial sums (bulk type)
+  void *d_scratch = nullptr;     // bulk-type wave function (mixed H apply input / output)
+  void *d_scratch2 = nullptr;
+  double *d_partials = nullptr;
+  int max_parts = 0;
+  double *h_partials = nullptr;  // pinned
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int sm_count = 1;
+};
+
+struct qdg_wf {
+  qdg_plan *plan;
+  cplx<double> *d = nullptr;  // S * npts complex128
+};
+
+struct qdg_prop {
+  qdg_plan *plan;
+  std::string name;
+  int kind = 0;
+  std::map<std::string, std::string> params;
+  double dt = 0;
+  bool imag = false, backward = false;
+  cd c0 = 0;
+  bool inited = false;
+  // Cheby
+  int order = 0;
+  double scaling = 1, prec = 1e-10;
+  cd offset = 0;
+  std::vector<double> coeff;
+  void *k0 = nullptr, *k1 = nullptr;  // bulk type
+  qdg::ChebyState *d_cs = nullptr;
+  qdg::ChebyState *h_cs = nullptr;    // pinned
+  // GSPO
+  int ngroups = 0;
+  std::vector<int> group_kinetic;     // 1: FFT member, 0: potential member
+  std::vector<qdg::Couplings> gcp_h;
+  std::vector<qdg::Couplings *> gcp_d;
+  std::vector<double *> gcoef_d;
+  std::vector<std::vector<void *>> gtab;  // [group][dim] S*n exp tables
+  // Krylov
+  int kord = 20, aorder = 0;
+  double err = 1e-12, conv = 1e-12;
+  std::vector<void *> lzb;
+  void *kbuf = nullptr;
+  void *kwide = nullptr;  // FP64 copy of one basis vector (mixed precision)
+};
+
+namespace {
+
+template <typename T> struct Bulk;
+
+long long wf_elems(const qdg_plan *p) { return p->npts * p->S; }
+
+double parse_d(const qdg_prop *p, const char *k) { return atof(p->params.at(k).c_str()); }
+bool has(const qdg_prop *p, const char *k) { return p->params.count(k) > 0; }
+
+void parse_params(const char *s, std::map<std::string, std::string> &out) {
+  if (!s) return;
+  std::string str(s);
+  for (char &c : str)
+    if (c == ';' || c == ',' || c == '\t' || c == '\n') c = ' ';
+  size_t i = 0;
+  while (i < str.size()) {
+    while (i < str.size() && str[i] == ' ') ++i;
+    size_t j = i;
+    while (j < str.size() && str[j] != ' ') ++j;
+    std::string kv = str.substr(i, j - i);
+    size_t eq = kv.find('=');
+    if (eq != std::string::npos) out[kv.substr(0, eq)] = kv.substr(eq + 1);
+    i = j;
+  }
+}
+
+// ------------------------------------------------------ energy range
+// Emax/Emin of one operator (OGridNablaSq.cpp:89-106, OGridPotential.cpp:124-132,
+// OGridDipole.cpp:36-44).
+cd term_emax(const qdg_plan *p, const qdg_hterm &t) {
+  const long long n = p->npts;
+  if (t.kind == QDG_TERM_KINETIC) {
+    double T = 0;
+    for (int d = 0; d < p->nd; ++d)
+      if (t.mass[d] > 0) T += 1 / (t.mass[d] * p->dx[d] * p->dx[d]);
+    return T * (M_PI * M_PI / 2);
+  }
+  const double *g = p->grids_h.data() + (long long)t.grid * n;
+  double gm = *std::max_element(g, g + n);
+  if (t.kind == QDG_TERM_POTENTIAL) return gm;
+  const double *l = p->lasers_h.data() + (long long)t.laser * p->laser_nt;
+  return gm * *std::max_element(l, l + p->laser_nt);
+}
+cd term_emin(const qdg_plan *p, const qdg_hterm &t) {
+  if (t.kind != QDG_TERM_POTENTIAL) return 0.0;
+  const double *g = p->grids_h.data() + (long long)t.grid * p->npts;
+  return *std::min_element(g, g + p->npts);
+}
+bool term_at(const qdg_hterm &t, int i, int j) {
+  return (t.row == i && t.col == j) || (t.row != t.col && t.row == j && t.col == i);
+}
+
+// OSum::Emax/Emin (OSum.cpp:28-51) for one state; OMultistate::Emax/Emin
+// (OMultistate.cpp:163-203): extreme eigenvalue of the |E_ij| matrix.
+void compute_erange(qdg_plan *p) {
+  if (p->S == 1) {
+    cd a = 0, b = 0;
+    for (auto &t : p->terms) { a += term_emax(p, t); b += term_emin(p, t); }
+    p->emax = a; p->emin = b;
+    return;
+  }
+  const int S = p->S;
+  std::vector<double> mx(S * S, 0.0), mn(S * S, 0.0), w, z;
+  for (int i = 0; i < S; ++i)
+    for (int j = 0; j < S; ++j) {
+      cd a = 0, b = 0;
+      bool any = false;
+      for (auto &t : p->terms)
+        if (term_at(t, i, j)) { a += term_emax(p, t); b += term_emin(p, t); any = true; }
+      if (any) { mx[i * S + j] = std::abs(a); mn[i * S + j] = std::abs(b); }
+    }
+  qdg::host::sym_eig(S, mx, w, z);
+  p->emax = w[S - 1];
+  qdg::host::sym_eig(S, mn, w, z);
+  p->emin = w[0];
+}
+
+// ---------------------------------------------------------- geometry
+int choose_tw(const qdg_plan *p, int d, int nsub) {
+  const DimInfo &di = p->dim[d];
+  const long long lines = p->npts / di.n;
+  const long long limit = (d == 0) ? lines : di.stride;  // TW must divide this
+  const int target_elems = p->precision == QDG_PREC_FP64 ? 2048 : 4096;
+  int best = 1;
+  for (int tw = 2; tw <= 32; tw *= 2) {
+    if (limit % tw) break;
+    if ((long long)tw * nsub * di.n > target_elems) break;
+    const long long items = (lines / tw) * (p->S / nsub);
+    if (items < p->sm_count) break;  // keep every SM busy
+    best = tw;
+  }
+  return best;
+}
+
+size_t pass_smem(const qdg_plan *p, int d, int TW, int nsub) {
+  return (size_t)p->dim[d].n * (1 + 2 * (size_t)TW * nsub) * p->csize;
+}
+
+template <typename T>
+void fill_geometry(const qdg_plan *p, int d, int nsub, qdg::PassArgs<T> &a) {
+  const DimInfo &di = p->dim[d];
+  const int TW = nsub == 1 ? di.TW_k : di.TW_e;
+  a.N = di.n;
+  a.TW = TW;
+  a.S = p->S;
+  a.nsub = nsub;
+  a.npts = p->npts;
+  a.rp = di.rp;
+  a.tw = reinterpret_cast<const cplx<T> *>(di.tw);
+  a.kfac = di.kfac;
+  if (d == 0) {
+    a.es = 1; a.ls = di.n; a.tiles_per_hi = 1; a.hi_stride = (long long)TW * di.n;
+  } else {
+    a.es = (int)di.stride; a.ls = 1; a.tiles_per_hi = (int)(di.stride / TW); a.hi_stride = di.stride * di.n;
+  }
+  a.ntiles = p->npts / ((long long)di.n * TW);
+}
+
+template <typename T>
+qdg_status launch_one(qdg_plan *p, int mode, int d, qdg::PassArgs<T> &a, int *nblocks_out) {
+  const int nsub = a.nsub;
+  const size_t smem = pass_smem(p, d, a.TW, nsub);
+  if (smem > 227 * 1024) return fail(QDG_EUNSUPPORTED, "grid line too long for the shared-memory FFT at this precision/state count");
+  const int block = 256;
+  const int per_sm = qdg::pass_max_blocks<T>(mode, p->S, block, smem);
+  const long long items = a.ntiles * (p->S / nsub);
+  long long grid = std::min<long long>(items, (long long)per_sm * p->sm_count);
+  if (grid > p->max_parts) grid = p->max_parts;
+  if (grid < 1) grid = 1;
+  if (nblocks_out) *nblocks_out = (int)grid;
+  CK(qdg::launch_pass<T>(mode, a, (int)grid, block, smem, p->stream));
+  return QDG_OK;
+}
+
+// One application of H (all passes).  final_mode selects the epilogue of
+// the last pass; `a` carries the epilogue arguments.  Returns the number of
+// blocks of the last pass (partials written).
+template <typename T>
+qdg_status run_h(qdg_plan *p, int final_mode, const cplx<T> *phi, qdg::PassArgs<T> a, int *nparts) {
+  a.phi = phi;
+  a.P = reinterpret_cast<cplx<T> *>(p->d_P);
+  a.multi_pass = p->nd > 1;
+  a.cp = p->d_cp;
+  a.coef = p->d_coef;
+  a.grids = reinterpret_cast<const T *>(p->d_grids);
+  a.partials = p->d_partials;
+  for (int d = 0; d < p->nd; ++d) {
+    const bool last = d == p->nd - 1;
+    const int mode = last ? final_mode : (d == 0 ? qdg::PM_KIN_FIRST : qdg::PM_KIN_ACC);
+    fill_geometry<T>(p, d, last ? p->S : 1, a);
+    qdg_status s = launch_one<T>(p, mode, d, a, last ? nparts : nullptr);
+    if (s != QDG_OK) return s;
+  }
+  return QDG_OK;
+}
+
+template <typename T>
+qdg_status upload_tables(qdg_plan *p) {
+  const int S = p->S;
+  for (int d = 0; d < p->nd; ++d) {
+    DimInfo &di = p->dim[d];
+    const int n = di.n;
+    std::vector<cplx<T>> tw(n);
+    const long double pi = 3.141592653589793238462643383279502884L;
+    for (int m = 0; m < n; ++m) {
+      const long double ang = -2.0L * pi * (long double)m / (long double)n;
+      tw[m].re = (T)cosl(ang);
+      tw[m].im = (T)sinl(ang);
+    }
+    CK(cudaMalloc(&di.tw, sizeof(cplx<T>) * n));
+    CK(cudaMemcpy(di.tw, tw.data(), sizeof(cplx<T>) * n, cudaMemcpyHostToDevice));
+    // kinetic multipliers per state: sum over the state's GridNablaSq terms
+    std::vector<double> kf(S, 0.0);
+    for (auto &t : p->terms)
+      if (t.kind == QDG_TERM_KINETIC) kf[t.row] += (p->dk[d] * p->dk[d]) / (2.0 * t.mass[d]) / (double)n;
+    CK(cudaMalloc(&di.kfac, sizeof(double) * S));
+    CK(cudaMemcpy(di.kfac, kf.data(), sizeof(double) * S, cudaMemcpyHostToDevice));
+  }
+  // grids in the bulk type
+  std::vector<T> g(p->grids_h.size());
+  for (size_t i = 0; i < g.size(); ++i) g[i] = (T)p->grids_h[i];
+  CK(cudaMalloc(&p->d_grids, sizeof(T) * std::max<size_t>(1, g.size())));
+  if (!g.empty()) CK(cudaMemcpy(p->d_grids, g.data(), sizeof(T) * g.size(), cudaMemcpyHostToDevice));
+  CK(cudaMalloc(&p->d_P, sizeof(cplx<T>) * wf_elems(p)));
+  CK(cudaMalloc(&p->d_scratch, sizeof(cplx<T>) * wf_elems(p)));
+  CK(cudaMalloc(&p->d_scratch2, sizeof(cplx<T>) * wf_elems(p)));
+  return QDG_OK;
+}
+
+void free_plan(qdg_plan *p) {
+  for (int d = 0; d < QDG_MAX_DIMS; ++d) {
+    if (p->dim[d].tw) cudaFree(p->dim[d].tw);
+    if (p->dim[d].kfac) cudaFree(p->dim[d].kfac);
+  }
+  if (p->d_grids) cudaFree(p->d_grids);
+  if (p->d_lasers) cudaFree(p->d_lasers);
+  if (p->d_cp) cudaFree(p->d_cp);
+  if (p->d_coef) cudaFree(p->d_coef);
+  if (p->d_P) cudaFree(p->d_P);
+  if (p->d_scratch) cudaFree(p->d_scratch);
+  if (p->d_scratch2) cudaFree(p->d_scratch2);
+  if (p->d_partials) cudaFree(p->d_partials);
+  if (p->h_partials) cudaFreeHost(p->h_partials);
+  if (p->own_stream && p->stream) cudaStreamDestroy(p->stream);
+  delete p;
+}
+
+// Couplings of the terms selected by `pick` (kinetic terms excluded).
+template <typename F>
+qdg_status build_couplings(const qdg_plan *p, F pick, qdg::Couplings &cp) {
+  cp.ne = 0;
+  for (auto &t : p->terms) {
+    if (t.kind == QDG_TERM_KINETIC || !pick(t)) continue;
+    const int nrep = t.row != t.col ? 2 : 1;
+    for (int r = 0; r < nrep; ++r) {
+      if (cp.ne >= qdg::kMaxCouplings) return fail(QDG_EUNSUPPORTED, "too many potential/dipole matrix entries");
+      cp.row[cp.ne] = r ? t.col : t.row;
+      cp.col[cp.ne] = r ? t.row : t.col;
+      cp.gid[cp.ne] = t.grid;
+      cp.lid[cp.ne] = t.kind == QDG_TERM_DIPOLE ? t.laser : -1;
+      cp.ne++;
+    }
+  }
+  return QDG_OK;
+}
+
+// Sum of per-block per-state partial dot products (fixed order on the host).
+qdg_status finish_dots(qdg_plan *p, int grid, std::vector<cd> &per_state) {
+  const int S = p->S;
+  CK(cudaMemcpyAsync(p->h_partials, p->d_partials, sizeof(double) * 2 * S * grid, cudaMemcpyDeviceToHost, p->stream));
+  CK(cudaStreamSynchronize(p->stream));
+  per_state.assign(S, 0.0);
+  for (int b = 0; b < grid; ++b)
+    for (int s = 0; s < S; ++s)
+      per_state[s] += cd(p->h_partials[(b * S + s) * 2], p->h_partials[(b * S + s) * 2 + 1]);
+  return QDG_OK;
+}
+
+int dots_grid(const qdg_plan *p) {
+  long long g = (p->npts + 255) / 256;
+  g = std::min<long long>(g, std::min<long long>(p->max_parts / std::max(1, p->S), 2LL * p->sm_count));
+  return (int)std::max<long long>(1, g);
+}
+
+// <a|b> per state with the grid weight prod dx (WFGridCartesian.cpp:62-117).
+template <typename TA, typename TB>
+qdg_status dots(qdg_plan *p, const cplx<TA> *a, const cplx<TB> *b, std::vector<cd> &per_state) {
+  const int grid = dots_grid(p);
+  CK(qdg::launch_dots<TA, TB>(a, b, p->S, p->npts, p->d_partials, grid, p->stream));
+  qdg_status s = finish_dots(p, grid, per_state);
+  if (s != QDG_OK) return s;
+  double w = 1.0;
+  for (int d = 0; d < p->nd; ++d) w *= p->dx[d];
+  for (auto &v : per_state) v *= w;
+  return QDG_OK;
+}
+
+cd total(const std::vector<cd> &v) {
+  cd t = 0;
+  for (auto &x : v) t += x;
+  return t;
+}
+
+// H psi into the bulk-type scratch buffer `out` (psi is FP64).
+template <typename T>
+qdg_status h_apply_bulk(qdg_plan *p, const cplx<double> *psi, cplx<T> *out, long long step) {
+  CK(qdg::launch_set_coefs(p->d_coef, p->d_cp, p->d_lasers, p->laser_nt, step, p->stream));
+  const cplx<T> *in;
+  if (sizeof(T) == sizeof(double)) {
+    in = reinterpret_cast<const cplx<T> *>(psi);
+  } else {
+    CK(qdg::launch_convert<T>(reinterpret_cast<cplx<T> *>(p->d_scratch2), psi, wf_elems(p), p->stream));
+    in = reinterpret_cast<const cplx<T> *>(p->d_scratch2);
+  }
+  qdg::PassArgs<T> a;
+  memset(&a, 0, sizeof(a));
+  a.out = out;
+  int np = 0;
+  return run_h<T>(p, qdg::PM_HAPPLY, in, a, &np);
+}
+
+// ------------------------------------------------------------ Chebyshev
+// OCheby::Init (src/qdlib/OCheby.cpp:358-493).
+qdg_status cheby_init(qdg_prop *P) {
+  qdg_plan *p = P->plan;
+  P->order = 0;
+  if (has(P, "order")) {
+    P->order = atoi(P->params["order"].c_str());
+    if (P->order < 1) return fail(QDG_EINVAL, "Chebychev recursion order invalid");
+  }
+  cd Emax = p->emax, Emin = p->emin;
+  if (has(P, "Emax")) Emax.real(parse_d(P, "Emax"));
+  if (has(P, "Emax_im")) Emax.imag(parse_d(P, "Emax_im"));
+  if (has(P, "Emin")) Emin.real(parse_d(P, "Emin"));
+  if (has(P, "Emin_im")) Emin.imag(parse_d(P, "Emin_im"));
+  if (!P->imag) P->offset = cd((Emax + Emin).real() / 2, (Emax + Emin).imag());
+  else P->offset = Emin - std::abs(Emin) * 0.05;
+  if (P->offset.imag() != 0 || std::fabs(P->c0.imag()) == 0) P->scaling = std::abs(Emax - Emin) * 1.05;
+  else P->scaling = std::abs(Emax - Emin) / 2;
+  if (P->order <= 0) P->order = std::abs(int(20 * P->scaling * P->dt));
+  if (P->order < 10) P->order = 10;
+  if (has(P, "scaling")) P->scaling = parse_d(P, "scaling");
+  if (has(P, "order")) P->order = atoi(P->params["order"].c_str());
+  if (P->order < 3) return fail(QDG_EINVAL, "Chebychev recursion must be at least 3");
+  std::vector<double> b;
+  int zeroes;
+  const double R = P->scaling * P->dt;
+  if (std::fabs(P->c0.imag()) != 0 && std::fabs(P->c0.real()) == 0) zeroes = qdg::host::bessel_j(P->order, R, b);
+  else if (std::fabs(P->c0.imag()) == 0 && std::fabs(P->c0.real()) != 0) zeroes = qdg::host::bessel_i_scaled(P->order, R, b);
+  else return fail(QDG_EINVAL, "Chebychev propagator doesn't support mixed real/complex exponents");
+  P->order -= zeroes;
+  if (!has(P, "order")) {
+    const double precission = 1e-32;  // BESSEL_DELTA (OCheby.h:10)
+    int i = 2;
+    while (i < P->order && std::fabs(b[i - 1] - b[i - 2]) > precission) i++;
+    P->order = i;
+  }
+  if (P->order > 0 && !P->imag && P->order <= int(P->scaling * P->dt))
+    return fail(QDG_EINVAL, "Chebychev recursion order is to small");
+  P->coeff.assign(P->order, 0.0);
+  P->coeff[0] = b[0];
+  for (int i = 1; i < P->order; ++i) P->coeff[i] = 2.0 * b[i];
+  if (has(P, "prec")) P->prec = parse_d(P, "prec");
+  const size_t bytes = p->csize * wf_elems(p);
+  CK(cudaMalloc(&P->k0, bytes));
+  CK(cudaMalloc(&P->k1, bytes));
+  CK(cudaMalloc(&P->d_cs, sizeof(qdg::ChebyState)));
+  CK(cudaMemset(P->d_cs, 0, sizeof(qdg::ChebyState)));
+  CK(cudaMallocHost(&P->h_cs, sizeof(qdg::ChebyState)));
+  return QDG_OK;
+}
+
+// One Chebyshev step (OCheby::real_time_step / imag_time_step) with the
+// convergence decision on the device: no host synchronisation inside.
+template <typename T>
+qdg_status cheby_enqueue(qdg_prop *P, cplx<double> *psi, long long step) {
+  qdg_plan *p = P->plan;
+  cudaStream_t st = p->stream;
+  CK(qdg::launch_set_coefs(p->d_coef, p->d_cp, p->d_lasers, p->laser_nt, step, st));
+  CK(qdg::launch_cheby_begin(P->d_cs, P->order, st));
+  cplx<T> *k0 = reinterpret_cast<cplx<T> *>(P->k0);
+  cplx<T> *k1 = reinterpret_cast<cplx<T> *>(P->k1);
+  CK(qdg::launch_convert<T>(k0, psi, wf_elems(p), st));  // ket0 = Psi
+  const cd ex = P->c0 / P->dt;
+  const cd ph = std::exp(P->c0 * P->offset);
+  qdg::PassArgs<T> a;
+  memset(&a, 0, sizeof(a));
+  a.psi = psi;
+  a.offset = C(P->offset);
+  a.imag = P->imag ? 1 : 0;
+  a.done = &P->d_cs->done;
+  // phi_1 = (H - offset) psi * exp/scaling; psi = psi c0 + phi_1 c1
+  a.k0 = k1;
+  a.fac = C(ex / P->scaling);
+  a.c0p = C(P->coeff[0] * ph);
+  a.c1p = C(P->coeff[1] * ph);
+  int np = 0;
+  qdg_status s = run_h<T>(p, qdg::PM_CHEBY_FIRST, k0, a, &np);
+  if (s != QDG_OK) return s;
+  const int offim0 = P->offset.imag() == 0 ? 1 : 0;
+  CK(qdg::launch_cheby_finalize(P->d_cs, p->d_partials, np, 1, 1, P->order, P->prec, a.imag, offim0, st));
+  a.fac = C(2.0 * ex / P->scaling);
+  for (int i = 2; i < P->order; ++i) {
+    a.k0 = k0;  // phi_{n-2} in, phi_n out
+    a.coeff = C(P->coeff[i] * ph);
+    s = run_h<T>(p, qdg::PM_CHEBY_TERM, k1, a, &np);
+    if (s != QDG_OK) return s;
+    CK(qdg::launch_cheby_finalize(P->d_cs, p->d_partials, np, 0, i, P->order, P->prec, a.imag, offim0, st));
+    std::swap(k0, k1);
+  }
+  CK(qdg::launch_cheby_end(P->d_cs, st));
+  return QDG_OK;
+}
+
+// ------------------------------------------------------------------ GSPO
+// OGSPO::Init (OGSPO.cpp:61-105): members A, B, C, ... must each have a
+// diagonal representation: an FFT member (GridNablaSq on every state) or a
+// potential member (per grid point S x S matrix).
+qdg_status gspo_init(qdg_prop *P) {
+  qdg_plan *p = P->plan;
+  int ng = 0;
+  for (auto &t : p->terms) ng = std::max(ng, t.group + 1);
+  if (ng < 1) return fail(QDG_EINVAL, "GSPO is empty!");
+  if (ng > QDG_MAX_GROUPS) return fail(QDG_EINVAL, "too many GSPO members");
+  P->ngroups = ng;
+  P->group_kinetic.assign(ng, 0);
+  P->gcp_h.resize(ng);
+  P->gcp_d.assign(ng, nullptr);
+  P->gcoef_d.assign(ng, nullptr);
+  P->gtab.assign(ng, std::vector<void *>(p->nd, nullptr));
+  for (int g = 0; g < ng; ++g) {
+    bool any = false, kin = false, pot = false;
+    for (auto &t : p->terms)
+      if (t.group == g) { any = true; (t.kind == QDG_TERM_KINETIC ? kin : pot) = true; }
+    if (!any) return fail(QDG_EINVAL, "GSPO misses an operator. Sequence must be A, B, C, ...");
+    if (kin && pot) return fail(QDG_EUNSUPPORTED, "GSPO: Operator has no diagonal representation");
+    P->group_kinetic[g] = kin ? 1 : 0;
+    const double sf = g == 0 ? 1.0 : 0.5;  // OGSPO::InitExp: first member full step, others half
+    if (kin) {
+      for (int s = 0; s < p->S; ++s) {
+        int c = 0;
+        for (auto &t : p->terms)
+          if (t.group == g && t.kind == QDG_TERM_KINETIC && t.row == s) ++c;
+        if (c != 1) return fail(QDG_EUNSUPPORTED, "GSPO kinetic member needs one GridNablaSq per state");
+      }
+      // exp(c sf dk^2 k^2/(2m)) / N_d per dimension and state (time independent)
+      for (int d = 0; d < p->nd; ++d) {
+        const int n = p->dim[d].n;
+        std::vector<std::complex<long double>> tab((size_t)p->S * n);
+        for (auto &t : p->terms) {
+          if (t.group != g || t.kind != QDG_TERM_KINETIC) continue;
+          const long double f = (long double)p->dk[d] * p->dk[d] / (2.0L * t.mass[d]);
+          for (int i = 0; i < n; ++i) {
+            const long double kq = std::min(i, n - i);
+            const std::complex<long double> z = std::complex<long double>(P->c0.real(), P->c0.imag()) * (long double)sf * (f * kq * kq);
+            tab[(size_t)t.row * n + i] = std::exp(z) / (long double)n;
+          }
+        }
+        if (p->precision == QDG_PREC_FP64) {
+          std::vector<cplx<double>> h(tab.size());
+          for (size_t i = 0; i < tab.size(); ++i) { h[i].re = (double)tab[i].real(); h[i].im = (double)tab[i].imag(); }
+          CK(cudaMalloc(&P->gtab[g][d], sizeof(cplx<double>) * h.size()));
+          CK(cudaMemcpy(P->gtab[g][d], h.data(), sizeof(cplx<double>) * h.size(), cudaMemcpyHostToDevice));
+        } else {
+          std::vector<cplx<float>> h(tab.size());
+          for (size_t i = 0; i < tab.size(); ++i) { h[i].re = (float)tab[i].real(); h[i].im = (float)tab[i].imag(); }
+          CK(cudaMalloc(&P->gtab[g][d], sizeof(cplx<float>) * h.size()));
+          CK(cudaMemcpy(P->gtab[g][d], h.data(), sizeof(cplx<float>) * h.size(), cudaMemcpyHostToDevice));
+        }
+      }
+    } else {
+      qdg_status s = build_couplings(p, [g](const qdg_hterm &t) { return t.group == g; }, P->gcp_h[g]);
+      if (s != QDG_OK) return s;
+      bool offd = false;
+      for (int e = 0; e < P->gcp_h[g].ne; ++e) offd |= P->gcp_h[g].row[e] != P->gcp_h[g].col[e];
+      if (offd && p->S > 2) return fail(QDG_EUNSUPPORTED, "GSPO coupled potential member supports 2 states");
+      CK(cudaMalloc(&P->gcp_d[g], sizeof(qdg::Couplings)));
+      CK(cudaMemcpy(P->gcp_d[g], &P->gcp_h[g], sizeof(qdg::Couplings), cudaMemcpyHostToDevice));
+      CK(cudaMalloc(&P->gcoef_d[g], sizeof(double) * qdg::kMaxCouplings));
+    }
+  }
+  if (p->precision != QDG_PREC_FP64) CK(cudaMalloc(&P->k0, p->csize * wf_elems(p)));
+  return QDG_OK;
+}
+
+template <typename T>
+qdg_status gspo_member(qdg_prop *P, int g, cplx<T> *x, long long step) {
+  qdg_plan *p = P->plan;
+  const double sf = g == 0 ? 1.0 : 0.5;
+  if (P->group_kinetic[g]) {
+    qdg::PassArgs<T> a;
+    memset(&a, 0, sizeof(a));
+    for (int d = 0; d < p->nd; ++d) {
+      fill_geometry<T>(p, d, 1, a);
+      a.phi = x;
+      a.out = x;
+      a.gtab = reinterpret_cast<const cplx<T> *>(P->gtab[g][d]);
+      qdg_status s = launch_one<T>(p, qdg::PM_GSPO_KIN, d, a, nullptr);
+      if (s != QDG_OK) return s;
+    }
+  } else {
+    CK(qdg::launch_set_coefs(P->gcoef_d[g], P->gcp_d[g], p->d_lasers, p->laser_nt, step, p->stream));
+    CK(qdg::launch_gspo_potential<T>(x, p->S, p->npts, P->gcp_d[g], P->gcoef_d[g],
+                                     reinterpret_cast<const T *>(p->d_grids), C(P->c0 * sf), p->stream));
+  }
+  return QDG_OK;
+}
+
+// OGSPO::Apply (OGSPO.cpp:114-139): e^{C/2} e^{B/2} e^{A} e^{B/2} e^{C/2}.
+template <typename T>
+qdg_status gspo_enqueue(qdg_prop *P, cplx<double> *psi, long long step) {
+  qdg_plan *p = P->plan;
+  cplx<T> *x;
+  if (sizeof(T) == sizeof(double)) x = reinterpret_cast<cplx<T> *>(psi);
+  else {
+    x = reinterpret_cast<cplx<T> *>(P->k0);
+    CK(qdg::launch_convert<T>(x, psi, wf_elems(p), p->stream));
+  }
+  for (int i = P->ngroups - 1; i > 0; --i) {
+    qdg_status s = gspo_member<T>(P, i, x, step);
+    if (s != QDG_OK) return s;
+  }
+  for (int i = 0; i < P->ngroups; ++i) {
+    qdg_status s = gspo_member<T>(P, i, x, step);
+    if (s != QDG_OK) return s;
+  }
+  if (sizeof(T) != sizeof(double)) CK(qdg::launch_widen<T>(psi, x, wf_elems(p), p->stream));
+  return QDG_OK;
+}
+
+// ---------------------------------------------------------------- Krylov
+template <typename T>
+qdg_status krylov_alloc(qdg_prop *P) {
+  qdg_plan *p = P->plan;
+  P->lzb.assign(P->kord + 1, nullptr);
+  for (auto &v : P->lzb) CK(cudaMalloc(&v, sizeof(cplx<T>) * wf_elems(p)));
+  CK(cudaMalloc(&P->kbuf, sizeof(cplx<T>) * wf_elems(p)));
+  if (sizeof(T) != sizeof(double)) CK(cudaMalloc(&P->kwide, sizeof(cplx<double>) * wf_elems(p)));
+  return QDG_OK;
+}
+
+template <typename T>
+qdg_status hq(qdg_prop *P, const cplx<T> *q, cplx<T> *out, long long step) {
+  qdg_plan *p = P->plan;
+  qdg::PassArgs<T> a;
+  memset(&a, 0, sizeof(a));
+  a.out = out;
+  int np;
+  return run_h<T>(p, qdg::PM_HAPPLY, q, a, &np);
+}
+
+// OSIL::BuildLZB / DiagLZB (src/qdlib/OSIL.cpp:83-185), FP64 scalars.
+template <typename T>
+qdg_status sil_step(qdg_prop *P, cplx<double> *psi, long long step, int *used) {
+  qdg_plan *p = P->plan;
+  const long long n = wf_elems(p);
+  const int order = P->kord;
+  std::vector<cplx<T> *> L(order);
+  for (int i = 0; i < order; ++i) L[i] = reinterpret_cast<cplx<T> *>(P->lzb[i]);
+  cplx<T> *buf0 = reinterpret_cast<cplx<T> *>(P->kbuf);
+  std::vector<double> alpha(order, 0.0), beta(order, 0.0);
+  std::vector<cd> d;
+  qdg_status s;
+  CK(qdg::launch_set_coefs(p->d_coef, p->d_cp, p->d_lasers, p->laser_nt, step, p->stream));
+  if ((s = dots<double, double>(p, psi, psi, d)) != QDG_OK) return s;
+  const double psinorm = std::sqrt(total(d).real());
+  CK(qdg::launch_convert<T>(L[0], psi, n, p->stream));
+  if ((s = hq<T>(P, L[0], buf0, step)) != QDG_OK) return s;
+  if ((s = dots<T, T>(p, L[0], buf0, d)) != QDG_OK) return s;
+  alpha[0] = total(d).real();
+  CK(cudaMemcpyAsync(L[1], buf0, sizeof(cplx<T>) * n, cudaMemcpyDeviceToDevice, p->stream));
+  CK(qdg::launch_lincomb<T>(L[1], L[0], cplx<double>{1.0, 0.0}, cplx<double>{-alpha[0], 0.0}, n, p->stream));
+  if ((s = dots<T, T>(p, L[1], L[1], d)) != QDG_OK) return s;
+  beta[0] = std::sqrt(total(d).real());
+  CK(qdg::launch_lincomb<T>(L[1], (const cplx<T> *)nullptr, cplx<double>{1.0 / beta[0], 0.0}, cplx<double>{0, 0}, n, p->stream));
+  int convorder = 2, it;
+  for (it = 2; it < order; ++it) {
+    double err = std::pow(P->dt, it - 2) * beta[0];
+    for (int i = 1; i < it - 2; ++i) err *= beta[i] / double(i);
+    err = std::fabs(err);
+    convorder++;
+    if ((s = hq<T>(P, L[it - 1], L[it], step)) != QDG_OK) return s;
+    if ((s = dots<T, T>(p, L[it - 1], L[it], d)) != QDG_OK) return s;
+    alpha[it - 1] = total(d).real();
+    CK(qdg::launch_lincomb<T>(L[it], L[it - 1], cplx<double>{1, 0}, cplx<double>{-alpha[it - 1], 0}, n, p->stream));
+    CK(qdg::launch_lincomb<T>(L[it], L[it - 2], cplx<double>{1, 0}, cplx<double>{-beta[it - 2], 0}, n, p->stream));
+    if ((s = dots<T, T>(p, L[it], L[it], d)) != QDG_OK) return s;
+    beta[it - 1] = std::sqrt(total(d).real());
+    CK(qdg::launch_lincomb<T>(L[it], (const cplx<T> *)nullptr, cplx<double>{1.0 / beta[it - 1], 0}, cplx<double>{0, 0}, n, p->stream));
+    if (err < P->err * psinorm) break;
+  }
+  if (it == order) {  // alpha of the last vector (the break case recomputes an identical value)
+    if ((s = hq<T>(P, L[it - 1], buf0, step)) != QDG_OK) return s;
+    if ((s = dots<T, T>(p, L[it - 1], buf0, d)) != QDG_OK) return s;
+    alpha[it - 1] = total(d).real();
+  }
+  // Z exp(c0 Lambda) Z^T e0 of the full order x order tridiagonal matrix (LapackDiag dstev)
+  std::vector<double> Tm((size_t)order * order, 0.0), w, z;
+  for (int i = 0; i < order; ++i) Tm[(size_t)i * order + i] = alpha[i];
+  for (int i = 0; i + 1 < order; ++i) { Tm[(size_t)i * order + i + 1] = beta[i]; Tm[(size_t)(i + 1) * order + i] = beta[i]; }
+  qdg::host::sym_eig(order, Tm, w, z);
+  std::vector<cd> vect(order);
+  for (int i = 0; i < order; ++i) {
+    cd acc = 0;
+    for (int k = 0; k < order; ++k) acc += z[(size_t)i * order + k] * z[k] * std::exp(P->c0 * w[k]);
+    vect[i] = acc;
+  }
+  // psi = vect[0] psi + sum_i vect[i] q_i, accumulated in FP64
+  CK(qdg::launch_lincomb<double>(psi, (const cplx<double> *)nullptr, C(vect[0]), cplx<double>{0, 0}, n, p->stream));
+  for (int i = 1; i < convorder; ++i) {
+    if (sizeof(T) == sizeof(double)) {
+      CK(qdg::launch_lincomb<double>(psi, reinterpret_cast<const cplx<double> *>(L[i]), cplx<double>{1, 0}, C(vect[i]), n, p->stream));
+    } else {
+      cplx<double> *wide = reinterpret_cast<cplx<double> *>(P->kwide);
+      CK(qdg::launch_widen<T>(wide, L[i], n, p->stream));
+      CK(qdg::launch_lincomb<double>(psi, wide, cplx<double>{1, 0}, C(vect[i]), n, p->stream));
+    }
+  }
+  if (used) *used = convorder;
+  return QDG_OK;
+}
+
+// OArnoldi::BuildLZB / DiagLZB / Propagate (src/qdlib/OArnoldi.cpp:86-199):
+// modified Gram-Schmidt in the reference order, FP64 scalars.
+template <typename T>
+qdg_status arnoldi_step(qdg_prop *P, cplx<double> *psi, long long step, int *used) {
+  qdg_plan *p = P->plan;
+  const long long n = wf_elems(p);
+  const int maxorder = P->kord;
+  if (P->aorder == 0) P->aorder = maxorder;
+  std::vector<cplx<T> *> L(maxorder);
+  for (int i = 0; i < maxorder; ++i) L[i] = reinterpret_cast<cplx<T> *>(P->lzb[i]);
+  cplx<T> *buf0 = reinterpret_cast<cplx<T> *>(P->kbuf);
+  std::vector<cd> tHA((size_t)maxorder * maxorder, 0.0), d;
+  qdg_status s;
+  CK(qdg::launch_set_coefs(p->d_coef, p->d_cp, p->d_lasers, p->laser_nt, step, p->stream));
+  if ((s = dots<double, double>(p, psi, psi, d)) != QDG_OK) return s;
+  const double PsiNorm = std::sqrt(total(d).real());
+  CK(qdg::launch_convert<T>(L[0], psi, n, p->stream));
+  for (int it = 1; it < maxorder; ++it) {
+    if ((s = hq<T>(P, L[it - 1], buf0, step)) != QDG_OK) return s;
+    for (int j = 0; j <= it - 1; ++j) {
+      if ((s = dots<T, T>(p, L[j], buf0, d)) != QDG_OK) return s;
+      const cd h = total(d);
+      tHA[(size_t)j * maxorder + it - 1] = h;
+      CK(qdg::launch_lincomb<T>(buf0, L[j], cplx<double>{1, 0}, C(-h), n, p->stream));
+    }
+    if ((s = dots<T, T>(p, buf0, buf0, d)) != QDG_OK) return s;
+    const double nrm = std::sqrt(total(d).real());
+    if (nrm < 1e-11) break;  // ARNOLDI_UNDERRUN (OArnoldi.h:12)
+    tHA[(size_t)it * maxorder + it - 1] = nrm;
+    CK(qdg::launch_lincomb<T>(buf0, (const cplx<T> *)nullptr, cplx<double>{1.0 / nrm, 0}, cplx<double>{0, 0}, n, p->stream));
+    CK(cudaMemcpyAsync(L[it], buf0, sizeof(cplx<T>) * n, cudaMemcpyDeviceToDevice, p->stream));
+    P->aorder = it + 1;
+    cd err = std::pow(P->dt, it - 2) * tHA[(size_t)1 * maxorder + 0] * PsiNorm;
+    for (int i = 1; i < it - 2; ++i) err *= tHA[(size_t)(i + 1) * maxorder + i] / double(i);
+    if (std::abs(err) < P->conv) break;
+  }
+  const int order = P->aorder;
+  if ((s = hq<T>(P, L[order - 1], buf0, step)) != QDG_OK) return s;
+  for (int j = 0; j < order; ++j) {
+    if ((s = dots<T, T>(p, L[j], buf0, d)) != QDG_OK) return s;
+    tHA[(size_t)j * maxorder + order - 1] = total(d);
+  }
+  std::vector<cd> HA((size_t)order * order);
+  for (int i = 0; i < order; ++i)
+    for (int j = 0; j < order; ++j) HA[(size_t)i * order + j] = tHA[(size_t)i * maxorder + j];
+  std::vector<cd> vect = qdg::host::expm_e0(order, HA, P->c0);
+  CK(qdg::launch_lincomb<double>(psi, (const cplx<double> *)nullptr, C(vect[0]), cplx<double>{0, 0}, n, p->stream));
+  for (int i = 1; i < order; ++i) {
+    if (sizeof(T) == sizeof(double)) {
+      CK(qdg::launch_lincomb<double>(psi, reinterpret_cast<const cplx<double> *>(L[i]), cplx<double>{1, 0}, C(vect[i]), n, p->stream));
+    } else {
+      cplx<double> *wide = reinterpret_cast<cplx<double> *>(P->kwide);
+      CK(qdg::launch_widen<T>(wide, L[i], n, p->stream));
+      CK(qdg::launch_lincomb<double>(psi, wide, cplx<double>{1, 0}, C(vect[i]), n, p->stream));
+    }
+  }
+  if (used) *used = order;
+  return QDG_OK;
+}
+
+template <typename T>
+qdg_status prop_step_t(qdg_prop *P, cplx<double> *psi, long long step, int *used, bool sync) {
+  qdg_plan *p = P->plan;
+  if (P->kind == 1) {
+    qdg_status s = cheby_enqueue<T>(P, psi, step);
+    if (s != QDG_OK) return s;
+    if (sync) {
+      CK(cudaMemcpyAsync(P->h_cs, P->d_cs, sizeof(qdg::ChebyState), cudaMemcpyDeviceToHost, p->stream));
+      CK(cudaStreamSynchronize(p->stream));
+      if (used) *used = P->h_cs->terms;
+      if (P->h_cs->status == QDG_ENONFINITE) return fail(QDG_ENONFINITE, "Norm is not a number");
+    }
+    return QDG_OK;
+  }
+  if (P->kind == 2) {
+    qdg_status s = gspo_enqueue<T>(P, psi, step);
+    if (used) *used = 2 * P->ngroups - 1;
+    if (s == QDG_OK && sync) CK(cudaStreamSynchronize(p->stream));
+    return s;
+  }
+  if (P->kind == 3) return sil_step<T>(P, psi, step, used);
+  return arnoldi_step<T>(P, psi, step, used);
+}
+
+qdg_status prop_step(qdg_prop *P, cplx<double> *psi, long long step, int *used, bool sync) {
+  if (P->plan->precision == QDG_PREC_FP64) return prop_step_t<double>(P, psi, step, used, sync);
+  return prop_step_t<float>(P, psi, step, used, sync);
+}
+
+}  // namespace
+
+// ====================================================================== ABI
+extern "C" {
+
+const char *qdg_last_error(void) { return g_last_error.c_str(); }
+int32_t qdg_abi_version(void) { return QDG_ABI_VERSION; }
+
+qdg_status qdg_plan_create(const qdg_hplan_desc *desc, int32_t precision, qdg_plan **out) {
+  if (!desc || !out) return fail(QDG_EINVAL, "null argument");
+  *out = nullptr;
+  if (precision != QDG_PREC_FP64 && precision != QDG_PREC_MIXED) return fail(QDG_EINVAL, "unknown precision");
+  const qdg_grid &g = desc->grid;
+  if (g.ndims < 1 || g.ndims > QDG_MAX_DIMS) return fail(QDG_EINVAL, "invalid number of grid dimensions");
+  if (desc->nstates < 1 || desc->nstates > qdg::kMaxStates) return fail(QDG_EUNSUPPORTED, "number of states outside 1..8");
+  if (desc->nterms < 1 || !desc->terms) return fail(QDG_EINVAL, "Hamiltonian is empty");
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  qdg_plan *p = new qdg_plan();
+  p->grid = g;
+  p->S = desc->nstates;
+  p->nd = g.ndims;
+  p->precision = precision;
+  p->csize = precision == QDG_PREC_FP64 ? sizeof(cplx<double>) : sizeof(cplx<float>);
+  long long stride = 1;
+  for (int d = 0; d < g.ndims; ++d) {
+    if (g.n[d] < 2) { free_plan(p); return fail(QDG_EINVAL, "Zero points grid defined"); }
+    if (g.xmax[d] - g.xmin[d] <= 0) { free_plan(p); return fail(QDG_EINVAL, "Zero length grid defined"); }
+    p->dx[d] = (g.xmax[d] - g.xmin[d]) / double(g.n[d] - 1);          // GridSystem::Dx
+    p->dk[d] = (2 * M_PI) / (g.xmax[d] - g.xmin[d] + p->dx[d]);        // Kspace::Dk
+    p->dim[d].n = g.n[d];
+    p->dim[d].stride = stride;
+    if (!radix_plan(g.n[d], p->dim[d].rp)) { free_plan(p); return fail(QDG_EUNSUPPORTED, "grid size must be 2^a 3^b 5^c"); }
+    stride *= g.n[d];
+  }
+  p->npts = stride;
+  p->terms.assign(desc->terms, desc->terms + desc->nterms);
+  p->ngrids = desc->ngrids;
+  p->nlasers = desc->nlasers;
+  p->laser_nt = desc->laser_nt;
+  for (auto &t : p->terms) {
+    if (t.row < 0 || t.col < 0 || t.row >= p->S || t.col >= p->S) { free_plan(p); return fail(QDG_EINVAL, "matrix element outside the states"); }
+    if (t.kind == QDG_TERM_KINETIC) {
+      if (t.row != t.col) { free_plan(p); return fail(QDG_EUNSUPPORTED, "kinetic operator off the diagonal"); }
+      for (int d = 0; d < p->nd; ++d)
+        if (!(t.mass[d] > 0)) { free_plan(p); return fail(QDG_EINVAL, "Zero mass defined"); }
+    } else if (t.kind == QDG_TERM_POTENTIAL || t.kind == QDG_TERM_DIPOLE) {
+      if (t.grid < 0 || t.grid >= p->ngrids || !desc->grid_data) { free_plan(p); return fail(QDG_EINVAL, "potential grid index out of range"); }
+      if (t.kind == QDG_TERM_DIPOLE && (t.laser < 0 || t.laser >= p->nlasers || p->laser_nt < 1 || !desc->laser_data)) {
+        free_plan(p); return fail(QDG_EINVAL, "dipole operator without a laser field");
+      }
+    } else { free_plan(p); return fail(QDG_EUNSUPPORTED, "unknown term kind"); }
+  }
+  if (p->ngrids > 0) p->grids_h.assign(desc->grid_data, desc->grid_data + (long long)p->ngrids * p->npts);
+  if (p->nlasers > 0) p->lasers_h.assign(desc->laser_data, desc->laser_data + (long long)p->nlasers * p->laser_nt);
+  for (double v : p->grids_h) if (!std::isfinite(v)) { free_plan(p); return fail(QDG_EINVAL, "non-finite value in a potential grid"); }
+  compute_erange(p);
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) { free_plan(p); return fail(QDG_ECUDA, "cudaGetDeviceProperties failed"); }
+  p->sm_count = prop.multiProcessorCount;
+  for (int d = 0; d < p->nd; ++d) {
+    p->dim[d].TW_k = choose_tw(p, d, 1);
+    p->dim[d].TW_e = choose_tw(p, d, p->S);
+  }
+  qdg_status s = build_couplings(p, [](const qdg_hterm &) { return true; }, p->cp_h);
+  if (s != QDG_OK) { free_plan(p); return s; }
+  auto cleanup = [&](qdg_status st) { free_plan(p); return st; };
+  if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess) return cleanup(fail(QDG_ECUDA, "stream"));
+  p->own_stream = true;
+  if (cudaMalloc(&p->d_cp, sizeof(qdg::Couplings)) != cudaSuccess ||
+      cudaMemcpy(p->d_cp, &p->cp_h, sizeof(qdg::Couplings), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMalloc(&p->d_coef, sizeof(double) * qdg::kMaxCouplings) != cudaSuccess)
+    return cleanup(fail(QDG_ENOMEM, "device allocation failed"));
+  const size_t lbytes = sizeof(double) * std::max<size_t>(1, p->lasers_h.size());
+  if (cudaMalloc(&p->d_lasers, lbytes) != cudaSuccess) return cleanup(fail(QDG_ENOMEM, "device allocation failed"));
+  if (!p->lasers_h.empty() && cudaMemcpy(p->d_lasers, p->lasers_h.data(), lbytes, cudaMemcpyHostToDevice) != cudaSuccess)
+    return cleanup(fail(QDG_ECUDA, "laser upload"));
+  p->max_parts = std::max(4096, 2 * qdg::kMaxStates * 2 * p->sm_count);
+  if (cudaMalloc(&p->d_partials, sizeof(double) * 2 * qdg::kMaxStates * p->max_parts) != cudaSuccess ||
+      cudaMallocHost(&p->h_partials, sizeof(double) * 2 * qdg::kMaxStates * p->max_parts) != cudaSuccess)
+    return cleanup(fail(QDG_ENOMEM, "device allocation failed"));
+  s = precision == QDG_PREC_FP64 ? upload_tables<double>(p) : upload_tables<float>(p);
+  if (s != QDG_OK) return cleanup(s);
+  *out = p;
+  return QDG_OK;
+}
+
+qdg_status qdg_plan_destroy(qdg_plan *plan) {
+  if (!plan) return QDG_OK;
+  cudaStreamSynchronize(plan->stream);
+  free_plan(plan);
+  return QDG_OK;
+}
+
+qdg_status qdg_plan_erange(const qdg_plan *plan, double emax[2], double emin[2]) {
+  if (!plan || !emax || !emin) return fail(QDG_EINVAL, "null argument");
+  emax[0] = plan->emax.real(); emax[1] = plan->emax.imag();
+  emin[0] = plan->emin.real(); emin[1] = plan->emin.imag();
+  return QDG_OK;
+}
+
+qdg_status qdg_plan_set_stream(qdg_plan *plan, void *cuda_stream) {
+  if (!plan) return fail(QDG_EINVAL, "null plan");
+  CK(cudaStreamSynchronize(plan->stream));
+  if (cuda_stream) {
+    if (plan->own_stream) cudaStreamDestroy(plan->stream);
+    plan->stream = (cudaStream_t)cuda_stream;
+    plan->own_stream = false;
+  }
+  return QDG_OK;
+}
+
+qdg_status qdg_plan_synchronize(qdg_plan *plan) {
+  if (!plan) return fail(QDG_EINVAL, "null plan");
+  CK(cudaStreamSynchronize(plan->stream));
+  return QDG_OK;
+}
+
+qdg_status qdg_wf_create(qdg_plan *plan, qdg_wf **out) {
+  if (!plan || !out) return fail(QDG_EINVAL, "null argument");
+  qdg_wf *w = new qdg_wf();
+  w->plan = plan;
+  if (cudaMalloc(&w->d, sizeof(cplx<double>) * wf_elems(plan)) != cudaSuccess) {
+    delete w;
+    return fail(QDG_ENOMEM, "device allocation failed");
+  }
+  cudaMemsetAsync(w->d, 0, sizeof(cplx<double>) * wf_elems(plan), plan->stream);
+  *out = w;
+  return QDG_OK;
+}
+
+qdg_status qdg_wf_destroy(qdg_wf *wf) {
+  if (!wf) return QDG_OK;
+  cudaStreamSynchronize(wf->plan->stream);
+  cudaFree(wf->d);
+  delete wf;
+  return QDG_OK;
+}
+
+qdg_status qdg_wf_upload(qdg_wf *wf, const double *host) {
+  if (!wf || !host) return fail(QDG_EINVAL, "null argument");
+  CK(cudaMemcpyAsync(wf->d, host, sizeof(cplx<double>) * wf_elems(wf->plan), cudaMemcpyHostToDevice, wf->plan->stream));
+  CK(cudaStreamSynchronize(wf->plan->stream));
+  return QDG_OK;
+}
+
+qdg_status qdg_wf_download(const qdg_wf *wf, double *host) {
+  if (!wf || !host) return fail(QDG_EINVAL, "null argument");
+  CK(cudaMemcpyAsync(host, wf->d, sizeof(cplx<double>) * wf_elems(wf->plan), cudaMemcpyDeviceToHost, wf->plan->stream));
+  CK(cudaStreamSynchronize(wf->plan->stream));
+  return QDG_OK;
+}
+
+qdg_status qdg_wf_copy(qdg_wf *dst, const qdg_wf *src) {
+  if (!dst || !src || dst->plan != src->plan) return fail(QDG_EINVAL, "wave functions of different plans");
+  CK(cudaMemcpyAsync(dst->d, src->d, sizeof(cplx<double>) * wf_elems(dst->plan), cudaMemcpyDeviceToDevice, dst->plan->stream));
+  return QDG_OK;
+}
+
+qdg_status qdg_h_apply(qdg_plan *plan, const qdg_wf *in, qdg_wf *out, int64_t step) {
+  if (!plan || !in || !out || in->plan != plan || out->plan != plan) return fail(QDG_EINVAL, "bad arguments");
+  if (in == out) return fail(QDG_EINVAL, "H apply needs distinct input and output");
+  qdg_status s;
+  if (plan->precision == QDG_PREC_FP64) {
+    s = h_apply_bulk<double>(plan, in->d, out->d, step);
+  } else {
+    cplx<float> *o = reinterpret_cast<cplx<float> *>(plan->d_scratch);
+    s = h_apply_bulk<float>(plan, in->d, o, step);
+    if (s == QDG_OK) CK(qdg::launch_widen<float>(out->d, o, wf_elems(plan), plan->stream));
+  }
+  if (s != QDG_OK) return s;
+  CK(cudaStreamSynchronize(plan->stream));
+  return QDG_OK;
+}
+
+qdg_status qdg_observables_compute(qdg_plan *plan, const qdg_wf *psi, const qdg_wf *psi0, int64_t step,
+                                   qdg_observables *out) {
+  if (!plan || !psi || !out || psi->plan != plan) return fail(QDG_EINVAL, "bad arguments");
+  memset(out, 0, sizeof(*out));
+  std::vector<cd> d;
+  qdg_status s;
+  if ((s = dots<double, double>(plan, psi->d, psi->d, d)) != QDG_OK) return s;
+  double n2 = 0;
+  for (int i = 0; i < plan->S; ++i) { out->pops[i] = d[i].real(); n2 += d[i].real(); }
+  out->norm2 = n2;
+  if (!std::isfinite(n2)) return fail(QDG_ENONFINITE, "Norm is not a number");
+  if (plan->precision == QDG_PREC_FP64) {
+    cplx<double> *o = reinterpret_cast<cplx<double> *>(plan->d_scratch);
+    if ((s = h_apply_bulk<double>(plan, psi->d, o, step)) != QDG_OK) return s;
+    if ((s = dots<double, double>(plan, psi->d, o, d)) != QDG_OK) return s;
+  } else {
+    cplx<float> *o = reinterpret_cast<cplx<float> *>(plan->d_scratch);
+    if ((s = h_apply_bulk<float>(plan, psi->d, o, step)) != QDG_OK) return s;
+    if ((s = dots<double, float>(plan, psi->d, o, d)) != QDG_OK) return s;
+  }
+  out->energy = total(d).real();
+  if (psi0) {
+    if (psi0->plan != plan) return fail(QDG_EINVAL, "psi0 of another plan");
+    if ((s = dots<double, double>(plan, psi->d, psi0->d, d)) != QDG_OK) return s;
+    const cd ac = total(d);
+    out->autocorr_re = ac.real();
+    out->autocorr_im = ac.imag();
+  }
+  return QDG_OK;
+}
+
+qdg_status qdg_prop_create(qdg_plan *plan, const char *name, const char *params, double dt, int32_t imaginary_time,
+                           int32_t backward, qdg_prop **out) {
+  if (!plan || !name || !out) return fail(QDG_EINVAL, "null argument");
+  *out = nullptr;
+  if (!(dt != 0) || !std::isfinite(dt)) return fail(QDG_EINVAL, "No time step defined");
+  qdg_prop *P = new qdg_prop();
+  P->plan = plan;
+  P->name = name;
+  parse_params(params, P->params);
+  P->dt = dt;
+  P->imag = imaginary_time != 0;
+  P->backward = backward != 0;
+  // OPropagator exponent c0 (OPropagator.h:44-131)
+  const cd I(0, 1);
+  if (P->imag) P->c0 = P->backward ? cd(-dt) : cd(dt);
+  else P->c0 = P->backward ? I * dt : -I * dt;
+  if (P->name == "Cheby") P->kind = 1;
+  else if (P->name == "GSPO") P->kind = 2;
+  else if (P->name == "SIL") P->kind = 3;
+  else if (P->name == "Arnoldi") P->kind = 4;
+  else { delete P; return fail(QDG_EINVAL, "unknown propagator: " + std::string(name)); }
+  if (P->kind >= 3) {
+    if (has(P, "order")) P->kord = atoi(P->params["order"].c_str());
+    if (P->kord < 3) { delete P; return fail(QDG_EINVAL, "order doesn't make sense"); }
+    if (has(P, "err")) P->err = parse_d(P, "err");
+    if (has(P, "conv")) P->conv = parse_d(P, "conv");
+  }
+  *out = P;
+  return QDG_OK;
+}
+
+qdg_status qdg_prop_destroy(qdg_prop *P) {
+  if (!P) return QDG_OK;
+  cudaStreamSynchronize(P->plan->stream);
+  if (P->k0) cudaFree(P->k0);
+  if (P->k1) cudaFree(P->k1);
+  if (P->d_cs) cudaFree(P->d_cs);
+  if (P->h_cs) cudaFreeHost(P->h_cs);
+  for (auto &g : P->gtab) for (auto v : g) if (v) cudaFree(v);
+  for (auto v : P->gcp_d) if (v) cudaFree(v);
+  for (auto v : P->gcoef_d) if (v) cudaFree(v);
+  for (auto v : P->lzb) if (v) cudaFree(v);
+  if (P->kbuf) cudaFree(P->kbuf);
+  if (P->kwide) cudaFree(P->kwide);
+  delete P;
+  return QDG_OK;
+}
+
+qdg_status qdg_prop_init(qdg_prop *P) {
+  if (!P) return fail(QDG_EINVAL, "null propagator");
+  if (P->inited) return QDG_OK;  // avoid init twice (OCheby.cpp:371)
+  qdg_status s;
+  if (P->kind == 1) s = cheby_init(P);
+  else if (P->kind == 2) s = gspo_init(P);
+  else s = P->plan->precision == QDG_PREC_FP64 ? krylov_alloc<double>(P) : krylov_alloc<float>(P);
+  if (s == QDG_OK) P->inited = true;
+  return s;
+}
+
+qdg_status qdg_prop_get_info(const qdg_prop *P, qdg_prop_info *info) {
+  if (!P || !info) return fail(QDG_EINVAL, "null argument");
+  info->kind = P->kind;
+  info->order = P->kind == 1 ? P->order : P->kord;
+  info->scaling = P->scaling;
+  info->offset_re = P->offset.real();
+  info->offset_im = P->offset.imag();
+  info->exponent_re = P->c0.real();
+  info->exponent_im = P->c0.imag();
+  return QDG_OK;
+}
+
+qdg_status qdg_prop_get_coeffs(const qdg_prop *P, double *coeffs, int32_t capacity) {
+  if (!P) return fail(QDG_EINVAL, "null propagator");
+  const int n = std::min<int>(capacity, (int)P->coeff.size());
+  for (int i = 0; i < n; ++i) coeffs[i] = P->coeff[i];
+  return QDG_OK;
+}
+
+qdg_status qdg_prop_apply(qdg_prop *P, qdg_wf *psi, int64_t step, int32_t *terms_used) {
+  if (!P || !psi || psi->plan != P->plan) return fail(QDG_EINVAL, "bad arguments");
+  if (!P->inited) return fail(QDG_EINVAL, "propagator not initialised");
+  int used = 0;
+  qdg_status s = prop_step(P, psi->d, step, &used, true);
+  if (terms_used) *terms_used = used;
+  return s;
+}
+
+qdg_status qdg_prop_apply_host(qdg_prop *P, qdg_wf *scratch, double *host_psi, int64_t step, int32_t *terms_used) {
+  if (!P || !scratch || !host_psi || scratch->plan != P->plan) return fail(QDG_EINVAL, "bad arguments");
+  qdg_plan *p = P->plan;
+  CK(cudaMemcpyAsync(scratch->d, host_psi, sizeof(cplx<double>) * wf_elems(p), cudaMemcpyHostToDevice, p->stream));
+  int used = 0;
+  qdg_status s = prop_step(P, scratch->d, step, &used, false);
+  if (s != QDG_OK) return s;
+  CK(cudaMemcpyAsync(host_psi, scratch->d, sizeof(cplx<double>) * wf_elems(p), cudaMemcpyDeviceToHost, p->stream));
+  if (P->kind == 1) CK(cudaMemcpyAsync(P->h_cs, P->d_cs, sizeof(qdg::ChebyState), cudaMemcpyDeviceToHost, p->stream));
+  CK(cudaStreamSynchronize(p->stream));
+  if (P->kind == 1) {
+    used = P->h_cs->terms;
+    if (P->h_cs->status == QDG_ENONFINITE) return fail(QDG_ENONFINITE, "Norm is not a number");
+  }
+  if (terms_used) *terms_used = used;
+  return QDG_OK;
+}
+
+qdg_status qdg_prop_run(qdg_prop *P, qdg_wf *psi, int64_t step0, int32_t nsteps, int64_t *terms_total) {
+  if (!P || !psi || psi->plan != P->plan || nsteps < 0) return fail(QDG_EINVAL, "bad arguments");
+  if (!P->inited) return fail(QDG_EINVAL, "propagator not initialised");
+  long long tot = 0, before = 0;
+  if (P->kind == 1) {
+    CK(cudaMemcpyAsync(P->h_cs, P->d_cs, sizeof(qdg::ChebyState), cudaMemcpyDeviceToHost, P->plan->stream));
+    CK(cudaStreamSynchronize(P->plan->stream));
+    before = P->h_cs->total;
+  }
+  for (int i = 0; i < nsteps; ++i) {
+    int used = 0;
+    // Chebyshev and GSPO steps are queued without host synchronisation;
+    // the Chebyshev term count is read back once at the end.
+    const bool sync = P->kind >= 3;
+    qdg_status s = prop_step(P, psi->d, step0 + i, &used, sync);
+    if (s != QDG_OK) return s;
+    tot += used;
+  }
+  CK(cudaStreamSynchronize(P->plan->stream));
+  if (P->kind == 1) {
+    CK(cudaMemcpy(P->h_cs, P->d_cs, sizeof(qdg::ChebyState), cudaMemcpyDeviceToHost));
+    if (P->h_cs->status == QDG_ENONFINITE) return fail(QDG_ENONFINITE, "Norm is not a number");
+    tot = P->h_cs->total - before;
+  }
+  if (terms_total) *terms_total = tot;
+  return QDG_OK;
+}
+
+}  // extern "C"

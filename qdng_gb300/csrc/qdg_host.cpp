@@ -1,0 +1,164 @@
+// qdg_host.cpp -- host-side numerics of the engine (see qdg_host.h).
+#include "qdg_host.h"
+
+#include <algorithm>
+#include <cmath>
+
+namespace qdg {
+namespace host {
+
+// AMOS/SLATEC underflow limit: 1000 * tiny / eps.
+static int trailing_underflow(std::vector<double> &out) {
+  const double ascle = 1.0e3 * 2.2250738585072014e-308 / 2.220446049250313e-16;
+  int nz = 0;
+  for (int i = (int)out.size() - 1; i >= 0; --i) {
+    if (std::fabs(out[i]) < ascle) { out[i] = 0.0; ++nz; } else break;
+  }
+  return nz;
+}
+
+static int miller_top(int N, double x) {
+  const double m = std::max<double>(N, x);
+  int s = (int)(m + 40 + 6 * std::sqrt(m));
+  return s + (s & 1);
+}
+
+// Miller's backward recurrence (Abramowitz & Stegun 9.12 / 9.6.26): start
+// far above the wanted orders, recur J_{k-1} = (2k/x) J_k - J_{k+1}, and
+// normalise with J_0 + 2 (J_2 + J_4 + ...) = 1 (A&S 9.1.46).  Values are
+// rescaled in place when they grow large; the extended exponent range of
+// long double keeps the tail of very high orders representable.
+int bessel_j(int N, double x, std::vector<double> &out) {
+  out.assign(N, 0.0);
+  if (N <= 0) return 0;
+  if (x == 0.0) { out[0] = 1.0; return trailing_underflow(out); }
+  const int top = miller_top(N, x);
+  std::vector<long double> v(top + 2, 0.0L);
+  v[top] = 1e-20L;
+  const long double lim = 1e300L;
+  const long double ix = 1.0L / (long double)x;
+  for (int k = top; k >= 1; --k) {
+    v[k - 1] = (2.0L * k) * ix * v[k] - v[k + 1];
+    if (fabsl(v[k - 1]) > lim) {
+      for (int j = k - 1; j <= top; ++j) v[j] /= lim;
+    }
+  }
+  long double norm = v[0];
+  for (int k = 2; k <= top; k += 2) norm += 2.0L * v[k];
+  for (int n = 0; n < N; ++n) out[n] = (double)(v[n] / norm);
+  return trailing_underflow(out);
+}
+
+// Same recurrence for I_n with a plus sign; e^x = I_0 + 2 sum_{k>=1} I_k (A&S 9.6.37).
+int bessel_i_scaled(int N, double x, std::vector<double> &out) {
+  out.assign(N, 0.0);
+  if (N <= 0) return 0;
+  if (x == 0.0) { out[0] = 1.0; return trailing_underflow(out); }
+  const int top = miller_top(N, x);
+  std::vector<long double> v(top + 2, 0.0L);
+  v[top] = 1e-20L;
+  const long double lim = 1e300L;
+  const long double ix = 1.0L / (long double)x;
+  for (int k = top; k >= 1; --k) {
+    v[k - 1] = (2.0L * k) * ix * v[k] + v[k + 1];
+    if (v[k - 1] > lim) {
+      for (int j = k - 1; j <= top; ++j) v[j] /= lim;
+    }
+  }
+  long double norm = v[0];
+  for (int k = 1; k <= top; ++k) norm += 2.0L * v[k];
+  for (int n = 0; n < N; ++n) out[n] = (double)(v[n] / norm);
+  return trailing_underflow(out);
+}
+
+// Cyclic Jacobi rotations (Golub & Van Loan, 8.5) in double precision.
+void sym_eig(int n, const std::vector<double> &a_in, std::vector<double> &w, std::vector<double> &z) {
+  std::vector<double> a = a_in;
+  z.assign((size_t)n * n, 0.0);
+  for (int i = 0; i < n; ++i) z[(size_t)i * n + i] = 1.0;
+  for (int sweep = 0; sweep < 64; ++sweep) {
+    double off = 0.0, diag = 0.0;
+    for (int p = 0; p < n; ++p) {
+      diag += a[(size_t)p * n + p] * a[(size_t)p * n + p];
+      for (int q = p + 1; q < n; ++q) off += a[(size_t)p * n + q] * a[(size_t)p * n + q];
+    }
+    if (off <= 1e-34 * (diag + 1e-300)) break;
+    for (int p = 0; p < n; ++p) {
+      for (int q = p + 1; q < n; ++q) {
+        const double apq = a[(size_t)p * n + q];
+        if (apq == 0.0) continue;
+        const double theta = (a[(size_t)q * n + q] - a[(size_t)p * n + p]) / (2.0 * apq);
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < n; ++k) {
+          const double akp = a[(size_t)k * n + p], akq = a[(size_t)k * n + q];
+          a[(size_t)k * n + p] = c * akp - s * akq;
+          a[(size_t)k * n + q] = s * akp + c * akq;
+        }
+        for (int k = 0; k < n; ++k) {
+          const double apk = a[(size_t)p * n + k], aqk = a[(size_t)q * n + k];
+          a[(size_t)p * n + k] = c * apk - s * aqk;
+          a[(size_t)q * n + k] = s * apk + c * aqk;
+        }
+        for (int k = 0; k < n; ++k) {
+          const double zkp = z[(size_t)k * n + p], zkq = z[(size_t)k * n + q];
+          z[(size_t)k * n + p] = c * zkp - s * zkq;
+          z[(size_t)k * n + q] = s * zkp + c * zkq;
+        }
+      }
+    }
+  }
+  std::vector<int> idx(n);
+  for (int i = 0; i < n; ++i) idx[i] = i;
+  std::sort(idx.begin(), idx.end(), [&](int x, int y) { return a[(size_t)x * n + x] < a[(size_t)y * n + y]; });
+  w.resize(n);
+  std::vector<double> zs((size_t)n * n);
+  for (int j = 0; j < n; ++j) {
+    w[j] = a[(size_t)idx[j] * n + idx[j]];
+    for (int k = 0; k < n; ++k) zs[(size_t)k * n + j] = z[(size_t)k * n + idx[j]];
+  }
+  z.swap(zs);
+}
+
+// Scaling and squaring with a Taylor polynomial (Moler & Van Loan 2003,
+// method 3) applied to the first column only after the squarings.
+std::vector<cd> expm_e0(int n, const std::vector<cd> &A, cd c) {
+  std::vector<cd> M((size_t)n * n);
+  double nrm = 0.0;
+  for (int i = 0; i < n; ++i) {
+    double row = 0.0;
+    for (int j = 0; j < n; ++j) { M[(size_t)i * n + j] = A[(size_t)i * n + j] * c; row += std::abs(M[(size_t)i * n + j]); }
+    nrm = std::max(nrm, row);
+  }
+  int s = 0;
+  while (nrm > 0.5) { nrm *= 0.5; ++s; }
+  const double sc = std::ldexp(1.0, -s);
+  for (auto &x : M) x *= sc;
+  std::vector<cd> E((size_t)n * n, 0.0), P((size_t)n * n, 0.0), Q((size_t)n * n);
+  for (int i = 0; i < n; ++i) { E[(size_t)i * n + i] = 1.0; P[(size_t)i * n + i] = 1.0; }
+  for (int k = 1; k <= 30; ++k) {
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) {
+        cd acc = 0.0;
+        for (int l = 0; l < n; ++l) acc += P[(size_t)i * n + l] * M[(size_t)l * n + j];
+        Q[(size_t)i * n + j] = acc / (double)k;
+      }
+    P.swap(Q);
+    for (size_t i = 0; i < E.size(); ++i) E[i] += P[i];
+  }
+  for (int r = 0; r < s; ++r) {
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) {
+        cd acc = 0.0;
+        for (int l = 0; l < n; ++l) acc += E[(size_t)i * n + l] * E[(size_t)l * n + j];
+        Q[(size_t)i * n + j] = acc;
+      }
+    E.swap(Q);
+  }
+  std::vector<cd> v(n);
+  for (int i = 0; i < n; ++i) v[i] = E[(size_t)i * n];
+  return v;
+}
+
+}  // namespace host
+}  // namespace qdg

@@ -1,0 +1,34 @@
+// qdg_host.h -- host-side numerics of the engine (no CUDA).
+//
+// Small problems that QDng hands to SLATEC and LAPACK and that stay on the
+// host here: Bessel coefficients of the Chebyshev expansion, symmetric
+// eigenproblems of the Multistate energy range and of the Lanczos matrix,
+// and the exponential of the small Arnoldi Hessenberg matrix.
+#pragma once
+
+#include <complex>
+#include <vector>
+
+namespace qdg {
+namespace host {
+
+typedef std::complex<double> cd;
+
+// J_n(x), n = 0..N-1, as SLATEC ZBESJ (kode 1) returns them to
+// QDLIB::BesselJ0 (src/linalg/Bessel.cpp:22-58); returns the number of
+// trailing components that underflow (ZBESJ's NZ).
+int bessel_j(int N, double x, std::vector<double> &out);
+// e^{-x} I_n(x), n = 0..N-1 (ZBESI kode 2, src/linalg/Bessel.cpp:61-97).
+int bessel_i_scaled(int N, double x, std::vector<double> &out);
+
+// Real symmetric eigenproblem (stands in for LAPACK dsyev/dstev as wrapped
+// in src/linalg/LapackDiag.cpp:22-100): a is n x n row-major; eigenvalues
+// ascending in w, eigenvectors as columns of z (row-major).
+void sym_eig(int n, const std::vector<double> &a, std::vector<double> &w, std::vector<double> &z);
+
+// v = exp(c A) e_0 for a small complex matrix A (row-major), the vector
+// OArnoldi::Propagate forms with zhseqr/zhsein/zgetri (OArnoldi.cpp:169-186).
+std::vector<cd> expm_e0(int n, const std::vector<cd> &A, cd c);
+
+}  // namespace host
+}  // namespace qdg

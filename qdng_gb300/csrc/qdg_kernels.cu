@@ -1,0 +1,420 @@
+// qdg_kernels.cu -- sm_103a kernels of the propagation engine.
+//
+// The hot kernel is the line pass: a block loads a tile of grid lines along
+// one dimension for one or all electronic states, runs the unnormalised FFT
+// in shared memory, multiplies by the k-space kinetic factor, transforms
+// back, and finishes with an epilogue.  A Hamiltonian application over a
+// D-dimensional grid is D passes (the kinetic operator is separable:
+// T = sum_d T_d, T_d = IFFT_d k_d^2/(2m_d) FFT_d / N_d, which equals
+// QDng's IFFT_nd [sum_d k_d^2/(2m_d)] FFT_nd / N of Diff::DnDxn,
+// src/qdlib/Diff.cpp:203-218).  The last pass adds the potential matrix and,
+// for the Chebyshev propagator, runs the three-term recurrence, the psi
+// accumulation and the norm reduction in the same sweep
+// (src/qdlib/OCheby.cpp:92-198, 200-297).
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "qdg_kernels.cuh"
+
+namespace qdg {
+
+__device__ __forceinline__ cplx<double> dmul(cplx<double> a, cplx<double> b) { return cmul(a, b); }
+
+// Point (w, i) of a tile from a flat index: consecutive indices walk the
+// contiguous direction in memory (along the line when es == 1, across the
+// TW lines otherwise) so global accesses coalesce.
+__device__ __forceinline__ void tile_coord(int idx, int TW, int N, int es, int &w, int &i) {
+  if (es == 1) { w = idx / N; i = idx - w * N; }
+  else { i = idx / TW; w = idx - i * TW; }
+}
+
+template <typename T, int MODE, int SS>
+__global__ void __launch_bounds__(256) linepass_kernel(PassArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double red[32];
+  if (a.done != nullptr && *a.done) return;  // Chebyshev series already converged
+
+  const int N = a.N;
+  const int TW = a.TW;
+  const int nsub = a.nsub;
+  const int L = TW * nsub;
+  cplx<T> *tws = reinterpret_cast<cplx<T> *>(smem_raw);
+  cplx<T> *b0 = tws + N;
+  cplx<T> *b1 = b0 + (size_t)L * N;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) tws[i] = a.tw[i];
+  __syncthreads();
+
+  double acc = 0.0;
+  const int nsplit = a.S / nsub;
+  const long long nitems = a.ntiles * nsplit;
+  const long long npts = a.npts;
+  const int S = (SS > 0) ? SS : a.S;
+
+  for (long long item = blockIdx.x; item < nitems; item += gridDim.x) {
+    const long long tile = item / nsplit;
+    const int s0 = (int)(item - tile * nsplit) * nsub;
+    const long long hi = tile / a.tiles_per_hi;
+    const long long base = hi * a.hi_stride + (tile - hi * a.tiles_per_hi) * TW;
+
+    // load the tile: smem line (sl*TW + w), element i
+    const int tileN = TW * N;
+    for (int idx = threadIdx.x; idx < nsub * tileN; idx += blockDim.x) {
+      const int sl = idx / tileN;
+      int w, i;
+      tile_coord(idx - sl * tileN, TW, N, a.es, w, i);
+      const long long p = base + (long long)w * a.ls + (long long)i * a.es;
+      b0[(sl * TW + w) * N + i] = ld(a.phi + (long long)(s0 + sl) * npts + p);
+    }
+    __syncthreads();
+
+    int cur = fft_lines<T>(b0, b1, a.rp, L, tws, -1);
+    cplx<T> *bc = cur ? b1 : b0;
+    for (int idx = threadIdx.x; idx < L * N; idx += blockDim.x) {
+      const int l = idx / N;
+      const int i = idx - l * N;
+      const int s = s0 + l / TW;
+      if (MODE == PM_GSPO_KIN) {
+        bc[idx] = cmul(bc[idx], a.gtab[(long long)s * N + i]);
+      } else {
+        const int kq = min(i, N - i);
+        const T f = (T)(a.kfac[s] * (double)kq * (double)kq);
+        bc[idx] = cmulr(bc[idx], f);
+      }
+    }
+    __syncthreads();
+    int cur2 = fft_lines<T>(bc, cur ? b0 : b1, a.rp, L, tws, +1);
+    // fft_lines returns the index relative to its own (bc, other) pair
+    cplx<T> *res = cur2 ? (cur ? b0 : b1) : bc;
+
+    if (MODE == PM_KIN_FIRST || MODE == PM_KIN_ACC || MODE == PM_GSPO_KIN) {
+      for (int idx = threadIdx.x; idx < nsub * tileN; idx += blockDim.x) {
+        const int sl = idx / tileN;
+        int w, i;
+        tile_coord(idx - sl * tileN, TW, N, a.es, w, i);
+        const long long p = base + (long long)w * a.ls + (long long)i * a.es;
+        const long long g = (long long)(s0 + sl) * npts + p;
+        cplx<T> v = res[(sl * TW + w) * N + i];
+        if (MODE == PM_KIN_FIRST) st(a.P + g, v);
+        else if (MODE == PM_KIN_ACC) st(a.P + g, ld(a.P + g) + v);
+        else st(a.out + g, v);
+      }
+    } else {
+      // coupled epilogue: every point of the tile for all S states
+      for (int idx = threadIdx.x; idx < tileN; idx += blockDim.x) {
+        int w, i;
+        tile_coord(idx, TW, N, a.es, w, i);
+        const long long p = base + (long long)w * a.ls + (long long)i * a.es;
+        cplx<T> ph[(SS > 0) ? SS : kMaxStates];
+        cplx<T> h[(SS > 0) ? SS : kMaxStates];
+#pragma unroll
+        for (int s = 0; s < ((SS > 0) ? SS : kMaxStates); ++s) {
+          if (s < S) {
+            ph[s] = ld(a.phi + (long long)s * npts + p);
+            h[s] = res[(s * TW + w) * N + i];
+            if (a.multi_pass) h[s] = h[s] + ld(a.P + (long long)s * npts + p);
+          }
+        }
+        const int ne = a.cp->ne;
+        for (int e = 0; e < ne; ++e) {
+          const int r = a.cp->row[e], c = a.cp->col[e];
+          const T v = (T)(a.coef[e]) * a.grids[(long long)a.cp->gid[e] * npts + p];
+#pragma unroll
+          for (int s = 0; s < ((SS > 0) ? SS : kMaxStates); ++s)
+            if (s == r) {
+#pragma unroll
+              for (int q = 0; q < ((SS > 0) ? SS : kMaxStates); ++q)
+                if (q == c) h[s] = h[s] + cmulr(ph[q], v);
+            }
+        }
+#pragma unroll
+        for (int s = 0; s < ((SS > 0) ? SS : kMaxStates); ++s) {
+          if (s >= S) break;
+          const long long g = (long long)s * npts + p;
+          if (MODE == PM_HAPPLY) {
+            st(a.out + g, h[s]);
+          } else {
+            const cplx<double> hd = ccast<double>(h[s]);
+            const cplx<double> pd = ccast<double>(ph[s]);
+            const cplx<double> bf = dmul(hd - dmul(a.offset, pd), a.fac);
+            if (MODE == PM_CHEBY_FIRST) {
+              const cplx<double> ps = ld(a.psi + g);
+              acc += cabs2(ps);
+              st(a.k0 + g, ccast<T>(bf));                      // phi_1
+              st(a.psi + g, dmul(ps, a.c0p) + dmul(bf, a.c1p)); // psi*c0 + phi_1*c1
+            } else {
+              const cplx<double> km2 = ccast<double>(ld(a.k0 + g));
+              const cplx<double> k2 = a.imag ? bf - km2 : bf + km2;
+              st(a.k0 + g, ccast<T>(k2));
+              const cplx<double> ps = ld(a.psi + g) + dmul(k2, a.coeff);
+              st(a.psi + g, ps);
+              acc += cabs2(ps);
+            }
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (MODE == PM_CHEBY_FIRST || MODE == PM_CHEBY_TERM) {
+    const double t = block_sum(acc, red);
+    if (threadIdx.x == 0) a.partials[blockIdx.x] = t;
+  }
+}
+
+template <typename T, int MODE, int SS>
+static void *kernel_ptr() { return (void *)linepass_kernel<T, MODE, SS>; }
+
+template <typename T>
+static void *select_kernel(int mode, int S) {
+  switch (mode) {
+    case PM_KIN_FIRST: return kernel_ptr<T, PM_KIN_FIRST, 1>();
+    case PM_KIN_ACC: return kernel_ptr<T, PM_KIN_ACC, 1>();
+    case PM_GSPO_KIN: return kernel_ptr<T, PM_GSPO_KIN, 1>();
+    case PM_HAPPLY:
+      return S == 1 ? kernel_ptr<T, PM_HAPPLY, 1>() : S == 2 ? kernel_ptr<T, PM_HAPPLY, 2>() : kernel_ptr<T, PM_HAPPLY, 0>();
+    case PM_CHEBY_FIRST:
+      return S == 1 ? kernel_ptr<T, PM_CHEBY_FIRST, 1>() : S == 2 ? kernel_ptr<T, PM_CHEBY_FIRST, 2>()
+                                                                  : kernel_ptr<T, PM_CHEBY_FIRST, 0>();
+    case PM_CHEBY_TERM:
+      return S == 1 ? kernel_ptr<T, PM_CHEBY_TERM, 1>() : S == 2 ? kernel_ptr<T, PM_CHEBY_TERM, 2>()
+                                                                 : kernel_ptr<T, PM_CHEBY_TERM, 0>();
+  }
+  return nullptr;
+}
+
+template <typename T>
+cudaError_t launch_pass(int mode, const PassArgs<T> &a, int grid, int block, size_t smem, cudaStream_t st) {
+  void *k = select_kernel<T>(mode, a.S);
+  if (!k) return cudaErrorInvalidValue;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  void *args[] = {(void *)&a};
+  return cudaLaunchKernel(k, dim3(grid), dim3(block), args, smem, st);
+}
+
+template <typename T>
+int pass_max_blocks(int mode, int S, int block, size_t smem) {
+  void *k = select_kernel<T>(mode, S);
+  if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, block, smem) != cudaSuccess) return 1;
+  return nb > 0 ? nb : 1;
+}
+
+template cudaError_t launch_pass<double>(int, const PassArgs<double> &, int, int, size_t, cudaStream_t);
+template cudaError_t launch_pass<float>(int, const PassArgs<float> &, int, int, size_t, cudaStream_t);
+template int pass_max_blocks<double>(int, int, int, size_t);
+template int pass_max_blocks<float>(int, int, int, size_t);
+
+// ---------------------------------------------------------------- control
+__global__ void cheby_begin_kernel(ChebyState *cs, int order) {
+  cs->norm0 = 0; cs->norm_last = 0; cs->done = 0; cs->terms = order; cs->status = 0;
+}
+
+// Sums the per-block norms in a fixed order and applies the reference's
+// series cut (OCheby.cpp:178-182 real time, 285-289 imaginary time).
+__global__ void cheby_finalize_kernel(ChebyState *cs, const double *partials, int nparts, int first, int term,
+                                      int order, double prec, int imag, int offim0) {
+  __shared__ double red[32];
+  if (cs->done) return;
+  double v = 0;
+  for (int i = threadIdx.x; i < nparts; i += blockDim.x) v += partials[i];
+  const double tot = block_sum(v, red);
+  if (threadIdx.x != 0) return;
+  if (!isfinite(tot)) { cs->status = 2; cs->done = 1; cs->terms = first ? 2 : term + 1; return; }
+  if (first) { cs->norm0 = tot; return; }
+  if (!imag) {
+    const double nconv = fabs(cs->norm0 - tot) / cs->norm0;
+    if (nconv < prec && offim0) { cs->done = 1; cs->terms = term + 1; }
+  } else {
+    if (fabs(tot - cs->norm_last) / cs->norm_last < prec) { cs->done = 1; cs->terms = term + 1; }
+    cs->norm_last = tot;
+  }
+}
+
+cudaError_t launch_cheby_begin(ChebyState *cs, int order, cudaStream_t st) {
+  cheby_begin_kernel<<<1, 1, 0, st>>>(cs, order);
+  return cudaGetLastError();
+}
+
+__global__ void cheby_end_kernel(ChebyState *cs) { cs->total += cs->terms; }
+
+cudaError_t launch_cheby_end(ChebyState *cs, cudaStream_t st) {
+  cheby_end_kernel<<<1, 1, 0, st>>>(cs);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cheby_finalize(ChebyState *cs, const double *partials, int nparts, int first, int term,
+                                  int order, double prec, int imag, int offim0, cudaStream_t st) {
+  cheby_finalize_kernel<<<1, 256, 0, st>>>(cs, partials, nparts, first, term, order, prec, imag, offim0);
+  return cudaGetLastError();
+}
+
+__global__ void set_coefs_kernel(double *coef, const Couplings *cp, const double *lasers, int nt, long long step) {
+  for (int e = threadIdx.x; e < cp->ne; e += blockDim.x) {
+    const int l = cp->lid[e];
+    double v = 1.0;
+    if (l >= 0) v = (step >= 0 && step < nt) ? -lasers[(long long)l * nt + step] : 0.0;
+    coef[e] = v;
+  }
+}
+
+cudaError_t launch_set_coefs(double *coef, const Couplings *cp, const double *lasers, int laser_nt, long long step,
+                             cudaStream_t st) {
+  set_coefs_kernel<<<1, 64, 0, st>>>(coef, cp, lasers, laser_nt, step);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ elementwise
+template <typename T>
+__global__ void convert_kernel(cplx<T> *dst, const cplx<double> *src, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    st(dst + i, ccast<T>(ld(src + i)));
+}
+template <typename T>
+__global__ void widen_kernel(cplx<double> *dst, const cplx<T> *src, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    st(dst + i, ccast<double>(ld(src + i)));
+}
+
+static int ew_grid(long long n) {
+  long long g = (n + 255) / 256;
+  return (int)(g > 4096 ? 4096 : (g < 1 ? 1 : g));
+}
+
+template <typename T>
+cudaError_t launch_convert(cplx<T> *dst, const cplx<double> *src, long long n, cudaStream_t st) {
+  convert_kernel<T><<<ew_grid(n), 256, 0, st>>>(dst, src, n);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch_widen(cplx<double> *dst, const cplx<T> *src, long long n, cudaStream_t st) {
+  widen_kernel<T><<<ew_grid(n), 256, 0, st>>>(dst, src, n);
+  return cudaGetLastError();
+}
+template cudaError_t launch_convert<double>(cplx<double> *, const cplx<double> *, long long, cudaStream_t);
+template cudaError_t launch_convert<float>(cplx<float> *, const cplx<double> *, long long, cudaStream_t);
+template cudaError_t launch_widen<double>(cplx<double> *, const cplx<double> *, long long, cudaStream_t);
+template cudaError_t launch_widen<float>(cplx<double> *, const cplx<float> *, long long, cudaStream_t);
+
+template <typename T>
+__global__ void lincomb_kernel(cplx<T> *y, const cplx<T> *x, cplx<double> a, cplx<double> b, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    cplx<double> yv = ccast<double>(ld(y + i));
+    cplx<double> r = dmul(yv, a);
+    if (x) r = r + dmul(ccast<double>(ld(x + i)), b);
+    st(y + i, ccast<T>(r));
+  }
+}
+template <typename T>
+cudaError_t launch_lincomb(cplx<T> *y, const cplx<T> *x, cplx<double> a, cplx<double> b, long long n,
+                           cudaStream_t st) {
+  lincomb_kernel<T><<<ew_grid(n), 256, 0, st>>>(y, x, a, b, n);
+  return cudaGetLastError();
+}
+template cudaError_t launch_lincomb<double>(cplx<double> *, const cplx<double> *, cplx<double>, cplx<double>,
+                                            long long, cudaStream_t);
+template cudaError_t launch_lincomb<float>(cplx<float> *, const cplx<float> *, cplx<double>, cplx<double>,
+                                           long long, cudaStream_t);
+
+// Per-state sum conj(a) b, FP64 accumulation, fixed reduction order.
+template <typename T, typename U>
+__global__ void dots_kernel(const cplx<T> *a, const cplx<U> *b, int S, long long npts, double *partials) {
+  __shared__ double red[32];
+  for (int s = 0; s < S; ++s) {
+    double re = 0, im = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npts;
+         i += (long long)gridDim.x * blockDim.x) {
+      const cplx<double> x = ccast<double>(ld(a + s * npts + i));
+      const cplx<double> y = ccast<double>(ld(b + s * npts + i));
+      re += x.re * y.re + x.im * y.im;
+      im += x.re * y.im - x.im * y.re;
+    }
+    const double tr = block_sum(re, red);
+    const double ti = block_sum(im, red);
+    if (threadIdx.x == 0) {
+      partials[((long long)blockIdx.x * S + s) * 2 + 0] = tr;
+      partials[((long long)blockIdx.x * S + s) * 2 + 1] = ti;
+    }
+  }
+}
+template <typename T, typename U>
+cudaError_t launch_dots(const cplx<T> *a, const cplx<U> *b, int S, long long npts, double *partials, int grid,
+                        cudaStream_t st) {
+  dots_kernel<T, U><<<grid, 256, 0, st>>>(a, b, S, npts, partials);
+  return cudaGetLastError();
+}
+template cudaError_t launch_dots<double, double>(const cplx<double> *, const cplx<double> *, int, long long, double *,
+                                                 int, cudaStream_t);
+template cudaError_t launch_dots<float, float>(const cplx<float> *, const cplx<float> *, int, long long, double *,
+                                               int, cudaStream_t);
+template cudaError_t launch_dots<double, float>(const cplx<double> *, const cplx<float> *, int, long long, double *,
+                                                int, cudaStream_t);
+template cudaError_t launch_dots<float, double>(const cplx<float> *, const cplx<double> *, int, long long, double *,
+                                                int, cudaStream_t);
+
+// ------------------------------------------------------------------ GSPO
+__device__ __forceinline__ cplx<double> cexpd(cplx<double> z) {
+  double s, c;
+  sincos(z.im, &s, &c);
+  const double e = exp(z.re);
+  return mk(e * c, e * s);
+}
+
+// exp(c M) psi at one point for a real symmetric 1x1 / 2x2 matrix M.
+// 2x2: exp(cM) = e^{c m} [cosh(c r) I + sinh(c r)/r (M - m I)], m = (a+d)/2,
+// r = sqrt(((a-d)/2)^2 + b^2) -- the spectral form of the per-point
+// eigenbasis transform of TransformMSD (TransformMSD.cpp:47-62,84-98).
+template <typename T>
+__global__ void gspo_potential_kernel(cplx<T> *psi, int S, long long npts, const Couplings *cp, const double *coef,
+                                      const T *grids, cplx<double> c) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npts; p += (long long)gridDim.x * blockDim.x) {
+    double m[kMaxStates * kMaxStates];
+    for (int i = 0; i < S * S; ++i) m[i] = 0;
+    for (int e = 0; e < cp->ne; ++e) m[cp->row[e] * S + cp->col[e]] += coef[e] * (double)grids[(long long)cp->gid[e] * npts + p];
+    if (S == 2 && (m[1] != 0.0 || m[2] != 0.0)) {
+      const double a = m[0], d = m[3], b = m[1];
+      const double mm = 0.5 * (a + d), h = 0.5 * (a - d);
+      const double r = sqrt(h * h + b * b);
+      const cplx<double> em = cexpd(mk(c.re * mm, c.im * mm));
+      const cplx<double> z = mk(c.re * r, c.im * r);
+      const cplx<double> ep = cexpd(z), en = cexpd(mk(-z.re, -z.im));
+      const cplx<double> ch = mk(0.5 * (ep.re + en.re), 0.5 * (ep.im + en.im));
+      cplx<double> shr;  // sinh(z)/r
+      if (r * sqrt(c.re * c.re + c.im * c.im) < 1e-4) {
+        const cplx<double> z2 = dmul(z, z);
+        shr = dmul(c, mk(1.0 + z2.re / 6.0, z2.im / 6.0));
+      } else {
+        shr = mk(0.5 * (ep.re - en.re) / r, 0.5 * (ep.im - en.im) / r);
+      }
+      const cplx<double> x0 = ccast<double>(ld(psi + p));
+      const cplx<double> x1 = ccast<double>(ld(psi + npts + p));
+      // (M - m I) = [[h, b], [b, -h]]
+      const cplx<double> y0 = dmul(ch, x0) + dmul(shr, mk(h * x0.re + b * x1.re, h * x0.im + b * x1.im));
+      const cplx<double> y1 = dmul(ch, x1) + dmul(shr, mk(b * x0.re - h * x1.re, b * x0.im - h * x1.im));
+      st(psi + p, ccast<T>(dmul(em, y0)));
+      st(psi + npts + p, ccast<T>(dmul(em, y1)));
+    } else {
+      for (int s = 0; s < S; ++s) {
+        const double v = m[s * S + s];
+        const cplx<double> f = cexpd(mk(c.re * v, c.im * v));
+        st(psi + s * npts + p, ccast<T>(dmul(f, ccast<double>(ld(psi + s * npts + p)))));
+      }
+    }
+  }
+}
+
+template <typename T>
+cudaError_t launch_gspo_potential(cplx<T> *psi, int S, long long npts, const Couplings *cp, const double *coef,
+                                  const T *grids, cplx<double> c, cudaStream_t st) {
+  gspo_potential_kernel<T><<<ew_grid(npts), 256, 0, st>>>(psi, S, npts, cp, coef, grids, c);
+  return cudaGetLastError();
+}
+template cudaError_t launch_gspo_potential<double>(cplx<double> *, int, long long, const Couplings *, const double *,
+                                                   const double *, cplx<double>, cudaStream_t);
+template cudaError_t launch_gspo_potential<float>(cplx<float> *, int, long long, const Couplings *, const double *,
+                                                  const float *, cplx<double>, cudaStream_t);
+
+}  // namespace qdg

@@ -1,0 +1,124 @@
+// qdg_kernels.cuh -- kernel argument blocks and launch entry points shared by
+// the kernel translation units and the host API.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "qdg_device.cuh"
+
+namespace qdg {
+
+// Epilogue of a line pass.
+enum PassMode {
+  PM_KIN_FIRST = 0,   // P  = T_d phi                   (first of several kinetic passes)
+  PM_KIN_ACC = 1,     // P += T_d phi                   (middle passes)
+  PM_HAPPLY = 2,      // out = P + T_d phi + W phi       (last pass: H phi)
+  PM_CHEBY_FIRST = 3, // last pass of H psi + first Chebyshev terms (OCheby.cpp:99-111)
+  PM_CHEBY_TERM = 4,  // last pass of H phi_{n-1} + recurrence + accumulation (OCheby.cpp:120-175)
+  PM_GSPO_KIN = 5     // phi <- IFFT_d exp(c T_d) FFT_d phi / N_d in place (OGSPO kinetic member)
+};
+
+static const int kMaxStates = 8;      // states handled by the fused kernels
+static const int kMaxCouplings = 64;  // potential / dipole matrix entries
+
+// Potential-matrix entries of H: H_{row,col} += coef_e * grid[gid][x] with
+// coef_e = 1 (OGridPotential) or -E_lid(step) (OGridDipole, field lid).
+// Hermitian mirrors are listed explicitly.
+struct Couplings {
+  int ne;
+  int row[kMaxCouplings];
+  int col[kMaxCouplings];
+  int gid[kMaxCouplings];
+  int lid[kMaxCouplings];  // -1: static potential
+};
+
+template <typename T>
+struct PassArgs {
+  // geometry of the lines of this pass
+  int N;            // line length
+  int es;           // element stride along a line
+  int ls;           // stride between the TW lines of a tile
+  int TW;           // lines per tile (per state)
+  int tiles_per_hi; // tiles inside one block of stride_d * N_d points
+  long long hi_stride;  // stride_d * N_d
+  long long ntiles;
+  int S;            // states of the wave function
+  int nsub;         // states per work item (1, or S when the epilogue couples states)
+  long long npts;   // points per state
+  RadixPlan rp;
+  const cplx<T> *tw;   // N twiddles exp(-2 pi i m/N)
+  const double *kfac;  // [S] kinetic multiplier for this dim: dk^2/(2m) (times 1/N for H passes)
+  // buffers (state stride npts)
+  const cplx<T> *phi;  // input
+  cplx<T> *P;          // kinetic partial sums of earlier passes
+  cplx<T> *out;        // PM_HAPPLY output, PM_GSPO_KIN in-place target
+  cplx<double> *psi;   // Chebyshev accumulator (always FP64)
+  cplx<T> *k0;         // phi_{n-2} in, phi_n out (PM_CHEBY_TERM); phi_1 out (PM_CHEBY_FIRST)
+  // potential matrix
+  const Couplings *cp;     // device copy
+  const double *coef;      // [ne] coefficient of each entry at this step
+  const T *grids;          // [ngrids][npts]
+  int multi_pass;          // P holds kinetic parts of earlier passes
+  // Chebyshev scalars (FP64)
+  cplx<double> offset;     // energy offset (OCheby::_offset)
+  cplx<double> fac;        // _exp/_scaling (first) or 2*_exp/_scaling (terms)
+  cplx<double> c0p, c1p;   // coeff[0], coeff[1] times exp(c0*offset)
+  cplx<double> coeff;      // coeff[i] times exp(c0*offset)
+  int imag;                // imaginary-time recursion (minus sign, OCheby.cpp:276)
+  double *partials;        // per-block partial sums (norms)
+  const int *done;         // Chebyshev series converged: skip the work
+  // GSPO kinetic member: per-state exp(c T_d(k)) / N_d tables, S x N entries
+  const cplx<T> *gtab;
+};
+
+// Per-step Chebyshev control block in device memory.
+struct ChebyState {
+  long long total;   // terms summed over all steps since the propagator was set up
+  double norm0;      // raw norm of psi before the step
+  double norm_last;  // imaginary time: previous accumulated norm
+  int done;          // series converged (or error): later terms are skipped
+  int terms;         // terms used in the step
+  int status;        // QDG_OK or QDG_ENONFINITE
+  int pad;
+};
+
+// coef[e] for clock step `step` (Laser::Get, src/qdlib/Laser.cpp:125-128).
+cudaError_t launch_set_coefs(double *coef, const Couplings *cp, const double *lasers, int laser_nt, long long step,
+                             cudaStream_t st);
+
+// launchers (qdg_kernels.cu)
+template <typename T>
+cudaError_t launch_pass(int mode, const PassArgs<T> &a, int grid, int block, size_t smem, cudaStream_t st);
+template <typename T>
+int pass_max_blocks(int mode, int S, int block, size_t smem);
+
+cudaError_t launch_cheby_finalize(ChebyState *cs, const double *partials, int nparts, int first, int term,
+                                  int order, double prec, int imag, int offset_imag_zero, cudaStream_t st);
+cudaError_t launch_cheby_begin(ChebyState *cs, int order, cudaStream_t st);
+cudaError_t launch_cheby_end(ChebyState *cs, cudaStream_t st);
+
+// psi (FP64) -> phi (T) copy (OCheby: ket0->FastCopy(*Psi))
+template <typename T>
+cudaError_t launch_convert(cplx<T> *dst, const cplx<double> *src, long long n, cudaStream_t st);
+template <typename T>
+cudaError_t launch_widen(cplx<double> *dst, const cplx<T> *src, long long n, cudaStream_t st);
+
+// Per-state complex dot products sum conj(a)*b: partials[block][state] (re, im).
+template <typename T, typename U>
+cudaError_t launch_dots(const cplx<T> *a, const cplx<U> *b, int S, long long npts, double *partials, int grid,
+                        cudaStream_t st);
+
+// GSPO potential member: psi <- exp(c * M(x)) psi per grid point, where
+// M(x) = sum coef_e grid_e(x) over the member's entries (ODMultistate with
+// TransformMSD per-point diagonalisation, ODMultistate.cpp:115-182).
+template <typename T>
+cudaError_t launch_gspo_potential(cplx<T> *psi, int S, long long npts, const Couplings *cp, const double *coef,
+                                  const T *grids, cplx<double> c, cudaStream_t st);
+
+// y = a*y + b*x over n complex values (Krylov updates, normalisation).
+template <typename T>
+cudaError_t launch_lincomb(cplx<T> *y, const cplx<T> *x, cplx<double> a, cplx<double> b, long long n,
+                           cudaStream_t st);
+
+}  // namespace qdg

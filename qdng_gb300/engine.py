@@ -1,0 +1,153 @@
+"""Python front end of the engine's C ABI (used by tests, smoke and bench).
+
+Mirrors the QDng call pattern: a plan is the device image of the operator
+tree (Init(WaveFunction*)), a Propagator mirrors OCheby / OGSPO / OSIL /
+OArnoldi (Init, Apply) and observables mirror Reporter::Analyze.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from ._lib import QDGError, check, load
+
+PRECISIONS = {"fp64": abi.PREC_FP64, "mixed": abi.PREC_MIXED}
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Plan:
+    def __init__(self, hplan, precision="fp64"):
+        self.lib = load()
+        self.hplan = hplan
+        self.S = hplan.nstates
+        self.npts = hplan.npts
+        self.precision = precision
+        h = C.c_void_p()
+        check(self.lib.qdg_plan_create(C.byref(hplan.desc), PRECISIONS[precision], C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.qdg_plan_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def erange(self):
+        a, b = np.zeros(2), np.zeros(2)
+        check(self.lib.qdg_plan_erange(self.h, _dp(a), _dp(b)))
+        return complex(a[0], a[1]), complex(b[0], b[1])
+
+    def synchronize(self):
+        check(self.lib.qdg_plan_synchronize(self.h))
+
+    def wavefunction(self, psi=None):
+        w = WaveFunction(self)
+        if psi is not None:
+            w.upload(psi)
+        return w
+
+    def h_apply(self, win, wout, step=0):
+        check(self.lib.qdg_h_apply(self.h, win.h, wout.h, step))
+
+    def observables(self, psi, psi0=None, step=0):
+        o = abi.Observables()
+        check(self.lib.qdg_observables_compute(self.h, psi.h, psi0.h if psi0 is not None else None, step,
+                                               C.byref(o)))
+        return dict(norm2=o.norm2, pops=np.array(o.pops[:self.S]), energy=o.energy,
+                    autocorr=complex(o.autocorr_re, o.autocorr_im))
+
+
+class WaveFunction:
+    def __init__(self, plan):
+        self.plan = plan
+        self.lib = plan.lib
+        h = C.c_void_p()
+        check(self.lib.qdg_wf_create(plan.h, C.byref(h)))
+        self.h = h
+        self.size = plan.S * plan.npts
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.qdg_wf_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def upload(self, psi):
+        a = np.ascontiguousarray(psi, dtype=np.complex128).reshape(-1)
+        assert a.size == self.size
+        check(self.lib.qdg_wf_upload(self.h, _dp(a)))
+
+    def download(self):
+        out = np.empty(self.size, dtype=np.complex128)
+        check(self.lib.qdg_wf_download(self.h, _dp(out)))
+        return out
+
+    def copy_from(self, other):
+        check(self.lib.qdg_wf_copy(self.h, other.h))
+
+
+class Propagator:
+    """OCheby / OGSPO / OSIL / OArnoldi on the device."""
+
+    def __init__(self, plan, name, params="", dt=1.0, imaginary_time=False, backward=False):
+        self.plan = plan
+        self.lib = plan.lib
+        h = C.c_void_p()
+        check(self.lib.qdg_prop_create(plan.h, name.encode(), params.encode(), dt, int(imaginary_time),
+                                       int(backward), C.byref(h)))
+        self.h = h
+        check(self.lib.qdg_prop_init(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.qdg_prop_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def info(self):
+        i = abi.PropInfo()
+        check(self.lib.qdg_prop_get_info(self.h, C.byref(i)))
+        return dict(kind=i.kind, order=i.order, scaling=i.scaling, offset=complex(i.offset_re, i.offset_im),
+                    exponent=complex(i.exponent_re, i.exponent_im))
+
+    def coeffs(self):
+        n = self.info()["order"]
+        out = np.zeros(max(1, n))
+        check(self.lib.qdg_prop_get_coeffs(self.h, _dp(out), n))
+        return out[:n]
+
+    def apply(self, wf, step):
+        used = C.c_int32(0)
+        check(self.lib.qdg_prop_apply(self.h, wf.h, step, C.byref(used)))
+        return used.value
+
+    def apply_host(self, scratch, psi, step):
+        """The drop-in call: psi is a host complex128 array updated in place."""
+        assert psi.dtype == np.complex128 and psi.flags.c_contiguous
+        used = C.c_int32(0)
+        check(self.lib.qdg_prop_apply_host(self.h, scratch.h, _dp(psi), step, C.byref(used)))
+        return used.value
+
+    def run(self, wf, step0, nsteps):
+        tot = C.c_int64(0)
+        check(self.lib.qdg_prop_run(self.h, wf.h, step0, nsteps, C.byref(tot)))
+        return tot.value
+
+    def propagate(self, wf, psi0_wf, nsteps, start=0):
+        """ProgPropa loop with the Reporter on the device: report then step."""
+        rows, terms = [], []
+        for i in range(nsteps):
+            step = start + i
+            o = self.plan.observables(wf, psi0_wf, step)
+            rows.append([o["norm2"], *o["pops"], o["energy"], o["autocorr"].real, o["autocorr"].imag])
+            terms.append(self.apply(wf, step))
+        return np.array(rows), np.array(terms)
+
+
+__all__ = ["Plan", "WaveFunction", "Propagator", "QDGError"]

@@ -1,0 +1,245 @@
+"""GPU parity: the engine (through the C ABI) against the CPU oracle.
+
+Tolerances: the FP64 path must match the oracle to 1e-12 relative on norm
+and autocorrelation (the engine's contract); H*psi itself agrees to ~1e-13.
+The mixed path (FP32 bulk) is held to 1e-6 relative on autocorrelation and
+populations over short runs.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from qdng_gb300 import operators as op
+from tests import cases
+
+pytestmark = pytest.mark.gpu
+
+RTOL_FP64 = 1e-12
+
+
+@pytest.fixture(scope="module")
+def eng():
+    from qdng_gb300 import build, engine
+    build.build()
+    return engine
+
+
+def rel(a, b):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def small_2d_two_state(nx=32, ny=24):
+    g = op.GridSystem([nx, ny], [-4.0, -3.0], [4.0, 3.5])
+    X, Y = g.mesh()
+    V1 = 0.5 * 0.02 * (X ** 2 + Y ** 2)
+    V2 = 0.5 * 0.02 * ((X - 1) ** 2 + Y ** 2) + 0.05
+    V12 = 0.01 * np.exp(-(X - 0.5) ** 2 - Y ** 2)
+    T = op.GridNablaSq([1836.0, 3672.0])
+    hp = op.HPlan(g, op.Multistate({(0, 0): op.Sum([T, op.GridPotential(V1)]),
+                                    (1, 1): op.Sum([T, op.GridPotential(V2)]),
+                                    (0, 1): op.GridPotential(V12)}))
+    rng = np.random.default_rng(5)
+    psi = (rng.normal(size=hp.size) + 1j * rng.normal(size=hp.size))
+    psi /= np.sqrt((np.abs(psi) ** 2).sum() * np.prod(g.dx))
+    return hp, psi
+
+
+def small_3d(shape=(16, 8, 12)):
+    g = op.GridSystem(list(shape), [-6.0] * 3, [6.0] * 3)
+    Q = g.mesh()
+    V = 0.005 * Q[0] ** 2 + 0.0075 * Q[1] ** 2 + 0.01 * Q[2] ** 2 + 0.001 * Q[0] * Q[1] * Q[2]
+    hp = op.HPlan(g, op.Sum([op.GridNablaSq([1836.0, 900.0, 2000.0]), op.GridPotential(V)]))
+    psi = np.exp(-sum((Q[i] - 0.3) ** 2 for i in range(3))).reshape(-1).astype(np.complex128)
+    psi /= np.sqrt((np.abs(psi) ** 2).sum() * np.prod(g.dx))
+    return hp, psi
+
+
+H_CASES = ["tgp", "tgplms", "2d2s", "3d", "odd"]
+
+
+def build_h_case(name, fixtures):
+    if name == "tgp":
+        hp, psi, _ = cases.tgp_expec(fixtures)
+    elif name == "tgplms":
+        hp, psi, _ = cases.tgplms(fixtures)
+        psi = psi + 0.3j * np.roll(psi, 7)
+    elif name == "2d2s":
+        hp, psi = small_2d_two_state()
+    elif name == "3d":
+        hp, psi = small_3d()
+    else:  # 3^a 5^b line lengths
+        g = op.GridSystem([45, 12], [0.0, 0.0], [3.0, 2.0])
+        X, Y = g.mesh()
+        hp = op.HPlan(g, op.Sum([op.GridNablaSq([3.0, 5.0]), op.GridPotential(0.3 * X ** 2 + Y)]))
+        rng = np.random.default_rng(9)
+        psi = rng.normal(size=hp.size) + 1j * rng.normal(size=hp.size)
+    return hp, psi
+
+
+@pytest.mark.parametrize("name", H_CASES)
+def test_h_apply_fp64(eng, fixtures, name):
+    hp, psi = build_h_case(name, fixtures)
+    ref = O.System(hp).h_apply(psi, step=3)
+    plan = eng.Plan(hp, "fp64")
+    a, b = plan.wavefunction(psi), plan.wavefunction()
+    plan.h_apply(a, b, step=3)
+    assert rel(b.download(), ref) < 1e-13
+
+
+@pytest.mark.parametrize("name", H_CASES)
+def test_h_apply_mixed(eng, fixtures, name):
+    hp, psi = build_h_case(name, fixtures)
+    ref = O.System(hp).h_apply(psi, step=3)
+    plan = eng.Plan(hp, "mixed")
+    a, b = plan.wavefunction(psi), plan.wavefunction()
+    plan.h_apply(a, b, step=3)
+    assert rel(b.download(), ref) < 2e-5
+
+
+def test_erange_and_coeffs(eng, fixtures):
+    for hp, _, run in [cases.tgp_expec(fixtures), cases.tgpms(fixtures), cases.tgplms(fixtures),
+                       cases.cfg2_two_state(n=64)]:
+        S = O.System(hp)
+        plan = eng.Plan(hp, "fp64")
+        e1, e2 = plan.erange()
+        o1, o2 = S.erange()
+        assert abs(e1 - o1) <= 1e-13 * abs(o1) and abs(e2 - o2) <= 1e-13 * max(abs(o1), 1e-300)
+        P = eng.Propagator(plan, "Cheby", run["params"], dt=run["dt"])
+        Q = O.Propagator(S, "Cheby", run["params"], dt=run["dt"])
+        assert P.info()["order"] == Q.info()["order"]
+        assert abs(P.info()["scaling"] - Q.info()["scaling"]) <= 1e-14 * Q.info()["scaling"]
+        assert np.abs(P.coeffs() - Q.coeffs()).max() < 1e-14
+
+
+def _run_both(eng, hp, psi, run, nsteps, precision="fp64", imag=False, backward=False):
+    S = O.System(hp)
+    Q = O.Propagator(S, run["name"], run["params"], dt=run["dt"], imaginary_time=imag, backward=backward)
+    x = psi.copy()
+    obs_o, terms_o = Q.propagate(x, psi.copy(), nsteps)
+    plan = eng.Plan(hp, precision)
+    P = eng.Propagator(plan, run["name"], run["params"], dt=run["dt"], imaginary_time=imag, backward=backward)
+    w, w0 = plan.wavefunction(psi), plan.wavefunction(psi)
+    obs_g, terms_g = P.propagate(w, w0, nsteps)
+    return obs_o, terms_o, x, obs_g, terms_g, w.download()
+
+
+def _assert_parity(hp, obs_o, terms_o, x, obs_g, terms_g, xg, rtol=RTOL_FP64, check_terms=True):
+    S = hp.nstates
+    if check_terms:
+        assert list(terms_o) == list(terms_g)
+    # norm and autocorrelation, relative to their magnitude
+    assert np.abs(obs_g[:, 0] - obs_o[:, 0]).max() <= rtol * np.abs(obs_o[:, 0]).max()
+    ac_o = obs_o[:, 2 + S] + 1j * obs_o[:, 3 + S]
+    ac_g = obs_g[:, 2 + S] + 1j * obs_g[:, 3 + S]
+    assert np.abs(ac_g - ac_o).max() <= rtol * max(np.abs(ac_o).max(), 1e-300)
+    assert rel(xg, x) <= 100 * rtol
+
+
+def test_cheby_tgp_expec_parity(eng, fixtures):
+    hp, psi, run = cases.tgp_expec(fixtures)
+    _assert_parity(hp, *_run_both(eng, hp, psi, run, 40))
+
+
+def test_cheby_multistate_laser_parity(eng, fixtures):
+    hp, psi, run = cases.tgplms(fixtures)
+    _assert_parity(hp, *_run_both(eng, hp, psi, run, 60))
+
+
+def test_cheby_2d_two_state_parity(eng):
+    hp, psi, run = cases.cfg2_two_state(n=64)
+    _assert_parity(hp, *_run_both(eng, hp, psi, run, 10))
+
+
+def test_cheby_cfg2_full_grid_parity(eng):
+    """256^2 two-state grid of the benchmark, a few steps."""
+    hp, psi, run = cases.cfg2_two_state(n=256)
+    _assert_parity(hp, *_run_both(eng, hp, psi, run, 3))
+
+
+def test_cheby_3d_parity(eng):
+    hp, psi = small_3d()
+    run = dict(name="Cheby", params="", dt=10.0)
+    _assert_parity(hp, *_run_both(eng, hp, psi, run, 8))
+
+
+def test_cheby_imag_parity(eng, fixtures):
+    hp, psi, run = cases.tge(fixtures, "Cheby")
+    _assert_parity(hp, *_run_both(eng, hp, psi, run, 20, imag=True, backward=True), rtol=1e-11)
+
+
+def test_gspo_parity(eng, fixtures):
+    hp, psi, run = cases.tgpms(fixtures, gspo=True)
+    _assert_parity(hp, *_run_both(eng, hp, psi, run, 50), check_terms=False)
+    hp, psi, run = cases.tgpl_ir_pulse(fixtures, gspo=True)
+    _assert_parity(hp, *_run_both(eng, hp, psi, run, 50), check_terms=False)
+
+
+def test_gspo_coupled_2d_parity(eng):
+    hp, psi, run = cases.cfg2_two_state(n=64, gspo=True)
+    _assert_parity(hp, *_run_both(eng, hp, psi, run, 20), check_terms=False)
+
+
+def test_sil_parity(eng, fixtures):
+    hp, psi, run = cases.tgplms(fixtures, sil=True)
+    _assert_parity(hp, *_run_both(eng, hp, psi, run, 30))
+
+
+def test_arnoldi_parity(eng, fixtures):
+    hp, psi, run = cases.tgplms(fixtures)
+    run = dict(run, name="Arnoldi", params="order=16")
+    _assert_parity(hp, *_run_both(eng, hp, psi, run, 30), rtol=1e-11)
+
+
+def test_tgp_expec_golden_on_gpu(eng, fixtures, golden):
+    """The whole TGP-Expec run on the device reproduces QDng's printed line."""
+    hp, psi, run = cases.tgp_expec(fixtures)
+    plan = eng.Plan(hp, "fp64")
+    P = eng.Propagator(plan, run["name"], run["params"], dt=run["dt"])
+    w, w0 = plan.wavefunction(psi), plan.wavefunction(psi)
+    P.run(w, 0, 999)
+    o = plan.observables(w, w0, 999)
+    vals = golden["propagation"]["TGP-Expec"]["values"]
+    assert abs(o["norm2"] - vals[2]) <= 0.5e-6
+    assert abs(o["energy"] - vals[3]) <= 0.5e-8 + 1e-12
+    assert abs(o["autocorr"].real - vals[4][0]) <= 0.5e-8 + 1e-12
+    assert abs(o["autocorr"].imag - vals[4][1]) <= 0.5e-8 + 1e-12
+
+
+def test_mixed_cheby_error(eng):
+    hp, psi, run = cases.cfg2_two_state(n=64)
+    obs_o, _, x, obs_g, _, xg = _run_both(eng, hp, psi, run, 10, precision="mixed")
+    S = hp.nstates
+    ac_o = obs_o[:, 2 + S] + 1j * obs_o[:, 3 + S]
+    ac_g = obs_g[:, 2 + S] + 1j * obs_g[:, 3 + S]
+    assert np.abs(ac_g - ac_o).max() <= 1e-6 * np.abs(ac_o).max()
+    assert np.abs(obs_g[:, 1:1 + S] - obs_o[:, 1:1 + S]).max() <= 1e-6
+
+
+def test_nonfinite_norm_reports_enonfinite(eng, fixtures):
+    from qdng_gb300 import abi
+    hp, psi, run = cases.tgp_expec(fixtures)
+    plan = eng.Plan(hp, "fp64")
+    P = eng.Propagator(plan, run["name"], run["params"], dt=run["dt"])
+    bad = psi.copy()
+    bad[5] = np.nan
+    w = plan.wavefunction(bad)
+    with pytest.raises(eng.QDGError) as e:
+        P.apply(w, 0)
+    assert e.value.status == abi.QDG_ENONFINITE
+
+
+def test_apply_host_matches_device(eng, fixtures):
+    hp, psi, run = cases.tgplms(fixtures)
+    plan = eng.Plan(hp, "fp64")
+    P1 = eng.Propagator(plan, run["name"], run["params"], dt=run["dt"])
+    P2 = eng.Propagator(plan, run["name"], run["params"], dt=run["dt"])
+    w = plan.wavefunction(psi)
+    scratch = plan.wavefunction()
+    host = psi.copy()
+    for step in range(5):
+        t1 = P1.apply(w, step)
+        t2 = P2.apply_host(scratch, host, step)
+        assert t1 == t2
+    assert np.array_equal(w.download(), host)
