@@ -1,0 +1,355 @@
+"""Benchmark: QDng Chebyshev propagation of the 256x256 two-state grid.
+
+Workload (benchmark configs[1], Chebyshev part): 2-D two-state
+diabatic model, 256 x 256 grid on [-4,4]^2, masses (1836, 3672), harmonic
+surfaces with k = 0.02, Gaussian coupling V12 = 0.01 exp(-(x-0.5)^2 - y^2),
+displaced Gaussian start on state 1, dt = 5 a.u.  One "step" is one
+Chebyshev time step U(dt) psi (the series is cut by the reference's norm
+criterion).  Metric: grid-pt*steps/s = (states * grid points) * steps / s.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|mixed]
+    python bench.py --impl reference ...   # the reference algorithm on the host cores
+
+Timing: per step, L2 is flushed by writing a 512 MB buffer (outside the
+timed interval); each step is bracketed by CUDA events on the engine's
+stream.  `e2e` repeats the steps through the drop-in call with the wave
+function in pinned host memory (upload, step, download inside the timed
+region).  N > 1: independent replicas (the single-wavepacket path does not
+shard), timing = max over ranks, value = sum of the ranks' work / that time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# Algorithmic bytes per Chebyshev term (one launch of the fused term kernel):
+# N_pts * [S*5*c + (S + C + D)*r]; c/r = bytes per complex/real.
+def term_bytes(npts, S, C, D, precision):
+    if precision == "fp64":
+        return npts * (S * 5 * 16 + (S + C + D) * 8)
+    return npts * (S * 56 + (S + C + D) * 4)  # phi FP32 (3 x 8 B) + psi FP64 (2 x 16 B)
+
+
+def read_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    mx = float(f[2])
+                except ValueError:
+                    continue
+                for n, v in zip(names, f[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        except Exception:
+            pass
+        finally:
+            try:
+                os.unlink(self.path)
+            except Exception:
+                pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def workload(precision):
+    from tests import cases
+    hp, psi, run = cases.cfg2_two_state(n=256)
+    cfg = {"workload": "cfg2 two-state 2-D Chebyshev, 256x256 grid x 2 states, dt=5 a.u.",
+           "grid": [256, 256], "states": 2, "dt": 5.0, "precision": precision,
+           "l2": "flushed between timed steps (512 MB write)"}
+    return hp, psi, run, cfg
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        # one process per GPU; the engine uses the device made visible here
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+    return world, rank, local
+
+
+def reduce_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def cpu_reference(hp, psi, run, steps, warmup, budget_s=None):
+    """The reference algorithm (oracle port) on all host cores."""
+    from oracle import oracle as O
+    threads = O.threads(os.cpu_count() or 1)
+    S = O.System(hp)
+    P = O.Propagator(S, run["name"], run["params"], dt=run["dt"])
+    x = psi.copy()
+    for i in range(warmup):
+        P.apply(x, i)
+    t0 = time.perf_counter()
+    n = 0
+    while n < steps:
+        P.apply(x, warmup + n)
+        n += 1
+        if budget_s is not None and time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return hp.size * n / dt, threads, n, dt
+
+
+def engine_arm(args, world, rank, local):
+    import numpy as np
+    import torch
+
+    from qdng_gb300 import build, engine
+
+    build.build()
+    hp, psi, run, cfg = workload(args.precision)
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    plan = engine.Plan(hp, args.precision)
+    plan.set_stream(stream.cuda_stream)
+    prop = engine.Propagator(plan, run["name"], run["params"], dt=run["dt"])
+    w = plan.wavefunction(psi)
+    info = prop.info()
+
+    step = 0
+    for _ in range(args.warmup):
+        prop.run(w, step, 1)
+        step += 1
+
+    def timed_steps(k, profile=False):
+        nonlocal step
+        evs = []
+        terms = 0
+        if profile:
+            plan.profile(True)
+        for _ in range(k):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            terms += prop.run(w, step, 1)
+            b.record(stream)
+            evs.append((a, b))
+            step += 1
+        torch.cuda.synchronize()
+        ms = sum(a.elapsed_time(b) for a, b in evs)
+        prof = plan.profile_read() if profile else None
+        if profile:
+            plan.profile(False)
+        return ms, terms, prof
+
+    barrier(world)
+    torch.cuda.synchronize()
+    l0 = engine.kernel_launches()
+    with ClockSampler(local) as clk:
+        ms, terms, _ = timed_steps(args.steps)
+    launches = engine.kernel_launches() - l0
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = clk.summary()
+    ms_max = reduce_max(ms, world)
+    value = hp.size * args.steps * world / (ms_max / 1e3)
+
+    # dominant kernel: per-launch device time of every line pass, same workload
+    pms, _, (prof_ms, prof_n) = timed_steps(args.steps, profile=True)
+    modes = engine.PASS_MODES
+    top = int(np.argmax(prof_ms[:len(modes)]))
+    npts, S = hp.npts, hp.nstates
+    C = 1  # distinct off-diagonal coupling grids (V12)
+    D = 0
+    peak, peak_src = read_peak()
+    roof = None
+    if prof_n[top] > 0:
+        avg_s = prof_ms[top] / prof_n[top] / 1e3
+        if modes[top] == "cheby_term":
+            per_launch = term_bytes(npts, S, C, D, args.precision)
+            what = "one Chebyshev term: read phi_{n-1}, phi_{n-2}, psi, potentials; write phi_n, psi"
+        else:
+            per_launch = npts * S * 2 * (16 if args.precision == "fp64" else 8)
+            what = "kinetic line pass: read phi, write partial sums"
+        ach = per_launch / avg_s / 1e9
+        roof = {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(ach / peak, 4), "traffic": None, "kernel": f"linepass_kernel ({modes[top]})",
+                "algorithmic_bytes_per_launch": per_launch, "bytes_note": what,
+                "avg_launch_us": round(avg_s * 1e6, 2), "peak_source": peak_src + " (MEASURED_PEAKS.json hbm_gbs)"}
+    per_mode = {modes[i]: {"ms": round(float(prof_ms[i]), 3), "launches": int(prof_n[i])}
+                for i in range(len(modes)) if prof_n[i] > 0}
+    term_rate = None
+    if terms > 0:
+        term_s = (ms / 1e3) / terms
+        tb = term_bytes(npts, S, C, D, args.precision)
+        term_rate = {"terms_per_step": terms / args.steps, "us_per_term": round(term_s * 1e6, 2),
+                     "algorithmic_GBps_per_term": round(tb / term_s / 1e9, 1)}
+
+    # e2e through the drop-in call with host (pinned) buffers
+    host = torch.empty(hp.size * 2, dtype=torch.float64, pin_memory=True).numpy().view(np.complex128)
+    host[:] = psi
+    scratch = plan.wavefunction()
+    e2e_s = 0.0
+    for i in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        prop.apply_host(scratch, host, i)
+        e2e_s += time.perf_counter() - t0
+    e2e_s = reduce_max(e2e_s, world)
+    e2e_val = hp.size * args.steps * world / e2e_s
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        v, threads, n, dt = cpu_reference(hp, psi, run, steps=10 ** 6, warmup=1, budget_s=args.cpu_budget)
+        cpu = {"value": round(v, 1), "unit": "grid-pt*steps/s", "cores": threads, "kind": "port",
+               "sample": f"{n} Chebyshev steps of the same 256x256x2 workload in {dt:.1f} s "
+                         f"(oracle restatement of OCheby, OpenMP FFT lines)"}
+
+    line = {
+        "metric": "grid-pt*steps/s (Chebyshev, 256^2 x 2 states)",
+        "value": round(value, 1),
+        "unit": "grid-pt*steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms_max / args.steps, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+        "data": "synthetic (seeded analytic potentials and Gaussian start, BASELINE configs[1])",
+        "config": dict(cfg, parallelism="replicas" if world > 1 else "single",
+                       cheby_order=info["order"]),
+        "e2e": {"value": round(e2e_val, 1), "unit": "grid-pt*steps/s",
+                "h2d_bytes_per_step": hp.size * 16, "d2h_bytes_per_step": hp.size * 16},
+        "gpu_launches": int(launches),
+        "roofline": roof,
+        "per_term": term_rate,
+        "pass_profile": per_mode,
+        "clocks": clocks,
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def reference_arm(args, world, rank):
+    if rank != 0:
+        return
+    hp, psi, run, cfg = workload("fp64")
+    v, threads, n, dt = cpu_reference(hp, psi, run, steps=args.steps, warmup=args.warmup)
+    line = {
+        "metric": "grid-pt*steps/s (Chebyshev, 256^2 x 2 states)",
+        "value": round(v, 1),
+        "unit": "grid-pt*steps/s",
+        "n_gpus": world,
+        "steps": n,
+        "warmup": args.warmup,
+        "ms_per_step": round(dt / n * 1e3, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded analytic potentials and Gaussian start, BASELINE configs[1])",
+        "config": dict(cfg, l2="n/a (host)"),
+        "impl": "reference",
+        "cpu_baseline": {"value": round(v, 1), "unit": "grid-pt*steps/s", "cores": threads, "kind": "port",
+                         "sample": f"{n} Chebyshev steps of the 256x256x2 workload on {threads} host threads "
+                                   "(QDng is not buildable here: FFTW/LAPACK/SLATEC/protobuf missing; "
+                                   "the oracle restatement of OCheby stands in)"},
+        "e2e": {"value": round(v, 1), "unit": "grid-pt*steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        reference_arm(args, world, rank)
+    else:
+        engine_arm(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

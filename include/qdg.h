@@ -193,6 +193,17 @@ qdg_status qdg_prop_apply_host(qdg_prop *prop, qdg_wf *scratch, double *host_psi
 qdg_status qdg_prop_run(qdg_prop *prop, qdg_wf *psi, int64_t step0, int32_t nsteps,
                         int64_t *terms_total);
 
+/* ---- engine instrumentation (no counterpart in the reference) ---------- */
+
+/* Kernels this library has launched in the process so far. */
+int64_t qdg_kernel_launches(void);
+/* Time every line-pass launch of the plan with CUDA events on its stream. */
+qdg_status qdg_profile_enable(qdg_plan *plan, int32_t on);
+/* Per pass mode (0 kinetic first, 1 kinetic middle, 2 H apply, 3 Chebyshev
+ * first term, 4 Chebyshev term, 5 split-operator kinetic): summed device ms
+ * and launch counts since the last read; resets the counters. */
+qdg_status qdg_profile_read(qdg_plan *plan, double ms[8], int64_t launches[8]);
+
 #ifdef __cplusplus
 }
 #endif

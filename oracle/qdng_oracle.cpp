@@ -374,7 +374,8 @@ static void h_apply(const System &s, const cd *in, cd *out, long step) {
   std::vector<cd> buf(N);
   for (int i = 0; i < s.S; ++i) {
     cd *o = out + i * N;
-    std::fill(o, o + N, cd(0));
+    #pragma omp parallel for schedule(static) if (N >= 8192)
+    for (long p = 0; p < N; ++p) o[p] = 0;
     for (int j = 0; j < s.S; ++j) {
       const cd *x = in + j * N;
       int kt = 0;
@@ -382,20 +383,27 @@ static void h_apply(const System &s, const cd *in, cd *out, long step) {
         const qdg_hterm &t = s.terms[ti];
         bool kin = t.kind == QDG_TERM_KINETIC;
         if (term_at(t, i, j)) {
+          /* elementwise codelets are OpenMP loops in the reference (src/math/codelets) */
           if (kin) {
-            std::copy(x, x + N, buf.begin());
-            s.fft.exec(buf.data(), -1);
-            const std::vector<double> &tab = s.ktab[kt];
+            cd *b = buf.data();
+            #pragma omp parallel for schedule(static) if (N >= 8192)
+            for (long p = 0; p < N; ++p) b[p] = x[p];
+            s.fft.exec(b, -1);
+            const double *tab = s.ktab[kt].data();
             double d = 1.0 / double(N);
-            for (long p = 0; p < N; ++p) buf[p] = buf[p] * tab[p] * d;
-            s.fft.exec(buf.data(), +1);
-            for (long p = 0; p < N; ++p) o[p] += buf[p];
+            #pragma omp parallel for schedule(static) if (N >= 8192)
+            for (long p = 0; p < N; ++p) b[p] = b[p] * tab[p] * d;
+            s.fft.exec(b, +1);
+            #pragma omp parallel for schedule(static) if (N >= 8192)
+            for (long p = 0; p < N; ++p) o[p] += b[p];
           } else if (t.kind == QDG_TERM_POTENTIAL) {
             const double *v = s.grids[t.grid].data();
+            #pragma omp parallel for schedule(static) if (N >= 8192)
             for (long p = 0; p < N; ++p) o[p] += x[p] * v[p];
           } else {
             const double *v = s.grids[t.grid].data();
             double e = (-1) * laser_at(s, t.laser, step);
+            #pragma omp parallel for schedule(static) if (N >= 8192)
             for (long p = 0; p < N; ++p) o[p] += x[p] * v[p] * e;
           }
         }

@@ -92,6 +92,15 @@ struct qdg_plan {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   int sm_count = 1;
+  // Wave functions and propagators of this plan still alive.  A plan whose
+  // destroy call comes first is freed with its last child (callers such as
+  // QDng's Collector release objects in no fixed order).
+  int children = 0;
+  bool destroy_pending = false;
+  // optional per-launch timing of the line passes
+  bool profiling = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<int> ev_mode;   // mode of launch i (events 2i, 2i+1)
 };
 
 struct qdg_wf {
@@ -261,6 +270,19 @@ qdg_status launch_one(qdg_plan *p, int mode, int d, qdg::PassArgs<T> &a, int *nb
   if (grid > p->max_parts) grid = p->max_parts;
   if (grid < 1) grid = 1;
   if (nblocks_out) *nblocks_out = (int)grid;
+  if (p->profiling) {
+    const size_t i = p->ev_mode.size();
+    while (p->ev_pool.size() < 2 * (i + 1)) {
+      cudaEvent_t e;
+      CK(cudaEventCreate(&e));
+      p->ev_pool.push_back(e);
+    }
+    p->ev_mode.push_back(mode);
+    CK(cudaEventRecord(p->ev_pool[2 * i], p->stream));
+    CK(qdg::launch_pass<T>(mode, a, (int)grid, block, smem, p->stream));
+    CK(cudaEventRecord(p->ev_pool[2 * i + 1], p->stream));
+    return QDG_OK;
+  }
   CK(qdg::launch_pass<T>(mode, a, (int)grid, block, smem, p->stream));
   return QDG_OK;
 }
@@ -335,7 +357,15 @@ void free_plan(qdg_plan *p) {
   if (p->d_partials) cudaFree(p->d_partials);
   if (p->h_partials) cudaFreeHost(p->h_partials);
   if (p->own_stream && p->stream) cudaStreamDestroy(p->stream);
+  for (auto e : p->ev_pool) cudaEventDestroy(e);
   delete p;
+}
+
+void release_child(qdg_plan *p) {
+  if (--p->children == 0 && p->destroy_pending) {
+    cudaStreamSynchronize(p->stream);
+    free_plan(p);
+  }
 }
 
 // Couplings of the terms selected by `pick` (kinetic terms excluded).
@@ -892,6 +922,10 @@ qdg_status qdg_plan_create(const qdg_hplan_desc *desc, int32_t precision, qdg_pl
 qdg_status qdg_plan_destroy(qdg_plan *plan) {
   if (!plan) return QDG_OK;
   cudaStreamSynchronize(plan->stream);
+  if (plan->children > 0) {
+    plan->destroy_pending = true;
+    return QDG_OK;
+  }
   free_plan(plan);
   return QDG_OK;
 }
@@ -929,15 +963,18 @@ qdg_status qdg_wf_create(qdg_plan *plan, qdg_wf **out) {
     return fail(QDG_ENOMEM, "device allocation failed");
   }
   cudaMemsetAsync(w->d, 0, sizeof(cplx<double>) * wf_elems(plan), plan->stream);
+  plan->children++;
   *out = w;
   return QDG_OK;
 }
 
 qdg_status qdg_wf_destroy(qdg_wf *wf) {
   if (!wf) return QDG_OK;
-  cudaStreamSynchronize(wf->plan->stream);
+  qdg_plan *p = wf->plan;
+  cudaStreamSynchronize(p->stream);
   cudaFree(wf->d);
   delete wf;
+  release_child(p);
   return QDG_OK;
 }
 
@@ -1035,13 +1072,15 @@ qdg_status qdg_prop_create(qdg_plan *plan, const char *name, const char *params,
     if (has(P, "err")) P->err = parse_d(P, "err");
     if (has(P, "conv")) P->conv = parse_d(P, "conv");
   }
+  plan->children++;
   *out = P;
   return QDG_OK;
 }
 
 qdg_status qdg_prop_destroy(qdg_prop *P) {
   if (!P) return QDG_OK;
-  cudaStreamSynchronize(P->plan->stream);
+  qdg_plan *plan = P->plan;
+  cudaStreamSynchronize(plan->stream);
   if (P->k0) cudaFree(P->k0);
   if (P->k1) cudaFree(P->k1);
   if (P->d_cs) cudaFree(P->d_cs);
@@ -1053,6 +1092,7 @@ qdg_status qdg_prop_destroy(qdg_prop *P) {
   if (P->kbuf) cudaFree(P->kbuf);
   if (P->kwide) cudaFree(P->kwide);
   delete P;
+  release_child(plan);
   return QDG_OK;
 }
 
@@ -1138,6 +1178,30 @@ qdg_status qdg_prop_run(qdg_prop *P, qdg_wf *psi, int64_t step0, int32_t nsteps,
     tot = P->h_cs->total - before;
   }
   if (terms_total) *terms_total = tot;
+  return QDG_OK;
+}
+
+int64_t qdg_kernel_launches(void) { return qdg::launch_counter(); }
+
+qdg_status qdg_profile_enable(qdg_plan *plan, int32_t on) {
+  if (!plan) return fail(QDG_EINVAL, "null plan");
+  CK(cudaStreamSynchronize(plan->stream));
+  plan->profiling = on != 0;
+  plan->ev_mode.clear();
+  return QDG_OK;
+}
+
+qdg_status qdg_profile_read(qdg_plan *plan, double ms[8], int64_t launches[8]) {
+  if (!plan || !ms || !launches) return fail(QDG_EINVAL, "null argument");
+  for (int i = 0; i < 8; ++i) { ms[i] = 0; launches[i] = 0; }
+  CK(cudaStreamSynchronize(plan->stream));
+  for (size_t i = 0; i < plan->ev_mode.size(); ++i) {
+    float t = 0;
+    CK(cudaEventElapsedTime(&t, plan->ev_pool[2 * i], plan->ev_pool[2 * i + 1]));
+    const int m = plan->ev_mode[i];
+    if (m >= 0 && m < 8) { ms[m] += t; launches[m]++; }
+  }
+  plan->ev_mode.clear();
   return QDG_OK;
 }
 

@@ -14,9 +14,15 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <atomic>
+
 #include "qdg_kernels.cuh"
 
 namespace qdg {
+
+static std::atomic<long long> g_launches{0};
+long long launch_counter() { return g_launches.load(); }
+#define COUNT_LAUNCH() g_launches.fetch_add(1)
 
 __device__ __forceinline__ cplx<double> dmul(cplx<double> a, cplx<double> b) { return cmul(a, b); }
 
@@ -191,6 +197,7 @@ cudaError_t launch_pass(int mode, const PassArgs<T> &a, int grid, int block, siz
     if (e != cudaSuccess) return e;
   }
   void *args[] = {(void *)&a};
+  COUNT_LAUNCH();
   return cudaLaunchKernel(k, dim3(grid), dim3(block), args, smem, st);
 }
 
@@ -236,6 +243,7 @@ __global__ void cheby_finalize_kernel(ChebyState *cs, const double *partials, in
 
 cudaError_t launch_cheby_begin(ChebyState *cs, int order, cudaStream_t st) {
   cheby_begin_kernel<<<1, 1, 0, st>>>(cs, order);
+  COUNT_LAUNCH();
   return cudaGetLastError();
 }
 
@@ -243,12 +251,14 @@ __global__ void cheby_end_kernel(ChebyState *cs) { cs->total += cs->terms; }
 
 cudaError_t launch_cheby_end(ChebyState *cs, cudaStream_t st) {
   cheby_end_kernel<<<1, 1, 0, st>>>(cs);
+  COUNT_LAUNCH();
   return cudaGetLastError();
 }
 
 cudaError_t launch_cheby_finalize(ChebyState *cs, const double *partials, int nparts, int first, int term,
                                   int order, double prec, int imag, int offim0, cudaStream_t st) {
   cheby_finalize_kernel<<<1, 256, 0, st>>>(cs, partials, nparts, first, term, order, prec, imag, offim0);
+  COUNT_LAUNCH();
   return cudaGetLastError();
 }
 
@@ -264,6 +274,7 @@ __global__ void set_coefs_kernel(double *coef, const Couplings *cp, const double
 cudaError_t launch_set_coefs(double *coef, const Couplings *cp, const double *lasers, int laser_nt, long long step,
                              cudaStream_t st) {
   set_coefs_kernel<<<1, 64, 0, st>>>(coef, cp, lasers, laser_nt, step);
+  COUNT_LAUNCH();
   return cudaGetLastError();
 }
 
@@ -287,11 +298,13 @@ static int ew_grid(long long n) {
 template <typename T>
 cudaError_t launch_convert(cplx<T> *dst, const cplx<double> *src, long long n, cudaStream_t st) {
   convert_kernel<T><<<ew_grid(n), 256, 0, st>>>(dst, src, n);
+  COUNT_LAUNCH();
   return cudaGetLastError();
 }
 template <typename T>
 cudaError_t launch_widen(cplx<double> *dst, const cplx<T> *src, long long n, cudaStream_t st) {
   widen_kernel<T><<<ew_grid(n), 256, 0, st>>>(dst, src, n);
+  COUNT_LAUNCH();
   return cudaGetLastError();
 }
 template cudaError_t launch_convert<double>(cplx<double> *, const cplx<double> *, long long, cudaStream_t);
@@ -312,6 +325,7 @@ template <typename T>
 cudaError_t launch_lincomb(cplx<T> *y, const cplx<T> *x, cplx<double> a, cplx<double> b, long long n,
                            cudaStream_t st) {
   lincomb_kernel<T><<<ew_grid(n), 256, 0, st>>>(y, x, a, b, n);
+  COUNT_LAUNCH();
   return cudaGetLastError();
 }
 template cudaError_t launch_lincomb<double>(cplx<double> *, const cplx<double> *, cplx<double>, cplx<double>,
@@ -344,6 +358,7 @@ template <typename T, typename U>
 cudaError_t launch_dots(const cplx<T> *a, const cplx<U> *b, int S, long long npts, double *partials, int grid,
                         cudaStream_t st) {
   dots_kernel<T, U><<<grid, 256, 0, st>>>(a, b, S, npts, partials);
+  COUNT_LAUNCH();
   return cudaGetLastError();
 }
 template cudaError_t launch_dots<double, double>(const cplx<double> *, const cplx<double> *, int, long long, double *,
@@ -410,6 +425,7 @@ template <typename T>
 cudaError_t launch_gspo_potential(cplx<T> *psi, int S, long long npts, const Couplings *cp, const double *coef,
                                   const T *grids, cplx<double> c, cudaStream_t st) {
   gspo_potential_kernel<T><<<ew_grid(npts), 256, 0, st>>>(psi, S, npts, cp, coef, grids, c);
+  COUNT_LAUNCH();
   return cudaGetLastError();
 }
 template cudaError_t launch_gspo_potential<double>(cplx<double> *, int, long long, const Couplings *, const double *,

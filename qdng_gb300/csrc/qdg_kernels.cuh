@@ -87,6 +87,9 @@ struct ChebyState {
 cudaError_t launch_set_coefs(double *coef, const Couplings *cp, const double *lasers, int laser_nt, long long step,
                              cudaStream_t st);
 
+// Kernels launched by this library in the process (all launchers count).
+long long launch_counter();
+
 // launchers (qdg_kernels.cu)
 template <typename T>
 cudaError_t launch_pass(int mode, const PassArgs<T> &a, int grid, int block, size_t smem, cudaStream_t st);

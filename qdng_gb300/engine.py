@@ -4,6 +4,7 @@ Mirrors the QDng call pattern: a plan is the device image of the operator
 tree (Init(WaveFunction*)), a Propagator mirrors OCheby / OGSPO / OSIL /
 OArnoldi (Init, Apply) and observables mirror Reporter::Analyze.
 """
+import atexit
 import ctypes as C
 
 import numpy as np
@@ -12,6 +13,11 @@ from . import abi
 from ._lib import QDGError, check, load
 
 PRECISIONS = {"fp64": abi.PREC_FP64, "mixed": abi.PREC_MIXED}
+
+# At interpreter exit the CUDA runtime may already be torn down; handles are
+# then left to process teardown instead of being released one by one.
+_exiting = [False]
+atexit.register(lambda: _exiting.__setitem__(0, True))
 
 
 def _dp(a):
@@ -30,9 +36,9 @@ class Plan:
         self.h = h
 
     def close(self):
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and not _exiting[0]:
             self.lib.qdg_plan_destroy(self.h)
-            self.h = None
+        self.h = None
 
     __del__ = close
 
@@ -43,6 +49,18 @@ class Plan:
 
     def synchronize(self):
         check(self.lib.qdg_plan_synchronize(self.h))
+
+    def set_stream(self, cuda_stream_ptr):
+        check(self.lib.qdg_plan_set_stream(self.h, C.c_void_p(cuda_stream_ptr)))
+
+    def profile(self, on=True):
+        check(self.lib.qdg_profile_enable(self.h, int(on)))
+
+    def profile_read(self):
+        ms = np.zeros(8)
+        n = np.zeros(8, dtype=np.int64)
+        check(self.lib.qdg_profile_read(self.h, _dp(ms), n.ctypes.data_as(C.POINTER(C.c_int64))))
+        return ms, n
 
     def wavefunction(self, psi=None):
         w = WaveFunction(self)
@@ -71,9 +89,9 @@ class WaveFunction:
         self.size = plan.S * plan.npts
 
     def close(self):
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and not _exiting[0]:
             self.lib.qdg_wf_destroy(self.h)
-            self.h = None
+        self.h = None
 
     __del__ = close
 
@@ -104,9 +122,9 @@ class Propagator:
         check(self.lib.qdg_prop_init(self.h))
 
     def close(self):
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and not _exiting[0]:
             self.lib.qdg_prop_destroy(self.h)
-            self.h = None
+        self.h = None
 
     __del__ = close
 
@@ -150,4 +168,10 @@ class Propagator:
         return np.array(rows), np.array(terms)
 
 
-__all__ = ["Plan", "WaveFunction", "Propagator", "QDGError"]
+def kernel_launches():
+    return load().qdg_kernel_launches()
+
+
+PASS_MODES = ["kin_first", "kin_acc", "h_apply", "cheby_first", "cheby_term", "gspo_kin"]
+
+__all__ = ["Plan", "WaveFunction", "Propagator", "QDGError", "kernel_launches", "PASS_MODES"]

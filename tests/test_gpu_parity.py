@@ -95,7 +95,7 @@ def test_h_apply_mixed(eng, fixtures, name):
     plan = eng.Plan(hp, "mixed")
     a, b = plan.wavefunction(psi), plan.wavefunction()
     plan.h_apply(a, b, step=3)
-    assert rel(b.download(), ref) < 2e-5
+    assert rel(b.download(), ref) < 5e-5
 
 
 def test_erange_and_coeffs(eng, fixtures):
