@@ -84,6 +84,10 @@ struct qdg_plan {
   qdg::Couplings *d_cp = nullptr;
   double *d_coef = nullptr;
   void *d_P = nullptr;           // kinetic partial sums (bulk type)
+  void *d_Pd[QDG_MAX_DIMS] = {nullptr, nullptr, nullptr, nullptr};  // T_d phi per dimension
+  size_t kin_smem = 0;
+  int kin_grid = 1, comb_grid = 1;
+  std::map<long long, int> occ_cache;  // (mode, smem) -> resident blocks per SM
   void *d_scratch = nullptr;     // bulk-type wave function (mixed H apply input / output)
   void *d_scratch2 = nullptr;
   double *d_partials = nullptr;
@@ -125,6 +129,12 @@ struct qdg_prop {
   void *k0 = nullptr, *k1 = nullptr;  // bulk type
   qdg::ChebyState *d_cs = nullptr;
   qdg::ChebyState *h_cs = nullptr;    // pinned
+  // one captured graph of the whole Chebyshev step per (psi buffer, stream)
+  cudaGraphExec_t graph = nullptr;
+  void *graph_psi = nullptr;
+  cudaStream_t graph_stream = nullptr;
+  long long graph_launches = 0;
+  bool graphs_ok = true;
   // GSPO
   int ngroups = 0;
   std::vector<int> group_kinetic;     // 1: FFT member, 0: potential member
@@ -259,54 +269,134 @@ void fill_geometry(const qdg_plan *p, int d, int nsub, qdg::PassArgs<T> &a) {
 }
 
 template <typename T>
+qdg_status prof_begin(qdg_plan *p, int mode, size_t *slot);
+qdg_status prof_end(qdg_plan *p, size_t slot);
+
+template <typename T>
 qdg_status launch_one(qdg_plan *p, int mode, int d, qdg::PassArgs<T> &a, int *nblocks_out) {
   const int nsub = a.nsub;
   const size_t smem = pass_smem(p, d, a.TW, nsub);
   if (smem > 227 * 1024) return fail(QDG_EUNSUPPORTED, "grid line too long for the shared-memory FFT at this precision/state count");
   const int block = 256;
-  const int per_sm = qdg::pass_max_blocks<T>(mode, p->S, block, smem);
+  const long long key = ((long long)mode << 40) | ((long long)(sizeof(T)) << 32) | (long long)smem;
+  auto it = p->occ_cache.find(key);
+  int per_sm;
+  if (it != p->occ_cache.end()) per_sm = it->second;
+  else p->occ_cache[key] = per_sm = qdg::pass_max_blocks<T>(mode, p->S, block, smem);
   const long long items = a.ntiles * (p->S / nsub);
   long long grid = std::min<long long>(items, (long long)per_sm * p->sm_count);
   if (grid > p->max_parts) grid = p->max_parts;
   if (grid < 1) grid = 1;
   if (nblocks_out) *nblocks_out = (int)grid;
-  if (p->profiling) {
-    const size_t i = p->ev_mode.size();
-    while (p->ev_pool.size() < 2 * (i + 1)) {
-      cudaEvent_t e;
-      CK(cudaEventCreate(&e));
-      p->ev_pool.push_back(e);
-    }
-    p->ev_mode.push_back(mode);
-    CK(cudaEventRecord(p->ev_pool[2 * i], p->stream));
-    CK(qdg::launch_pass<T>(mode, a, (int)grid, block, smem, p->stream));
-    CK(cudaEventRecord(p->ev_pool[2 * i + 1], p->stream));
-    return QDG_OK;
-  }
+  size_t slot = 0;
+  qdg_status s = prof_begin<T>(p, mode, &slot);
+  if (s != QDG_OK) return s;
   CK(qdg::launch_pass<T>(mode, a, (int)grid, block, smem, p->stream));
+  return prof_end(p, slot);
+}
+
+// Epilogue arguments of one H application.
+struct Epi {
+  void *out = nullptr;
+  cplx<double> *psi = nullptr;
+  void *k0 = nullptr;
+  cd offset = 0, fac = 0, c0p = 0, c1p = 0, coeff = 0;
+  int imag = 0;
+  const int *done = nullptr;
+  qdg::ChebyCut cut{};
+};
+
+template <typename T>
+qdg_status prof_begin(qdg_plan *p, int mode, size_t *slot) {
+  if (!p->profiling) return QDG_OK;
+  const size_t i = p->ev_mode.size();
+  while (p->ev_pool.size() < 2 * (i + 1)) {
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    p->ev_pool.push_back(e);
+  }
+  p->ev_mode.push_back(mode);
+  *slot = i;
+  CK(cudaEventRecord(p->ev_pool[2 * i], p->stream));
+  return QDG_OK;
+}
+qdg_status prof_end(qdg_plan *p, size_t slot) {
+  if (!p->profiling) return QDG_OK;
+  CK(cudaEventRecord(p->ev_pool[2 * slot + 1], p->stream));
   return QDG_OK;
 }
 
-// One application of H (all passes).  final_mode selects the epilogue of
-// the last pass; `a` carries the epilogue arguments.  Returns the number of
-// blocks of the last pass (partials written).
+// One application of H.  One-dimensional grids: a single fused line pass
+// (FFT, k^2, inverse FFT, potential matrix and epilogue).  Higher
+// dimensions: one launch computing T_d phi for all d, then one point-wise
+// launch that sums them, adds the potential matrix and runs the epilogue.
 template <typename T>
-qdg_status run_h(qdg_plan *p, int final_mode, const cplx<T> *phi, qdg::PassArgs<T> a, int *nparts) {
-  a.phi = phi;
-  a.P = reinterpret_cast<cplx<T> *>(p->d_P);
-  a.multi_pass = p->nd > 1;
-  a.cp = p->d_cp;
-  a.coef = p->d_coef;
-  a.grids = reinterpret_cast<const T *>(p->d_grids);
-  a.partials = p->d_partials;
-  for (int d = 0; d < p->nd; ++d) {
-    const bool last = d == p->nd - 1;
-    const int mode = last ? final_mode : (d == 0 ? qdg::PM_KIN_FIRST : qdg::PM_KIN_ACC);
-    fill_geometry<T>(p, d, last ? p->S : 1, a);
-    qdg_status s = launch_one<T>(p, mode, d, a, last ? nparts : nullptr);
-    if (s != QDG_OK) return s;
+qdg_status run_h(qdg_plan *p, int final_mode, const cplx<T> *phi, const Epi &e) {
+  if (p->nd == 1) {
+    qdg::PassArgs<T> a;
+    memset(&a, 0, sizeof(a));
+    fill_geometry<T>(p, 0, p->S, a);
+    a.phi = phi;
+    a.out = reinterpret_cast<cplx<T> *>(e.out);
+    a.psi = e.psi;
+    a.k0 = reinterpret_cast<cplx<T> *>(e.k0);
+    a.cp = p->d_cp;
+    a.coef = p->d_coef;
+    a.grids = reinterpret_cast<const T *>(p->d_grids);
+    a.multi_pass = 0;
+    a.offset = C(e.offset); a.fac = C(e.fac); a.c0p = C(e.c0p); a.c1p = C(e.c1p); a.coeff = C(e.coeff);
+    a.imag = e.imag;
+    a.partials = p->d_partials;
+    a.done = e.done;
+    a.cut = e.cut;
+    return launch_one<T>(p, final_mode, 0, a, nullptr);
   }
-  return QDG_OK;
+  qdg::KinArgs<T> k;
+  memset(&k, 0, sizeof(k));
+  k.nd = p->nd;
+  k.S = p->S;
+  k.npts = p->npts;
+  k.phi = phi;
+  k.done = e.done;
+  long long items = 0;
+  for (int d = 0; d < p->nd; ++d) {
+    qdg::PassArgs<T> g;
+    memset(&g, 0, sizeof(g));
+    fill_geometry<T>(p, d, 1, g);
+    qdg::DimPass<T> &dp = k.dp[d];
+    dp.N = g.N; dp.es = g.es; dp.ls = g.ls; dp.TW = g.TW; dp.tiles_per_hi = g.tiles_per_hi;
+    dp.hi_stride = g.hi_stride; dp.ntiles = g.ntiles; dp.rp = g.rp; dp.tw = g.tw; dp.kfac = g.kfac;
+    dp.P = reinterpret_cast<cplx<T> *>(p->d_Pd[d]);
+    k.item_start[d] = items;
+    items += g.ntiles * p->S;
+  }
+  k.item_start[p->nd] = items;
+  size_t slot = 0;
+  qdg_status s = prof_begin<T>(p, qdg::PM_KIN_FIRST, &slot);
+  if (s != QDG_OK) return s;
+  CK(qdg::launch_kin_all<T>(k, (int)std::min<long long>(items, p->kin_grid), 256, p->kin_smem, p->stream));
+  if ((s = prof_end(p, slot)) != QDG_OK) return s;
+
+  qdg::CombArgs<T> c;
+  memset(&c, 0, sizeof(c));
+  c.S = p->S;
+  c.nd = p->nd;
+  c.npts = p->npts;
+  c.phi = phi;
+  for (int d = 0; d < p->nd; ++d) c.P[d] = reinterpret_cast<const cplx<T> *>(p->d_Pd[d]);
+  c.out = reinterpret_cast<cplx<T> *>(e.out);
+  c.psi = e.psi;
+  c.k0 = reinterpret_cast<cplx<T> *>(e.k0);
+  c.cp = p->d_cp;
+  c.coef = p->d_coef;
+  c.grids = reinterpret_cast<const T *>(p->d_grids);
+  c.offset = C(e.offset); c.fac = C(e.fac); c.c0p = C(e.c0p); c.c1p = C(e.c1p); c.coeff = C(e.coeff);
+  c.imag = e.imag;
+  c.partials = p->d_partials;
+  c.cut = e.cut;
+  if ((s = prof_begin<T>(p, final_mode, &slot)) != QDG_OK) return s;
+  CK(qdg::launch_combine<T>(final_mode, c, p->comb_grid, 256, p->stream));
+  return prof_end(p, slot);
 }
 
 template <typename T>
@@ -337,6 +427,24 @@ qdg_status upload_tables(qdg_plan *p) {
   CK(cudaMalloc(&p->d_grids, sizeof(T) * std::max<size_t>(1, g.size())));
   if (!g.empty()) CK(cudaMemcpy(p->d_grids, g.data(), sizeof(T) * g.size(), cudaMemcpyHostToDevice));
   CK(cudaMalloc(&p->d_P, sizeof(cplx<T>) * wf_elems(p)));
+  if (p->nd > 1) {
+    size_t smem = 0;
+    long long items = 0;
+    for (int d = 0; d < p->nd; ++d) {
+      CK(cudaMalloc(&p->d_Pd[d], sizeof(cplx<T>) * wf_elems(p)));
+      smem = std::max(smem, pass_smem(p, d, p->dim[d].TW_k, 1));
+      items += (p->npts / ((long long)p->dim[d].n * p->dim[d].TW_k)) * p->S;
+    }
+    if (smem > 227 * 1024) return fail(QDG_EUNSUPPORTED, "grid line too long for the shared-memory FFT");
+    p->kin_smem = smem;
+    const int per_sm = qdg::kin_all_max_blocks<T>(256, smem);
+    p->kin_grid = (int)std::min<long long>(items, (long long)per_sm * p->sm_count);
+  }
+  {
+    long long g = (p->npts + 255) / 256;
+    g = std::min<long long>(g, 8LL * p->sm_count);
+    p->comb_grid = (int)std::min<long long>(std::max<long long>(g, 1), p->max_parts);
+  }
   CK(cudaMalloc(&p->d_scratch, sizeof(cplx<T>) * wf_elems(p)));
   CK(cudaMalloc(&p->d_scratch2, sizeof(cplx<T>) * wf_elems(p)));
   return QDG_OK;
@@ -352,6 +460,8 @@ void free_plan(qdg_plan *p) {
   if (p->d_cp) cudaFree(p->d_cp);
   if (p->d_coef) cudaFree(p->d_coef);
   if (p->d_P) cudaFree(p->d_P);
+  for (int d = 0; d < QDG_MAX_DIMS; ++d)
+    if (p->d_Pd[d]) cudaFree(p->d_Pd[d]);
   if (p->d_scratch) cudaFree(p->d_scratch);
   if (p->d_scratch2) cudaFree(p->d_scratch2);
   if (p->d_partials) cudaFree(p->d_partials);
@@ -435,11 +545,9 @@ qdg_status h_apply_bulk(qdg_plan *p, const cplx<double> *psi, cplx<T> *out, long
     CK(qdg::launch_convert<T>(reinterpret_cast<cplx<T> *>(p->d_scratch2), psi, wf_elems(p), p->stream));
     in = reinterpret_cast<const cplx<T> *>(p->d_scratch2);
   }
-  qdg::PassArgs<T> a;
-  memset(&a, 0, sizeof(a));
-  a.out = out;
-  int np = 0;
-  return run_h<T>(p, qdg::PM_HAPPLY, in, a, &np);
+  Epi e;
+  e.out = out;
+  return run_h<T>(p, qdg::PM_HAPPLY, in, e);
 }
 
 // ------------------------------------------------------------ Chebyshev
@@ -493,45 +601,79 @@ qdg_status cheby_init(qdg_prop *P) {
   return QDG_OK;
 }
 
-// One Chebyshev step (OCheby::real_time_step / imag_time_step) with the
-// convergence decision on the device: no host synchronisation inside.
+// The device work of one Chebyshev step (OCheby::real_time_step /
+// imag_time_step) after the field coefficients are set: no host
+// synchronisation; the series cut is decided on the device by the last
+// block of each term and later terms skip their work.
 template <typename T>
-qdg_status cheby_enqueue(qdg_prop *P, cplx<double> *psi, long long step) {
+qdg_status cheby_body(qdg_prop *P, cplx<double> *psi) {
   qdg_plan *p = P->plan;
   cudaStream_t st = p->stream;
-  CK(qdg::launch_set_coefs(p->d_coef, p->d_cp, p->d_lasers, p->laser_nt, step, st));
   CK(qdg::launch_cheby_begin(P->d_cs, P->order, st));
   cplx<T> *k0 = reinterpret_cast<cplx<T> *>(P->k0);
   cplx<T> *k1 = reinterpret_cast<cplx<T> *>(P->k1);
   CK(qdg::launch_convert<T>(k0, psi, wf_elems(p), st));  // ket0 = Psi
   const cd ex = P->c0 / P->dt;
   const cd ph = std::exp(P->c0 * P->offset);
-  qdg::PassArgs<T> a;
-  memset(&a, 0, sizeof(a));
-  a.psi = psi;
-  a.offset = C(P->offset);
-  a.imag = P->imag ? 1 : 0;
-  a.done = &P->d_cs->done;
+  Epi e;
+  e.psi = psi;
+  e.offset = P->offset;
+  e.imag = P->imag ? 1 : 0;
+  e.done = &P->d_cs->done;
+  e.cut.cs = P->d_cs;
+  e.cut.prec = P->prec;
+  e.cut.imag = e.imag;
+  e.cut.offim0 = P->offset.imag() == 0 ? 1 : 0;
   // phi_1 = (H - offset) psi * exp/scaling; psi = psi c0 + phi_1 c1
-  a.k0 = k1;
-  a.fac = C(ex / P->scaling);
-  a.c0p = C(P->coeff[0] * ph);
-  a.c1p = C(P->coeff[1] * ph);
-  int np = 0;
-  qdg_status s = run_h<T>(p, qdg::PM_CHEBY_FIRST, k0, a, &np);
+  e.k0 = k1;
+  e.fac = ex / P->scaling;
+  e.c0p = P->coeff[0] * ph;
+  e.c1p = P->coeff[1] * ph;
+  e.cut.first = 1;
+  e.cut.term = 1;
+  qdg_status s = run_h<T>(p, qdg::PM_CHEBY_FIRST, k0, e);
   if (s != QDG_OK) return s;
-  const int offim0 = P->offset.imag() == 0 ? 1 : 0;
-  CK(qdg::launch_cheby_finalize(P->d_cs, p->d_partials, np, 1, 1, P->order, P->prec, a.imag, offim0, st));
-  a.fac = C(2.0 * ex / P->scaling);
+  e.fac = 2.0 * ex / P->scaling;
+  e.cut.first = 0;
   for (int i = 2; i < P->order; ++i) {
-    a.k0 = k0;  // phi_{n-2} in, phi_n out
-    a.coeff = C(P->coeff[i] * ph);
-    s = run_h<T>(p, qdg::PM_CHEBY_TERM, k1, a, &np);
-    if (s != QDG_OK) return s;
-    CK(qdg::launch_cheby_finalize(P->d_cs, p->d_partials, np, 0, i, P->order, P->prec, a.imag, offim0, st));
+    e.k0 = k0;  // phi_{n-2} in, phi_n out
+    e.coeff = P->coeff[i] * ph;
+    e.cut.term = i;
+    if ((s = run_h<T>(p, qdg::PM_CHEBY_TERM, k1, e)) != QDG_OK) return s;
     std::swap(k0, k1);
   }
   CK(qdg::launch_cheby_end(P->d_cs, st));
+  return QDG_OK;
+}
+
+template <typename T>
+qdg_status cheby_enqueue(qdg_prop *P, cplx<double> *psi, long long step) {
+  qdg_plan *p = P->plan;
+  CK(qdg::launch_set_coefs(p->d_coef, p->d_cp, p->d_lasers, p->laser_nt, step, p->stream));
+  if (p->profiling || !P->graphs_ok) return cheby_body<T>(P, psi);
+  if (!P->graph || P->graph_psi != psi || P->graph_stream != p->stream) {
+    if (P->graph) { cudaGraphExecDestroy(P->graph); P->graph = nullptr; }
+    cudaGraph_t g = nullptr;
+    const long long l0 = qdg::launch_counter();
+    CK(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeRelaxed));
+    qdg_status s = cheby_body<T>(P, psi);
+    cudaError_t ce = cudaStreamEndCapture(p->stream, &g);
+    if (s != QDG_OK) { if (g) cudaGraphDestroy(g); return s; }
+    if (ce != cudaSuccess || cudaGraphInstantiate(&P->graph, g, 0) != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+      P->graph = nullptr;
+      P->graphs_ok = false;  // stream capture unavailable: launch the kernels one by one
+      return cheby_body<T>(P, psi);
+    }
+    cudaGraphDestroy(g);
+    P->graph_launches = qdg::launch_counter() - l0;
+    qdg::add_launches(-P->graph_launches);  // counted again at every replay
+    P->graph_psi = psi;
+    P->graph_stream = p->stream;
+  }
+  CK(cudaGraphLaunch(P->graph, p->stream));
+  qdg::add_launches(P->graph_launches);
   return QDG_OK;
 }
 
@@ -664,12 +806,9 @@ qdg_status krylov_alloc(qdg_prop *P) {
 
 template <typename T>
 qdg_status hq(qdg_prop *P, const cplx<T> *q, cplx<T> *out, long long step) {
-  qdg_plan *p = P->plan;
-  qdg::PassArgs<T> a;
-  memset(&a, 0, sizeof(a));
-  a.out = out;
-  int np;
-  return run_h<T>(p, qdg::PM_HAPPLY, q, a, &np);
+  Epi e;
+  e.out = out;
+  return run_h<T>(P->plan, qdg::PM_HAPPLY, q, e);
 }
 
 // OSIL::BuildLZB / DiagLZB (src/qdlib/OSIL.cpp:83-185), FP64 scalars.
@@ -1083,6 +1222,7 @@ qdg_status qdg_prop_destroy(qdg_prop *P) {
   cudaStreamSynchronize(plan->stream);
   if (P->k0) cudaFree(P->k0);
   if (P->k1) cudaFree(P->k1);
+  if (P->graph) cudaGraphExecDestroy(P->graph);
   if (P->d_cs) cudaFree(P->d_cs);
   if (P->h_cs) cudaFreeHost(P->h_cs);
   for (auto &g : P->gtab) for (auto v : g) if (v) cudaFree(v);

@@ -22,6 +22,7 @@ namespace qdg {
 
 static std::atomic<long long> g_launches{0};
 long long launch_counter() { return g_launches.load(); }
+void add_launches(long long n) { g_launches.fetch_add(n); }
 #define COUNT_LAUNCH() g_launches.fetch_add(1)
 
 __device__ __forceinline__ cplx<double> dmul(cplx<double> a, cplx<double> b) { return cmul(a, b); }
@@ -32,6 +33,39 @@ __device__ __forceinline__ cplx<double> dmul(cplx<double> a, cplx<double> b) { r
 __device__ __forceinline__ void tile_coord(int idx, int TW, int N, int es, int &w, int &i) {
   if (es == 1) { w = idx / N; i = idx - w * N; }
   else { i = idx / TW; w = idx - i * TW; }
+}
+
+// Block-level end of a Chebyshev term: store this block's norm partial, and
+// let the last block to arrive sum all partials in block order and apply the
+// reference's series cut.  No block waits for another (threadfence
+// reduction: the last arriving block does the work).
+__device__ void cheby_term_finish(double acc, double *red, double *partials, const ChebyCut &cut) {
+  __shared__ int am_last;
+  const double t = block_sum(acc, red);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = t;
+    __threadfence();
+    const unsigned int prev = atomicAdd(&cut.cs->arrive, 1u);
+    am_last = (prev == gridDim.x - 1) ? 1 : 0;
+  }
+  __syncthreads();
+  if (!am_last) return;
+  __threadfence();
+  double v = 0.0;
+  for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) v += __ldcg(partials + i);
+  const double tot = block_sum(v, red);
+  if (threadIdx.x != 0) return;
+  ChebyState *cs = cut.cs;
+  cs->arrive = 0;
+  if (!isfinite(tot)) { cs->status = 2; cs->done = 1; cs->terms = cut.first ? 2 : cut.term + 1; return; }
+  if (cut.first) { cs->norm0 = tot; return; }
+  if (!cut.imag) {
+    const double nconv = fabs(cs->norm0 - tot) / cs->norm0;
+    if (nconv < cut.prec && cut.offim0) { cs->done = 1; cs->terms = cut.term + 1; }
+  } else {
+    if (fabs(tot - cs->norm_last) / cs->norm_last < cut.prec) { cs->done = 1; cs->terms = cut.term + 1; }
+    cs->norm_last = tot;
+  }
 }
 
 template <typename T, int MODE, int SS>
@@ -161,11 +195,168 @@ __global__ void __launch_bounds__(256) linepass_kernel(PassArgs<T> a) {
     }
     __syncthreads();
   }
-  if (MODE == PM_CHEBY_FIRST || MODE == PM_CHEBY_TERM) {
-    const double t = block_sum(acc, red);
-    if (threadIdx.x == 0) a.partials[blockIdx.x] = t;
+  if (MODE == PM_CHEBY_FIRST || MODE == PM_CHEBY_TERM) cheby_term_finish(acc, red, a.partials, a.cut);
+}
+
+// ------------------------------------------------ all-dimension kinetic pass
+// Work items are (dimension, line tile, state); each computes T_d phi on its
+// lines with the shared-memory FFT and stores it to P_d.
+template <typename T>
+__global__ void __launch_bounds__(256) kin_all_kernel(KinArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  if (a.done != nullptr && *a.done) return;
+  const long long nitems = a.item_start[a.nd];
+  const long long npts = a.npts;
+  int cur_dim = -1;
+  cplx<T> *tws = reinterpret_cast<cplx<T> *>(smem_raw);
+  for (long long item = blockIdx.x; item < nitems; item += gridDim.x) {
+    int d = 0;
+    while (item >= a.item_start[d + 1]) ++d;
+    const DimPass<T> &g = a.dp[d];
+    const int N = g.N, TW = g.TW;
+    cplx<T> *b0 = tws + N;
+    cplx<T> *b1 = b0 + (size_t)TW * N;
+    if (d != cur_dim) {
+      __syncthreads();
+      for (int i = threadIdx.x; i < N; i += blockDim.x) tws[i] = g.tw[i];
+      cur_dim = d;
+    }
+    const long long local = item - a.item_start[d];
+    const long long tile = local / a.S;
+    const int s = (int)(local - tile * a.S);
+    const long long hi = tile / g.tiles_per_hi;
+    const long long base = hi * g.hi_stride + (tile - hi * g.tiles_per_hi) * TW;
+    const int tileN = TW * N;
+    const cplx<T> *src = a.phi + (long long)s * npts;
+    for (int idx = threadIdx.x; idx < tileN; idx += blockDim.x) {
+      int w, i;
+      tile_coord(idx, TW, N, g.es, w, i);
+      b0[w * N + i] = ld(src + base + (long long)w * g.ls + (long long)i * g.es);
+    }
+    __syncthreads();
+    const int cur = fft_lines<T>(b0, b1, g.rp, TW, tws, -1);
+    cplx<T> *bc = cur ? b1 : b0;
+    const double kf = g.kfac[s];
+    for (int idx = threadIdx.x; idx < tileN; idx += blockDim.x) {
+      const int i = idx % N;
+      const int kq = min(i, N - i);
+      bc[idx] = cmulr(bc[idx], (T)(kf * (double)kq * (double)kq));
+    }
+    __syncthreads();
+    const int cur2 = fft_lines<T>(bc, cur ? b0 : b1, g.rp, TW, tws, +1);
+    const cplx<T> *res = cur2 ? (cur ? b0 : b1) : bc;
+    cplx<T> *dst = g.P + (long long)s * npts;
+    for (int idx = threadIdx.x; idx < tileN; idx += blockDim.x) {
+      int w, i;
+      tile_coord(idx, TW, N, g.es, w, i);
+      st(dst + base + (long long)w * g.ls + (long long)i * g.es, res[w * N + i]);
+    }
+    __syncthreads();
   }
 }
+
+// ------------------------------------------------------------ combine pass
+template <typename T, int MODE, int SS>
+__global__ void __launch_bounds__(256) combine_kernel(CombArgs<T> a) {
+  __shared__ double red[32];
+  if (a.cut.cs != nullptr && a.cut.cs->done) return;
+  const long long npts = a.npts;
+  const int S = (SS > 0) ? SS : a.S;
+  constexpr int SM = (SS > 0) ? SS : kMaxStates;
+  double acc = 0.0;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npts; p += (long long)gridDim.x * blockDim.x) {
+    cplx<T> ph[SM], h[SM];
+#pragma unroll
+    for (int s = 0; s < SM; ++s) {
+      if (s < S) {
+        const long long g = (long long)s * npts + p;
+        ph[s] = ld(a.phi + g);
+        cplx<T> v = ld(a.P[0] + g);
+        for (int d = 1; d < a.nd; ++d) v = v + ld(a.P[d] + g);
+        h[s] = v;
+      }
+    }
+    const int ne = a.cp->ne;
+    for (int e = 0; e < ne; ++e) {
+      const int r = a.cp->row[e], c = a.cp->col[e];
+      const T v = (T)(a.coef[e]) * a.grids[(long long)a.cp->gid[e] * npts + p];
+#pragma unroll
+      for (int s = 0; s < SM; ++s)
+        if (s == r) {
+#pragma unroll
+          for (int q = 0; q < SM; ++q)
+            if (q == c) h[s] = h[s] + cmulr(ph[q], v);
+        }
+    }
+#pragma unroll
+    for (int s = 0; s < SM; ++s) {
+      if (s >= S) break;
+      const long long g = (long long)s * npts + p;
+      if (MODE == PM_HAPPLY) {
+        st(a.out + g, h[s]);
+      } else {
+        const cplx<double> bf = dmul(ccast<double>(h[s]) - dmul(a.offset, ccast<double>(ph[s])), a.fac);
+        if (MODE == PM_CHEBY_FIRST) {
+          const cplx<double> ps = ld(a.psi + g);
+          acc += cabs2(ps);
+          st(a.k0 + g, ccast<T>(bf));
+          st(a.psi + g, dmul(ps, a.c0p) + dmul(bf, a.c1p));
+        } else {
+          const cplx<double> km2 = ccast<double>(ld(a.k0 + g));
+          const cplx<double> k2 = a.imag ? bf - km2 : bf + km2;
+          st(a.k0 + g, ccast<T>(k2));
+          const cplx<double> ps = ld(a.psi + g) + dmul(k2, a.coeff);
+          st(a.psi + g, ps);
+          acc += cabs2(ps);
+        }
+      }
+    }
+  }
+  if (MODE == PM_CHEBY_FIRST || MODE == PM_CHEBY_TERM) cheby_term_finish(acc, red, a.partials, a.cut);
+}
+
+template <typename T>
+cudaError_t launch_kin_all(const KinArgs<T> &a, int grid, int block, size_t smem, cudaStream_t st) {
+  void *k = (void *)kin_all_kernel<T>;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  void *args[] = {(void *)&a};
+  COUNT_LAUNCH();
+  return cudaLaunchKernel(k, dim3(grid), dim3(block), args, smem, st);
+}
+
+template <typename T>
+int kin_all_max_blocks(int block, size_t smem) {
+  void *k = (void *)kin_all_kernel<T>;
+  if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, block, smem) != cudaSuccess) return 1;
+  return nb > 0 ? nb : 1;
+}
+
+template <typename T, int MODE>
+static void *comb_ptr(int S) {
+  return S == 1 ? (void *)combine_kernel<T, MODE, 1> : S == 2 ? (void *)combine_kernel<T, MODE, 2>
+                                                              : (void *)combine_kernel<T, MODE, 0>;
+}
+
+template <typename T>
+cudaError_t launch_combine(int mode, const CombArgs<T> &a, int grid, int block, cudaStream_t st) {
+  void *k = mode == PM_HAPPLY ? comb_ptr<T, PM_HAPPLY>(a.S)
+            : mode == PM_CHEBY_FIRST ? comb_ptr<T, PM_CHEBY_FIRST>(a.S) : comb_ptr<T, PM_CHEBY_TERM>(a.S);
+  void *args[] = {(void *)&a};
+  COUNT_LAUNCH();
+  return cudaLaunchKernel(k, dim3(grid), dim3(block), args, 0, st);
+}
+
+template cudaError_t launch_kin_all<double>(const KinArgs<double> &, int, int, size_t, cudaStream_t);
+template cudaError_t launch_kin_all<float>(const KinArgs<float> &, int, int, size_t, cudaStream_t);
+template int kin_all_max_blocks<double>(int, size_t);
+template int kin_all_max_blocks<float>(int, size_t);
+template cudaError_t launch_combine<double>(int, const CombArgs<double> &, int, int, cudaStream_t);
+template cudaError_t launch_combine<float>(int, const CombArgs<float> &, int, int, cudaStream_t);
 
 template <typename T, int MODE, int SS>
 static void *kernel_ptr() { return (void *)linepass_kernel<T, MODE, SS>; }
@@ -217,7 +408,7 @@ template int pass_max_blocks<float>(int, int, int, size_t);
 
 // ---------------------------------------------------------------- control
 __global__ void cheby_begin_kernel(ChebyState *cs, int order) {
-  cs->norm0 = 0; cs->norm_last = 0; cs->done = 0; cs->terms = order; cs->status = 0;
+  cs->norm0 = 0; cs->norm_last = 0; cs->done = 0; cs->terms = order; cs->status = 0; cs->arrive = 0;
 }
 
 // Sums the per-block norms in a fixed order and applies the reference's

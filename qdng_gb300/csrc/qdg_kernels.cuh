@@ -33,6 +33,29 @@ struct Couplings {
   int lid[kMaxCouplings];  // -1: static potential
 };
 
+// Per-step Chebyshev control block in device memory.
+struct ChebyState {
+  long long total;   // terms summed over all steps since the propagator was set up
+  double norm0;      // raw norm of psi before the step
+  double norm_last;  // imaginary time: previous accumulated norm
+  int done;          // series converged (or error): later terms are skipped
+  int terms;         // terms used in the step
+  int status;        // QDG_OK or QDG_ENONFINITE
+  unsigned int arrive;  // blocks of the current reduction that have stored their partial sum
+};
+
+// Series-cut parameters handed to the kernel that finishes a Chebyshev term:
+// its last block sums the per-block norms in a fixed order and applies the
+// reference's criterion (OCheby.cpp:178-182 real time, 285-289 imaginary).
+struct ChebyCut {
+  ChebyState *cs;   // nullptr: no reduction (H apply)
+  int first;        // 1: raw norm of psi before the step (OCheby::raw_norm)
+  int term;         // index i of the term just added
+  double prec;
+  int imag;
+  int offim0;       // offset has no imaginary part (break allowed)
+};
+
 template <typename T>
 struct PassArgs {
   // geometry of the lines of this pass
@@ -68,27 +91,69 @@ struct PassArgs {
   int imag;                // imaginary-time recursion (minus sign, OCheby.cpp:276)
   double *partials;        // per-block partial sums (norms)
   const int *done;         // Chebyshev series converged: skip the work
+  ChebyCut cut;            // fused series cut (Chebyshev modes)
   // GSPO kinetic member: per-state exp(c T_d(k)) / N_d tables, S x N entries
   const cplx<T> *gtab;
 };
 
-// Per-step Chebyshev control block in device memory.
-struct ChebyState {
-  long long total;   // terms summed over all steps since the propagator was set up
-  double norm0;      // raw norm of psi before the step
-  double norm_last;  // imaginary time: previous accumulated norm
-  int done;          // series converged (or error): later terms are skipped
-  int terms;         // terms used in the step
-  int status;        // QDG_OK or QDG_ENONFINITE
-  int pad;
+// One dimension of an all-dimension kinetic launch.
+template <typename T>
+struct DimPass {
+  int N, es, ls, TW, tiles_per_hi;
+  long long hi_stride, ntiles;
+  RadixPlan rp;
+  const cplx<T> *tw;
+  const double *kfac;   // [S] dk^2/(2m)/N
+  cplx<T> *P;           // T_d phi output (state stride npts)
 };
+
+// T_d phi for every dimension d in one launch (the kinetic operator is a sum
+// of independent one-dimensional parts).
+template <typename T>
+struct KinArgs {
+  int nd, S;
+  long long npts;
+  const cplx<T> *phi;
+  DimPass<T> dp[4];
+  long long item_start[5];  // first work item of each dimension
+  const int *done;
+};
+
+// Point-wise finish of H phi: sum_d T_d phi + potential matrix, then the
+// epilogue (H apply output or the Chebyshev recurrence).
+template <typename T>
+struct CombArgs {
+  int S, nd;
+  long long npts;
+  const cplx<T> *phi;
+  const cplx<T> *P[4];
+  cplx<T> *out;
+  cplx<double> *psi;
+  cplx<T> *k0;
+  const Couplings *cp;
+  const double *coef;
+  const T *grids;
+  cplx<double> offset, fac, c0p, c1p, coeff;
+  int imag;
+  double *partials;
+  ChebyCut cut;
+};
+
+template <typename T>
+cudaError_t launch_kin_all(const KinArgs<T> &a, int grid, int block, size_t smem, cudaStream_t st);
+template <typename T>
+int kin_all_max_blocks(int block, size_t smem);
+template <typename T>
+cudaError_t launch_combine(int mode, const CombArgs<T> &a, int grid, int block, cudaStream_t st);
 
 // coef[e] for clock step `step` (Laser::Get, src/qdlib/Laser.cpp:125-128).
 cudaError_t launch_set_coefs(double *coef, const Couplings *cp, const double *lasers, int laser_nt, long long step,
                              cudaStream_t st);
 
-// Kernels launched by this library in the process (all launchers count).
+// Kernels launched by this library in the process (all launchers count;
+// replays of captured graphs are added by the caller).
 long long launch_counter();
+void add_launches(long long n);
 
 // launchers (qdg_kernels.cu)
 template <typename T>

@@ -243,3 +243,29 @@ def test_apply_host_matches_device(eng, fixtures):
         t2 = P2.apply_host(scratch, host, step)
         assert t1 == t2
     assert np.array_equal(w.download(), host)
+
+
+def test_graph_and_eager_steps_agree_bitwise(eng):
+    """A captured Chebyshev step and the same step launched kernel by kernel
+    (profiling mode) give bit-identical wave functions and term counts."""
+    hp, psi, run = cases.cfg2_two_state(n=64)
+    plan = eng.Plan(hp, "fp64")
+    P = eng.Propagator(plan, run["name"], run["params"], dt=run["dt"])
+    w1, w2 = plan.wavefunction(psi), plan.wavefunction(psi)
+    t1 = [P.apply(w1, s) for s in range(4)]
+    plan.profile(True)
+    t2 = [P.apply(w2, s) for s in range(4)]
+    plan.profile(False)
+    assert t1 == t2
+    assert np.array_equal(w1.download(), w2.download())
+
+
+def test_run_counts_terms(eng, fixtures):
+    hp, psi, run = cases.tgp_expec(fixtures)
+    plan = eng.Plan(hp, "fp64")
+    P = eng.Propagator(plan, run["name"], run["params"], dt=run["dt"])
+    Q = O.Propagator(O.System(hp), run["name"], run["params"], dt=run["dt"])
+    w = plan.wavefunction(psi)
+    x = psi.copy()
+    expect = sum(Q.apply(x, s) for s in range(10))
+    assert P.run(w, 0, 10) == expect
