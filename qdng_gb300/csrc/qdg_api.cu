@@ -133,8 +133,12 @@ struct qdg_prop {
   cudaGraphExec_t graph = nullptr;
   void *graph_psi = nullptr;
   cudaStream_t graph_stream = nullptr;
-  long long graph_launches = 0;
+  long long graph_launches = 0;     // kernels of the prologue and epilogue
+  long long body_launches = 0;      // kernels of one term of the while body
   bool graphs_ok = true;
+  bool while_ok = true;             // device-driven term loop (conditional while node)
+  bool graph_is_while = false;
+  cplx<double> *d_coeffs = nullptr; // coeff[i] exp(c0 offset), i < order
   // GSPO
   int ngroups = 0;
   std::vector<int> group_kinetic;     // 1: FFT member, 0: potential member
@@ -304,6 +308,7 @@ struct Epi {
   int imag = 0;
   const int *done = nullptr;
   qdg::ChebyCut cut{};
+  const void *bufs[2] = {nullptr, nullptr};  // device-driven term loop (cut.dyn)
 };
 
 template <typename T>
@@ -349,6 +354,8 @@ qdg_status run_h(qdg_plan *p, int final_mode, const cplx<T> *phi, const Epi &e) 
     a.partials = p->d_partials;
     a.done = e.done;
     a.cut = e.cut;
+    a.bufs[0] = reinterpret_cast<const cplx<T> *>(e.bufs[0]);
+    a.bufs[1] = reinterpret_cast<const cplx<T> *>(e.bufs[1]);
     return launch_one<T>(p, final_mode, 0, a, nullptr);
   }
   qdg::KinArgs<T> k;
@@ -358,6 +365,10 @@ qdg_status run_h(qdg_plan *p, int final_mode, const cplx<T> *phi, const Epi &e) 
   k.npts = p->npts;
   k.phi = phi;
   k.done = e.done;
+  k.cs = e.cut.cs;
+  k.dyn = e.cut.dyn;
+  k.bufs[0] = reinterpret_cast<const cplx<T> *>(e.bufs[0]);
+  k.bufs[1] = reinterpret_cast<const cplx<T> *>(e.bufs[1]);
   long long items = 0;
   for (int d = 0; d < p->nd; ++d) {
     qdg::PassArgs<T> g;
@@ -394,6 +405,8 @@ qdg_status run_h(qdg_plan *p, int final_mode, const cplx<T> *phi, const Epi &e) 
   c.imag = e.imag;
   c.partials = p->d_partials;
   c.cut = e.cut;
+  c.bufs[0] = reinterpret_cast<const cplx<T> *>(e.bufs[0]);
+  c.bufs[1] = reinterpret_cast<const cplx<T> *>(e.bufs[1]);
   if ((s = prof_begin<T>(p, final_mode, &slot)) != QDG_OK) return s;
   CK(qdg::launch_combine<T>(final_mode, c, p->comb_grid, 256, p->stream));
   return prof_end(p, slot);
@@ -597,24 +610,20 @@ qdg_status cheby_init(qdg_prop *P) {
   CK(cudaMalloc(&P->k1, bytes));
   CK(cudaMalloc(&P->d_cs, sizeof(qdg::ChebyState)));
   CK(cudaMemset(P->d_cs, 0, sizeof(qdg::ChebyState)));
+  {
+    const cd ph = std::exp(P->c0 * P->offset);
+    std::vector<cplx<double>> hc(P->order);
+    for (int i = 0; i < P->order; ++i) hc[i] = C(P->coeff[i] * ph);
+    CK(cudaMalloc(&P->d_coeffs, sizeof(cplx<double>) * P->order));
+    CK(cudaMemcpy(P->d_coeffs, hc.data(), sizeof(cplx<double>) * P->order, cudaMemcpyHostToDevice));
+  }
   CK(cudaMallocHost(&P->h_cs, sizeof(qdg::ChebyState)));
   return QDG_OK;
 }
 
-// The device work of one Chebyshev step (OCheby::real_time_step /
-// imag_time_step) after the field coefficients are set: no host
-// synchronisation; the series cut is decided on the device by the last
-// block of each term and later terms skip their work.
+// Epilogue arguments shared by all terms of a Chebyshev step.
 template <typename T>
-qdg_status cheby_body(qdg_prop *P, cplx<double> *psi) {
-  qdg_plan *p = P->plan;
-  cudaStream_t st = p->stream;
-  CK(qdg::launch_cheby_begin(P->d_cs, P->order, st));
-  cplx<T> *k0 = reinterpret_cast<cplx<T> *>(P->k0);
-  cplx<T> *k1 = reinterpret_cast<cplx<T> *>(P->k1);
-  CK(qdg::launch_convert<T>(k0, psi, wf_elems(p), st));  // ket0 = Psi
-  const cd ex = P->c0 / P->dt;
-  const cd ph = std::exp(P->c0 * P->offset);
+Epi cheby_epi(qdg_prop *P, cplx<double> *psi) {
   Epi e;
   e.psi = psi;
   e.offset = P->offset;
@@ -624,17 +633,51 @@ qdg_status cheby_body(qdg_prop *P, cplx<double> *psi) {
   e.cut.prec = P->prec;
   e.cut.imag = e.imag;
   e.cut.offim0 = P->offset.imag() == 0 ? 1 : 0;
-  // phi_1 = (H - offset) psi * exp/scaling; psi = psi c0 + phi_1 c1
-  e.k0 = k1;
+  e.cut.diff = P->plan->precision == QDG_PREC_MIXED ? 1 : 0;
+  e.cut.order = P->order;
+  e.cut.coeffs = P->d_coeffs;
+  e.bufs[0] = P->k0;
+  e.bufs[1] = P->k1;
+  return e;
+}
+
+// Begin, psi copy and the first two terms of the series (OCheby.cpp:99-111):
+// phi_1 = (H - offset) psi exp/scaling; psi = psi c0 + phi_1 c1.
+template <typename T>
+qdg_status cheby_prologue(qdg_prop *P, cplx<double> *psi, unsigned long long cond, int use_cond) {
+  qdg_plan *p = P->plan;
+  CK(qdg::launch_cheby_begin(P->d_cs, P->order, cond, use_cond, p->stream));
+  cplx<T> *k0 = reinterpret_cast<cplx<T> *>(P->k0);
+  CK(qdg::launch_convert<T>(k0, psi, wf_elems(p), p->stream));  // ket0 = Psi
+  const cd ex = P->c0 / P->dt;
+  const cd ph = std::exp(P->c0 * P->offset);
+  Epi e = cheby_epi<T>(P, psi);
+  e.k0 = P->k1;
   e.fac = ex / P->scaling;
   e.c0p = P->coeff[0] * ph;
   e.c1p = P->coeff[1] * ph;
   e.cut.first = 1;
   e.cut.term = 1;
-  qdg_status s = run_h<T>(p, qdg::PM_CHEBY_FIRST, k0, e);
+  e.cut.cond = cond;
+  e.cut.use_cond = use_cond;
+  return run_h<T>(p, qdg::PM_CHEBY_FIRST, k0, e);
+}
+
+// The device work of one Chebyshev step (OCheby::real_time_step /
+// imag_time_step), every term launched from the host: no host
+// synchronisation; the series cut is decided on the device by the last
+// block of each term and later terms skip their work.
+template <typename T>
+qdg_status cheby_body(qdg_prop *P, cplx<double> *psi) {
+  qdg_plan *p = P->plan;
+  qdg_status s = cheby_prologue<T>(P, psi, 0, 0);
   if (s != QDG_OK) return s;
+  cplx<T> *k0 = reinterpret_cast<cplx<T> *>(P->k0);
+  cplx<T> *k1 = reinterpret_cast<cplx<T> *>(P->k1);
+  const cd ex = P->c0 / P->dt;
+  const cd ph = std::exp(P->c0 * P->offset);
+  Epi e = cheby_epi<T>(P, psi);
   e.fac = 2.0 * ex / P->scaling;
-  e.cut.first = 0;
   for (int i = 2; i < P->order; ++i) {
     e.k0 = k0;  // phi_{n-2} in, phi_n out
     e.coeff = P->coeff[i] * ph;
@@ -642,7 +685,104 @@ qdg_status cheby_body(qdg_prop *P, cplx<double> *psi) {
     if ((s = run_h<T>(p, qdg::PM_CHEBY_TERM, k1, e)) != QDG_OK) return s;
     std::swap(k0, k1);
   }
-  CK(qdg::launch_cheby_end(P->d_cs, st));
+  CK(qdg::launch_cheby_end(P->d_cs, p->stream));
+  return QDG_OK;
+}
+
+// One term of the device-driven loop: the term index, the buffers and the
+// coefficient come from the device state; the last block of the term ends
+// the loop (conditional while node) once the series is cut.
+template <typename T>
+qdg_status cheby_dyn_term(qdg_prop *P, cplx<double> *psi, unsigned long long cond) {
+  Epi e = cheby_epi<T>(P, psi);
+  e.fac = 2.0 * (P->c0 / P->dt) / P->scaling;
+  e.cut.dyn = 1;
+  e.cut.cond = cond;
+  e.cut.use_cond = 1;
+  return run_h<T>(P->plan, qdg::PM_CHEBY_TERM, nullptr, e);
+}
+
+// Graph of a whole step with a conditional while node around one term:
+// terms after the series cut cost nothing.
+template <typename T>
+qdg_status build_while_graph(qdg_prop *P, cplx<double> *psi, cudaGraphExec_t *exec) {
+  qdg_plan *p = P->plan;
+  cudaStream_t st = p->stream;
+  cudaGraph_t g = nullptr;
+  CK(cudaGraphCreate(&g, 0));
+  cudaGraphConditionalHandle cond;
+  if (cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return fail(QDG_ECUDA, "conditional handle");
+  }
+  const long long l0 = qdg::launch_counter();
+  if (cudaStreamBeginCaptureToGraph(st, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return fail(QDG_ECUDA, "capture to graph");
+  }
+  qdg_status s = cheby_prologue<T>(P, psi, cond, 1);
+  cudaStreamCaptureStatus cst;
+  const cudaGraphNode_t *deps = nullptr;
+  size_t ndeps = 0;
+  cudaGraphNode_t wnode = nullptr;
+  cudaGraph_t body = nullptr;
+  bool ok = s == QDG_OK && cudaStreamGetCaptureInfo(st, &cst, nullptr, nullptr, &deps, nullptr, &ndeps) == cudaSuccess;
+  if (ok) {
+    cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+    np.conditional.handle = cond;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    ok = cudaGraphAddNode(&wnode, g, deps, nullptr, ndeps, &np) == cudaSuccess;
+    if (ok) {
+      body = np.conditional.phGraph_out[0];
+      ok = cudaStreamUpdateCaptureDependencies(st, &wnode, nullptr, 1, cudaStreamSetCaptureDependencies) == cudaSuccess;
+    }
+  }
+  if (ok) ok = qdg::launch_cheby_end(P->d_cs, st) == cudaSuccess;
+  cudaGraph_t gout = nullptr;
+  const bool ended = cudaStreamEndCapture(st, &gout) == cudaSuccess;
+  const long long l1 = qdg::launch_counter();
+  if (ok && ended) {
+    ok = cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) == cudaSuccess;
+    if (ok) {
+      qdg_status s2 = cheby_dyn_term<T>(P, psi, cond);
+      cudaGraph_t bout = nullptr;
+      ok = cudaStreamEndCapture(st, &bout) == cudaSuccess && s2 == QDG_OK;
+    }
+  }
+  if (ok && ended) ok = cudaGraphInstantiate(exec, g, 0) == cudaSuccess;
+  cudaGraphDestroy(g);
+  const long long l2 = qdg::launch_counter();
+  qdg::add_launches(-(l2 - l0));
+  if (!ok || !ended) {
+    cudaGetLastError();
+    if (s != QDG_OK) return s;
+    return fail(QDG_ECUDA, "conditional graph unavailable");
+  }
+  P->graph_launches = l1 - l0;
+  P->body_launches = l2 - l1;
+  return QDG_OK;
+}
+
+template <typename T>
+qdg_status build_static_graph(qdg_prop *P, cplx<double> *psi, cudaGraphExec_t *exec) {
+  qdg_plan *p = P->plan;
+  cudaGraph_t g = nullptr;
+  const long long l0 = qdg::launch_counter();
+  CK(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeRelaxed));
+  qdg_status s = cheby_body<T>(P, psi);
+  cudaError_t ce = cudaStreamEndCapture(p->stream, &g);
+  const long long l1 = qdg::launch_counter();
+  qdg::add_launches(-(l1 - l0));
+  if (s != QDG_OK) { if (g) cudaGraphDestroy(g); return s; }
+  if (ce != cudaSuccess || cudaGraphInstantiate(exec, g, 0) != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    return fail(QDG_ECUDA, "stream capture unavailable");
+  }
+  cudaGraphDestroy(g);
+  P->graph_launches = l1 - l0;
+  P->body_launches = 0;
   return QDG_OK;
 }
 
@@ -653,28 +793,28 @@ qdg_status cheby_enqueue(qdg_prop *P, cplx<double> *psi, long long step) {
   if (p->profiling || !P->graphs_ok) return cheby_body<T>(P, psi);
   if (!P->graph || P->graph_psi != psi || P->graph_stream != p->stream) {
     if (P->graph) { cudaGraphExecDestroy(P->graph); P->graph = nullptr; }
-    cudaGraph_t g = nullptr;
-    const long long l0 = qdg::launch_counter();
-    CK(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeRelaxed));
-    qdg_status s = cheby_body<T>(P, psi);
-    cudaError_t ce = cudaStreamEndCapture(p->stream, &g);
-    if (s != QDG_OK) { if (g) cudaGraphDestroy(g); return s; }
-    if (ce != cudaSuccess || cudaGraphInstantiate(&P->graph, g, 0) != cudaSuccess) {
-      if (g) cudaGraphDestroy(g);
-      cudaGetLastError();
-      P->graph = nullptr;
-      P->graphs_ok = false;  // stream capture unavailable: launch the kernels one by one
-      return cheby_body<T>(P, psi);
+    qdg_status s = QDG_ECUDA;
+    if (P->while_ok) {
+      s = build_while_graph<T>(P, psi, &P->graph);
+      P->graph_is_while = s == QDG_OK;
+      if (s != QDG_OK) { P->while_ok = false; P->graph = nullptr; }
     }
-    cudaGraphDestroy(g);
-    P->graph_launches = qdg::launch_counter() - l0;
-    qdg::add_launches(-P->graph_launches);  // counted again at every replay
+    if (s != QDG_OK) {
+      s = build_static_graph<T>(P, psi, &P->graph);
+      P->graph_is_while = false;
+      if (s != QDG_OK) { P->graphs_ok = false; P->graph = nullptr; return cheby_body<T>(P, psi); }
+    }
     P->graph_psi = psi;
     P->graph_stream = p->stream;
   }
   CK(cudaGraphLaunch(P->graph, p->stream));
   qdg::add_launches(P->graph_launches);
   return QDG_OK;
+}
+
+// Kernels the while body ran: (terms - 2) term bodies per step.
+void count_body_launches(qdg_prop *P, long long terms, long long steps) {
+  if (P->graph && P->graph_is_while) qdg::add_launches(P->body_launches * std::max(0LL, terms - 2 * steps));
 }
 
 // ------------------------------------------------------------------ GSPO
@@ -952,6 +1092,7 @@ qdg_status prop_step_t(qdg_prop *P, cplx<double> *psi, long long step, int *used
       CK(cudaMemcpyAsync(P->h_cs, P->d_cs, sizeof(qdg::ChebyState), cudaMemcpyDeviceToHost, p->stream));
       CK(cudaStreamSynchronize(p->stream));
       if (used) *used = P->h_cs->terms;
+      count_body_launches(P, P->h_cs->terms, 1);
       if (P->h_cs->status == QDG_ENONFINITE) return fail(QDG_ENONFINITE, "Norm is not a number");
     }
     return QDG_OK;
@@ -1223,6 +1364,7 @@ qdg_status qdg_prop_destroy(qdg_prop *P) {
   if (P->k0) cudaFree(P->k0);
   if (P->k1) cudaFree(P->k1);
   if (P->graph) cudaGraphExecDestroy(P->graph);
+  if (P->d_coeffs) cudaFree(P->d_coeffs);
   if (P->d_cs) cudaFree(P->d_cs);
   if (P->h_cs) cudaFreeHost(P->h_cs);
   for (auto &g : P->gtab) for (auto v : g) if (v) cudaFree(v);
@@ -1287,6 +1429,7 @@ qdg_status qdg_prop_apply_host(qdg_prop *P, qdg_wf *scratch, double *host_psi, i
   CK(cudaStreamSynchronize(p->stream));
   if (P->kind == 1) {
     used = P->h_cs->terms;
+    count_body_launches(P, used, 1);
     if (P->h_cs->status == QDG_ENONFINITE) return fail(QDG_ENONFINITE, "Norm is not a number");
   }
   if (terms_used) *terms_used = used;
@@ -1316,6 +1459,7 @@ qdg_status qdg_prop_run(qdg_prop *P, qdg_wf *psi, int64_t step0, int32_t nsteps,
     CK(cudaMemcpy(P->h_cs, P->d_cs, sizeof(qdg::ChebyState), cudaMemcpyDeviceToHost));
     if (P->h_cs->status == QDG_ENONFINITE) return fail(QDG_ENONFINITE, "Norm is not a number");
     tot = P->h_cs->total - before;
+    count_body_launches(P, tot, nsteps);
   }
   if (terms_total) *terms_total = tot;
   return QDG_OK;

@@ -39,7 +39,7 @@ __device__ __forceinline__ void tile_coord(int idx, int TW, int N, int es, int &
 // let the last block to arrive sum all partials in block order and apply the
 // reference's series cut.  No block waits for another (threadfence
 // reduction: the last arriving block does the work).
-__device__ void cheby_term_finish(double acc, double *red, double *partials, const ChebyCut &cut) {
+__device__ void cheby_term_finish(double acc, double *red, double *partials, const ChebyCut &cut, int term) {
   __shared__ int am_last;
   const double t = block_sum(acc, red);
   if (threadIdx.x == 0) {
@@ -57,14 +57,24 @@ __device__ void cheby_term_finish(double acc, double *red, double *partials, con
   if (threadIdx.x != 0) return;
   ChebyState *cs = cut.cs;
   cs->arrive = 0;
-  if (!isfinite(tot)) { cs->status = 2; cs->done = 1; cs->terms = cut.first ? 2 : cut.term + 1; return; }
-  if (cut.first) { cs->norm0 = tot; return; }
-  if (!cut.imag) {
-    const double nconv = fabs(cs->norm0 - tot) / cs->norm0;
-    if (nconv < cut.prec && cut.offim0) { cs->done = 1; cs->terms = cut.term + 1; }
+  if (!isfinite(tot)) {
+    cs->status = 2; cs->done = 1; cs->terms = cut.first ? 2 : term + 1;
+  } else if (cut.first) {
+    cs->norm0 = tot;
+    cs->acc_last = tot;
+  } else if (!cut.imag) {
+    const double ref = cut.diff ? cs->acc_last : cs->norm0;
+    const double nconv = fabs(ref - tot) / cs->norm0;
+    if (nconv < cut.prec && cut.offim0) { cs->done = 1; cs->terms = term + 1; }
+    cs->acc_last = tot;
   } else {
-    if (fabs(tot - cs->norm_last) / cs->norm_last < cut.prec) { cs->done = 1; cs->terms = cut.term + 1; }
+    if (fabs(tot - cs->norm_last) / cs->norm_last < cut.prec) { cs->done = 1; cs->terms = term + 1; }
     cs->norm_last = tot;
+  }
+  if (cut.use_cond) {
+    const int next = cut.first ? 2 : term + 1;
+    if (cs->done || next >= cut.order) cudaGraphSetConditional(cut.cond, 0u);
+    else cs->i = next;
   }
 }
 
@@ -89,6 +99,16 @@ __global__ void __launch_bounds__(256) linepass_kernel(PassArgs<T> a) {
   const long long nitems = a.ntiles * nsplit;
   const long long npts = a.npts;
   const int S = (SS > 0) ? SS : a.S;
+  int term = a.cut.term;
+  const cplx<T> *phi = a.phi;
+  cplx<T> *kout = a.k0;
+  cplx<double> coeff = a.coeff;
+  if (a.cut.dyn) {
+    term = a.cut.cs->i;
+    phi = a.bufs[(term + 1) & 1];
+    kout = const_cast<cplx<T> *>(a.bufs[term & 1]);
+    coeff = a.cut.coeffs[term];
+  }
 
   for (long long item = blockIdx.x; item < nitems; item += gridDim.x) {
     const long long tile = item / nsplit;
@@ -103,7 +123,7 @@ __global__ void __launch_bounds__(256) linepass_kernel(PassArgs<T> a) {
       int w, i;
       tile_coord(idx - sl * tileN, TW, N, a.es, w, i);
       const long long p = base + (long long)w * a.ls + (long long)i * a.es;
-      b0[(sl * TW + w) * N + i] = ld(a.phi + (long long)(s0 + sl) * npts + p);
+      b0[(sl * TW + w) * N + i] = ld(phi + (long long)(s0 + sl) * npts + p);
     }
     __syncthreads();
 
@@ -149,7 +169,7 @@ __global__ void __launch_bounds__(256) linepass_kernel(PassArgs<T> a) {
 #pragma unroll
         for (int s = 0; s < ((SS > 0) ? SS : kMaxStates); ++s) {
           if (s < S) {
-            ph[s] = ld(a.phi + (long long)s * npts + p);
+            ph[s] = ld(phi + (long long)s * npts + p);
             h[s] = res[(s * TW + w) * N + i];
             if (a.multi_pass) h[s] = h[s] + ld(a.P + (long long)s * npts + p);
           }
@@ -179,13 +199,13 @@ __global__ void __launch_bounds__(256) linepass_kernel(PassArgs<T> a) {
             if (MODE == PM_CHEBY_FIRST) {
               const cplx<double> ps = ld(a.psi + g);
               acc += cabs2(ps);
-              st(a.k0 + g, ccast<T>(bf));                      // phi_1
+              st(kout + g, ccast<T>(bf));                      // phi_1
               st(a.psi + g, dmul(ps, a.c0p) + dmul(bf, a.c1p)); // psi*c0 + phi_1*c1
             } else {
-              const cplx<double> km2 = ccast<double>(ld(a.k0 + g));
+              const cplx<double> km2 = ccast<double>(ld(kout + g));
               const cplx<double> k2 = a.imag ? bf - km2 : bf + km2;
-              st(a.k0 + g, ccast<T>(k2));
-              const cplx<double> ps = ld(a.psi + g) + dmul(k2, a.coeff);
+              st(kout + g, ccast<T>(k2));
+              const cplx<double> ps = ld(a.psi + g) + dmul(k2, coeff);
               st(a.psi + g, ps);
               acc += cabs2(ps);
             }
@@ -195,7 +215,7 @@ __global__ void __launch_bounds__(256) linepass_kernel(PassArgs<T> a) {
     }
     __syncthreads();
   }
-  if (MODE == PM_CHEBY_FIRST || MODE == PM_CHEBY_TERM) cheby_term_finish(acc, red, a.partials, a.cut);
+  if (MODE == PM_CHEBY_FIRST || MODE == PM_CHEBY_TERM) cheby_term_finish(acc, red, a.partials, a.cut, term);
 }
 
 // ------------------------------------------------ all-dimension kinetic pass
@@ -205,6 +225,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) kin_all_kernel(KinArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   if (a.done != nullptr && *a.done) return;
+  const cplx<T> *phi = a.dyn ? a.bufs[(a.cs->i + 1) & 1] : a.phi;
   const long long nitems = a.item_start[a.nd];
   const long long npts = a.npts;
   int cur_dim = -1;
@@ -227,7 +248,7 @@ __global__ void __launch_bounds__(256) kin_all_kernel(KinArgs<T> a) {
     const long long hi = tile / g.tiles_per_hi;
     const long long base = hi * g.hi_stride + (tile - hi * g.tiles_per_hi) * TW;
     const int tileN = TW * N;
-    const cplx<T> *src = a.phi + (long long)s * npts;
+    const cplx<T> *src = phi + (long long)s * npts;
     for (int idx = threadIdx.x; idx < tileN; idx += blockDim.x) {
       int w, i;
       tile_coord(idx, TW, N, g.es, w, i);
@@ -264,13 +285,23 @@ __global__ void __launch_bounds__(256) combine_kernel(CombArgs<T> a) {
   const int S = (SS > 0) ? SS : a.S;
   constexpr int SM = (SS > 0) ? SS : kMaxStates;
   double acc = 0.0;
+  int term = a.cut.term;
+  const cplx<T> *phi = a.phi;
+  cplx<T> *kout = a.k0;
+  cplx<double> coeff = a.coeff;
+  if (a.cut.dyn) {
+    term = a.cut.cs->i;
+    phi = a.bufs[(term + 1) & 1];
+    kout = const_cast<cplx<T> *>(a.bufs[term & 1]);
+    coeff = a.cut.coeffs[term];
+  }
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npts; p += (long long)gridDim.x * blockDim.x) {
     cplx<T> ph[SM], h[SM];
 #pragma unroll
     for (int s = 0; s < SM; ++s) {
       if (s < S) {
         const long long g = (long long)s * npts + p;
-        ph[s] = ld(a.phi + g);
+        ph[s] = ld(phi + g);
         cplx<T> v = ld(a.P[0] + g);
         for (int d = 1; d < a.nd; ++d) v = v + ld(a.P[d] + g);
         h[s] = v;
@@ -299,20 +330,20 @@ __global__ void __launch_bounds__(256) combine_kernel(CombArgs<T> a) {
         if (MODE == PM_CHEBY_FIRST) {
           const cplx<double> ps = ld(a.psi + g);
           acc += cabs2(ps);
-          st(a.k0 + g, ccast<T>(bf));
+          st(kout + g, ccast<T>(bf));
           st(a.psi + g, dmul(ps, a.c0p) + dmul(bf, a.c1p));
         } else {
-          const cplx<double> km2 = ccast<double>(ld(a.k0 + g));
+          const cplx<double> km2 = ccast<double>(ld(kout + g));
           const cplx<double> k2 = a.imag ? bf - km2 : bf + km2;
-          st(a.k0 + g, ccast<T>(k2));
-          const cplx<double> ps = ld(a.psi + g) + dmul(k2, a.coeff);
+          st(kout + g, ccast<T>(k2));
+          const cplx<double> ps = ld(a.psi + g) + dmul(k2, coeff);
           st(a.psi + g, ps);
           acc += cabs2(ps);
         }
       }
     }
   }
-  if (MODE == PM_CHEBY_FIRST || MODE == PM_CHEBY_TERM) cheby_term_finish(acc, red, a.partials, a.cut);
+  if (MODE == PM_CHEBY_FIRST || MODE == PM_CHEBY_TERM) cheby_term_finish(acc, red, a.partials, a.cut, term);
 }
 
 template <typename T>
@@ -407,8 +438,10 @@ template int pass_max_blocks<double>(int, int, int, size_t);
 template int pass_max_blocks<float>(int, int, int, size_t);
 
 // ---------------------------------------------------------------- control
-__global__ void cheby_begin_kernel(ChebyState *cs, int order) {
+__global__ void cheby_begin_kernel(ChebyState *cs, int order, unsigned long long cond, int use_cond) {
   cs->norm0 = 0; cs->norm_last = 0; cs->done = 0; cs->terms = order; cs->status = 0; cs->arrive = 0;
+  cs->i = 2; cs->acc_last = 0;
+  if (use_cond) cudaGraphSetConditional(cond, order > 2 ? 1u : 0u);
 }
 
 // Sums the per-block norms in a fixed order and applies the reference's
@@ -432,8 +465,8 @@ __global__ void cheby_finalize_kernel(ChebyState *cs, const double *partials, in
   }
 }
 
-cudaError_t launch_cheby_begin(ChebyState *cs, int order, cudaStream_t st) {
-  cheby_begin_kernel<<<1, 1, 0, st>>>(cs, order);
+cudaError_t launch_cheby_begin(ChebyState *cs, int order, unsigned long long cond, int use_cond, cudaStream_t st) {
+  cheby_begin_kernel<<<1, 1, 0, st>>>(cs, order, cond, use_cond);
   COUNT_LAUNCH();
   return cudaGetLastError();
 }

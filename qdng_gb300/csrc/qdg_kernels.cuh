@@ -42,6 +42,8 @@ struct ChebyState {
   int terms;         // terms used in the step
   int status;        // QDG_OK or QDG_ENONFINITE
   unsigned int arrive;  // blocks of the current reduction that have stored their partial sum
+  int i;             // index of the next term (device-driven term loop)
+  double acc_last;   // accumulated norm after the previous term (differential cut)
 };
 
 // Series-cut parameters handed to the kernel that finishes a Chebyshev term:
@@ -50,10 +52,17 @@ struct ChebyState {
 struct ChebyCut {
   ChebyState *cs;   // nullptr: no reduction (H apply)
   int first;        // 1: raw norm of psi before the step (OCheby::raw_norm)
-  int term;         // index i of the term just added
+  int term;         // index i of the term just added (static launches)
   double prec;
   int imag;
   int offim0;       // offset has no imaginary part (break allowed)
+  int diff;         // mixed precision: compare with the previous term's norm, not the initial one
+  // device-driven term loop (one graph body per term inside a while node)
+  int dyn;                      // take the term index from cs->i and the buffers by its parity
+  int order;
+  const cplx<double> *coeffs;   // [order] coeff[i] exp(c0 offset)
+  unsigned long long cond;      // cudaGraphConditionalHandle of the while node
+  int use_cond;
 };
 
 template <typename T>
@@ -92,6 +101,7 @@ struct PassArgs {
   double *partials;        // per-block partial sums (norms)
   const int *done;         // Chebyshev series converged: skip the work
   ChebyCut cut;            // fused series cut (Chebyshev modes)
+  const cplx<T> *bufs[2];  // device-driven term loop: phi = bufs[(i+1)&1], k0 = bufs[i&1]
   // GSPO kinetic member: per-state exp(c T_d(k)) / N_d tables, S x N entries
   const cplx<T> *gtab;
 };
@@ -117,6 +127,10 @@ struct KinArgs {
   DimPass<T> dp[4];
   long long item_start[5];  // first work item of each dimension
   const int *done;
+  // device-driven term loop: phi = bufs[(cs->i + 1) & 1]
+  const ChebyState *cs;
+  const cplx<T> *bufs[2];
+  int dyn;
 };
 
 // Point-wise finish of H phi: sum_d T_d phi + potential matrix, then the
@@ -137,6 +151,7 @@ struct CombArgs {
   int imag;
   double *partials;
   ChebyCut cut;
+  const cplx<T> *bufs[2];  // device-driven term loop: phi = bufs[(i+1)&1], k0 = bufs[i&1]
 };
 
 template <typename T>
@@ -163,7 +178,7 @@ int pass_max_blocks(int mode, int S, int block, size_t smem);
 
 cudaError_t launch_cheby_finalize(ChebyState *cs, const double *partials, int nparts, int first, int term,
                                   int order, double prec, int imag, int offset_imag_zero, cudaStream_t st);
-cudaError_t launch_cheby_begin(ChebyState *cs, int order, cudaStream_t st);
+cudaError_t launch_cheby_begin(ChebyState *cs, int order, unsigned long long cond, int use_cond, cudaStream_t st);
 cudaError_t launch_cheby_end(ChebyState *cs, cudaStream_t st);
 
 // psi (FP64) -> phi (T) copy (OCheby: ket0->FastCopy(*Psi))
