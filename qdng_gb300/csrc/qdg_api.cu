@@ -92,6 +92,8 @@ struct qdg_plan {
   void *d_scratch2 = nullptr;
   double *d_partials = nullptr;
   int max_parts = 0;
+  qdg::GridBarrier *d_bar = nullptr;
+  qdg::GridBarrier *h_bar = nullptr;  // pinned copy for the timeout check
   double *h_partials = nullptr;  // pinned
   cudaStream_t stream = nullptr;
   bool own_stream = false;
@@ -139,6 +141,10 @@ struct qdg_prop {
   bool while_ok = true;             // device-driven term loop (conditional while node)
   bool graph_is_while = false;
   cplx<double> *d_coeffs = nullptr; // coeff[i] exp(c0 offset), i < order
+  double *d_a = nullptr;            // real coefficients coeff[i]
+  int step_grid = 0;                // persistent step kernel: blocks (0: unavailable)
+  size_t step_smem = 0;
+  int step_tw1 = 1;
   // GSPO
   int ngroups = 0;
   std::vector<int> group_kinetic;     // 1: FFT member, 0: potential member
@@ -478,6 +484,8 @@ void free_plan(qdg_plan *p) {
   if (p->d_scratch) cudaFree(p->d_scratch);
   if (p->d_scratch2) cudaFree(p->d_scratch2);
   if (p->d_partials) cudaFree(p->d_partials);
+  if (p->d_bar) cudaFree(p->d_bar);
+  if (p->h_bar) cudaFreeHost(p->h_bar);
   if (p->h_partials) cudaFreeHost(p->h_partials);
   if (p->own_stream && p->stream) cudaStreamDestroy(p->stream);
   for (auto e : p->ev_pool) cudaEventDestroy(e);
@@ -564,6 +572,83 @@ qdg_status h_apply_bulk(qdg_plan *p, const cplx<double> *psi, cplx<T> *out, long
 }
 
 // ------------------------------------------------------------ Chebyshev
+// Persistent step kernel configuration (cooperative launch: every block
+// resident).  step_grid stays 0 when the kernel cannot be made resident.
+template <typename T>
+qdg_status step_setup(qdg_prop *P) {
+  qdg_plan *p = P->plan;
+  const char *env = getenv("QDG_CHEBY_MODE");
+  if (env && strcmp(env, "graph") == 0) return QDG_OK;
+  size_t smem = 0;
+  if (p->nd == 1) {
+    P->step_tw1 = p->dim[0].TW_e;
+    smem = pass_smem(p, 0, P->step_tw1, p->S);
+  } else {
+    for (int d = 0; d < p->nd; ++d) smem = std::max(smem, pass_smem(p, d, p->dim[d].TW_k, 1));
+  }
+  if (smem > 227 * 1024) return QDG_OK;
+  const int per_sm = qdg::cheby_step_max_blocks<T>(p->S, 256, smem);
+  if (per_sm <= 0) return QDG_OK;
+  long long want;
+  if (p->nd == 1) want = p->npts / ((long long)p->dim[0].n * P->step_tw1);
+  else want = (long long)per_sm * p->sm_count;
+  want = std::min<long long>(want, (long long)per_sm * p->sm_count);
+  want = std::min<long long>(want, p->max_parts);
+  P->step_grid = (int)std::max<long long>(1, want);
+  P->step_smem = smem;
+  return QDG_OK;
+}
+
+template <typename T>
+qdg_status cheby_step_persistent(qdg_prop *P, cplx<double> *psi, long long step) {
+  qdg_plan *p = P->plan;
+  CK(qdg::launch_set_coefs(p->d_coef, p->d_cp, p->d_lasers, p->laser_nt, step, p->stream));
+  qdg::StepArgs<T> a;
+  memset(&a, 0, sizeof(a));
+  a.nd = p->nd;
+  a.S = p->S;
+  a.npts = p->npts;
+  long long items = 0;
+  for (int d = 0; d < p->nd; ++d) {
+    qdg::PassArgs<T> g;
+    memset(&g, 0, sizeof(g));
+    fill_geometry<T>(p, d, 1, g);
+    qdg::DimPass<T> &dp = a.dp[d];
+    dp.N = g.N; dp.es = g.es; dp.ls = g.ls; dp.TW = g.TW; dp.tiles_per_hi = g.tiles_per_hi;
+    dp.hi_stride = g.hi_stride; dp.ntiles = g.ntiles; dp.rp = g.rp; dp.tw = g.tw; dp.kfac = g.kfac;
+    dp.P = reinterpret_cast<cplx<T> *>(p->d_Pd[d]);
+    a.item_start[d] = items;
+    items += g.ntiles * p->S;
+  }
+  a.item_start[p->nd] = items;
+  a.TW1 = P->step_tw1;
+  a.psi = psi;
+  a.buf[0] = reinterpret_cast<cplx<T> *>(P->k0);
+  a.buf[1] = reinterpret_cast<cplx<T> *>(P->k1);
+  a.cp = p->d_cp;
+  a.coef = p->d_coef;
+  a.grids = reinterpret_cast<const T *>(p->d_grids);
+  const cd ex = P->c0 / P->dt;
+  a.offset = C(P->offset);
+  a.fac1 = C(ex / P->scaling);
+  a.fac = C(2.0 * ex / P->scaling);
+  a.ph = C(std::exp(P->c0 * P->offset));
+  a.a = P->d_a;
+  a.order = P->order;
+  a.prec = P->prec;
+  a.imag = P->imag ? 1 : 0;
+  a.offim0 = P->offset.imag() == 0 ? 1 : 0;
+  a.diff = p->precision == QDG_PREC_MIXED ? 1 : 0;
+  a.partials = p->d_partials;
+  a.cs = P->d_cs;
+  a.bar = p->d_bar;
+  size_t slot = 0;
+  qdg_status s = prof_begin<T>(p, 6, &slot);
+  if (s != QDG_OK) return s;
+  CK(qdg::launch_cheby_step<T>(a, P->step_grid, 256, P->step_smem, p->stream));
+  return prof_end(p, slot);
+}
+
 // OCheby::Init (src/qdlib/OCheby.cpp:358-493).
 qdg_status cheby_init(qdg_prop *P) {
   qdg_plan *p = P->plan;
@@ -616,7 +701,11 @@ qdg_status cheby_init(qdg_prop *P) {
     for (int i = 0; i < P->order; ++i) hc[i] = C(P->coeff[i] * ph);
     CK(cudaMalloc(&P->d_coeffs, sizeof(cplx<double>) * P->order));
     CK(cudaMemcpy(P->d_coeffs, hc.data(), sizeof(cplx<double>) * P->order, cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&P->d_a, sizeof(double) * P->order));
+    CK(cudaMemcpy(P->d_a, P->coeff.data(), sizeof(double) * P->order, cudaMemcpyHostToDevice));
   }
+  qdg_status ps = p->precision == QDG_PREC_FP64 ? step_setup<double>(P) : step_setup<float>(P);
+  if (ps != QDG_OK) return ps;
   CK(cudaMallocHost(&P->h_cs, sizeof(qdg::ChebyState)));
   return QDG_OK;
 }
@@ -809,6 +898,17 @@ qdg_status cheby_enqueue(qdg_prop *P, cplx<double> *psi, long long step) {
   }
   CK(cudaGraphLaunch(P->graph, p->stream));
   qdg::add_launches(P->graph_launches);
+  return QDG_OK;
+}
+
+// After a synchronisation: did a grid barrier of the step kernel time out?
+qdg_status check_barrier(qdg_plan *p) {
+  CK(cudaMemcpy(p->h_bar, p->d_bar, sizeof(qdg::GridBarrier), cudaMemcpyDeviceToHost));
+  if (p->h_bar->err) {
+    qdg::GridBarrier z{};
+    CK(cudaMemcpy(p->d_bar, &z, sizeof(z), cudaMemcpyHostToDevice));
+    return fail(QDG_ETIMEOUT, "grid barrier of the Chebyshev step kernel timed out");
+  }
   return QDG_OK;
 }
 
@@ -1086,13 +1186,14 @@ template <typename T>
 qdg_status prop_step_t(qdg_prop *P, cplx<double> *psi, long long step, int *used, bool sync) {
   qdg_plan *p = P->plan;
   if (P->kind == 1) {
-    qdg_status s = cheby_enqueue<T>(P, psi, step);
+    qdg_status s = P->step_grid > 0 ? cheby_step_persistent<T>(P, psi, step) : cheby_enqueue<T>(P, psi, step);
     if (s != QDG_OK) return s;
     if (sync) {
       CK(cudaMemcpyAsync(P->h_cs, P->d_cs, sizeof(qdg::ChebyState), cudaMemcpyDeviceToHost, p->stream));
       CK(cudaStreamSynchronize(p->stream));
       if (used) *used = P->h_cs->terms;
       count_body_launches(P, P->h_cs->terms, 1);
+      if (P->step_grid > 0) { qdg_status sb = check_barrier(p); if (sb != QDG_OK) return sb; }
       if (P->h_cs->status == QDG_ENONFINITE) return fail(QDG_ENONFINITE, "Norm is not a number");
     }
     return QDG_OK;
@@ -1192,6 +1293,10 @@ qdg_status qdg_plan_create(const qdg_hplan_desc *desc, int32_t precision, qdg_pl
   p->max_parts = std::max(4096, 2 * qdg::kMaxStates * 2 * p->sm_count);
   if (cudaMalloc(&p->d_partials, sizeof(double) * 2 * qdg::kMaxStates * p->max_parts) != cudaSuccess ||
       cudaMallocHost(&p->h_partials, sizeof(double) * 2 * qdg::kMaxStates * p->max_parts) != cudaSuccess)
+    return cleanup(fail(QDG_ENOMEM, "device allocation failed"));
+  if (cudaMalloc(&p->d_bar, sizeof(qdg::GridBarrier)) != cudaSuccess ||
+      cudaMemset(p->d_bar, 0, sizeof(qdg::GridBarrier)) != cudaSuccess ||
+      cudaMallocHost(&p->h_bar, sizeof(qdg::GridBarrier)) != cudaSuccess)
     return cleanup(fail(QDG_ENOMEM, "device allocation failed"));
   s = precision == QDG_PREC_FP64 ? upload_tables<double>(p) : upload_tables<float>(p);
   if (s != QDG_OK) return cleanup(s);
@@ -1365,6 +1470,7 @@ qdg_status qdg_prop_destroy(qdg_prop *P) {
   if (P->k1) cudaFree(P->k1);
   if (P->graph) cudaGraphExecDestroy(P->graph);
   if (P->d_coeffs) cudaFree(P->d_coeffs);
+  if (P->d_a) cudaFree(P->d_a);
   if (P->d_cs) cudaFree(P->d_cs);
   if (P->h_cs) cudaFreeHost(P->h_cs);
   for (auto &g : P->gtab) for (auto v : g) if (v) cudaFree(v);
@@ -1430,6 +1536,7 @@ qdg_status qdg_prop_apply_host(qdg_prop *P, qdg_wf *scratch, double *host_psi, i
   if (P->kind == 1) {
     used = P->h_cs->terms;
     count_body_launches(P, used, 1);
+    if (P->step_grid > 0) { qdg_status sb = check_barrier(p); if (sb != QDG_OK) return sb; }
     if (P->h_cs->status == QDG_ENONFINITE) return fail(QDG_ENONFINITE, "Norm is not a number");
   }
   if (terms_used) *terms_used = used;
@@ -1460,6 +1567,7 @@ qdg_status qdg_prop_run(qdg_prop *P, qdg_wf *psi, int64_t step0, int32_t nsteps,
     if (P->h_cs->status == QDG_ENONFINITE) return fail(QDG_ENONFINITE, "Norm is not a number");
     tot = P->h_cs->total - before;
     count_body_launches(P, tot, nsteps);
+    if (P->step_grid > 0) { qdg_status sb = check_barrier(P->plan); if (sb != QDG_OK) return sb; }
   }
   if (terms_total) *terms_total = tot;
   return QDG_OK;

@@ -130,6 +130,14 @@ __device__ int fft_lines(cplx<T> *buf0, cplx<T> *buf1, const RadixPlan &rp, int 
   return cur;
 }
 
+// Point (w, i) of a tile of TW lines from a flat index: consecutive indices
+// walk the contiguous direction in memory (along the line when es == 1,
+// across the TW lines otherwise) so that global accesses coalesce.
+__device__ __forceinline__ void tile_coord(int idx, int TW, int N, int es, int &w, int &i) {
+  if (es == 1) { w = idx / N; i = idx - w * N; }
+  else { i = idx / TW; w = idx - i * TW; }
+}
+
 // Deterministic block sum of one double per thread (fixed shuffle tree).
 __device__ __forceinline__ double block_sum(double v, double *red) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);

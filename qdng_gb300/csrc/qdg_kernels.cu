@@ -27,13 +27,6 @@ void add_launches(long long n) { g_launches.fetch_add(n); }
 
 __device__ __forceinline__ cplx<double> dmul(cplx<double> a, cplx<double> b) { return cmul(a, b); }
 
-// Point (w, i) of a tile from a flat index: consecutive indices walk the
-// contiguous direction in memory (along the line when es == 1, across the
-// TW lines otherwise) so global accesses coalesce.
-__device__ __forceinline__ void tile_coord(int idx, int TW, int N, int es, int &w, int &i) {
-  if (es == 1) { w = idx / N; i = idx - w * N; }
-  else { i = idx / TW; w = idx - i * TW; }
-}
 
 // Block-level end of a Chebyshev term: store this block's norm partial, and
 // let the last block to arrive sum all partials in block order and apply the

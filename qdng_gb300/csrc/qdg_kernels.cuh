@@ -154,6 +154,45 @@ struct CombArgs {
   const cplx<T> *bufs[2];  // device-driven term loop: phi = bufs[(i+1)&1], k0 = bufs[i&1]
 };
 
+// Grid-wide barrier state of the persistent step kernel (device memory,
+// zeroed once; the last block of each barrier resets `count`).
+struct GridBarrier {
+  unsigned int count;
+  unsigned int gen;
+  int err;   // a block gave up waiting (bounded spin)
+  int pad;
+};
+// Polls of a barrier flag before a block gives up (~0.3 s with back-off).
+static const unsigned int kBarrierSpinLimit = 1u << 22;
+
+// One Chebyshev step in one cooperative launch (qdg_persistent.cu).
+template <typename T>
+struct StepArgs {
+  int nd, S;
+  long long npts;
+  DimPass<T> dp[4];          // kinetic passes (P_d outputs); dp[0] also the 1-D line geometry
+  long long item_start[5];
+  int TW1;                   // 1-D grids: lines per tile (all states in one block)
+  cplx<double> *psi;
+  cplx<T> *buf[2];           // phi buffers (ket0 / ket1)
+  const Couplings *cp;
+  const double *coef;
+  const T *grids;
+  cplx<double> offset, fac1, fac, ph;  // offset, exp/scaling, 2 exp/scaling, exp(c0 offset)
+  const double *a;           // real series coefficients a_i (J_0, 2 J_i / I_0, 2 I_i)
+  int order;
+  double prec;
+  int imag, offim0, diff;
+  double *partials;
+  ChebyState *cs;
+  GridBarrier *bar;
+};
+
+template <typename T>
+int cheby_step_max_blocks(int S, int block, size_t smem);
+template <typename T>
+cudaError_t launch_cheby_step(const StepArgs<T> &a, int grid, int block, size_t smem, cudaStream_t st);
+
 template <typename T>
 cudaError_t launch_kin_all(const KinArgs<T> &a, int grid, int block, size_t smem, cudaStream_t st);
 template <typename T>

@@ -1,0 +1,356 @@
+// qdg_persistent.cu -- one Chebyshev time step as one persistent kernel.
+//
+// The step of OCheby::real_time_step / imag_time_step
+// (src/qdlib/OCheby.cpp:92-297) is a chain of up to `order` dependent
+// Hamiltonian applications, each far shorter than a kernel launch on a
+// 256x256 grid.  Here every block of a cooperative launch (all blocks
+// resident by construction) walks the whole series:
+//
+//   psi -> phi_0;                                         grid barrier
+//   term 1: T_d phi_0 for every d (FFT line items);       grid barrier
+//           H phi_0, phi_1, psi = a_0 psi + a_1 phi_1;    grid barrier + norm sum
+//   term i: T_d phi_{i-1} ...;                            grid barrier
+//           phi_i = 2 X (H - E) phi_{i-1} +- phi_{i-2}, psi += a_i phi_i,
+//           norm of psi;                                  grid barrier + norm sum
+//   ... until the reference's norm cut; psi *= exp(c0 offset).
+//
+// Every block sums the per-block norms in the same order, so all blocks
+// take the same decision without another barrier.  The coefficients a_i are
+// real (2 J_i or 2 I_i); the common phase exp(c0 offset) that the reference
+// folds into each of them (OCheby.cpp:107,122) is applied once at the end.
+// One-dimensional grids fuse the FFT and the point work of a line (a block
+// owns its lines for the whole step), leaving one barrier per term.
+// Grid barriers spin with an iteration limit; on timeout a flag is raised
+// and the kernel returns (the host reports QDG_ETIMEOUT).
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "qdg_kernels.cuh"
+
+namespace qdg {
+
+__device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int *p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Sense-free generation barrier over all blocks of the grid.  Returns false
+// when any block gave up waiting (then every block leaves the step).
+__device__ bool grid_sync(GridBarrier *b) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned int g = ld_acquire_u32(&b->gen);
+    __threadfence();
+    const unsigned int arrived = atomicAdd(&b->count, 1u);
+    if (arrived == gridDim.x - 1) {
+      atomicExch(&b->count, 0u);
+      __threadfence();
+      atomicAdd(&b->gen, 1u);
+    } else {
+      unsigned int spins = 0;
+      while (ld_acquire_u32(&b->gen) == g) {
+        if (++spins > kBarrierSpinLimit) {
+          atomicExch(&b->err, 1);
+          break;
+        }
+        __nanosleep(40);
+      }
+    }
+    __threadfence();
+    ok = atomicAdd(&b->err, 0) == 0;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// sum of the per-block partials, same order in every block; valid on thread 0
+__device__ double sum_partials(const double *partials, double *red) {
+  double v = 0.0;
+  for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) v += __ldcg(partials + i);
+  return block_sum(v, red);
+}
+
+// T_d phi for every dimension: items (dimension, tile, state) over the grid.
+template <typename T>
+__device__ void phase_kinetic(const StepArgs<T> &a, const cplx<T> *phi, cplx<T> *smem) {
+  const long long nitems = a.item_start[a.nd];
+  int cur_dim = -1;
+  cplx<T> *tws = smem;
+  for (long long item = blockIdx.x; item < nitems; item += gridDim.x) {
+    int d = 0;
+    while (item >= a.item_start[d + 1]) ++d;
+    const DimPass<T> &g = a.dp[d];
+    const int N = g.N, TW = g.TW;
+    cplx<T> *b0 = tws + N;
+    cplx<T> *b1 = b0 + (size_t)TW * N;
+    __syncthreads();
+    if (d != cur_dim) {
+      for (int i = threadIdx.x; i < N; i += blockDim.x) tws[i] = g.tw[i];
+      cur_dim = d;
+    }
+    const long long local = item - a.item_start[d];
+    const long long tile = local / a.S;
+    const int s = (int)(local - tile * a.S);
+    const long long hi = tile / g.tiles_per_hi;
+    const long long base = hi * g.hi_stride + (tile - hi * g.tiles_per_hi) * TW;
+    const int tileN = TW * N;
+    const cplx<T> *src = phi + (long long)s * a.npts;
+    for (int idx = threadIdx.x; idx < tileN; idx += blockDim.x) {
+      int w, i;
+      tile_coord(idx, TW, N, g.es, w, i);
+      b0[w * N + i] = ld(src + base + (long long)w * g.ls + (long long)i * g.es);
+    }
+    __syncthreads();
+    const int cur = fft_lines<T>(b0, b1, g.rp, TW, tws, -1);
+    cplx<T> *bc = cur ? b1 : b0;
+    const double kf = g.kfac[s];
+    for (int idx = threadIdx.x; idx < tileN; idx += blockDim.x) {
+      const int i = idx % N;
+      const int kq = min(i, N - i);
+      bc[idx] = cmulr(bc[idx], (T)(kf * (double)kq * (double)kq));
+    }
+    __syncthreads();
+    const int cur2 = fft_lines<T>(bc, cur ? b0 : b1, g.rp, TW, tws, +1);
+    const cplx<T> *res = cur2 ? (cur ? b0 : b1) : bc;
+    cplx<T> *dst = g.P + (long long)s * a.npts;
+    for (int idx = threadIdx.x; idx < tileN; idx += blockDim.x) {
+      int w, i;
+      tile_coord(idx, TW, N, g.es, w, i);
+      st(dst + base + (long long)w * g.ls + (long long)i * g.es, res[w * N + i]);
+    }
+  }
+  __syncthreads();
+}
+
+// Point work of one term at point p for all states: H phi from the kinetic
+// parts h[] and the potential matrix, then the recurrence.
+template <typename T, int SM, bool FIRST>
+__device__ __forceinline__ void point_term(const StepArgs<T> &a, long long p, const cplx<T> *ph, cplx<T> *h,
+                                           cplx<T> *kout, double coeff_i, int S, double &acc) {
+  const int ne = a.cp->ne;
+  for (int e = 0; e < ne; ++e) {
+    const int r = a.cp->row[e], c = a.cp->col[e];
+    const T v = (T)(a.coef[e]) * a.grids[(long long)a.cp->gid[e] * a.npts + p];
+#pragma unroll
+    for (int s = 0; s < SM; ++s)
+      if (s == r) {
+#pragma unroll
+        for (int q = 0; q < SM; ++q)
+          if (q == c) h[s] = h[s] + cmulr(ph[q], v);
+      }
+  }
+  const cplx<T> off = ccast<T>(a.offset);
+#pragma unroll
+  for (int s = 0; s < SM; ++s) {
+    if (s >= S) break;
+    const long long g = (long long)s * a.npts + p;
+    if (FIRST) {
+      const cplx<T> bf = cmul(h[s] - cmul(off, ph[s]), ccast<T>(a.fac1));
+      const cplx<double> ps = ld(a.psi + g);
+      acc += cabs2(ps);
+      st(kout + g, bf);
+      const cplx<double> b = ccast<double>(bf);
+      st(a.psi + g, mk(ps.re * a.a[0] + b.re * a.a[1], ps.im * a.a[0] + b.im * a.a[1]));
+    } else {
+      const cplx<T> bf = cmul(h[s] - cmul(off, ph[s]), ccast<T>(a.fac));
+      const cplx<T> km2 = ld(kout + g);
+      const cplx<T> k2 = a.imag ? bf - km2 : bf + km2;
+      st(kout + g, k2);
+      cplx<double> ps = ld(a.psi + g);
+      ps.re += coeff_i * (double)k2.re;
+      ps.im += coeff_i * (double)k2.im;
+      st(a.psi + g, ps);
+      acc += cabs2(ps);
+    }
+  }
+}
+
+// Point-wise part of a term on a grid of two or more dimensions.
+template <typename T, int SS, bool FIRST>
+__device__ void phase_points(const StepArgs<T> &a, const cplx<T> *phi, cplx<T> *kout, double coeff_i,
+                             double &acc) {
+  constexpr int SM = (SS > 0) ? SS : kMaxStates;
+  const int S = (SS > 0) ? SS : a.S;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < a.npts;
+       p += (long long)gridDim.x * blockDim.x) {
+    cplx<T> ph[SM], h[SM];
+#pragma unroll
+    for (int s = 0; s < SM; ++s) {
+      if (s < S) {
+        const long long g = (long long)s * a.npts + p;
+        ph[s] = ld(phi + g);
+        cplx<T> v = ld(a.dp[0].P + g);
+        for (int d = 1; d < a.nd; ++d) v = v + ld(a.dp[d].P + g);
+        h[s] = v;
+      }
+    }
+    point_term<T, SM, FIRST>(a, p, ph, h, kout, coeff_i, S, acc);
+  }
+}
+
+// One-dimensional grid: FFT, k^2, inverse FFT and point work of a tile of
+// lines for all states in one block.
+template <typename T, int SS, bool FIRST>
+__device__ void phase_lines(const StepArgs<T> &a, const cplx<T> *phi, cplx<T> *kout, double coeff_i, double &acc,
+                            cplx<T> *smem) {
+  constexpr int SM = (SS > 0) ? SS : kMaxStates;
+  const int S = (SS > 0) ? SS : a.S;
+  const DimPass<T> &g = a.dp[0];
+  const int N = g.N, TW = a.TW1;
+  const int L = TW * S;
+  cplx<T> *tws = smem;
+  cplx<T> *b0 = tws + N;
+  cplx<T> *b1 = b0 + (size_t)L * N;
+  const long long ntiles = a.npts / ((long long)N * TW);
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const long long base = tile * TW * N;
+    __syncthreads();
+    for (int i = threadIdx.x; i < N; i += blockDim.x) tws[i] = g.tw[i];
+    for (int idx = threadIdx.x; idx < L * N; idx += blockDim.x) {
+      const int l = idx / N, i = idx - l * N;
+      const int s = l / TW, w = l - s * TW;
+      b0[idx] = ld(phi + (long long)s * a.npts + base + (long long)w * N + i);
+    }
+    __syncthreads();
+    const int cur = fft_lines<T>(b0, b1, g.rp, L, tws, -1);
+    cplx<T> *bc = cur ? b1 : b0;
+    for (int idx = threadIdx.x; idx < L * N; idx += blockDim.x) {
+      const int l = idx / N, i = idx - l * N;
+      const int kq = min(i, N - i);
+      bc[idx] = cmulr(bc[idx], (T)(g.kfac[l / TW] * (double)kq * (double)kq));
+    }
+    __syncthreads();
+    const int cur2 = fft_lines<T>(bc, cur ? b0 : b1, g.rp, L, tws, +1);
+    const cplx<T> *res = cur2 ? (cur ? b0 : b1) : bc;
+    for (int idx = threadIdx.x; idx < TW * N; idx += blockDim.x) {
+      const int w = idx / N, i = idx - w * N;
+      const long long p = base + (long long)w * N + i;
+      cplx<T> ph[SM], h[SM];
+#pragma unroll
+      for (int s = 0; s < SM; ++s)
+        if (s < S) {
+          ph[s] = ld(phi + (long long)s * a.npts + p);
+          h[s] = res[(s * TW + w) * N + i];
+        }
+      point_term<T, SM, FIRST>(a, p, ph, h, kout, coeff_i, S, acc);
+    }
+  }
+  __syncthreads();
+}
+
+template <typename T, int SS>
+__global__ void __launch_bounds__(256) cheby_step_kernel(StepArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double red[32];
+  __shared__ double tot_s;
+  cplx<T> *smem = reinterpret_cast<cplx<T> *>(smem_raw);
+  const long long n = a.npts * a.S;
+  const long long gtid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long gstride = (long long)gridDim.x * blockDim.x;
+
+  // phi_0 = psi (OCheby: ket0->FastCopy(*Psi))
+  for (long long i = gtid; i < n; i += gstride) st(a.buf[0] + i, ccast<T>(ld(a.psi + i)));
+  if (!grid_sync(a.bar)) return;
+
+  // first two terms; the reduction gives the raw norm of psi before the step
+  double acc = 0.0;
+  if (a.nd == 1) {
+    phase_lines<T, SS, true>(a, a.buf[0], a.buf[1], 0.0, acc, smem);
+  } else {
+    phase_kinetic<T>(a, a.buf[0], smem);
+    if (!grid_sync(a.bar)) return;
+    phase_points<T, SS, true>(a, a.buf[0], a.buf[1], 0.0, acc);
+  }
+  double t = block_sum(acc, red);
+  if (threadIdx.x == 0) a.partials[blockIdx.x] = t;
+  if (!grid_sync(a.bar)) return;
+  t = sum_partials(a.partials, red);
+  if (threadIdx.x == 0) tot_s = t;
+  __syncthreads();
+  const double norm0 = tot_s;
+  bool done = !isfinite(norm0);
+  int status = done ? 2 : 0;
+  int used = 2;
+  double last = norm0;  // accumulated norm after the previous term
+  double norm_last = 0.0;
+
+  for (int i = 2; i < a.order && !done; ++i) {
+    const cplx<T> *phi = a.buf[(i + 1) & 1];  // phi_{i-1}
+    cplx<T> *kout = a.buf[i & 1];             // phi_{i-2} in, phi_i out
+    acc = 0.0;
+    if (a.nd == 1) {
+      phase_lines<T, SS, false>(a, phi, kout, a.a[i], acc, smem);
+    } else {
+      phase_kinetic<T>(a, phi, smem);
+      if (!grid_sync(a.bar)) return;
+      phase_points<T, SS, false>(a, phi, kout, a.a[i], acc);
+    }
+    t = block_sum(acc, red);
+    if (threadIdx.x == 0) a.partials[blockIdx.x] = t;
+    if (!grid_sync(a.bar)) return;
+    t = sum_partials(a.partials, red);
+    if (threadIdx.x == 0) tot_s = t;
+    __syncthreads();
+    const double tot = tot_s;
+    used = i + 1;
+    if (!isfinite(tot)) {
+      done = true;
+      status = 2;
+    } else if (!a.imag) {
+      // OCheby.cpp:179-182 (mixed precision: change against the previous term)
+      const double ref = a.diff ? last : norm0;
+      if (fabs(ref - tot) / norm0 < a.prec && a.offim0) done = true;
+    } else {
+      // OCheby.cpp:286-289
+      if (fabs(tot - norm_last) / norm_last < a.prec) done = true;
+      norm_last = tot;
+    }
+    last = tot;
+  }
+
+  // common phase exp(c0 offset) of all coefficients
+  for (long long i = gtid; i < n; i += gstride) st(a.psi + i, cmul(ld(a.psi + i), a.ph));
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    a.cs->terms = used;
+    a.cs->total += used;
+    a.cs->status = status;
+    a.cs->norm0 = norm0;
+  }
+}
+
+template <typename T>
+static void *step_ptr(int S) {
+  return S == 1 ? (void *)cheby_step_kernel<T, 1> : S == 2 ? (void *)cheby_step_kernel<T, 2>
+                                                           : (void *)cheby_step_kernel<T, 0>;
+}
+
+template <typename T>
+int cheby_step_max_blocks(int S, int block, size_t smem) {
+  void *k = step_ptr<T>(S);
+  if (smem > 48 * 1024 && cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return 0;
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, block, smem) != cudaSuccess) return 0;
+  return nb;
+}
+
+template <typename T>
+cudaError_t launch_cheby_step(const StepArgs<T> &a, int grid, int block, size_t smem, cudaStream_t st) {
+  void *k = step_ptr<T>(a.S);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  void *args[] = {(void *)&a};
+  add_launches(1);
+  return cudaLaunchCooperativeKernel(k, dim3(grid), dim3(block), args, smem, st);
+}
+
+template int cheby_step_max_blocks<double>(int, int, size_t);
+template int cheby_step_max_blocks<float>(int, int, size_t);
+template cudaError_t launch_cheby_step<double>(const StepArgs<double> &, int, int, size_t, cudaStream_t);
+template cudaError_t launch_cheby_step<float>(const StepArgs<float> &, int, int, size_t, cudaStream_t);
+
+}  // namespace qdg

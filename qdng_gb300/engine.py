@@ -172,6 +172,6 @@ def kernel_launches():
     return load().qdg_kernel_launches()
 
 
-PASS_MODES = ["kin_first", "kin_acc", "h_apply", "cheby_first", "cheby_term", "gspo_kin"]
+PASS_MODES = ["kinetic", "kin_acc", "h_apply", "cheby_first", "cheby_term", "gspo_kin", "cheby_step"]
 
 __all__ = ["Plan", "WaveFunction", "Propagator", "QDGError", "kernel_launches", "PASS_MODES"]

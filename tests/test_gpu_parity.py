@@ -245,19 +245,30 @@ def test_apply_host_matches_device(eng, fixtures):
     assert np.array_equal(w.download(), host)
 
 
-def test_graph_and_eager_steps_agree_bitwise(eng):
-    """A captured Chebyshev step and the same step launched kernel by kernel
-    (profiling mode) give bit-identical wave functions and term counts."""
-    hp, psi, run = cases.cfg2_two_state(n=64)
+@pytest.mark.parametrize("case", ["2d", "1d"])
+def test_persistent_and_graph_steps_agree(eng, fixtures, monkeypatch, case):
+    """The persistent step kernel, the conditional-graph term loop and the
+    kernel-by-kernel launches (profiling mode) give the same terms and wave
+    functions to rounding (the persistent kernel applies the common phase
+    exp(c0 offset) once instead of per coefficient)."""
+    if case == "2d":
+        hp, psi, run = cases.cfg2_two_state(n=64)
+    else:
+        hp, psi, run = cases.tgplms(fixtures)
     plan = eng.Plan(hp, "fp64")
-    P = eng.Propagator(plan, run["name"], run["params"], dt=run["dt"])
-    w1, w2 = plan.wavefunction(psi), plan.wavefunction(psi)
-    t1 = [P.apply(w1, s) for s in range(4)]
+    P1 = eng.Propagator(plan, run["name"], run["params"], dt=run["dt"])
+    monkeypatch.setenv("QDG_CHEBY_MODE", "graph")
+    P2 = eng.Propagator(plan, run["name"], run["params"], dt=run["dt"])
+    monkeypatch.delenv("QDG_CHEBY_MODE")
+    w1, w2, w3 = plan.wavefunction(psi), plan.wavefunction(psi), plan.wavefunction(psi)
+    t1 = [P1.apply(w1, s) for s in range(4)]
+    t2 = [P2.apply(w2, s) for s in range(4)]
     plan.profile(True)
-    t2 = [P.apply(w2, s) for s in range(4)]
+    t3 = [P2.apply(w3, s) for s in range(4)]
     plan.profile(False)
-    assert t1 == t2
-    assert np.array_equal(w1.download(), w2.download())
+    assert t1 == t2 == t3
+    assert rel(w1.download(), w2.download()) < 1e-14
+    assert np.array_equal(w2.download(), w3.download())
 
 
 def test_run_counts_terms(eng, fixtures):
