@@ -205,7 +205,12 @@ def engine_arm(args, world, rank, local):
         prof = plan.profile_read() if profile else None
         if profile:
             plan.profile(False)
+            phases.update({k: round(v / 1e3 / max(terms - 2 * k_steps, 1), 3)
+                           for k, v in prop.phase_times().items()})
         return ms, terms, prof
+
+    phases = {}
+    k_steps = args.steps
 
     barrier(world)
     torch.cuda.synchronize()
@@ -303,6 +308,7 @@ def engine_arm(args, world, rank, local):
         "roofline": roof,
         "per_term": term_rate,
         "pass_profile": per_mode,
+        "step_phases_us_per_term": phases or None,
         "clocks": clocks,
         "cpu_baseline": cpu,
     }

@@ -203,6 +203,10 @@ qdg_status qdg_profile_enable(qdg_plan *plan, int32_t on);
  * first term, 4 Chebyshev term, 5 split-operator kinetic): summed device ms
  * and launch counts since the last read; resets the counters. */
 qdg_status qdg_profile_read(qdg_plan *plan, double ms[8], int64_t launches[8]);
+/* Chebyshev persistent step kernel, profiled steps since the last call:
+ * ns spent by block 0 in its own kinetic work, waiting at the barrier after
+ * it, in its own point work, and waiting at the norm barrier; resets them. */
+qdg_status qdg_prop_phase_times(qdg_prop *prop, double ns[4]);
 
 #ifdef __cplusplus
 }

@@ -118,6 +118,7 @@ SIGNATURES = [
     ("qdg_kernel_launches", _i64, []),
     ("qdg_profile_enable", _i32, [_vp, _i32]),
     ("qdg_profile_read", _i32, [_vp, _dp, C.POINTER(_i64)]),
+    ("qdg_prop_phase_times", _i32, [_vp, _dp]),
 ]
 
 

@@ -642,6 +642,7 @@ qdg_status cheby_step_persistent(qdg_prop *P, cplx<double> *psi, long long step)
   a.partials = p->d_partials;
   a.cs = P->d_cs;
   a.bar = p->d_bar;
+  a.trace = p->profiling ? 1 : 0;
   size_t slot = 0;
   qdg_status s = prof_begin<T>(p, 6, &slot);
   if (s != QDG_OK) return s;
@@ -1574,6 +1575,20 @@ qdg_status qdg_prop_run(qdg_prop *P, qdg_wf *psi, int64_t step0, int32_t nsteps,
 }
 
 int64_t qdg_kernel_launches(void) { return qdg::launch_counter(); }
+
+qdg_status qdg_prop_phase_times(qdg_prop *P, double ns[4]) {
+  if (!P || !ns) return fail(QDG_EINVAL, "null argument");
+  for (int k = 0; k < 4; ++k) ns[k] = 0;
+  if (P->kind != 1 || !P->d_cs) return QDG_OK;
+  CK(cudaStreamSynchronize(P->plan->stream));
+  qdg::ChebyState cs;
+  CK(cudaMemcpy(&cs, P->d_cs, sizeof(cs), cudaMemcpyDeviceToHost));
+  for (int k = 0; k < 4; ++k) ns[k] = (double)cs.t_phase[k];
+  unsigned long long z[4] = {0, 0, 0, 0};
+  CK(cudaMemcpy(reinterpret_cast<char *>(P->d_cs) + offsetof(qdg::ChebyState, t_phase), z, sizeof(z),
+                cudaMemcpyHostToDevice));
+  return QDG_OK;
+}
 
 qdg_status qdg_profile_enable(qdg_plan *plan, int32_t on) {
   if (!plan) return fail(QDG_EINVAL, "null plan");

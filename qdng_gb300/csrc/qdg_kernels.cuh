@@ -44,6 +44,10 @@ struct ChebyState {
   unsigned int arrive;  // blocks of the current reduction that have stored their partial sum
   int i;             // index of the next term (device-driven term loop)
   double acc_last;   // accumulated norm after the previous term (differential cut)
+  // phase timing of the persistent step kernel as seen by block 0 (ns,
+  // accumulated while tracing): own kinetic work, wait at the barrier after
+  // it, own point work, wait at the norm barrier
+  unsigned long long t_phase[4];
 };
 
 // Series-cut parameters handed to the kernel that finishes a Chebyshev term:
@@ -186,6 +190,7 @@ struct StepArgs {
   double *partials;
   ChebyState *cs;
   GridBarrier *bar;
+  int trace;                 // record phase times in cs->t_phase
 };
 
 template <typename T>

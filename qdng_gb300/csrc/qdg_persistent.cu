@@ -65,6 +65,12 @@ __device__ bool grid_sync(GridBarrier *b) {
   return ok != 0;
 }
 
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
 // sum of the per-block partials, same order in every block; valid on thread 0
 __device__ double sum_partials(const double *partials, double *red) {
   double v = 0.0;
@@ -276,20 +282,31 @@ __global__ void __launch_bounds__(256) cheby_step_kernel(StepArgs<T> a) {
   double last = norm0;  // accumulated norm after the previous term
   double norm_last = 0.0;
 
+  const bool tr = a.trace && blockIdx.x == 0 && threadIdx.x == 0;
+  unsigned long long tp[4] = {0, 0, 0, 0};
   for (int i = 2; i < a.order && !done; ++i) {
     const cplx<T> *phi = a.buf[(i + 1) & 1];  // phi_{i-1}
     cplx<T> *kout = a.buf[i & 1];             // phi_{i-2} in, phi_i out
     acc = 0.0;
+    unsigned long long t0 = tr ? gtimer() : 0, t1 = 0, t2 = 0, t3 = 0;
     if (a.nd == 1) {
       phase_lines<T, SS, false>(a, phi, kout, a.a[i], acc, smem);
+      if (tr) t1 = t2 = gtimer();
     } else {
       phase_kinetic<T>(a, phi, smem);
+      if (tr) t1 = gtimer();
       if (!grid_sync(a.bar)) return;
+      if (tr) t2 = gtimer();
       phase_points<T, SS, false>(a, phi, kout, a.a[i], acc);
     }
     t = block_sum(acc, red);
     if (threadIdx.x == 0) a.partials[blockIdx.x] = t;
+    if (tr) t3 = gtimer();
     if (!grid_sync(a.bar)) return;
+    if (tr) {
+      const unsigned long long t4 = gtimer();
+      tp[0] += t1 - t0; tp[1] += t2 - t1; tp[2] += t3 - t2; tp[3] += t4 - t3;
+    }
     t = sum_partials(a.partials, red);
     if (threadIdx.x == 0) tot_s = t;
     __syncthreads();
@@ -317,6 +334,8 @@ __global__ void __launch_bounds__(256) cheby_step_kernel(StepArgs<T> a) {
     a.cs->total += used;
     a.cs->status = status;
     a.cs->norm0 = norm0;
+    if (a.trace)
+      for (int k = 0; k < 4; ++k) a.cs->t_phase[k] += tp[k];
   }
 }
 

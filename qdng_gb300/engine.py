@@ -152,6 +152,12 @@ class Propagator:
         check(self.lib.qdg_prop_apply_host(self.h, scratch.h, _dp(psi), step, C.byref(used)))
         return used.value
 
+    def phase_times(self):
+        """Per-phase ns of the persistent step kernel while profiling (block 0's view)."""
+        ns = np.zeros(4)
+        check(self.lib.qdg_prop_phase_times(self.h, _dp(ns)))
+        return dict(kinetic=ns[0], barrier_after_kinetic=ns[1], points=ns[2], barrier_norm=ns[3])
+
     def run(self, wf, step0, nsteps):
         tot = C.c_int64(0)
         check(self.lib.qdg_prop_run(self.h, wf.h, step0, nsteps, C.byref(tot)))
