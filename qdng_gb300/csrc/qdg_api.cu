@@ -51,11 +51,15 @@ struct DimInfo {
   int TW_k, TW_e;     // lines per tile: kinetic-only passes, coupled epilogue pass
 };
 
+// Largest radices first: 16-point DFTs in registers halve the shared-memory
+// stages of a radix-4 plan (256 = 16 x 16, 1024 = 16 x 16 x 4, 384 = 16 x 8 x 3).
 bool radix_plan(int n, qdg::RadixPlan &rp) {
   rp.n = n; rp.nstages = 0;
   int m = n;
-  while (m % 4 == 0) { rp.radix[rp.nstages++] = 4; m /= 4; }
-  while (m % 2 == 0) { rp.radix[rp.nstages++] = 2; m /= 2; }
+  while (m % 16 == 0) { rp.radix[rp.nstages++] = 16; m /= 16; }
+  if (m % 8 == 0) { rp.radix[rp.nstages++] = 8; m /= 8; }
+  if (m % 4 == 0) { rp.radix[rp.nstages++] = 4; m /= 4; }
+  if (m % 2 == 0) { rp.radix[rp.nstages++] = 2; m /= 2; }
   while (m % 3 == 0) { rp.radix[rp.nstages++] = 3; m /= 3; }
   while (m % 5 == 0) { rp.radix[rp.nstages++] = 5; m /= 5; }
   if (rp.nstages > 16) return false;
@@ -145,6 +149,8 @@ struct qdg_prop {
   int step_grid = 0;                // persistent step kernel: blocks (0: unavailable)
   size_t step_smem = 0;
   int step_tw1 = 1;
+  long long line_start[QDG_MAX_DIMS + 1] = {0, 0, 0, 0, 0};
+  int lmax[QDG_MAX_DIMS] = {1, 1, 1, 1};
   // GSPO
   int ngroups = 0;
   std::vector<int> group_kinetic;     // 1: FFT member, 0: potential member
@@ -579,22 +585,49 @@ qdg_status step_setup(qdg_prop *P) {
   qdg_plan *p = P->plan;
   const char *env = getenv("QDG_CHEBY_MODE");
   if (env && strcmp(env, "graph") == 0) return QDG_OK;
-  size_t smem = 0;
+  const size_t cs = p->csize;
   if (p->nd == 1) {
     P->step_tw1 = p->dim[0].TW_e;
-    smem = pass_smem(p, 0, P->step_tw1, p->S);
-  } else {
-    for (int d = 0; d < p->nd; ++d) smem = std::max(smem, pass_smem(p, d, p->dim[d].TW_k, 1));
+    const size_t smem = pass_smem(p, 0, P->step_tw1, p->S);
+    if (smem > 227 * 1024) return QDG_OK;
+    const int per_sm = qdg::cheby_step_max_blocks<T>(p->S, 256, smem);
+    if (per_sm <= 0) return QDG_OK;
+    long long want = p->npts / ((long long)p->dim[0].n * P->step_tw1);
+    want = std::min<long long>(want, (long long)per_sm * p->sm_count);
+    P->step_grid = (int)std::max<long long>(1, std::min<long long>(want, p->max_parts));
+    P->step_smem = smem;
+    return QDG_OK;
   }
-  if (smem > 227 * 1024) return QDG_OK;
+  // kinetic lines of all dimensions, split into one contiguous run per block
+  long long total = 0;
+  for (int d = 0; d < p->nd; ++d) {
+    P->line_start[d] = total;
+    total += (p->npts / p->dim[d].n) * p->S;
+  }
+  P->line_start[p->nd] = total;
+  const size_t budget = 112 * 1024;  // shared memory per block for the line buffers
+  int grid = 0;
+  size_t smem = 0;
+  for (int iter = 0, per_sm = 0; iter < 3; ++iter) {
+    const size_t probe = iter == 0 ? 16 * 1024 : smem;
+    per_sm = qdg::cheby_step_max_blocks<T>(p->S, 256, probe);
+    if (per_sm <= 0) return QDG_OK;
+    grid = (int)std::min<long long>((long long)per_sm * p->sm_count, std::min<long long>(total, p->max_parts));
+    const long long chunk = (total + grid - 1) / grid;
+    smem = 0;
+    for (int d = 0; d < p->nd; ++d) {
+      const long long n = p->dim[d].n;
+      long long cap = (long long)((budget / cs - n) / (2 * n));
+      int lm = (int)std::max<long long>(1, std::min<long long>(chunk, cap));
+      P->lmax[d] = lm;
+      smem = std::max(smem, (size_t)(n * (1 + 2 * (size_t)lm)) * cs);
+    }
+    if (smem > 227 * 1024) return QDG_OK;
+    if (qdg::cheby_step_max_blocks<T>(p->S, 256, smem) >= per_sm) break;
+  }
   const int per_sm = qdg::cheby_step_max_blocks<T>(p->S, 256, smem);
   if (per_sm <= 0) return QDG_OK;
-  long long want;
-  if (p->nd == 1) want = p->npts / ((long long)p->dim[0].n * P->step_tw1);
-  else want = (long long)per_sm * p->sm_count;
-  want = std::min<long long>(want, (long long)per_sm * p->sm_count);
-  want = std::min<long long>(want, p->max_parts);
-  P->step_grid = (int)std::max<long long>(1, want);
+  P->step_grid = std::min(grid, per_sm * p->sm_count);
   P->step_smem = smem;
   return QDG_OK;
 }
@@ -621,6 +654,8 @@ qdg_status cheby_step_persistent(qdg_prop *P, cplx<double> *psi, long long step)
     items += g.ntiles * p->S;
   }
   a.item_start[p->nd] = items;
+  for (int d = 0; d <= p->nd; ++d) a.line_start[d] = P->line_start[d];
+  for (int d = 0; d < p->nd; ++d) a.lmax[d] = P->lmax[d];
   a.TW1 = P->step_tw1;
   a.psi = psi;
   a.buf[0] = reinterpret_cast<cplx<T> *>(P->k0);

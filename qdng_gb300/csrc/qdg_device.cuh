@@ -43,12 +43,83 @@ template <typename T> __device__ __forceinline__ void st(cplx<T> *p, cplx<T> c) 
   *reinterpret_cast<V *>(p) = v;
 }
 
-// Radix plan of one line length: N = prod radix[i], radices in {4, 2, 3, 5}.
+// Radix plan of one line length: N = prod radix[i], radices in {16, 8, 4, 2, 3, 5}.
 struct RadixPlan {
   int n;
   int nstages;
   int radix[16];
 };
+
+// ---- small DFTs in registers ---------------------------------------------
+// Constants of the 8th and 16th roots of unity (mathematical values).
+#define QDG_SQRT1_2 0.70710678118654752440
+#define QDG_COS_PI8 0.92387953251128675613
+#define QDG_SIN_PI8 0.38268343236508977173
+
+// multiply by -i (sign < 0) or +i (sign > 0)
+template <typename T> __device__ __forceinline__ cplx<T> rot90(cplx<T> a, int sign) {
+  return sign < 0 ? mk(a.im, -a.re) : mk(-a.im, a.re);
+}
+
+// 4-point DFT, in place: y_k = sum_n x_n exp(sign 2 pi i nk/4)
+template <typename T> __device__ __forceinline__ void dft4(cplx<T> &x0, cplx<T> &x1, cplx<T> &x2, cplx<T> &x3,
+                                                          int sign) {
+  const cplx<T> a0 = x0 + x2, a1 = x0 - x2, a2 = x1 + x3, a3 = rot90(x1 - x3, sign);
+  x0 = a0 + a2; x2 = a0 - a2; x1 = a1 + a3; x3 = a1 - a3;
+}
+
+// a * exp(sign 2 pi i m/16) for m = 1..9 with the special values of the
+// 8th roots of unity; m is a compile-time constant after unrolling.
+template <typename T> __device__ __forceinline__ cplx<T> tw16(cplx<T> a, int m, int sign) {
+  const T c = (T)QDG_COS_PI8, sn = (T)QDG_SIN_PI8, h = (T)QDG_SQRT1_2;
+  const T sg = sign < 0 ? (T)-1 : (T)1;
+  switch (m) {
+    case 0: return a;
+    case 1: return cmul(a, mk(c, sg * sn));
+    case 2: return mk(h * (a.re - sg * a.im), h * (a.im + sg * a.re));
+    case 3: return cmul(a, mk(sn, sg * c));
+    case 4: return rot90(a, sign);
+    case 6: return mk(h * (-a.re - sg * a.im), h * (-a.im + sg * a.re));
+    case 9: return cmul(a, mk(-c, -sg * sn));
+  }
+  return a;
+}
+
+// 8-point DFT (4 x 2): y[k1 + 4 k2] = sum_n2 W2^(n2 k2) W8^(n2 k1) sum_n1 x[2 n1 + n2] W4^(n1 k1)
+template <typename T> __device__ __forceinline__ void dft8(cplx<T> *x, int sign) {
+  dft4(x[0], x[2], x[4], x[6], sign);
+  dft4(x[1], x[3], x[5], x[7], sign);
+  // now x[2 k1 + n2] holds a[n2][k1]
+  cplx<T> y[8];
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) {
+    const cplx<T> a0 = x[2 * k1];
+    const cplx<T> a1 = tw16(x[2 * k1 + 1], 2 * k1, sign);  // W8^k1 = W16^(2 k1)
+    y[k1] = a0 + a1;
+    y[k1 + 4] = a0 - a1;
+  }
+#pragma unroll
+  for (int k = 0; k < 8; ++k) x[k] = y[k];
+}
+
+// 16-point DFT (4 x 4): y[k1 + 4 k2] = sum_n2 W4^(n2 k2) W16^(n2 k1) sum_n1 x[4 n1 + n2] W4^(n1 k1)
+template <typename T> __device__ __forceinline__ void dft16(cplx<T> *x, int sign) {
+#pragma unroll
+  for (int n2 = 0; n2 < 4; ++n2) dft4(x[n2], x[4 + n2], x[8 + n2], x[12 + n2], sign);
+  // x[4 k1 + n2] holds a[n2][k1]
+  cplx<T> y[16];
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) {
+    cplx<T> b0 = x[4 * k1 + 0];
+    cplx<T> b1 = tw16(x[4 * k1 + 1], k1, sign);
+    cplx<T> b2 = tw16(x[4 * k1 + 2], 2 * k1, sign);
+    cplx<T> b3 = tw16(x[4 * k1 + 3], 3 * k1, sign);
+    dft4(b0, b1, b2, b3, sign);
+    y[k1] = b0; y[k1 + 4] = b1; y[k1 + 8] = b2; y[k1 + 12] = b3;
+  }
+#pragma unroll
+  for (int k = 0; k < 16; ++k) x[k] = y[k];
+}
 
 // One Stockham stage over `nlines` lines of length N stored line after line
 // in `in` (line stride N); result in `out`.  Items are spread over all
@@ -56,7 +127,7 @@ struct RadixPlan {
 // (FFTW_FORWARD), +1 backward.  The Stockham autosort indexing follows the
 // classic formulation (Stockham 1966; Govindaraju et al., SC'08): item j
 // reads in[j + r*N/R], applies the stage twiddles w^(r*k), does the R-point
-// DFT and writes out[(j/Ns)*Ns*R + k + r*Ns], k = j mod Ns.
+// DFT in registers and writes out[(j/Ns)*Ns*R + k + r*Ns], k = j mod Ns.
 template <typename T, int R>
 __device__ __forceinline__ void stockham_stage(const cplx<T> *__restrict__ in, cplx<T> *__restrict__ out,
                                                int N, int nlines, int Ns, const cplx<T> *__restrict__ tw,
@@ -80,16 +151,19 @@ __device__ __forceinline__ void stockham_stage(const cplx<T> *__restrict__ in, c
         v[r] = cmul(v[r], w);
       }
     }
-    cplx<T> y[R];
     if (R == 2) {
-      y[0] = v[0] + v[1];
-      y[1] = v[0] - v[1];
+      const cplx<T> a = v[0];
+      v[0] = a + v[1];
+      v[1] = a - v[1];
     } else if (R == 4) {
-      cplx<T> a0 = v[0] + v[2], a1 = v[0] - v[2], a2 = v[1] + v[3], d = v[1] - v[3];
-      cplx<T> a3 = sign < 0 ? mk(d.im, -d.re) : mk(-d.im, d.re);
-      y[0] = a0 + a2; y[2] = a0 - a2; y[1] = a1 + a3; y[3] = a1 - a3;
+      dft4(v[0], v[1], v[2], v[3], sign);
+    } else if (R == 8) {
+      dft8(v, sign);
+    } else if (R == 16) {
+      dft16(v, sign);
     } else {
       // direct R-point DFT with the table entries of the R-th roots of unity
+      cplx<T> y[R];
 #pragma unroll
       for (int q = 0; q < R; ++q) {
         cplx<T> s = v[0];
@@ -101,15 +175,17 @@ __device__ __forceinline__ void stockham_stage(const cplx<T> *__restrict__ in, c
         }
         y[q] = s;
       }
+#pragma unroll
+      for (int q = 0; q < R; ++q) v[q] = y[q];
     }
     cplx<T> *dst = out + line * N + (j / Ns) * Ns * R + k;
 #pragma unroll
-    for (int r = 0; r < R; ++r) dst[r * Ns] = y[r];
+    for (int r = 0; r < R; ++r) dst[r * Ns] = v[r];
   }
 }
 
 // Full unnormalised FFT of `nlines` lines in shared memory.  Data starts in
-// buf[0]; returns the buffer index (0/1) that holds the result.  Every
+// buf0; returns the buffer index (0/1) that holds the result.  Every
 // thread of the block must call it (it synchronises between stages).
 template <typename T>
 __device__ int fft_lines(cplx<T> *buf0, cplx<T> *buf1, const RadixPlan &rp, int nlines,
@@ -119,7 +195,9 @@ __device__ int fft_lines(cplx<T> *buf0, cplx<T> *buf1, const RadixPlan &rp, int 
   int Ns = 1;
   for (int s = 0; s < rp.nstages; ++s) {
     const int R = rp.radix[s];
-    if (R == 4) stockham_stage<T, 4>(b[cur], b[cur ^ 1], rp.n, nlines, Ns, tw, sign);
+    if (R == 16) stockham_stage<T, 16>(b[cur], b[cur ^ 1], rp.n, nlines, Ns, tw, sign);
+    else if (R == 8) stockham_stage<T, 8>(b[cur], b[cur ^ 1], rp.n, nlines, Ns, tw, sign);
+    else if (R == 4) stockham_stage<T, 4>(b[cur], b[cur ^ 1], rp.n, nlines, Ns, tw, sign);
     else if (R == 2) stockham_stage<T, 2>(b[cur], b[cur ^ 1], rp.n, nlines, Ns, tw, sign);
     else if (R == 3) stockham_stage<T, 3>(b[cur], b[cur ^ 1], rp.n, nlines, Ns, tw, sign);
     else stockham_stage<T, 5>(b[cur], b[cur ^ 1], rp.n, nlines, Ns, tw, sign);

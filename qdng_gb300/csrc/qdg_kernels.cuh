@@ -176,6 +176,8 @@ struct StepArgs {
   long long npts;
   DimPass<T> dp[4];          // kinetic passes (P_d outputs); dp[0] also the 1-D line geometry
   long long item_start[5];
+  long long line_start[5];   // kinetic lines of dims < d (all states)
+  int lmax[4];               // lines of dim d one block transforms at once (shared memory)
   int TW1;                   // 1-D grids: lines per tile (all states in one block)
   cplx<double> *psi;
   cplx<T> *buf[2];           // phi buffers (ket0 / ket1)

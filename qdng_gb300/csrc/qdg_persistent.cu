@@ -78,54 +78,71 @@ __device__ double sum_partials(const double *partials, double *red) {
   return block_sum(v, red);
 }
 
-// T_d phi for every dimension: items (dimension, tile, state) over the grid.
+// T_d phi for every dimension.  The kinetic lines of all dimensions and
+// states are split into one contiguous run per block (balanced to within one
+// line); a block transforms up to lmax[d] lines of its run at once, so the
+// lines of a run are adjacent in memory (contiguous rows, or neighbouring
+// columns whose elements share memory segments).
 template <typename T>
 __device__ void phase_kinetic(const StepArgs<T> &a, const cplx<T> *phi, cplx<T> *smem) {
-  const long long nitems = a.item_start[a.nd];
+  const long long total = a.line_start[a.nd];
+  const long long G = gridDim.x;
+  const long long end = total * (blockIdx.x + 1) / G;
+  long long l = total * blockIdx.x / G;
   int cur_dim = -1;
   cplx<T> *tws = smem;
-  for (long long item = blockIdx.x; item < nitems; item += gridDim.x) {
+  while (l < end) {
     int d = 0;
-    while (item >= a.item_start[d + 1]) ++d;
+    while (l >= a.line_start[d + 1]) ++d;
     const DimPass<T> &g = a.dp[d];
-    const int N = g.N, TW = g.TW;
+    const int N = g.N;
+    const long long stride = g.ls == 1 ? (long long)g.es : 1;  // element stride of the lines of dim d
+    const long long nl = a.npts / N;                          // lines per state
+    const long long local = l - a.line_start[d];
+    const int s = (int)(local / nl);
+    const long long l0 = local - (long long)s * nl;
+    long long cnt = end - l;
+    if (cnt > nl - l0) cnt = nl - l0;
+    if (cnt > a.lmax[d]) cnt = a.lmax[d];
+    const int L = (int)cnt;
     cplx<T> *b0 = tws + N;
-    cplx<T> *b1 = b0 + (size_t)TW * N;
+    cplx<T> *b1 = b0 + (size_t)a.lmax[d] * N;
     __syncthreads();
     if (d != cur_dim) {
       for (int i = threadIdx.x; i < N; i += blockDim.x) tws[i] = g.tw[i];
       cur_dim = d;
     }
-    const long long local = item - a.item_start[d];
-    const long long tile = local / a.S;
-    const int s = (int)(local - tile * a.S);
-    const long long hi = tile / g.tiles_per_hi;
-    const long long base = hi * g.hi_stride + (tile - hi * g.tiles_per_hi) * TW;
-    const int tileN = TW * N;
     const cplx<T> *src = phi + (long long)s * a.npts;
-    for (int idx = threadIdx.x; idx < tileN; idx += blockDim.x) {
+    for (int idx = threadIdx.x; idx < L * N; idx += blockDim.x) {
       int w, i;
-      tile_coord(idx, TW, N, g.es, w, i);
-      b0[w * N + i] = ld(src + base + (long long)w * g.ls + (long long)i * g.es);
+      if (stride == 1) { w = idx / N; i = idx - w * N; }
+      else { i = idx / L; w = idx - i * L; }
+      const long long line = l0 + w;
+      const long long p = (line % stride) + (line / stride) * stride * N + (long long)i * stride;
+      b0[w * N + i] = ld(src + p);
     }
     __syncthreads();
-    const int cur = fft_lines<T>(b0, b1, g.rp, TW, tws, -1);
+    const int cur = fft_lines<T>(b0, b1, g.rp, L, tws, -1);
     cplx<T> *bc = cur ? b1 : b0;
     const double kf = g.kfac[s];
-    for (int idx = threadIdx.x; idx < tileN; idx += blockDim.x) {
+    for (int idx = threadIdx.x; idx < L * N; idx += blockDim.x) {
       const int i = idx % N;
       const int kq = min(i, N - i);
       bc[idx] = cmulr(bc[idx], (T)(kf * (double)kq * (double)kq));
     }
     __syncthreads();
-    const int cur2 = fft_lines<T>(bc, cur ? b0 : b1, g.rp, TW, tws, +1);
+    const int cur2 = fft_lines<T>(bc, cur ? b0 : b1, g.rp, L, tws, +1);
     const cplx<T> *res = cur2 ? (cur ? b0 : b1) : bc;
     cplx<T> *dst = g.P + (long long)s * a.npts;
-    for (int idx = threadIdx.x; idx < tileN; idx += blockDim.x) {
+    for (int idx = threadIdx.x; idx < L * N; idx += blockDim.x) {
       int w, i;
-      tile_coord(idx, TW, N, g.es, w, i);
-      st(dst + base + (long long)w * g.ls + (long long)i * g.es, res[w * N + i]);
+      if (stride == 1) { w = idx / N; i = idx - w * N; }
+      else { i = idx / L; w = idx - i * L; }
+      const long long line = l0 + w;
+      const long long p = (line % stride) + (line / stride) * stride * N + (long long)i * stride;
+      st(dst + p, res[w * N + i]);
     }
+    l += cnt;
   }
   __syncthreads();
 }
