@@ -89,6 +89,7 @@ struct qdg_plan {
   double *d_coef = nullptr;
   void *d_P = nullptr;           // kinetic partial sums (bulk type)
   void *d_Pd[QDG_MAX_DIMS] = {nullptr, nullptr, nullptr, nullptr};  // T_d phi per dimension
+  void *d_Pd2[QDG_MAX_DIMS] = {nullptr, nullptr, nullptr, nullptr}; // second set (step kernel double buffer)
   size_t kin_smem = 0;
   int kin_grid = 1, comb_grid = 1;
   std::map<long long, int> occ_cache;  // (mode, smem) -> resident blocks per SM
@@ -132,7 +133,7 @@ struct qdg_prop {
   double scaling = 1, prec = 1e-10;
   cd offset = 0;
   std::vector<double> coeff;
-  void *k0 = nullptr, *k1 = nullptr;  // bulk type
+  void *k0 = nullptr, *k1 = nullptr, *k2 = nullptr;  // bulk type
   qdg::ChebyState *d_cs = nullptr;
   qdg::ChebyState *h_cs = nullptr;    // pinned
   // one captured graph of the whole Chebyshev step per (psi buffer, stream)
@@ -457,6 +458,7 @@ qdg_status upload_tables(qdg_plan *p) {
     long long items = 0;
     for (int d = 0; d < p->nd; ++d) {
       CK(cudaMalloc(&p->d_Pd[d], sizeof(cplx<T>) * wf_elems(p)));
+      CK(cudaMalloc(&p->d_Pd2[d], sizeof(cplx<T>) * wf_elems(p)));
       smem = std::max(smem, pass_smem(p, d, p->dim[d].TW_k, 1));
       items += (p->npts / ((long long)p->dim[d].n * p->dim[d].TW_k)) * p->S;
     }
@@ -485,8 +487,10 @@ void free_plan(qdg_plan *p) {
   if (p->d_cp) cudaFree(p->d_cp);
   if (p->d_coef) cudaFree(p->d_coef);
   if (p->d_P) cudaFree(p->d_P);
-  for (int d = 0; d < QDG_MAX_DIMS; ++d)
+  for (int d = 0; d < QDG_MAX_DIMS; ++d) {
     if (p->d_Pd[d]) cudaFree(p->d_Pd[d]);
+    if (p->d_Pd2[d]) cudaFree(p->d_Pd2[d]);
+  }
   if (p->d_scratch) cudaFree(p->d_scratch);
   if (p->d_scratch2) cudaFree(p->d_scratch2);
   if (p->d_partials) cudaFree(p->d_partials);
@@ -660,6 +664,11 @@ qdg_status cheby_step_persistent(qdg_prop *P, cplx<double> *psi, long long step)
   a.psi = psi;
   a.buf[0] = reinterpret_cast<cplx<T> *>(P->k0);
   a.buf[1] = reinterpret_cast<cplx<T> *>(P->k1);
+  a.buf[2] = reinterpret_cast<cplx<T> *>(P->k2);
+  for (int d = 0; d < p->nd; ++d) {
+    a.Pn[0][d] = reinterpret_cast<cplx<T> *>(p->d_Pd[d]);
+    a.Pn[1][d] = reinterpret_cast<cplx<T> *>(p->d_Pd2[d]);
+  }
   a.cp = p->d_cp;
   a.coef = p->d_coef;
   a.grids = reinterpret_cast<const T *>(p->d_grids);
@@ -729,6 +738,7 @@ qdg_status cheby_init(qdg_prop *P) {
   const size_t bytes = p->csize * wf_elems(p);
   CK(cudaMalloc(&P->k0, bytes));
   CK(cudaMalloc(&P->k1, bytes));
+  CK(cudaMalloc(&P->k2, bytes));
   CK(cudaMalloc(&P->d_cs, sizeof(qdg::ChebyState)));
   CK(cudaMemset(P->d_cs, 0, sizeof(qdg::ChebyState)));
   {
@@ -1504,6 +1514,7 @@ qdg_status qdg_prop_destroy(qdg_prop *P) {
   cudaStreamSynchronize(plan->stream);
   if (P->k0) cudaFree(P->k0);
   if (P->k1) cudaFree(P->k1);
+  if (P->k2) cudaFree(P->k2);
   if (P->graph) cudaGraphExecDestroy(P->graph);
   if (P->d_coeffs) cudaFree(P->d_coeffs);
   if (P->d_a) cudaFree(P->d_a);

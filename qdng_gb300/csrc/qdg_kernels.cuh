@@ -180,7 +180,8 @@ struct StepArgs {
   int lmax[4];               // lines of dim d one block transforms at once (shared memory)
   int TW1;                   // 1-D grids: lines per tile (all states in one block)
   cplx<double> *psi;
-  cplx<T> *buf[2];           // phi buffers (ket0 / ket1)
+  cplx<T> *buf[3];           // rotating phi buffers (phi_{i-2}, phi_{i-1}, phi_i)
+  cplx<T> *Pn[2][4];         // kinetic parts T_d phi of the previous / next term (double buffered)
   const Couplings *cp;
   const double *coef;
   const T *grids;

@@ -55,7 +55,7 @@ __device__ bool grid_sync(GridBarrier *b) {
           atomicExch(&b->err, 1);
           break;
         }
-        __nanosleep(40);
+        if (spins > 512) __nanosleep(32);  // tight spin first, back off later
       }
     }
     __threadfence();
@@ -143,6 +143,130 @@ __device__ void phase_kinetic(const StepArgs<T> &a, const cplx<T> *phi, cplx<T> 
       st(dst + p, res[w * N + i]);
     }
     l += cnt;
+  }
+  __syncthreads();
+}
+
+// ---- one phase per term on grids of two or more dimensions -----------------
+// Phase i+1 computes phi_i point-wise while loading the lines of its kinetic
+// transforms (H phi_{i-1} = sum_d T_d phi_{i-1} + W phi_{i-1} from the
+// previous phase's P), so a term needs one grid barrier.  The lines along
+// dimension 0 (rows) cover every point of a state exactly once: their loaders
+// also store phi_i and update psi and its norm.  The other dimensions
+// recompute phi_i for their own points.
+enum PhaseKind { PK_START = 0, PK_FIRST = 1, PK_TERM = 2, PK_LAST = 3 };
+
+template <typename T, int SM>
+__device__ __forceinline__ cplx<T> phi_at(const StepArgs<T> &a, int kind, int s, long long p, const cplx<T> *phim1,
+                                          const cplx<T> *phim2, cplx<T> *const *Pprev, bool owner, cplx<T> *phout,
+                                          double coeff_i, double &acc) {
+  const long long npts = a.npts;
+  const long long g = (long long)s * npts + p;
+  if (kind == PK_START) return ld(phim1 + g);
+  // h = H phi_{i-1} at (s, p)
+  cplx<T> h = ld(Pprev[0] + g);
+  for (int d = 1; d < a.nd; ++d) h = h + ld(Pprev[d] + g);
+  const int ne = a.cp->ne;
+  for (int e = 0; e < ne; ++e) {
+    if (a.cp->row[e] != s) continue;
+    const T v = (T)(a.coef[e]) * a.grids[(long long)a.cp->gid[e] * npts + p];
+    h = h + cmulr(ld(phim1 + (long long)a.cp->col[e] * npts + p), v);
+  }
+  const cplx<T> off = ccast<T>(a.offset);
+  const cplx<T> pm1 = ld(phim1 + g);
+  if (kind == PK_FIRST) {
+    const cplx<T> bf = cmul(h - cmul(off, pm1), ccast<T>(a.fac1));
+    if (owner) {
+      const cplx<double> ps = ld(a.psi + g);
+      acc += cabs2(ps);
+      st(phout + g, bf);
+      const cplx<double> b = ccast<double>(bf);
+      st(a.psi + g, mk(ps.re * a.a[0] + b.re * a.a[1], ps.im * a.a[0] + b.im * a.a[1]));
+    }
+    return bf;
+  }
+  const cplx<T> bf = cmul(h - cmul(off, pm1), ccast<T>(a.fac));
+  const cplx<T> km2 = ld(phim2 + g);
+  const cplx<T> k2 = a.imag ? bf - km2 : bf + km2;
+  if (owner) {
+    st(phout + g, k2);
+    cplx<double> ps = ld(a.psi + g);
+    ps.re += coeff_i * (double)k2.re;
+    ps.im += coeff_i * (double)k2.im;
+    st(a.psi + g, ps);
+    acc += cabs2(ps);
+  }
+  return k2;
+}
+
+// Kinetic transforms of phi_i (computed on load) for every dimension;
+// results go to Pnext.  PK_LAST only finishes phi_i and psi (row lines).
+template <typename T, int SM>
+__device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *phim1, const cplx<T> *phim2,
+                            cplx<T> *phout, cplx<T> *const *Pprev, cplx<T> *const *Pnext, double coeff_i,
+                            double &acc, cplx<T> *smem) {
+  const long long total = a.line_start[a.nd];
+  const long long G = gridDim.x;
+  const long long end = total * (blockIdx.x + 1) / G;
+  long long l = total * blockIdx.x / G;
+  int cur_dim = -1;
+  cplx<T> *tws = smem;
+  while (l < end) {
+    int d = 0;
+    while (l >= a.line_start[d + 1]) ++d;
+    const DimPass<T> &g = a.dp[d];
+    const int N = g.N;
+    const long long stride = g.ls == 1 ? (long long)g.es : 1;
+    const long long nl = a.npts / N;
+    const long long local = l - a.line_start[d];
+    const int s = (int)(local / nl);
+    const long long l0 = local - (long long)s * nl;
+    long long cnt = end - l;
+    if (cnt > nl - l0) cnt = nl - l0;
+    if (cnt > a.lmax[d]) cnt = a.lmax[d];
+    const int L = (int)cnt;
+    l += cnt;
+    const bool owner = d == 0;
+    if (kind == PK_LAST && !owner) continue;
+    cplx<T> *b0 = tws + N;
+    cplx<T> *b1 = b0 + (size_t)a.lmax[d] * N;
+    __syncthreads();
+    if (d != cur_dim && kind != PK_LAST) {
+      for (int i = threadIdx.x; i < N; i += blockDim.x) tws[i] = g.tw[i];
+      cur_dim = d;
+    }
+#pragma unroll 4
+    for (int idx = threadIdx.x; idx < L * N; idx += blockDim.x) {
+      int w, i;
+      if (stride == 1) { w = idx / N; i = idx - w * N; }
+      else { i = idx / L; w = idx - i * L; }
+      const long long line = l0 + w;
+      const long long p = (line % stride) + (line / stride) * stride * N + (long long)i * stride;
+      const cplx<T> v = phi_at<T, SM>(a, kind, s, p, phim1, phim2, Pprev, owner, phout, coeff_i, acc);
+      if (kind != PK_LAST) b0[w * N + i] = v;
+    }
+    if (kind == PK_LAST) continue;
+    __syncthreads();
+    const int cur = fft_lines<T>(b0, b1, g.rp, L, tws, -1);
+    cplx<T> *bc = cur ? b1 : b0;
+    const double kf = g.kfac[s];
+    for (int idx = threadIdx.x; idx < L * N; idx += blockDim.x) {
+      const int i = idx % N;
+      const int kq = min(i, N - i);
+      bc[idx] = cmulr(bc[idx], (T)(kf * (double)kq * (double)kq));
+    }
+    __syncthreads();
+    const int cur2 = fft_lines<T>(bc, cur ? b0 : b1, g.rp, L, tws, +1);
+    const cplx<T> *res = cur2 ? (cur ? b0 : b1) : bc;
+    cplx<T> *dst = Pnext[d] + (long long)s * a.npts;
+    for (int idx = threadIdx.x; idx < L * N; idx += blockDim.x) {
+      int w, i;
+      if (stride == 1) { w = idx / N; i = idx - w * N; }
+      else { i = idx / L; w = idx - i * L; }
+      const long long line = l0 + w;
+      const long long p = (line % stride) + (line / stride) * stride * N + (long long)i * stride;
+      st(dst + p, res[w * N + i]);
+    }
   }
   __syncthreads();
 }
@@ -268,80 +392,104 @@ __global__ void __launch_bounds__(256) cheby_step_kernel(StepArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double red[32];
   __shared__ double tot_s;
+  constexpr int SM = (SS > 0) ? SS : kMaxStates;
   cplx<T> *smem = reinterpret_cast<cplx<T> *>(smem_raw);
   const long long n = a.npts * a.S;
   const long long gtid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const long long gstride = (long long)gridDim.x * blockDim.x;
+  const bool tr = a.trace && blockIdx.x == 0 && threadIdx.x == 0;
+  unsigned long long tp[4] = {0, 0, 0, 0};
 
   // phi_0 = psi (OCheby: ket0->FastCopy(*Psi))
   for (long long i = gtid; i < n; i += gstride) st(a.buf[0] + i, ccast<T>(ld(a.psi + i)));
   if (!grid_sync(a.bar)) return;
 
-  // first two terms; the reduction gives the raw norm of psi before the step
-  double acc = 0.0;
-  if (a.nd == 1) {
-    phase_lines<T, SS, true>(a, a.buf[0], a.buf[1], 0.0, acc, smem);
-  } else {
-    phase_kinetic<T>(a, a.buf[0], smem);
-    if (!grid_sync(a.bar)) return;
-    phase_points<T, SS, true>(a, a.buf[0], a.buf[1], 0.0, acc);
-  }
-  double t = block_sum(acc, red);
-  if (threadIdx.x == 0) a.partials[blockIdx.x] = t;
-  if (!grid_sync(a.bar)) return;
-  t = sum_partials(a.partials, red);
-  if (threadIdx.x == 0) tot_s = t;
-  __syncthreads();
-  const double norm0 = tot_s;
-  bool done = !isfinite(norm0);
-  int status = done ? 2 : 0;
-  int used = 2;
-  double last = norm0;  // accumulated norm after the previous term
-  double norm_last = 0.0;
+  double acc = 0.0, t;
+  double norm0 = 0.0, last = 0.0, norm_last = 0.0;
+  bool done = false;
+  int status = 0, used = 2;
 
-  const bool tr = a.trace && blockIdx.x == 0 && threadIdx.x == 0;
-  unsigned long long tp[4] = {0, 0, 0, 0};
-  for (int i = 2; i < a.order && !done; ++i) {
-    const cplx<T> *phi = a.buf[(i + 1) & 1];  // phi_{i-1}
-    cplx<T> *kout = a.buf[i & 1];             // phi_{i-2} in, phi_i out
-    acc = 0.0;
-    unsigned long long t0 = tr ? gtimer() : 0, t1 = 0, t2 = 0, t3 = 0;
-    if (a.nd == 1) {
-      phase_lines<T, SS, false>(a, phi, kout, a.a[i], acc, smem);
-      if (tr) t1 = t2 = gtimer();
-    } else {
-      phase_kinetic<T>(a, phi, smem);
-      if (tr) t1 = gtimer();
-      if (!grid_sync(a.bar)) return;
-      if (tr) t2 = gtimer();
-      phase_points<T, SS, false>(a, phi, kout, a.a[i], acc);
-    }
+  if (a.nd == 1) {
+    // first two terms; the reduction gives the raw norm of psi before the step
+    phase_lines<T, SS, true>(a, a.buf[0], a.buf[1], 0.0, acc, smem);
     t = block_sum(acc, red);
     if (threadIdx.x == 0) a.partials[blockIdx.x] = t;
-    if (tr) t3 = gtimer();
     if (!grid_sync(a.bar)) return;
-    if (tr) {
-      const unsigned long long t4 = gtimer();
-      tp[0] += t1 - t0; tp[1] += t2 - t1; tp[2] += t3 - t2; tp[3] += t4 - t3;
-    }
     t = sum_partials(a.partials, red);
     if (threadIdx.x == 0) tot_s = t;
     __syncthreads();
-    const double tot = tot_s;
-    used = i + 1;
-    if (!isfinite(tot)) {
-      done = true;
-      status = 2;
-    } else if (!a.imag) {
-      // OCheby.cpp:179-182 (mixed precision: change against the previous term)
-      const double ref = a.diff ? last : norm0;
-      if (fabs(ref - tot) / norm0 < a.prec && a.offim0) done = true;
-    } else {
-      // OCheby.cpp:286-289
-      if (fabs(tot - norm_last) / norm_last < a.prec) done = true;
-      norm_last = tot;
+    norm0 = last = tot_s;
+    done = !isfinite(norm0);
+    if (done) status = 2;
+    for (int i = 2; i < a.order && !done; ++i) {
+      const cplx<T> *phi = a.buf[(i + 1) & 1];
+      cplx<T> *kout = a.buf[i & 1];
+      acc = 0.0;
+      phase_lines<T, SS, false>(a, phi, kout, a.a[i], acc, smem);
+      t = block_sum(acc, red);
+      if (threadIdx.x == 0) a.partials[blockIdx.x] = t;
+      if (!grid_sync(a.bar)) return;
+      t = sum_partials(a.partials, red);
+      if (threadIdx.x == 0) tot_s = t;
+      __syncthreads();
+      const double tot = tot_s;
+      used = i + 1;
+      if (!isfinite(tot)) { done = true; status = 2; }
+      else if (!a.imag) {
+        const double ref = a.diff ? last : norm0;
+        if (fabs(ref - tot) / norm0 < a.prec && a.offim0) done = true;
+      } else {
+        if (fabs(tot - norm_last) / norm_last < a.prec) done = true;
+        norm_last = tot;
+      }
+      last = tot;
     }
-    last = tot;
+  } else {
+    // phase 1: T_d phi_0 -> P[1]
+    phase_fused<T, SM>(a, PK_START, a.buf[0], nullptr, nullptr, nullptr, a.Pn[1], 0.0, acc, smem);
+    if (!grid_sync(a.bar)) return;
+    // phase 2: phi_1 (+ psi = a0 psi + a1 phi_1, raw norm of psi) and T_d phi_1 -> P[0]
+    acc = 0.0;
+    phase_fused<T, SM>(a, a.order > 2 ? PK_FIRST : PK_LAST, a.buf[0], nullptr, a.buf[1], a.Pn[1], a.Pn[0], 0.0,
+                       acc, smem);
+    t = block_sum(acc, red);
+    if (threadIdx.x == 0) a.partials[blockIdx.x] = t;
+    if (!grid_sync(a.bar)) return;
+    t = sum_partials(a.partials, red);
+    if (threadIdx.x == 0) tot_s = t;
+    __syncthreads();
+    norm0 = last = tot_s;
+    done = !isfinite(norm0);
+    if (done) status = 2;
+    // phase i+1: phi_i from P[i&1], phi_{i-1} = buf[(i-1)%3], phi_{i-2} = buf[(i-2)%3] -> buf[i%3]
+    for (int i = 2; i < a.order && !done; ++i) {
+      acc = 0.0;
+      const unsigned long long t0 = tr ? gtimer() : 0;
+      const int kind = (i + 1 < a.order) ? PK_TERM : PK_LAST;
+      phase_fused<T, SM>(a, kind, a.buf[(i - 1) % 3], a.buf[(i - 2) % 3], a.buf[i % 3], a.Pn[i & 1],
+                         a.Pn[(i + 1) & 1], a.a[i], acc, smem);
+      const unsigned long long t1 = tr ? gtimer() : 0;
+      t = block_sum(acc, red);
+      if (threadIdx.x == 0) a.partials[blockIdx.x] = t;
+      if (!grid_sync(a.bar)) return;
+      if (tr) { const unsigned long long t2 = gtimer(); tp[0] += t1 - t0; tp[1] += t2 - t1; }
+      t = sum_partials(a.partials, red);
+      if (threadIdx.x == 0) tot_s = t;
+      __syncthreads();
+      const double tot = tot_s;
+      used = i + 1;
+      if (!isfinite(tot)) { done = true; status = 2; }
+      else if (!a.imag) {
+        // OCheby.cpp:179-182 (mixed precision: change against the previous term)
+        const double ref = a.diff ? last : norm0;
+        if (fabs(ref - tot) / norm0 < a.prec && a.offim0) done = true;
+      } else {
+        // OCheby.cpp:286-289
+        if (fabs(tot - norm_last) / norm_last < a.prec) done = true;
+        norm_last = tot;
+      }
+      last = tot;
+    }
   }
 
   // common phase exp(c0 offset) of all coefficients
