@@ -512,20 +512,33 @@ void release_child(qdg_plan *p) {
 // Couplings of the terms selected by `pick` (kinetic terms excluded).
 template <typename F>
 qdg_status build_couplings(const qdg_plan *p, F pick, qdg::Couplings &cp) {
-  cp.ne = 0;
+  struct E { int row, col, gid, lid; };
+  std::vector<E> es;
   for (auto &t : p->terms) {
     if (t.kind == QDG_TERM_KINETIC || !pick(t)) continue;
     const int nrep = t.row != t.col ? 2 : 1;
-    for (int r = 0; r < nrep; ++r) {
-      if (cp.ne >= qdg::kMaxCouplings) return fail(QDG_EUNSUPPORTED, "too many potential/dipole matrix entries");
-      cp.row[cp.ne] = r ? t.col : t.row;
-      cp.col[cp.ne] = r ? t.row : t.col;
-      cp.gid[cp.ne] = t.grid;
-      cp.lid[cp.ne] = t.kind == QDG_TERM_DIPOLE ? t.laser : -1;
-      cp.ne++;
-    }
+    for (int r = 0; r < nrep; ++r)
+      es.push_back({r ? t.col : t.row, r ? t.row : t.col, t.grid, t.kind == QDG_TERM_DIPOLE ? t.laser : -1});
+  }
+  if ((int)es.size() > qdg::kMaxCouplings) return fail(QDG_EUNSUPPORTED, "too many potential/dipole matrix entries");
+  std::stable_sort(es.begin(), es.end(), [](const E &a, const E &b) { return a.row < b.row; });
+  memset(&cp, 0, sizeof(cp));
+  cp.ne = (int)es.size();
+  for (int e = 0; e < cp.ne; ++e) {
+    cp.row[e] = es[e].row; cp.col[e] = es[e].col; cp.gid[e] = es[e].gid; cp.lid[e] = es[e].lid;
+  }
+  for (int s = 0, e = 0; s <= qdg::kMaxStates; ++s) {
+    while (e < cp.ne && cp.row[e] < s) ++e;
+    cp.rs[s] = e;
   }
   return QDG_OK;
+}
+
+// Largest number of potential-matrix entries in one row.
+int max_row_entries(const qdg::Couplings &cp) {
+  int m = 0;
+  for (int s = 0; s < qdg::kMaxStates; ++s) m = std::max(m, cp.rs[s + 1] - cp.rs[s]);
+  return m;
 }
 
 // Sum of per-block per-state partial dot products (fixed order on the host).
@@ -602,6 +615,7 @@ qdg_status step_setup(qdg_prop *P) {
     P->step_smem = smem;
     return QDG_OK;
   }
+  if (max_row_entries(p->cp_h) > qdg::kMaxRowEntries) return QDG_OK;
   // kinetic lines of all dimensions, split into one contiguous run per block
   long long total = 0;
   for (int d = 0; d < p->nd; ++d) {

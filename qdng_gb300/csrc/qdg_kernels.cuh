@@ -31,7 +31,10 @@ struct Couplings {
   int col[kMaxCouplings];
   int gid[kMaxCouplings];
   int lid[kMaxCouplings];  // -1: static potential
+  // entries sorted by row: entries of row s are [rs[s], rs[s+1]) (the list above is in this order)
+  int rs[kMaxStates + 1];
 };
+static const int kMaxRowEntries = 4;  // entries per row the fused step kernel unrolls
 
 // Per-step Chebyshev control block in device memory.
 struct ChebyState {

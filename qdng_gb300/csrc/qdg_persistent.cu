@@ -78,75 +78,6 @@ __device__ double sum_partials(const double *partials, double *red) {
   return block_sum(v, red);
 }
 
-// T_d phi for every dimension.  The kinetic lines of all dimensions and
-// states are split into one contiguous run per block (balanced to within one
-// line); a block transforms up to lmax[d] lines of its run at once, so the
-// lines of a run are adjacent in memory (contiguous rows, or neighbouring
-// columns whose elements share memory segments).
-template <typename T>
-__device__ void phase_kinetic(const StepArgs<T> &a, const cplx<T> *phi, cplx<T> *smem) {
-  const long long total = a.line_start[a.nd];
-  const long long G = gridDim.x;
-  const long long end = total * (blockIdx.x + 1) / G;
-  long long l = total * blockIdx.x / G;
-  int cur_dim = -1;
-  cplx<T> *tws = smem;
-  while (l < end) {
-    int d = 0;
-    while (l >= a.line_start[d + 1]) ++d;
-    const DimPass<T> &g = a.dp[d];
-    const int N = g.N;
-    const long long stride = g.ls == 1 ? (long long)g.es : 1;  // element stride of the lines of dim d
-    const long long nl = a.npts / N;                          // lines per state
-    const long long local = l - a.line_start[d];
-    const int s = (int)(local / nl);
-    const long long l0 = local - (long long)s * nl;
-    long long cnt = end - l;
-    if (cnt > nl - l0) cnt = nl - l0;
-    if (cnt > a.lmax[d]) cnt = a.lmax[d];
-    const int L = (int)cnt;
-    cplx<T> *b0 = tws + N;
-    cplx<T> *b1 = b0 + (size_t)a.lmax[d] * N;
-    __syncthreads();
-    if (d != cur_dim) {
-      for (int i = threadIdx.x; i < N; i += blockDim.x) tws[i] = g.tw[i];
-      cur_dim = d;
-    }
-    const cplx<T> *src = phi + (long long)s * a.npts;
-    for (int idx = threadIdx.x; idx < L * N; idx += blockDim.x) {
-      int w, i;
-      if (stride == 1) { w = idx / N; i = idx - w * N; }
-      else { i = idx / L; w = idx - i * L; }
-      const long long line = l0 + w;
-      const long long p = (line % stride) + (line / stride) * stride * N + (long long)i * stride;
-      b0[w * N + i] = ld(src + p);
-    }
-    __syncthreads();
-    const int cur = fft_lines<T>(b0, b1, g.rp, L, tws, -1);
-    cplx<T> *bc = cur ? b1 : b0;
-    const double kf = g.kfac[s];
-    for (int idx = threadIdx.x; idx < L * N; idx += blockDim.x) {
-      const int i = idx % N;
-      const int kq = min(i, N - i);
-      bc[idx] = cmulr(bc[idx], (T)(kf * (double)kq * (double)kq));
-    }
-    __syncthreads();
-    const int cur2 = fft_lines<T>(bc, cur ? b0 : b1, g.rp, L, tws, +1);
-    const cplx<T> *res = cur2 ? (cur ? b0 : b1) : bc;
-    cplx<T> *dst = g.P + (long long)s * a.npts;
-    for (int idx = threadIdx.x; idx < L * N; idx += blockDim.x) {
-      int w, i;
-      if (stride == 1) { w = idx / N; i = idx - w * N; }
-      else { i = idx / L; w = idx - i * L; }
-      const long long line = l0 + w;
-      const long long p = (line % stride) + (line / stride) * stride * N + (long long)i * stride;
-      st(dst + p, res[w * N + i]);
-    }
-    l += cnt;
-  }
-  __syncthreads();
-}
-
 // ---- one phase per term on grids of two or more dimensions -----------------
 // Phase i+1 computes phi_i point-wise while loading the lines of its kinetic
 // transforms (H phi_{i-1} = sum_d T_d phi_{i-1} + W phi_{i-1} from the
@@ -156,68 +87,34 @@ __device__ void phase_kinetic(const StepArgs<T> &a, const cplx<T> *phi, cplx<T> 
 // recompute phi_i for their own points.
 enum PhaseKind { PK_START = 0, PK_FIRST = 1, PK_TERM = 2, PK_LAST = 3 };
 
-template <typename T, int SM>
-__device__ __forceinline__ cplx<T> phi_at(const StepArgs<T> &a, int kind, int s, long long p, const cplx<T> *phim1,
-                                          const cplx<T> *phim2, cplx<T> *const *Pprev, bool owner, cplx<T> *phout,
-                                          double coeff_i, double &acc) {
-  const long long npts = a.npts;
-  const long long g = (long long)s * npts + p;
-  if (kind == PK_START) return ld(phim1 + g);
-  // h = H phi_{i-1} at (s, p)
-  cplx<T> h = ld(Pprev[0] + g);
-  for (int d = 1; d < a.nd; ++d) h = h + ld(Pprev[d] + g);
-  const int ne = a.cp->ne;
-  for (int e = 0; e < ne; ++e) {
-    if (a.cp->row[e] != s) continue;
-    const T v = (T)(a.coef[e]) * a.grids[(long long)a.cp->gid[e] * npts + p];
-    h = h + cmulr(ld(phim1 + (long long)a.cp->col[e] * npts + p), v);
-  }
-  const cplx<T> off = ccast<T>(a.offset);
-  const cplx<T> pm1 = ld(phim1 + g);
-  if (kind == PK_FIRST) {
-    const cplx<T> bf = cmul(h - cmul(off, pm1), ccast<T>(a.fac1));
-    if (owner) {
-      const cplx<double> ps = ld(a.psi + g);
-      acc += cabs2(ps);
-      st(phout + g, bf);
-      const cplx<double> b = ccast<double>(bf);
-      st(a.psi + g, mk(ps.re * a.a[0] + b.re * a.a[1], ps.im * a.a[0] + b.im * a.a[1]));
-    }
-    return bf;
-  }
-  const cplx<T> bf = cmul(h - cmul(off, pm1), ccast<T>(a.fac));
-  const cplx<T> km2 = ld(phim2 + g);
-  const cplx<T> k2 = a.imag ? bf - km2 : bf + km2;
-  if (owner) {
-    st(phout + g, k2);
-    cplx<double> ps = ld(a.psi + g);
-    ps.re += coeff_i * (double)k2.re;
-    ps.im += coeff_i * (double)k2.im;
-    st(a.psi + g, ps);
-    acc += cabs2(ps);
-  }
-  return k2;
-}
-
 // Kinetic transforms of phi_i (computed on load) for every dimension;
 // results go to Pnext.  PK_LAST only finishes phi_i and psi (row lines).
-template <typename T, int SM>
-__device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *phim1, const cplx<T> *phim2,
-                            cplx<T> *phout, cplx<T> *const *Pprev, cplx<T> *const *Pnext, double coeff_i,
-                            double &acc, cplx<T> *smem) {
-  const long long total = a.line_start[a.nd];
+// Loads of UNR points per thread are issued before any use or store, so the
+// latency of the L2 round trips overlaps.
+template <typename T, int ND, int SM>
+__device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__restrict__ phim1,
+                            const cplx<T> *__restrict__ phim2, cplx<T> *__restrict__ phout,
+                            cplx<T> *const *Pprev, cplx<T> *const *Pnext, double coeff_i, double &acc,
+                            cplx<T> *smem) {
+  constexpr int UNR = (sizeof(T) == 8 || SM > 2) ? 1 : 2;
+  constexpr int RE = kMaxRowEntries;
+  const long long npts = a.npts;
+  const long long total = a.line_start[ND];
   const long long G = gridDim.x;
   const long long end = total * (blockIdx.x + 1) / G;
   long long l = total * blockIdx.x / G;
   int cur_dim = -1;
   cplx<T> *tws = smem;
+  const cplx<T> off = ccast<T>(a.offset);
+  const cplx<T> fac = ccast<T>(kind == PK_FIRST ? a.fac1 : a.fac);
+  const T *__restrict__ grids = a.grids;
   while (l < end) {
     int d = 0;
     while (l >= a.line_start[d + 1]) ++d;
     const DimPass<T> &g = a.dp[d];
     const int N = g.N;
     const long long stride = g.ls == 1 ? (long long)g.es : 1;
-    const long long nl = a.npts / N;
+    const long long nl = npts / N;
     const long long local = l - a.line_start[d];
     const int s = (int)(local / nl);
     const long long l0 = local - (long long)s * nl;
@@ -235,22 +132,107 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *phim1
       for (int i = threadIdx.x; i < N; i += blockDim.x) tws[i] = g.tw[i];
       cur_dim = d;
     }
-#pragma unroll 4
-    for (int idx = threadIdx.x; idx < L * N; idx += blockDim.x) {
-      int w, i;
-      if (stride == 1) { w = idx / N; i = idx - w * N; }
-      else { i = idx / L; w = idx - i * L; }
-      const long long line = l0 + w;
-      const long long p = (line % stride) + (line / stride) * stride * N + (long long)i * stride;
-      const cplx<T> v = phi_at<T, SM>(a, kind, s, p, phim1, phim2, Pprev, owner, phout, coeff_i, acc);
-      if (kind != PK_LAST) b0[w * N + i] = v;
+    // potential-matrix entries of row s
+    const int e0 = a.cp->rs[s];
+    const int ne = a.cp->rs[s + 1] - e0;
+    int ecol[RE], egid[RE];
+    T ecoef[RE];
+#pragma unroll
+    for (int k = 0; k < RE; ++k) {
+      ecol[k] = k < ne ? a.cp->col[e0 + k] : 0;
+      egid[k] = k < ne ? a.cp->gid[e0 + k] : 0;
+      ecoef[k] = k < ne ? (T)a.coef[e0 + k] : (T)0;
+    }
+    const long long so = (long long)s * npts;
+    const int tot = L * N;
+    for (int base = threadIdx.x; base < tot; base += UNR * blockDim.x) {
+      long long pp[UNR];
+      int sidx[UNR];
+      cplx<T> v[UNR];
+      // ---- gather
+      cplx<T> hP[UNR], pm[UNR][SM], km2[UNR];
+      T vg[UNR][RE];
+      cplx<double> ps[UNR];
+#pragma unroll
+      for (int u = 0; u < UNR; ++u) {
+        const int idx = base + u * blockDim.x;
+        const bool ok = idx < tot;
+        int w = 0, i = 0;
+        if (ok) {
+          if (stride == 1) { w = idx / N; i = idx - w * N; }
+          else { i = idx / L; w = idx - i * L; }
+        }
+        sidx[u] = ok ? w * N + i : -1;
+        const long long line = l0 + w;
+        const long long p = (line % stride) + (line / stride) * stride * N + (long long)i * stride;
+        pp[u] = p;
+        if (!ok) continue;
+        if (kind == PK_START) { v[u] = ldg(phim1 + so + p); continue; }
+        cplx<T> h = ldg(Pprev[0] + so + p);
+#pragma unroll
+        for (int dd = 1; dd < ND; ++dd) h = h + ldg(Pprev[dd] + so + p);
+        hP[u] = h;
+#pragma unroll
+        for (int j = 0; j < SM; ++j)
+          if (j < a.S) pm[u][j] = ldg(phim1 + (long long)j * npts + p);
+#pragma unroll
+        for (int k = 0; k < RE; ++k) vg[u][k] = k < ne ? __ldg(grids + (long long)egid[k] * npts + p) : (T)0;
+        if (kind != PK_FIRST) km2[u] = ldg(phim2 + so + p);
+        if (owner) ps[u] = ld(a.psi + so + p);
+      }
+      // ---- compute and scatter
+#pragma unroll
+      for (int u = 0; u < UNR; ++u) {
+        if (sidx[u] < 0) continue;
+        if (kind != PK_START) {
+          cplx<T> h = hP[u];
+          cplx<T> self = pm[u][0];
+#pragma unroll
+          for (int j = 1; j < SM; ++j)
+            if (j == s) self = pm[u][j];
+#pragma unroll
+          for (int k = 0; k < RE; ++k) {
+            if (k < ne) {
+              cplx<T> x = pm[u][0];
+#pragma unroll
+              for (int j = 1; j < SM; ++j)
+                if (j == ecol[k]) x = pm[u][j];
+              h = h + cmulr(x, ecoef[k] * vg[u][k]);
+            }
+          }
+          const cplx<T> bf = cmul(h - cmul(off, self), fac);
+          const long long gidx = so + pp[u];
+          if (kind == PK_FIRST) {
+            v[u] = bf;
+            if (owner) {
+              const cplx<double> p0 = ps[u];
+              acc += cabs2(p0);
+              st(phout + gidx, bf);
+              const cplx<double> b = ccast<double>(bf);
+              st(a.psi + gidx, mk(p0.re * a.a[0] + b.re * a.a[1], p0.im * a.a[0] + b.im * a.a[1]));
+            }
+          } else {
+            const cplx<T> k2 = a.imag ? bf - km2[u] : bf + km2[u];
+            v[u] = k2;
+            if (owner) {
+              st(phout + gidx, k2);
+              cplx<double> p0 = ps[u];
+              p0.re += coeff_i * (double)k2.re;
+              p0.im += coeff_i * (double)k2.im;
+              st(a.psi + gidx, p0);
+              acc += cabs2(p0);
+            }
+          }
+        }
+        if (kind != PK_LAST) b0[sidx[u]] = v[u];
+      }
     }
     if (kind == PK_LAST) continue;
     __syncthreads();
     const int cur = fft_lines<T>(b0, b1, g.rp, L, tws, -1);
     cplx<T> *bc = cur ? b1 : b0;
     const double kf = g.kfac[s];
-    for (int idx = threadIdx.x; idx < L * N; idx += blockDim.x) {
+    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
       const int i = idx % N;
       const int kq = min(i, N - i);
       bc[idx] = cmulr(bc[idx], (T)(kf * (double)kq * (double)kq));
@@ -258,8 +240,8 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *phim1
     __syncthreads();
     const int cur2 = fft_lines<T>(bc, cur ? b0 : b1, g.rp, L, tws, +1);
     const cplx<T> *res = cur2 ? (cur ? b0 : b1) : bc;
-    cplx<T> *dst = Pnext[d] + (long long)s * a.npts;
-    for (int idx = threadIdx.x; idx < L * N; idx += blockDim.x) {
+    cplx<T> *dst = Pnext[d] + so;
+    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
       int w, i;
       if (stride == 1) { w = idx / N; i = idx - w * N; }
       else { i = idx / L; w = idx - i * L; }
@@ -314,29 +296,6 @@ __device__ __forceinline__ void point_term(const StepArgs<T> &a, long long p, co
   }
 }
 
-// Point-wise part of a term on a grid of two or more dimensions.
-template <typename T, int SS, bool FIRST>
-__device__ void phase_points(const StepArgs<T> &a, const cplx<T> *phi, cplx<T> *kout, double coeff_i,
-                             double &acc) {
-  constexpr int SM = (SS > 0) ? SS : kMaxStates;
-  const int S = (SS > 0) ? SS : a.S;
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < a.npts;
-       p += (long long)gridDim.x * blockDim.x) {
-    cplx<T> ph[SM], h[SM];
-#pragma unroll
-    for (int s = 0; s < SM; ++s) {
-      if (s < S) {
-        const long long g = (long long)s * a.npts + p;
-        ph[s] = ld(phi + g);
-        cplx<T> v = ld(a.dp[0].P + g);
-        for (int d = 1; d < a.nd; ++d) v = v + ld(a.dp[d].P + g);
-        h[s] = v;
-      }
-    }
-    point_term<T, SM, FIRST>(a, p, ph, h, kout, coeff_i, S, acc);
-  }
-}
-
 // One-dimensional grid: FFT, k^2, inverse FFT and point work of a tile of
 // lines for all states in one block.
 template <typename T, int SS, bool FIRST>
@@ -385,6 +344,15 @@ __device__ void phase_lines(const StepArgs<T> &a, const cplx<T> *phi, cplx<T> *k
     }
   }
   __syncthreads();
+}
+
+template <typename T, int SM>
+__device__ __forceinline__ void fused(const StepArgs<T> &a, int kind, const cplx<T> *phim1, const cplx<T> *phim2,
+                                      cplx<T> *phout, cplx<T> *const *Pprev, cplx<T> *const *Pnext, double coeff_i,
+                                      double &acc, cplx<T> *smem) {
+  if (a.nd == 2) phase_fused<T, 2, SM>(a, kind, phim1, phim2, phout, Pprev, Pnext, coeff_i, acc, smem);
+  else if (a.nd == 3) phase_fused<T, 3, SM>(a, kind, phim1, phim2, phout, Pprev, Pnext, coeff_i, acc, smem);
+  else phase_fused<T, 4, SM>(a, kind, phim1, phim2, phout, Pprev, Pnext, coeff_i, acc, smem);
 }
 
 template <typename T, int SS>
@@ -446,12 +414,12 @@ __global__ void __launch_bounds__(256) cheby_step_kernel(StepArgs<T> a) {
     }
   } else {
     // phase 1: T_d phi_0 -> P[1]
-    phase_fused<T, SM>(a, PK_START, a.buf[0], nullptr, nullptr, nullptr, a.Pn[1], 0.0, acc, smem);
+    fused<T, SM>(a, PK_START, a.buf[0], nullptr, nullptr, nullptr, a.Pn[1], 0.0, acc, smem);
     if (!grid_sync(a.bar)) return;
     // phase 2: phi_1 (+ psi = a0 psi + a1 phi_1, raw norm of psi) and T_d phi_1 -> P[0]
     acc = 0.0;
-    phase_fused<T, SM>(a, a.order > 2 ? PK_FIRST : PK_LAST, a.buf[0], nullptr, a.buf[1], a.Pn[1], a.Pn[0], 0.0,
-                       acc, smem);
+    fused<T, SM>(a, a.order > 2 ? PK_FIRST : PK_LAST, a.buf[0], nullptr, a.buf[1], a.Pn[1], a.Pn[0], 0.0, acc,
+                 smem);
     t = block_sum(acc, red);
     if (threadIdx.x == 0) a.partials[blockIdx.x] = t;
     if (!grid_sync(a.bar)) return;
@@ -466,8 +434,8 @@ __global__ void __launch_bounds__(256) cheby_step_kernel(StepArgs<T> a) {
       acc = 0.0;
       const unsigned long long t0 = tr ? gtimer() : 0;
       const int kind = (i + 1 < a.order) ? PK_TERM : PK_LAST;
-      phase_fused<T, SM>(a, kind, a.buf[(i - 1) % 3], a.buf[(i - 2) % 3], a.buf[i % 3], a.Pn[i & 1],
-                         a.Pn[(i + 1) & 1], a.a[i], acc, smem);
+      fused<T, SM>(a, kind, a.buf[(i - 1) % 3], a.buf[(i - 2) % 3], a.buf[i % 3], a.Pn[i & 1],
+                   a.Pn[(i + 1) & 1], a.a[i], acc, smem);
       const unsigned long long t1 = tr ? gtimer() : 0;
       t = block_sum(acc, red);
       if (threadIdx.x == 0) a.partials[blockIdx.x] = t;
