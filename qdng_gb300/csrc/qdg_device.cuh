@@ -32,6 +32,13 @@ template <typename T> __device__ __forceinline__ cplx<T> ldg(const cplx<T> *p) {
   V v = __ldg(reinterpret_cast<const V *>(p));
   return mk<T>(v.x, v.y);
 }
+// Load through L2 only: data written by other blocks earlier in the same
+// kernel (after a grid barrier) must not come from a stale L1 line.
+template <typename T> __device__ __forceinline__ cplx<T> ldcg(const cplx<T> *p) {
+  typedef typename vec2<T>::type V;
+  V v = __ldcg(reinterpret_cast<const V *>(p));
+  return mk<T>(v.x, v.y);
+}
 template <typename T> __device__ __forceinline__ cplx<T> ld(const cplx<T> *p) {
   typedef typename vec2<T>::type V;
   V v = *reinterpret_cast<const V *>(p);

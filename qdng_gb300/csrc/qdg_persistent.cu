@@ -167,18 +167,18 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
         const long long p = (line % stride) + (line / stride) * stride * N + (long long)i * stride;
         pp[u] = p;
         if (!ok) continue;
-        if (kind == PK_START) { v[u] = ldg(phim1 + so + p); continue; }
-        cplx<T> h = ldg(Pprev[0] + so + p);
+        if (kind == PK_START) { v[u] = ldcg(phim1 + so + p); continue; }
+        cplx<T> h = ldcg(Pprev[0] + so + p);
 #pragma unroll
-        for (int dd = 1; dd < ND; ++dd) h = h + ldg(Pprev[dd] + so + p);
+        for (int dd = 1; dd < ND; ++dd) h = h + ldcg(Pprev[dd] + so + p);
         hP[u] = h;
 #pragma unroll
         for (int j = 0; j < SM; ++j)
-          if (j < a.S) pm[u][j] = ldg(phim1 + (long long)j * npts + p);
+          if (j < a.S) pm[u][j] = ldcg(phim1 + (long long)j * npts + p);
 #pragma unroll
         for (int k = 0; k < RE; ++k) vg[u][k] = k < ne ? __ldg(grids + (long long)egid[k] * npts + p) : (T)0;
-        if (kind != PK_FIRST) km2[u] = ldg(phim2 + so + p);
-        if (owner) ps[u] = ld(a.psi + so + p);
+        if (kind != PK_FIRST) km2[u] = ldcg(phim2 + so + p);
+        if (owner) ps[u] = ldcg(a.psi + so + p);
       }
       // ---- compute and scatter
 #pragma unroll
@@ -277,17 +277,17 @@ __device__ __forceinline__ void point_term(const StepArgs<T> &a, long long p, co
     const long long g = (long long)s * a.npts + p;
     if (FIRST) {
       const cplx<T> bf = cmul(h[s] - cmul(off, ph[s]), ccast<T>(a.fac1));
-      const cplx<double> ps = ld(a.psi + g);
+      const cplx<double> ps = ldcg(a.psi + g);
       acc += cabs2(ps);
       st(kout + g, bf);
       const cplx<double> b = ccast<double>(bf);
       st(a.psi + g, mk(ps.re * a.a[0] + b.re * a.a[1], ps.im * a.a[0] + b.im * a.a[1]));
     } else {
       const cplx<T> bf = cmul(h[s] - cmul(off, ph[s]), ccast<T>(a.fac));
-      const cplx<T> km2 = ld(kout + g);
+      const cplx<T> km2 = ldcg(kout + g);
       const cplx<T> k2 = a.imag ? bf - km2 : bf + km2;
       st(kout + g, k2);
-      cplx<double> ps = ld(a.psi + g);
+      cplx<double> ps = ldcg(a.psi + g);
       ps.re += coeff_i * (double)k2.re;
       ps.im += coeff_i * (double)k2.im;
       st(a.psi + g, ps);
@@ -317,7 +317,7 @@ __device__ void phase_lines(const StepArgs<T> &a, const cplx<T> *phi, cplx<T> *k
     for (int idx = threadIdx.x; idx < L * N; idx += blockDim.x) {
       const int l = idx / N, i = idx - l * N;
       const int s = l / TW, w = l - s * TW;
-      b0[idx] = ld(phi + (long long)s * a.npts + base + (long long)w * N + i);
+      b0[idx] = ldcg(phi + (long long)s * a.npts + base + (long long)w * N + i);
     }
     __syncthreads();
     const int cur = fft_lines<T>(b0, b1, g.rp, L, tws, -1);
@@ -337,7 +337,7 @@ __device__ void phase_lines(const StepArgs<T> &a, const cplx<T> *phi, cplx<T> *k
 #pragma unroll
       for (int s = 0; s < SM; ++s)
         if (s < S) {
-          ph[s] = ld(phi + (long long)s * a.npts + p);
+          ph[s] = ldcg(phi + (long long)s * a.npts + p);
           h[s] = res[(s * TW + w) * N + i];
         }
       point_term<T, SM, FIRST>(a, p, ph, h, kout, coeff_i, S, acc);
@@ -461,7 +461,7 @@ __global__ void __launch_bounds__(256) cheby_step_kernel(StepArgs<T> a) {
   }
 
   // common phase exp(c0 offset) of all coefficients
-  for (long long i = gtid; i < n; i += gstride) st(a.psi + i, cmul(ld(a.psi + i), a.ph));
+  for (long long i = gtid; i < n; i += gstride) st(a.psi + i, cmul(ldcg(a.psi + i), a.ph));
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     a.cs->terms = used;
     a.cs->total += used;
