@@ -208,6 +208,29 @@ qdg_status qdg_profile_read(qdg_plan *plan, double ms[8], int64_t launches[8]);
  * it, in its own point work, and waiting at the norm barrier; resets them. */
 qdg_status qdg_prop_phase_times(qdg_prop *prop, double ns[4]);
 
+/* ---- H psi without device allocation ------------------------------------ */
+
+/* Bytes of the library's static device scratch used by qdg_h_apply_noalloc
+ * (held on every GPU that loads the library until the process exits). */
+#define QDG_NOALLOC_SCRATCH_BYTES (8 << 20)
+
+/* out = H(step) in, like qdg_h_apply, for callers that cannot allocate
+ * device memory (code running during CUDA graph capture, frameworks whose
+ * pool owns all device memory).  It calls no cudaMalloc/cudaFree: desc is a
+ * host struct whose grid_data and laser_data point to DEVICE arrays, psi_in
+ * and psi_out are device arrays of nstates*npoints complex128, and all
+ * scratch lives in one static device array of QDG_NOALLOC_SCRATCH_BYTES.
+ * Problems needing more scratch (ndims > 1: ndims * nstates * npoints * 16
+ * bytes plus small tables) fail with QDG_EINVAL.  FP64 only.  Work is
+ * queued on cuda_stream (NULL: the legacy default stream) without
+ * synchronising.  Every call shares the scratch array: calls whose kernels
+ * overlap on the GPU race, so serialise them on one stream.  The first call
+ * on a device looks up the array's address with that device current; make
+ * it before any stream capture.  This entry point has no counterpart in the
+ * reference. */
+qdg_status qdg_h_apply_noalloc(const qdg_hplan_desc *desc, const double *psi_in, double *psi_out,
+                               int64_t step, void *cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -119,6 +119,7 @@ SIGNATURES = [
     ("qdg_profile_enable", _i32, [_vp, _i32]),
     ("qdg_profile_read", _i32, [_vp, _dp, C.POINTER(_i64)]),
     ("qdg_prop_phase_times", _i32, [_vp, _dp]),
+    ("qdg_h_apply_noalloc", _i32, [C.POINTER(HPlanDesc), _dp, _dp, _i64, _vp]),
 ]
 
 

@@ -33,6 +33,12 @@ qdg_status fail(qdg_status s, const std::string &msg) {
   return s;
 }
 
+}  // namespace
+
+void qdg::set_last_error(const std::string &msg) { g_last_error = msg; }
+
+namespace {
+
 #define CK(...)                                                                           \
   do {                                                                                    \
     cudaError_t e_ = (__VA_ARGS__);                                                       \

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 #include "qdg_device.cuh"
 
 namespace qdg {
@@ -214,6 +216,9 @@ cudaError_t launch_combine(int mode, const CombArgs<T> &a, int grid, int block, 
 // coef[e] for clock step `step` (Laser::Get, src/qdlib/Laser.cpp:125-128).
 cudaError_t launch_set_coefs(double *coef, const Couplings *cp, const double *lasers, int laser_nt, long long step,
                              cudaStream_t st);
+
+// Message for qdg_last_error() on the calling thread (qdg_api.cu).
+void set_last_error(const std::string &msg);
 
 // Kernels launched by this library in the process (all launchers count;
 // replays of captured graphs are added by the caller).
