@@ -613,7 +613,7 @@ qdg_status step_setup(qdg_prop *P) {
     P->step_tw1 = p->dim[0].TW_e;
     const size_t smem = pass_smem(p, 0, P->step_tw1, p->S);
     if (smem > 227 * 1024) return QDG_OK;
-    const int per_sm = qdg::cheby_step_max_blocks<T>(p->S, 256, smem);
+    const int per_sm = qdg::cheby_step_max_blocks<T>(p->S, p->nd, 256, smem);
     if (per_sm <= 0) return QDG_OK;
     long long want = p->npts / ((long long)p->dim[0].n * P->step_tw1);
     want = std::min<long long>(want, (long long)per_sm * p->sm_count);
@@ -634,7 +634,7 @@ qdg_status step_setup(qdg_prop *P) {
   size_t smem = 0;
   for (int iter = 0, per_sm = 0; iter < 3; ++iter) {
     const size_t probe = iter == 0 ? 16 * 1024 : smem;
-    per_sm = qdg::cheby_step_max_blocks<T>(p->S, 256, probe);
+    per_sm = qdg::cheby_step_max_blocks<T>(p->S, p->nd, 256, probe);
     if (per_sm <= 0) return QDG_OK;
     grid = (int)std::min<long long>((long long)per_sm * p->sm_count, std::min<long long>(total, p->max_parts));
     const long long chunk = (total + grid - 1) / grid;
@@ -647,9 +647,9 @@ qdg_status step_setup(qdg_prop *P) {
       smem = std::max(smem, (size_t)(n * (1 + 2 * (size_t)lm)) * cs);
     }
     if (smem > 227 * 1024) return QDG_OK;
-    if (qdg::cheby_step_max_blocks<T>(p->S, 256, smem) >= per_sm) break;
+    if (qdg::cheby_step_max_blocks<T>(p->S, p->nd, 256, smem) >= per_sm) break;
   }
-  const int per_sm = qdg::cheby_step_max_blocks<T>(p->S, 256, smem);
+  const int per_sm = qdg::cheby_step_max_blocks<T>(p->S, p->nd, 256, smem);
   if (per_sm <= 0) return QDG_OK;
   P->step_grid = std::min(grid, per_sm * p->sm_count);
   P->step_smem = smem;

@@ -202,7 +202,7 @@ struct StepArgs {
 };
 
 template <typename T>
-int cheby_step_max_blocks(int S, int block, size_t smem);
+int cheby_step_max_blocks(int S, int nd, int block, size_t smem);
 template <typename T>
 cudaError_t launch_cheby_step(const StepArgs<T> &a, int grid, int block, size_t smem, cudaStream_t st);
 

@@ -346,17 +346,13 @@ __device__ void phase_lines(const StepArgs<T> &a, const cplx<T> *phi, cplx<T> *k
   __syncthreads();
 }
 
-template <typename T, int SM>
-__device__ __forceinline__ void fused(const StepArgs<T> &a, int kind, const cplx<T> *phim1, const cplx<T> *phim2,
-                                      cplx<T> *phout, cplx<T> *const *Pprev, cplx<T> *const *Pnext, double coeff_i,
-                                      double &acc, cplx<T> *smem) {
-  if (a.nd == 2) phase_fused<T, 2, SM>(a, kind, phim1, phim2, phout, Pprev, Pnext, coeff_i, acc, smem);
-  else if (a.nd == 3) phase_fused<T, 3, SM>(a, kind, phim1, phim2, phout, Pprev, Pnext, coeff_i, acc, smem);
-  else phase_fused<T, 4, SM>(a, kind, phim1, phim2, phout, Pprev, Pnext, coeff_i, acc, smem);
-}
+// Minimum resident blocks per SM the compiler must allow for (register cap):
+// the FP32 kernel is latency bound and needs more warps than the FP64 one.
+template <typename T> struct StepOcc { static const int value = 1; };
+template <> struct StepOcc<float> { static const int value = 2; };
 
-template <typename T, int SS>
-__global__ void __launch_bounds__(256) cheby_step_kernel(StepArgs<T> a) {
+template <typename T, int SS, int ND>
+__global__ void __launch_bounds__(256, StepOcc<T>::value) cheby_step_kernel(StepArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double red[32];
   __shared__ double tot_s;
@@ -377,7 +373,7 @@ __global__ void __launch_bounds__(256) cheby_step_kernel(StepArgs<T> a) {
   bool done = false;
   int status = 0, used = 2;
 
-  if (a.nd == 1) {
+  if (ND == 1) {
     // first two terms; the reduction gives the raw norm of psi before the step
     phase_lines<T, SS, true>(a, a.buf[0], a.buf[1], 0.0, acc, smem);
     t = block_sum(acc, red);
@@ -414,12 +410,12 @@ __global__ void __launch_bounds__(256) cheby_step_kernel(StepArgs<T> a) {
     }
   } else {
     // phase 1: T_d phi_0 -> P[1]
-    fused<T, SM>(a, PK_START, a.buf[0], nullptr, nullptr, nullptr, a.Pn[1], 0.0, acc, smem);
+    phase_fused<T, ND, SM>(a, PK_START, a.buf[0], nullptr, nullptr, nullptr, a.Pn[1], 0.0, acc, smem);
     if (!grid_sync(a.bar)) return;
     // phase 2: phi_1 (+ psi = a0 psi + a1 phi_1, raw norm of psi) and T_d phi_1 -> P[0]
     acc = 0.0;
-    fused<T, SM>(a, a.order > 2 ? PK_FIRST : PK_LAST, a.buf[0], nullptr, a.buf[1], a.Pn[1], a.Pn[0], 0.0, acc,
-                 smem);
+    phase_fused<T, ND, SM>(a, a.order > 2 ? PK_FIRST : PK_LAST, a.buf[0], nullptr, a.buf[1], a.Pn[1], a.Pn[0], 0.0,
+                           acc, smem);
     t = block_sum(acc, red);
     if (threadIdx.x == 0) a.partials[blockIdx.x] = t;
     if (!grid_sync(a.bar)) return;
@@ -434,8 +430,8 @@ __global__ void __launch_bounds__(256) cheby_step_kernel(StepArgs<T> a) {
       acc = 0.0;
       const unsigned long long t0 = tr ? gtimer() : 0;
       const int kind = (i + 1 < a.order) ? PK_TERM : PK_LAST;
-      fused<T, SM>(a, kind, a.buf[(i - 1) % 3], a.buf[(i - 2) % 3], a.buf[i % 3], a.Pn[i & 1],
-                   a.Pn[(i + 1) & 1], a.a[i], acc, smem);
+      phase_fused<T, ND, SM>(a, kind, a.buf[(i - 1) % 3], a.buf[(i - 2) % 3], a.buf[i % 3], a.Pn[i & 1],
+                             a.Pn[(i + 1) & 1], a.a[i], acc, smem);
       const unsigned long long t1 = tr ? gtimer() : 0;
       t = block_sum(acc, red);
       if (threadIdx.x == 0) a.partials[blockIdx.x] = t;
@@ -472,15 +468,25 @@ __global__ void __launch_bounds__(256) cheby_step_kernel(StepArgs<T> a) {
   }
 }
 
-template <typename T>
-static void *step_ptr(int S) {
-  return S == 1 ? (void *)cheby_step_kernel<T, 1> : S == 2 ? (void *)cheby_step_kernel<T, 2>
-                                                           : (void *)cheby_step_kernel<T, 0>;
+template <typename T, int ND>
+static void *step_ptr_nd(int S) {
+  return S == 1 ? (void *)cheby_step_kernel<T, 1, ND> : S == 2 ? (void *)cheby_step_kernel<T, 2, ND>
+                                                               : (void *)cheby_step_kernel<T, 0, ND>;
 }
 
 template <typename T>
-int cheby_step_max_blocks(int S, int block, size_t smem) {
-  void *k = step_ptr<T>(S);
+static void *step_ptr(int S, int nd) {
+  switch (nd) {
+    case 1: return step_ptr_nd<T, 1>(S);
+    case 2: return step_ptr_nd<T, 2>(S);
+    case 3: return step_ptr_nd<T, 3>(S);
+    default: return step_ptr_nd<T, 4>(S);
+  }
+}
+
+template <typename T>
+int cheby_step_max_blocks(int S, int nd, int block, size_t smem) {
+  void *k = step_ptr<T>(S, nd);
   if (smem > 48 * 1024 && cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return 0;
   int nb = 0;
@@ -490,7 +496,7 @@ int cheby_step_max_blocks(int S, int block, size_t smem) {
 
 template <typename T>
 cudaError_t launch_cheby_step(const StepArgs<T> &a, int grid, int block, size_t smem, cudaStream_t st) {
-  void *k = step_ptr<T>(a.S);
+  void *k = step_ptr<T>(a.S, a.nd);
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -500,8 +506,8 @@ cudaError_t launch_cheby_step(const StepArgs<T> &a, int grid, int block, size_t 
   return cudaLaunchCooperativeKernel(k, dim3(grid), dim3(block), args, smem, st);
 }
 
-template int cheby_step_max_blocks<double>(int, int, size_t);
-template int cheby_step_max_blocks<float>(int, int, size_t);
+template int cheby_step_max_blocks<double>(int, int, int, size_t);
+template int cheby_step_max_blocks<float>(int, int, int, size_t);
 template cudaError_t launch_cheby_step<double>(const StepArgs<double> &, int, int, size_t, cudaStream_t);
 template cudaError_t launch_cheby_step<float>(const StepArgs<float> &, int, int, size_t, cudaStream_t);
 
