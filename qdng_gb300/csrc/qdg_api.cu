@@ -54,6 +54,7 @@ struct DimInfo {
   qdg::RadixPlan rp;
   void *tw;           // n twiddles (cplx<T>)
   double *kfac;       // [S] dk^2/(2m)/n for H passes
+  void *ktab;         // [S][n] kfac[s] * min(i, n-i)^2 in the bulk type
   int TW_k, TW_e;     // lines per tile: kinetic-only passes, coupled epilogue pass
 };
 
@@ -452,6 +453,14 @@ qdg_status upload_tables(qdg_plan *p) {
       if (t.kind == QDG_TERM_KINETIC) kf[t.row] += (p->dk[d] * p->dk[d]) / (2.0 * t.mass[d]) / (double)n;
     CK(cudaMalloc(&di.kfac, sizeof(double) * S));
     CK(cudaMemcpy(di.kfac, kf.data(), sizeof(double) * S, cudaMemcpyHostToDevice));
+    std::vector<T> kt((size_t)S * n);
+    for (int st = 0; st < S; ++st)
+      for (int i = 0; i < n; ++i) {
+        const double kq = std::min(i, n - i);
+        kt[(size_t)st * n + i] = (T)(kf[st] * kq * kq);
+      }
+    CK(cudaMalloc(&di.ktab, sizeof(T) * kt.size()));
+    CK(cudaMemcpy(di.ktab, kt.data(), sizeof(T) * kt.size(), cudaMemcpyHostToDevice));
   }
   // grids in the bulk type
   std::vector<T> g(p->grids_h.size());
@@ -487,6 +496,7 @@ void free_plan(qdg_plan *p) {
   for (int d = 0; d < QDG_MAX_DIMS; ++d) {
     if (p->dim[d].tw) cudaFree(p->dim[d].tw);
     if (p->dim[d].kfac) cudaFree(p->dim[d].kfac);
+    if (p->dim[d].ktab) cudaFree(p->dim[d].ktab);
   }
   if (p->d_grids) cudaFree(p->d_grids);
   if (p->d_lasers) cudaFree(p->d_lasers);
@@ -674,6 +684,7 @@ qdg_status cheby_step_persistent(qdg_prop *P, cplx<double> *psi, long long step)
     dp.N = g.N; dp.es = g.es; dp.ls = g.ls; dp.TW = g.TW; dp.tiles_per_hi = g.tiles_per_hi;
     dp.hi_stride = g.hi_stride; dp.ntiles = g.ntiles; dp.rp = g.rp; dp.tw = g.tw; dp.kfac = g.kfac;
     dp.P = reinterpret_cast<cplx<T> *>(p->d_Pd[d]);
+    dp.ktab = reinterpret_cast<const T *>(p->dim[d].ktab);
     a.item_start[d] = items;
     items += g.ntiles * p->S;
   }

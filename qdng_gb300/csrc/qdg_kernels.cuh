@@ -124,6 +124,7 @@ struct DimPass {
   const cplx<T> *tw;
   const double *kfac;   // [S] dk^2/(2m)/N
   cplx<T> *P;           // T_d phi output (state stride npts)
+  const T *ktab;        // [S][N] kinetic multipliers kfac[s] * min(i, N-i)^2 (precomputed)
 };
 
 // T_d phi for every dimension d in one launch (the kinetic operator is a sum

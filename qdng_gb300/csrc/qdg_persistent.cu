@@ -24,6 +24,7 @@
 // and the kernel returns (the host reports QDG_ETIMEOUT).
 #include <cuda_runtime.h>
 #include <math.h>
+#include <stdlib.h>
 
 #include "qdg_kernels.cuh"
 
@@ -231,12 +232,8 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
     __syncthreads();
     const int cur = fft_lines<T>(b0, b1, g.rp, L, tws, -1);
     cplx<T> *bc = cur ? b1 : b0;
-    const double kf = g.kfac[s];
-    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
-      const int i = idx % N;
-      const int kq = min(i, N - i);
-      bc[idx] = cmulr(bc[idx], (T)(kf * (double)kq * (double)kq));
-    }
+    const T *__restrict__ kt = g.ktab + (long long)s * N;
+    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) bc[idx] = cmulr(bc[idx], __ldg(kt + idx % N));
     __syncthreads();
     const int cur2 = fft_lines<T>(bc, cur ? b0 : b1, g.rp, L, tws, +1);
     const cplx<T> *res = cur2 ? (cur ? b0 : b1) : bc;
@@ -324,8 +321,7 @@ __device__ void phase_lines(const StepArgs<T> &a, const cplx<T> *phi, cplx<T> *k
     cplx<T> *bc = cur ? b1 : b0;
     for (int idx = threadIdx.x; idx < L * N; idx += blockDim.x) {
       const int l = idx / N, i = idx - l * N;
-      const int kq = min(i, N - i);
-      bc[idx] = cmulr(bc[idx], (T)(g.kfac[l / TW] * (double)kq * (double)kq));
+      bc[idx] = cmulr(bc[idx], __ldg(g.ktab + (long long)(l / TW) * N + i));
     }
     __syncthreads();
     const int cur2 = fft_lines<T>(bc, cur ? b0 : b1, g.rp, L, tws, +1);
@@ -346,13 +342,11 @@ __device__ void phase_lines(const StepArgs<T> &a, const cplx<T> *phi, cplx<T> *k
   __syncthreads();
 }
 
-// Minimum resident blocks per SM the compiler must allow for (register cap):
-// the FP32 kernel is latency bound and needs more warps than the FP64 one.
-template <typename T> struct StepOcc { static const int value = 1; };
-template <> struct StepOcc<float> { static const int value = 2; };
-
-template <typename T, int SS, int ND>
-__global__ void __launch_bounds__(256, StepOcc<T>::value) cheby_step_kernel(StepArgs<T> a) {
+// OCC: minimum resident blocks per SM the compiler must allow for (register
+// cap).  The FP32 kernel is latency bound and needs the warps; the FP64 one
+// trades register spills against latency hiding (selectable at run time).
+template <typename T, int SS, int ND, int OCC>
+__global__ void __launch_bounds__(256, OCC) cheby_step_kernel(StepArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double red[32];
   __shared__ double tot_s;
@@ -468,20 +462,36 @@ __global__ void __launch_bounds__(256, StepOcc<T>::value) cheby_step_kernel(Step
   }
 }
 
-template <typename T, int ND>
+template <typename T, int ND, int OCC>
 static void *step_ptr_nd(int S) {
-  return S == 1 ? (void *)cheby_step_kernel<T, 1, ND> : S == 2 ? (void *)cheby_step_kernel<T, 2, ND>
-                                                               : (void *)cheby_step_kernel<T, 0, ND>;
+  return S == 1 ? (void *)cheby_step_kernel<T, 1, ND, OCC> : S == 2 ? (void *)cheby_step_kernel<T, 2, ND, OCC>
+                                                                    : (void *)cheby_step_kernel<T, 0, ND, OCC>;
+}
+
+template <typename T, int OCC>
+static void *step_ptr_occ(int S, int nd) {
+  switch (nd) {
+    case 1: return step_ptr_nd<T, 1, OCC>(S);
+    case 2: return step_ptr_nd<T, 2, OCC>(S);
+    case 3: return step_ptr_nd<T, 3, OCC>(S);
+    default: return step_ptr_nd<T, 4, OCC>(S);
+  }
+}
+
+// FP64: QDG_STEP_OCC=2 selects the variant compiled for two blocks per SM.
+static int fp64_occ() {
+  static int v = -1;
+  if (v < 0) {
+    const char *e = getenv("QDG_STEP_OCC");
+    v = (e && atoi(e) == 2) ? 2 : 1;
+  }
+  return v;
 }
 
 template <typename T>
 static void *step_ptr(int S, int nd) {
-  switch (nd) {
-    case 1: return step_ptr_nd<T, 1>(S);
-    case 2: return step_ptr_nd<T, 2>(S);
-    case 3: return step_ptr_nd<T, 3>(S);
-    default: return step_ptr_nd<T, 4>(S);
-  }
+  if (sizeof(T) == 4) return step_ptr_occ<T, 2>(S, nd);
+  return fp64_occ() == 2 ? step_ptr_occ<T, 2>(S, nd) : step_ptr_occ<T, 1>(S, nd);
 }
 
 template <typename T>
