@@ -652,7 +652,7 @@ qdg_status step_setup(qdg_prop *P) {
     for (int d = 0; d < p->nd; ++d) {
       const long long n = p->dim[d].n;
       long long cap = (long long)((budget / cs - n) / (2 * n));
-      int lm = (int)std::max<long long>(1, std::min<long long>(chunk, cap));
+      int lm = (int)std::max<long long>(1, std::min<long long>(std::min<long long>(chunk, cap), qdg::kMaxBatchLines));
       P->lmax[d] = lm;
       smem = std::max(smem, (size_t)(n * (1 + 2 * (size_t)lm)) * cs);
     }

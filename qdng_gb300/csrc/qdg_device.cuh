@@ -142,10 +142,22 @@ __device__ __forceinline__ void stockham_stage(const cplx<T> *__restrict__ in, c
   const int M = N / R;
   const int step = N / (Ns * R);
   const int items = nlines * M;
+  // powers of two (the usual case): shifts and masks instead of divisions
+  const bool pow2 = ((M & (M - 1)) == 0) && ((Ns & (Ns - 1)) == 0);
+  const int lgM = __ffs(M) - 1, lgNs = __ffs(Ns) - 1;
   for (int it = threadIdx.x; it < items; it += blockDim.x) {
-    const int line = it / M;
-    const int j = it - line * M;
-    const int k = j % Ns;
+    int line, j, k, q;
+    if (pow2) {
+      line = it >> lgM;
+      j = it & (M - 1);
+      k = j & (Ns - 1);
+      q = j >> lgNs;
+    } else {
+      line = it / M;
+      j = it - line * M;
+      q = j / Ns;
+      k = j - q * Ns;
+    }
     const cplx<T> *src = in + line * N;
     cplx<T> v[R];
 #pragma unroll
@@ -172,20 +184,20 @@ __device__ __forceinline__ void stockham_stage(const cplx<T> *__restrict__ in, c
       // direct R-point DFT with the table entries of the R-th roots of unity
       cplx<T> y[R];
 #pragma unroll
-      for (int q = 0; q < R; ++q) {
+      for (int qq = 0; qq < R; ++qq) {
         cplx<T> s = v[0];
 #pragma unroll
         for (int r = 1; r < R; ++r) {
-          cplx<T> w = tw[((r * q) % R) * M];
+          cplx<T> w = tw[((r * qq) % R) * M];
           if (sign > 0) w.im = -w.im;
           s = s + cmul(v[r], w);
         }
-        y[q] = s;
+        y[qq] = s;
       }
 #pragma unroll
-      for (int q = 0; q < R; ++q) v[q] = y[q];
+      for (int qq = 0; qq < R; ++qq) v[qq] = y[qq];
     }
-    cplx<T> *dst = out + line * N + (j / Ns) * Ns * R + k;
+    cplx<T> *dst = out + line * N + q * Ns * R + k;
 #pragma unroll
     for (int r = 0; r < R; ++r) dst[r * Ns] = v[r];
   }

@@ -37,6 +37,7 @@ struct Couplings {
   int rs[kMaxStates + 1];
 };
 static const int kMaxRowEntries = 4;  // entries per row the fused step kernel unrolls
+static const int kMaxBatchLines = 64; // lines one block of the step kernel transforms at once
 
 // Per-step Chebyshev control block in device memory.
 struct ChebyState {

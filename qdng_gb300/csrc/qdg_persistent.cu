@@ -106,6 +106,7 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
   long long l = total * blockIdx.x / G;
   int cur_dim = -1;
   cplx<T> *tws = smem;
+  __shared__ long long lbase[kMaxBatchLines];
   const cplx<T> off = ccast<T>(a.offset);
   const cplx<T> fac = ccast<T>(kind == PK_FIRST ? a.fac1 : a.fac);
   const T *__restrict__ grids = a.grids;
@@ -133,6 +134,13 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
       for (int i = threadIdx.x; i < N; i += blockDim.x) tws[i] = g.tw[i];
       cur_dim = d;
     }
+    // first point of each line of the batch (one 64-bit division per line)
+    if (threadIdx.x < L) {
+      const long long line = l0 + threadIdx.x;
+      lbase[threadIdx.x] = (line % stride) + (line / stride) * stride * N;
+    }
+    __syncthreads();
+    const int istr = (int)stride;  // element stride of a line (< 2^31 points per dimension block)
     // potential-matrix entries of row s
     const int e0 = a.cp->rs[s];
     const int ne = a.cp->rs[s + 1] - e0;
@@ -160,12 +168,11 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
         const bool ok = idx < tot;
         int w = 0, i = 0;
         if (ok) {
-          if (stride == 1) { w = idx / N; i = idx - w * N; }
+          if (istr == 1) { w = idx / N; i = idx - w * N; }
           else { i = idx / L; w = idx - i * L; }
         }
         sidx[u] = ok ? w * N + i : -1;
-        const long long line = l0 + w;
-        const long long p = (line % stride) + (line / stride) * stride * N + (long long)i * stride;
+        const long long p = lbase[w] + (long long)i * istr;
         pp[u] = p;
         if (!ok) continue;
         if (kind == PK_START) { v[u] = ldcg(phim1 + so + p); continue; }
@@ -233,18 +240,17 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
     const int cur = fft_lines<T>(b0, b1, g.rp, L, tws, -1);
     cplx<T> *bc = cur ? b1 : b0;
     const T *__restrict__ kt = g.ktab + (long long)s * N;
-    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) bc[idx] = cmulr(bc[idx], __ldg(kt + idx % N));
+    for (int w = 0; w < L; ++w)
+      for (int i = threadIdx.x; i < N; i += blockDim.x) bc[w * N + i] = cmulr(bc[w * N + i], __ldg(kt + i));
     __syncthreads();
     const int cur2 = fft_lines<T>(bc, cur ? b0 : b1, g.rp, L, tws, +1);
     const cplx<T> *res = cur2 ? (cur ? b0 : b1) : bc;
     cplx<T> *dst = Pnext[d] + so;
     for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
       int w, i;
-      if (stride == 1) { w = idx / N; i = idx - w * N; }
+      if (istr == 1) { w = idx / N; i = idx - w * N; }
       else { i = idx / L; w = idx - i * L; }
-      const long long line = l0 + w;
-      const long long p = (line % stride) + (line / stride) * stride * N + (long long)i * stride;
-      st(dst + p, res[w * N + i]);
+      st(dst + lbase[w] + (long long)i * istr, res[w * N + i]);
     }
   }
   __syncthreads();
