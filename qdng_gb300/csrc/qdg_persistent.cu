@@ -96,7 +96,8 @@ template <typename T, int ND, int SM>
 __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__restrict__ phim1,
                             const cplx<T> *__restrict__ phim2, cplx<T> *__restrict__ phout,
                             cplx<T> *const *Pprev, cplx<T> *const *Pnext, double coeff_i, double &acc,
-                            cplx<T> *smem) {
+                            cplx<T> *smem, unsigned long long *tp = nullptr) {
+  const bool tr = tp != nullptr && blockIdx.x == 0 && threadIdx.x == 0;
   constexpr int UNR = (sizeof(T) == 8 || SM > 2) ? 1 : 2;
   constexpr int RE = kMaxRowEntries;
   const long long npts = a.npts;
@@ -109,6 +110,8 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
   __shared__ long long lbase[kMaxBatchLines];
   const cplx<T> off = ccast<T>(a.offset);
   const cplx<T> fac = ccast<T>(kind == PK_FIRST ? a.fac1 : a.fac);
+  const bool off_real = a.offset.im == 0.0;
+  const bool fac_imag = (kind == PK_FIRST ? a.fac1.re : a.fac.re) == 0.0;
   const T *__restrict__ grids = a.grids;
   while (l < end) {
     int d = 0;
@@ -146,14 +149,17 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
     const int ne = a.cp->rs[s + 1] - e0;
     int ecol[RE], egid[RE];
     T ecoef[RE];
+    bool unit_coef = true;  // only static potentials (coefficient 1) in this row
 #pragma unroll
     for (int k = 0; k < RE; ++k) {
       ecol[k] = k < ne ? a.cp->col[e0 + k] : 0;
       egid[k] = k < ne ? a.cp->gid[e0 + k] : 0;
       ecoef[k] = k < ne ? (T)a.coef[e0 + k] : (T)0;
+      if (k < ne && ecoef[k] != (T)1) unit_coef = false;
     }
     const long long so = (long long)s * npts;
     const int tot = L * N;
+    unsigned long long tg0 = tr ? gtimer() : 0;
     for (int base = threadIdx.x; base < tot; base += UNR * blockDim.x) {
       long long pp[UNR];
       int sidx[UNR];
@@ -205,10 +211,21 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
 #pragma unroll
               for (int j = 1; j < SM; ++j)
                 if (j == ecol[k]) x = pm[u][j];
-              h = h + cmulr(x, ecoef[k] * vg[u][k]);
+              const T vv = unit_coef ? vg[u][k] : ecoef[k] * vg[u][k];
+              h.re = fma(x.re, vv, h.re);
+              h.im = fma(x.im, vv, h.im);
             }
           }
-          const cplx<T> bf = cmul(h - cmul(off, self), fac);
+          // (h - offset phi) * factor; a real offset and a purely imaginary
+          // factor (real-time propagation) need half the multiplications
+          cplx<T> hm;
+          if (off_real) {
+            hm.re = fma(-off.re, self.re, h.re);
+            hm.im = fma(-off.re, self.im, h.im);
+          } else {
+            hm = h - cmul(off, self);
+          }
+          const cplx<T> bf = fac_imag ? mk(-fac.im * hm.im, fac.im * hm.re) : cmul(hm, fac);
           const long long gidx = so + pp[u];
           if (kind == PK_FIRST) {
             v[u] = bf;
@@ -217,7 +234,7 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
               acc += cabs2(p0);
               st(phout + gidx, bf);
               const cplx<double> b = ccast<double>(bf);
-              st(a.psi + gidx, mk(p0.re * a.a[0] + b.re * a.a[1], p0.im * a.a[0] + b.im * a.a[1]));
+              st(a.psi + gidx, mk(fma(b.re, a.a[1], p0.re * a.a[0]), fma(b.im, a.a[1], p0.im * a.a[0])));
             }
           } else {
             const cplx<T> k2 = a.imag ? bf - km2[u] : bf + km2[u];
@@ -225,10 +242,10 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
             if (owner) {
               st(phout + gidx, k2);
               cplx<double> p0 = ps[u];
-              p0.re += coeff_i * (double)k2.re;
-              p0.im += coeff_i * (double)k2.im;
+              p0.re = fma(coeff_i, (double)k2.re, p0.re);
+              p0.im = fma(coeff_i, (double)k2.im, p0.im);
               st(a.psi + gidx, p0);
-              acc += cabs2(p0);
+              acc = fma(p0.re, p0.re, fma(p0.im, p0.im, acc));
             }
           }
         }
@@ -237,6 +254,7 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
     }
     if (kind == PK_LAST) continue;
     __syncthreads();
+    unsigned long long tg1 = tr ? gtimer() : 0;
     const int cur = fft_lines<T>(b0, b1, g.rp, L, tws, -1);
     cplx<T> *bc = cur ? b1 : b0;
     const T *__restrict__ kt = g.ktab + (long long)s * N;
@@ -245,12 +263,17 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
     __syncthreads();
     const int cur2 = fft_lines<T>(bc, cur ? b0 : b1, g.rp, L, tws, +1);
     const cplx<T> *res = cur2 ? (cur ? b0 : b1) : bc;
+    unsigned long long tg2 = tr ? gtimer() : 0;
     cplx<T> *dst = Pnext[d] + so;
     for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
       int w, i;
       if (istr == 1) { w = idx / N; i = idx - w * N; }
       else { i = idx / L; w = idx - i * L; }
       st(dst + lbase[w] + (long long)i * istr, res[w * N + i]);
+    }
+    if (tr) {
+      const unsigned long long tg3 = gtimer();
+      tp[0] += tg1 - tg0; tp[1] += tg2 - tg1; tp[2] += tg3 - tg2;
     }
   }
   __syncthreads();
@@ -363,6 +386,7 @@ __global__ void __launch_bounds__(256, OCC) cheby_step_kernel(StepArgs<T> a) {
   const long long gstride = (long long)gridDim.x * blockDim.x;
   const bool tr = a.trace && blockIdx.x == 0 && threadIdx.x == 0;
   unsigned long long tp[4] = {0, 0, 0, 0};
+  unsigned long long *tpi = tp;  // gather, FFT + multiply, store (inside the phase), barrier
 
   // phi_0 = psi (OCheby: ket0->FastCopy(*Psi))
   for (long long i = gtid; i < n; i += gstride) st(a.buf[0] + i, ccast<T>(ld(a.psi + i)));
@@ -431,12 +455,12 @@ __global__ void __launch_bounds__(256, OCC) cheby_step_kernel(StepArgs<T> a) {
       const unsigned long long t0 = tr ? gtimer() : 0;
       const int kind = (i + 1 < a.order) ? PK_TERM : PK_LAST;
       phase_fused<T, ND, SM>(a, kind, a.buf[(i - 1) % 3], a.buf[(i - 2) % 3], a.buf[i % 3], a.Pn[i & 1],
-                             a.Pn[(i + 1) & 1], a.a[i], acc, smem);
+                             a.Pn[(i + 1) & 1], a.a[i], acc, smem, tr ? tpi : nullptr);
       const unsigned long long t1 = tr ? gtimer() : 0;
       t = block_sum(acc, red);
       if (threadIdx.x == 0) a.partials[blockIdx.x] = t;
       if (!grid_sync(a.bar)) return;
-      if (tr) { const unsigned long long t2 = gtimer(); tp[0] += t1 - t0; tp[1] += t2 - t1; }
+      if (tr) { const unsigned long long t2 = gtimer(); tp[3] += t2 - t1; (void)t0; }
       t = sum_partials(a.partials, red);
       if (threadIdx.x == 0) tot_s = t;
       __syncthreads();

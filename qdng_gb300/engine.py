@@ -153,10 +153,11 @@ class Propagator:
         return used.value
 
     def phase_times(self):
-        """Per-phase ns of the persistent step kernel while profiling (block 0's view)."""
+        """ns spent by block 0 of the persistent step kernel while profiling: loading and
+        finishing phi (gather), the shared-memory FFTs, storing T_d phi, waiting at the barrier."""
         ns = np.zeros(4)
         check(self.lib.qdg_prop_phase_times(self.h, _dp(ns)))
-        return dict(kinetic=ns[0], barrier_after_kinetic=ns[1], points=ns[2], barrier_norm=ns[3])
+        return dict(gather=ns[0], fft=ns[1], store=ns[2], barrier=ns[3])
 
     def run(self, wf, step0, nsteps):
         tot = C.c_int64(0)
