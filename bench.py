@@ -316,6 +316,81 @@ def engine_arm(args, world, rank, local):
         print(json.dumps(line))
 
 
+def ensemble_arm(args, world, rank, local):
+    """BASELINE configs[3]: 512 laser-driven members, one persistent launch per
+    call; wavepackets/s = members x (steps / 5000) / time."""
+    import numpy as np
+    import torch
+
+    from qdng_gb300 import build, engine
+    from tests import cases
+
+    build.build()
+    torch.cuda.set_device(0)
+    ens = cases.cfg4_ensemble(n=args.members, seed=4)
+    if world > 1:  # shard members across ranks by LPT (no collective on the data path)
+        costs = [m["grid"].npts * np.log2(m["grid"].npts) for m in ens]
+        parts, _ = cases.lpt_partition(costs, world)
+        ens = [ens[i] for i in parts[rank]]
+    E = engine.Ensemble(ens, dt=10.0, precision=args.precision)
+    psi0 = [m["psi"] for m in ens]
+    E.upload(psi0)
+    E.run(0, args.warmup)
+    barrier(world)
+    torch.cuda.synchronize()
+    l0 = engine.kernel_launches()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        terms = E.run(args.warmup, args.steps)
+        dt_s = time.perf_counter() - t0
+    launches = engine.kernel_launches() - l0
+    clocks = clk.summary()
+    dt_max = reduce_max(dt_s, world)
+    total_members = args.members
+    value = total_members * (args.steps / 5000.0) / dt_max
+    # e2e: host psi (pinned) up, steps, down
+    host = [torch.from_numpy(np.ascontiguousarray(p).view(np.float64)).pin_memory() for p in psi0]
+    t0 = time.perf_counter()
+    E.upload([h.numpy().view(np.complex128) for h in host])
+    E.run(0, args.steps)
+    out = E.download()
+    e2e_s = reduce_max(time.perf_counter() - t0, world)
+    err = None
+    if args.precision == "mixed" and rank == 0:
+        R = engine.Ensemble(ens, dt=10.0, precision="fp64")
+        E.upload(psi0)
+        R.upload(psi0)
+        E.run(0, args.steps)
+        R.run(0, args.steps)
+        errs = [float(np.abs(a - b).max() / np.abs(b).max()) for a, b in zip(E.download(), R.download())]
+        err = {"max_rel_psi_error_vs_fp64": max(errs), "median": float(np.median(errs)), "steps": args.steps}
+    bytes_io = int(sum(p.size for p in psi0) * 16)
+    line = {
+        "metric": "wavepackets/s (512 laser-driven members, 5000 steps each)",
+        "value": round(value, 4),
+        "unit": "wavepackets/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(dt_max / args.steps * 1e3, 3),
+        "higher_is_better": True,
+        "scaling": "strong",
+        "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+        "data": "synthetic (seeded Morse members, BASELINE configs[3])",
+        "config": {"workload": "cfg4 ensemble: 512 members, 1-D 256-4096 / 2-D 64^2-256^2, dt=10, mass 1728",
+                   "precision": args.precision, "l2": "members larger than L2 in total (not flushed)",
+                   "terms_per_step_total": terms / args.steps},
+        "e2e": {"value": round(total_members * (args.steps / 5000.0) / e2e_s, 4), "unit": "wavepackets/s",
+                "h2d_bytes_per_step": bytes_io // args.steps, "d2h_bytes_per_step": bytes_io // args.steps},
+        "gpu_launches": int(launches),
+        "error_vs_fp64": err,
+        "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+
+
 def reference_arm(args, world, rank):
     if rank != 0:
         return
@@ -354,12 +429,16 @@ def main():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "ensemble"])
+    ap.add_argument("--members", type=int, default=512)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
         reference_arm(args, world, rank)
+    elif args.workload == "ensemble":
+        ensemble_arm(args, world, rank, local)
     else:
         engine_arm(args, world, rank, local)
     if world > 1:

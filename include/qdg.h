@@ -193,6 +193,41 @@ qdg_status qdg_prop_apply_host(qdg_prop *prop, qdg_wf *scratch, double *host_psi
 qdg_status qdg_prop_run(qdg_prop *prop, qdg_wf *psi, int64_t step0, int32_t nsteps,
                         int64_t *terms_total);
 
+/* ---- batched ensemble of independent wavepackets ------------------------ */
+
+/* One member: a single-state Hamiltonian Sum(GridNablaSq, GridPotential,
+ * GridDipole x laser) on its own 1-D or 2-D grid -- the operator tree of
+ * QDng's laser-driven grid propagations (tests/TGPL-IR-Pulse-Cheby.qdi.in) --
+ * propagated with OCheby's series (src/qdlib/OCheby.cpp:92-198, 358-493).
+ * Arrays are host memory, npoints doubles (laser: laser_nt samples, E(step)
+ * = laser[step], Laser.cpp:125-128); dipole/laser may be NULL. */
+typedef struct qdg_ensemble_member {
+  qdg_grid grid;
+  double mass[QDG_MAX_DIMS];
+  const double *potential;
+  const double *dipole;
+  const double *laser;
+  int32_t laser_nt;
+} qdg_ensemble_member;
+
+typedef struct qdg_ensemble qdg_ensemble;
+
+/* Builds the device image of n members, each with its own Chebyshev series
+ * (params: the OCheby attributes, shared by all members; forward real time
+ * with time step dt).  Members run in one persistent launch, taken from a
+ * device queue in descending cost order. */
+qdg_status qdg_ensemble_create(const qdg_ensemble_member *members, int32_t n, double dt, const char *params,
+                               int32_t precision, qdg_ensemble **out);
+qdg_status qdg_ensemble_destroy(qdg_ensemble *e);
+/* psi of all members, concatenated in member order (complex128). */
+qdg_status qdg_ensemble_upload(qdg_ensemble *e, const double *psi_all);
+qdg_status qdg_ensemble_download(const qdg_ensemble *e, double *psi_all);
+/* nsteps time steps of every member from clock step step0 (ProgPropa.cpp:317-327);
+ * terms_total receives the Chebyshev terms summed over members and steps. */
+qdg_status qdg_ensemble_run(qdg_ensemble *e, int64_t step0, int32_t nsteps, int64_t *terms_total);
+/* Series parameters of member i after create (order, scaling, offset). */
+qdg_status qdg_ensemble_member_info(const qdg_ensemble *e, int32_t i, qdg_prop_info *info);
+
 /* ---- engine instrumentation (no counterpart in the reference) ---------- */
 
 /* Kernels this library has launched in the process so far. */

@@ -87,6 +87,17 @@ class PropInfo(C.Structure):
     ]
 
 
+class EnsembleMember(C.Structure):
+    _fields_ = [
+        ("grid", Grid),
+        ("mass", C.c_double * QDG_MAX_DIMS),
+        ("potential", C.POINTER(C.c_double)),
+        ("dipole", C.POINTER(C.c_double)),
+        ("laser", C.POINTER(C.c_double)),
+        ("laser_nt", C.c_int32),
+    ]
+
+
 # Every symbol include/qdg.h declares: (name, restype, argtypes).
 _vp = C.c_void_p
 _i32 = C.c_int32
@@ -120,6 +131,12 @@ SIGNATURES = [
     ("qdg_profile_read", _i32, [_vp, _dp, C.POINTER(_i64)]),
     ("qdg_prop_phase_times", _i32, [_vp, _dp]),
     ("qdg_h_apply_noalloc", _i32, [C.POINTER(HPlanDesc), _dp, _dp, _i64, _vp]),
+    ("qdg_ensemble_create", _i32, [C.POINTER(EnsembleMember), _i32, C.c_double, C.c_char_p, _i32, C.POINTER(_vp)]),
+    ("qdg_ensemble_destroy", _i32, [_vp]),
+    ("qdg_ensemble_upload", _i32, [_vp, _dp]),
+    ("qdg_ensemble_download", _i32, [_vp, _dp]),
+    ("qdg_ensemble_run", _i32, [_vp, _i64, _i32, C.POINTER(_i64)]),
+    ("qdg_ensemble_member_info", _i32, [_vp, _i32, C.POINTER(PropInfo)]),
 ]
 
 

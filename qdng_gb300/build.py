@@ -16,7 +16,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libqdg.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["qdg_kernels.cu", "qdg_persistent.cu", "qdg_api.cu", "qdg_noalloc.cu", "qdg_host.cpp"]
+SOURCES = ["qdg_kernels.cu", "qdg_persistent.cu", "qdg_api.cu", "qdg_noalloc.cu", "qdg_ensemble.cu",
+           "qdg_host.cpp"]
 
 
 def nvcc():

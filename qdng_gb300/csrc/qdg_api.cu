@@ -728,44 +728,14 @@ qdg_status cheby_step_persistent(qdg_prop *P, cplx<double> *psi, long long step)
 // OCheby::Init (src/qdlib/OCheby.cpp:358-493).
 qdg_status cheby_init(qdg_prop *P) {
   qdg_plan *p = P->plan;
-  P->order = 0;
-  if (has(P, "order")) {
-    P->order = atoi(P->params["order"].c_str());
-    if (P->order < 1) return fail(QDG_EINVAL, "Chebychev recursion order invalid");
-  }
-  cd Emax = p->emax, Emin = p->emin;
-  if (has(P, "Emax")) Emax.real(parse_d(P, "Emax"));
-  if (has(P, "Emax_im")) Emax.imag(parse_d(P, "Emax_im"));
-  if (has(P, "Emin")) Emin.real(parse_d(P, "Emin"));
-  if (has(P, "Emin_im")) Emin.imag(parse_d(P, "Emin_im"));
-  if (!P->imag) P->offset = cd((Emax + Emin).real() / 2, (Emax + Emin).imag());
-  else P->offset = Emin - std::abs(Emin) * 0.05;
-  if (P->offset.imag() != 0 || std::fabs(P->c0.imag()) == 0) P->scaling = std::abs(Emax - Emin) * 1.05;
-  else P->scaling = std::abs(Emax - Emin) / 2;
-  if (P->order <= 0) P->order = std::abs(int(20 * P->scaling * P->dt));
-  if (P->order < 10) P->order = 10;
-  if (has(P, "scaling")) P->scaling = parse_d(P, "scaling");
-  if (has(P, "order")) P->order = atoi(P->params["order"].c_str());
-  if (P->order < 3) return fail(QDG_EINVAL, "Chebychev recursion must be at least 3");
-  std::vector<double> b;
-  int zeroes;
-  const double R = P->scaling * P->dt;
-  if (std::fabs(P->c0.imag()) != 0 && std::fabs(P->c0.real()) == 0) zeroes = qdg::host::bessel_j(P->order, R, b);
-  else if (std::fabs(P->c0.imag()) == 0 && std::fabs(P->c0.real()) != 0) zeroes = qdg::host::bessel_i_scaled(P->order, R, b);
-  else return fail(QDG_EINVAL, "Chebychev propagator doesn't support mixed real/complex exponents");
-  P->order -= zeroes;
-  if (!has(P, "order")) {
-    const double precission = 1e-32;  // BESSEL_DELTA (OCheby.h:10)
-    int i = 2;
-    while (i < P->order && std::fabs(b[i - 1] - b[i - 2]) > precission) i++;
-    P->order = i;
-  }
-  if (P->order > 0 && !P->imag && P->order <= int(P->scaling * P->dt))
-    return fail(QDG_EINVAL, "Chebychev recursion order is to small");
-  P->coeff.assign(P->order, 0.0);
-  P->coeff[0] = b[0];
-  for (int i = 1; i < P->order; ++i) P->coeff[i] = 2.0 * b[i];
-  if (has(P, "prec")) P->prec = parse_d(P, "prec");
+  qdg::host::ChebySeries cs;
+  const std::string err = qdg::host::cheby_series(p->emax, p->emin, P->dt, P->c0, P->imag, P->params, cs);
+  if (!err.empty()) return fail(QDG_EINVAL, err);
+  P->order = cs.order;
+  P->scaling = cs.scaling;
+  P->offset = cs.offset;
+  P->coeff = cs.coeff;
+  P->prec = cs.prec;
   const size_t bytes = p->csize * wf_elems(p);
   CK(cudaMalloc(&P->k0, bytes));
   CK(cudaMalloc(&P->k1, bytes));

@@ -1,0 +1,544 @@
+// qdg_ensemble.cu -- many independent wavepackets in one persistent launch.
+//
+// Each member is a single-state grid Hamiltonian Sum(GridNablaSq, GridPotential,
+// GridDipole x laser) on its own 1-D or 2-D grid (QDng's TGPL-IR-Pulse-Cheby
+// shape), propagated with the Chebyshev series of OCheby
+// (src/qdlib/OCheby.cpp:92-198) with its own order, scaling and offset.
+// Members are taken by blocks from a device work queue in descending cost
+// (largest first: list scheduling in LPT order), and one block runs a whole
+// member for all requested steps: every synchronisation is a block barrier,
+// so the launch has no grid-wide waits at all.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/qdg.h"
+#include "qdg_host.h"
+#include "qdg_kernels.cuh"
+
+namespace qdg {
+
+struct EnsMember {
+  int nd;
+  int n[2];
+  long long npts;
+  long long off;          // first point in the concatenated arrays
+  long long tw_off[2];    // twiddles of each dimension (complex elements)
+  long long kt_off[2];    // kinetic multipliers of each dimension
+  RadixPlan rp[2];
+  int lmax[2];            // lines per batch
+  int order;
+  long long coef_off;     // series coefficients a_i
+  cplx<double> offset, fac1, fac, ph;
+  double prec;
+  long long laser_off;    // -1: no field
+  int laser_nt;
+  int has_dipole;
+};
+
+template <typename T>
+struct EnsArgs {
+  const EnsMember *m;
+  const int *order;       // work order (member indices)
+  int n;
+  int *queue;
+  cplx<double> *psi;
+  cplx<T> *buf0, *buf1;   // phi_{i-1}, phi_{i-2} (in/out)
+  cplx<T> *P0, *P1;       // T_d phi per dimension
+  const T *V, *mu;
+  const double *lasers;
+  const double *coef;
+  const cplx<T> *tw;
+  const T *ktab;
+  long long step0;
+  int nsteps;
+  int diff;               // mixed precision: differential series cut
+  long long *terms;       // per member, accumulated
+  int *status;            // per member: 2 = non-finite norm
+};
+
+// T_d phi for every dimension of member m: lines in batches of lmax[d].
+template <typename T>
+__device__ void ens_kinetic(const EnsArgs<T> &a, const EnsMember &m, const cplx<T> *phi, cplx<T> *smem) {
+  __shared__ long long lb[64];
+  for (int d = 0; d < m.nd; ++d) {
+    const int N = m.n[d];
+    const long long stride = d == 0 ? 1 : m.n[0];
+    const long long nl = m.npts / N;
+    const cplx<T> *tw = a.tw + m.tw_off[d];
+    const T *kt = a.ktab + m.kt_off[d];
+    cplx<T> *dst = (d == 0 ? a.P0 : a.P1) + m.off;
+    cplx<T> *tws = smem;
+    cplx<T> *b0 = tws + N;
+    cplx<T> *b1 = b0 + (size_t)m.lmax[d] * N;
+    __syncthreads();
+    for (int i = threadIdx.x; i < N; i += blockDim.x) tws[i] = tw[i];
+    for (long long l0 = 0; l0 < nl; l0 += m.lmax[d]) {
+      const int L = (int)min((long long)m.lmax[d], nl - l0);
+      __syncthreads();
+      if (threadIdx.x < L) {
+        const long long line = l0 + threadIdx.x;
+        lb[threadIdx.x] = (line % stride) + (line / stride) * stride * N;
+      }
+      __syncthreads();
+      const int tot = L * N;
+      for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+        int w, i;
+        if (stride == 1) { w = idx / N; i = idx - w * N; }
+        else { i = idx / L; w = idx - i * L; }
+        b0[w * N + i] = ld(phi + m.off + lb[w] + (long long)i * stride);
+      }
+      __syncthreads();
+      const int cur = fft_lines<T>(b0, b1, m.rp[d], L, tws, -1);
+      cplx<T> *bc = cur ? b1 : b0;
+      for (int w = 0; w < L; ++w)
+        for (int i = threadIdx.x; i < N; i += blockDim.x) bc[w * N + i] = cmulr(bc[w * N + i], kt[i]);
+      __syncthreads();
+      const int cur2 = fft_lines<T>(bc, cur ? b0 : b1, m.rp[d], L, tws, +1);
+      const cplx<T> *res = cur2 ? (cur ? b0 : b1) : bc;
+      for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+        int w, i;
+        if (stride == 1) { w = idx / N; i = idx - w * N; }
+        else { i = idx / L; w = idx - i * L; }
+        st(dst + lb[w] + (long long)i * stride, res[w * N + i]);
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// Point work of one term; returns the block's partial norm.
+template <typename T, bool FIRST>
+__device__ double ens_points(const EnsArgs<T> &a, const EnsMember &m, const cplx<T> *phi, cplx<T> *kout,
+                             double ai, T field) {
+  double acc = 0.0;
+  const cplx<T> off = ccast<T>(m.offset);
+  const cplx<T> fac = ccast<T>(FIRST ? m.fac1 : m.fac);
+  for (long long p = threadIdx.x; p < m.npts; p += blockDim.x) {
+    const long long g = m.off + p;
+    const cplx<T> x = ld(phi + g);
+    cplx<T> h = ld(a.P0 + g);
+    if (m.nd > 1) h = h + ld(a.P1 + g);
+    T v = a.V[g];
+    if (m.has_dipole) v = v + field * a.mu[g];
+    h = h + cmulr(x, v);
+    const cplx<T> bf = cmul(h - cmul(off, x), fac);
+    if (FIRST) {
+      const cplx<double> ps = ld(a.psi + g);
+      acc += cabs2(ps);
+      st(kout + g, bf);
+      const cplx<double> b = ccast<double>(bf);
+      const double a0 = a.coef[m.coef_off], a1 = a.coef[m.coef_off + 1];
+      st(a.psi + g, mk(ps.re * a0 + b.re * a1, ps.im * a0 + b.im * a1));
+    } else {
+      const cplx<T> k2 = bf + ld(kout + g);
+      st(kout + g, k2);
+      cplx<double> ps = ld(a.psi + g);
+      ps.re += ai * (double)k2.re;
+      ps.im += ai * (double)k2.im;
+      st(a.psi + g, ps);
+      acc += cabs2(ps);
+    }
+  }
+  return acc;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) ensemble_kernel(EnsArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double red[32];
+  __shared__ double tot_s;
+  __shared__ int cur;
+  cplx<T> *smem = reinterpret_cast<cplx<T> *>(smem_raw);
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) cur = atomicAdd(a.queue, 1);
+    __syncthreads();
+    if (cur >= a.n) return;
+    const int mi = a.order[cur];
+    const EnsMember m = a.m[mi];
+    long long terms = 0;
+    int status = 0;
+    for (int k = 0; k < a.nsteps; ++k) {
+      const long long step = a.step0 + k;
+      // E(step) of Laser::Get (src/qdlib/Laser.cpp:125-128); the dipole term is -mu E
+      T field = (T)0;
+      if (m.has_dipole && step >= 0 && step < m.laser_nt) field = (T)(-a.lasers[m.laser_off + step]);
+      for (long long p = threadIdx.x; p < m.npts; p += blockDim.x)
+        st(a.buf0 + m.off + p, ccast<T>(ld(a.psi + m.off + p)));
+      ens_kinetic<T>(a, m, a.buf0, smem);
+      double t = block_sum(ens_points<T, true>(a, m, a.buf0, a.buf1, 0.0, field), red);
+      if (threadIdx.x == 0) tot_s = t;
+      __syncthreads();
+      const double norm0 = tot_s;
+      double last = norm0;
+      bool done = !isfinite(norm0);
+      if (done) status = 2;
+      int used = 2;
+      // phi_{i-1} in buf[(i+1)&1], phi_{i-2} in buf[i&1] (overwritten by phi_i)
+      for (int i = 2; i < m.order && !done; ++i) {
+        cplx<T> *phi = (i & 1) ? a.buf0 : a.buf1;
+        cplx<T> *kout = (i & 1) ? a.buf1 : a.buf0;
+        ens_kinetic<T>(a, m, phi, smem);
+        t = block_sum(ens_points<T, false>(a, m, phi, kout, a.coef[m.coef_off + i], field), red);
+        if (threadIdx.x == 0) tot_s = t;
+        __syncthreads();
+        const double tot = tot_s;
+        used = i + 1;
+        if (!isfinite(tot)) { done = true; status = 2; }
+        else {
+          const double ref = a.diff ? last : norm0;
+          if (fabs(ref - tot) / norm0 < m.prec && m.offset.im == 0.0) done = true;  // OCheby.cpp:179-182
+        }
+        last = tot;
+      }
+      for (long long p = threadIdx.x; p < m.npts; p += blockDim.x)
+        st(a.psi + m.off + p, cmul(ld(a.psi + m.off + p), m.ph));
+      terms += used;
+    }
+    if (threadIdx.x == 0) {
+      a.terms[mi] += terms;
+      if (status) a.status[mi] = status;
+    }
+  }
+}
+
+template <typename T>
+static int ensemble_occupancy(size_t smem) {
+  void *k = (void *)ensemble_kernel<T>;
+  if (smem > 48 * 1024 && cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return 0;
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, 256, smem) != cudaSuccess) return 0;
+  return nb;
+}
+
+}  // namespace qdg
+
+using qdg::cplx;
+typedef std::complex<double> cd;
+
+struct qdg_ensemble {
+  int n = 0;
+  int precision = QDG_PREC_MIXED;
+  size_t csize = 8;
+  double dt = 0;
+  std::vector<qdg::EnsMember> hm;
+  std::vector<int> order;
+  long long total_pts = 0;
+  // device
+  qdg::EnsMember *d_m = nullptr;
+  int *d_order = nullptr, *d_queue = nullptr, *d_status = nullptr;
+  long long *d_terms = nullptr;
+  cplx<double> *d_psi = nullptr;
+  void *d_buf0 = nullptr, *d_buf1 = nullptr, *d_P0 = nullptr, *d_P1 = nullptr;
+  void *d_V = nullptr, *d_mu = nullptr, *d_tw = nullptr, *d_kt = nullptr;
+  double *d_lasers = nullptr, *d_coef = nullptr;
+  size_t smem = 0;
+  int grid = 1;
+  cudaStream_t stream = nullptr;
+};
+
+namespace {
+
+qdg_status efail(qdg_status s, const std::string &m) {
+  qdg::set_last_error(m);
+  return s;
+}
+
+#define ECK(...)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (__VA_ARGS__);                                                       \
+    if (e_ != cudaSuccess) return efail(QDG_ECUDA, std::string(#__VA_ARGS__) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+bool radix_plan_e(int n, qdg::RadixPlan &rp) {
+  rp.n = n;
+  rp.nstages = 0;
+  int m = n;
+  while (m % 16 == 0) { rp.radix[rp.nstages++] = 16; m /= 16; }
+  if (m % 8 == 0) { rp.radix[rp.nstages++] = 8; m /= 8; }
+  if (m % 4 == 0) { rp.radix[rp.nstages++] = 4; m /= 4; }
+  if (m % 2 == 0) { rp.radix[rp.nstages++] = 2; m /= 2; }
+  while (m % 3 == 0) { rp.radix[rp.nstages++] = 3; m /= 3; }
+  while (m % 5 == 0) { rp.radix[rp.nstages++] = 5; m /= 5; }
+  return m == 1 && rp.nstages <= 16;
+}
+
+void parse_kv(const char *s, std::map<std::string, std::string> &out) {
+  if (!s) return;
+  std::string str(s);
+  for (char &c : str)
+    if (c == ';' || c == ',' || c == '\t' || c == '\n') c = ' ';
+  size_t i = 0;
+  while (i < str.size()) {
+    while (i < str.size() && str[i] == ' ') ++i;
+    size_t j = i;
+    while (j < str.size() && str[j] != ' ') ++j;
+    const std::string kv = str.substr(i, j - i);
+    const size_t eq = kv.find('=');
+    if (eq != std::string::npos) out[kv.substr(0, eq)] = kv.substr(eq + 1);
+    i = j;
+  }
+}
+
+template <typename T>
+qdg_status upload_vec(void **dst, const std::vector<T> &v) {
+  ECK(cudaMalloc(dst, sizeof(T) * std::max<size_t>(1, v.size())));
+  if (!v.empty()) ECK(cudaMemcpy(*dst, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+  return QDG_OK;
+}
+
+void free_ensemble(qdg_ensemble *e) {
+  void *ps[] = {e->d_m, e->d_order, e->d_queue, e->d_status, e->d_terms, e->d_psi, e->d_buf0, e->d_buf1, e->d_P0,
+                e->d_P1, e->d_V, e->d_mu, e->d_tw, e->d_kt, e->d_lasers, e->d_coef};
+  for (void *p : ps)
+    if (p) cudaFree(p);
+  if (e->stream) cudaStreamDestroy(e->stream);
+  delete e;
+}
+
+template <typename T>
+qdg_status build(qdg_ensemble *e, const qdg_ensemble_member *mem, const std::map<std::string, std::string> &params) {
+  const int n = e->n;
+  std::vector<T> V, mu, kt;
+  std::vector<cplx<T>> tw;
+  std::vector<double> lasers, coef;
+  std::map<int, long long> tw_at;  // twiddle table of each line length
+  std::vector<double> cost(n);
+  long long off = 0;
+  size_t smem = 0;
+  const cd c0 = cd(0, -e->dt);  // forward real-time exponent (OPropagator.h:62-77)
+  for (int k = 0; k < n; ++k) {
+    const qdg_ensemble_member &x = mem[k];
+    qdg::EnsMember m;
+    memset(&m, 0, sizeof(m));
+    if (x.grid.ndims < 1 || x.grid.ndims > 2) return efail(QDG_EUNSUPPORTED, "ensemble members are 1-D or 2-D grids");
+    if (!x.potential) return efail(QDG_EINVAL, "ensemble member without a potential");
+    m.nd = x.grid.ndims;
+    m.npts = 1;
+    double dx[2], dk[2], Tmax = 0;
+    for (int d = 0; d < m.nd; ++d) {
+      const int N = x.grid.n[d];
+      if (N < 2 || !(x.grid.xmax[d] > x.grid.xmin[d])) return efail(QDG_EINVAL, "invalid member grid");
+      if (!(x.mass[d] > 0)) return efail(QDG_EINVAL, "Zero mass defined");
+      if (!radix_plan_e(N, m.rp[d])) return efail(QDG_EUNSUPPORTED, "grid size must be 2^a 3^b 5^c");
+      m.n[d] = N;
+      m.npts *= N;
+      dx[d] = (x.grid.xmax[d] - x.grid.xmin[d]) / double(N - 1);
+      dk[d] = (2 * M_PI) / (x.grid.xmax[d] - x.grid.xmin[d] + dx[d]);
+      Tmax += 1 / (x.mass[d] * dx[d] * dx[d]);
+      if (!tw_at.count(N)) {
+        tw_at[N] = (long long)tw.size();
+        const long double pi = 3.141592653589793238462643383279502884L;
+        for (int i = 0; i < N; ++i) {
+          const long double ang = -2.0L * pi * i / N;
+          cplx<T> c;
+          c.re = (T)cosl(ang);
+          c.im = (T)sinl(ang);
+          tw.push_back(c);
+        }
+      }
+      m.tw_off[d] = tw_at[N];
+      m.kt_off[d] = (long long)kt.size();
+      const double kf = dk[d] * dk[d] / (2.0 * x.mass[d]) / N;
+      for (int i = 0; i < N; ++i) {
+        const double q = std::min(i, N - i);
+        kt.push_back((T)(kf * q * q));
+      }
+      m.lmax[d] = (int)std::max(1, std::min(64, 4096 / N));
+      smem = std::max(smem, (size_t)N * (1 + 2 * (size_t)m.lmax[d]) * sizeof(cplx<T>));
+    }
+    m.off = off;
+    off += m.npts;
+    const double vmax = *std::max_element(x.potential, x.potential + m.npts);
+    const double vmin = *std::min_element(x.potential, x.potential + m.npts);
+    for (long long i = 0; i < m.npts; ++i) V.push_back((T)x.potential[i]);
+    // OSum::Emax/Emin over (GridNablaSq, GridPotential, GridDipole)
+    cd emax = Tmax * (M_PI * M_PI / 2) + vmax, emin = vmin;
+    m.has_dipole = x.dipole && x.laser && x.laser_nt > 0;
+    if (m.has_dipole) {
+      const double mmax = *std::max_element(x.dipole, x.dipole + m.npts);
+      const double lmax = *std::max_element(x.laser, x.laser + x.laser_nt);
+      emax += mmax * lmax;  // OGridDipole::Emax (OGridDipole.cpp:36-39)
+      for (long long i = 0; i < m.npts; ++i) mu.push_back((T)x.dipole[i]);
+      m.laser_off = (long long)lasers.size();
+      m.laser_nt = x.laser_nt;
+      lasers.insert(lasers.end(), x.laser, x.laser + x.laser_nt);
+    } else {
+      for (long long i = 0; i < m.npts; ++i) mu.push_back((T)0);
+      m.laser_off = -1;
+    }
+    qdg::host::ChebySeries cs;
+    const std::string err = qdg::host::cheby_series(emax, emin, e->dt, c0, false, params, cs);
+    if (!err.empty()) return efail(QDG_EINVAL, err);
+    m.order = cs.order;
+    m.coef_off = (long long)coef.size();
+    coef.insert(coef.end(), cs.coeff.begin(), cs.coeff.end());
+    const cd ex = c0 / e->dt;
+    m.offset.re = cs.offset.real(); m.offset.im = cs.offset.imag();
+    const cd f1 = ex / cs.scaling, f = 2.0 * ex / cs.scaling, ph = std::exp(c0 * cs.offset);
+    m.fac1.re = f1.real(); m.fac1.im = f1.imag();
+    m.fac.re = f.real(); m.fac.im = f.imag();
+    m.ph.re = ph.real(); m.ph.im = ph.imag();
+    m.prec = cs.prec;
+    cost[k] = (double)m.npts * std::log2((double)m.npts + 1) * cs.order;
+    e->hm.push_back(m);
+  }
+  e->total_pts = off;
+  // largest first (LPT order for the dynamic queue)
+  e->order.resize(n);
+  std::iota(e->order.begin(), e->order.end(), 0);
+  std::stable_sort(e->order.begin(), e->order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+  if (smem > 227 * 1024) return efail(QDG_EUNSUPPORTED, "member line too long for the shared-memory FFT");
+  e->smem = smem;
+  qdg_status s;
+  if ((s = upload_vec(reinterpret_cast<void **>(&e->d_m), e->hm)) != QDG_OK) return s;
+  if ((s = upload_vec(reinterpret_cast<void **>(&e->d_order), e->order)) != QDG_OK) return s;
+  if ((s = upload_vec(&e->d_V, V)) != QDG_OK) return s;
+  if ((s = upload_vec(&e->d_mu, mu)) != QDG_OK) return s;
+  if ((s = upload_vec(&e->d_tw, tw)) != QDG_OK) return s;
+  if ((s = upload_vec(&e->d_kt, kt)) != QDG_OK) return s;
+  if ((s = upload_vec(reinterpret_cast<void **>(&e->d_lasers), lasers)) != QDG_OK) return s;
+  if ((s = upload_vec(reinterpret_cast<void **>(&e->d_coef), coef)) != QDG_OK) return s;
+  const size_t pts = (size_t)std::max<long long>(1, off);
+  ECK(cudaMalloc(&e->d_psi, sizeof(cplx<double>) * pts));
+  ECK(cudaMemset(e->d_psi, 0, sizeof(cplx<double>) * pts));
+  ECK(cudaMalloc(&e->d_buf0, sizeof(cplx<T>) * pts));
+  ECK(cudaMalloc(&e->d_buf1, sizeof(cplx<T>) * pts));
+  ECK(cudaMalloc(&e->d_P0, sizeof(cplx<T>) * pts));
+  ECK(cudaMalloc(&e->d_P1, sizeof(cplx<T>) * pts));
+  ECK(cudaMalloc(&e->d_queue, sizeof(int)));
+  ECK(cudaMalloc(&e->d_status, sizeof(int) * n));
+  ECK(cudaMemset(e->d_status, 0, sizeof(int) * n));
+  ECK(cudaMalloc(&e->d_terms, sizeof(long long) * n));
+  ECK(cudaMemset(e->d_terms, 0, sizeof(long long) * n));
+  const int occ = qdg::ensemble_occupancy<T>(smem);
+  if (occ <= 0) return efail(QDG_EUNSUPPORTED, "ensemble kernel cannot be resident");
+  int dev = 0, sms = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  e->grid = std::max(1, std::min(n, occ * sms));
+  ECK(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+  return QDG_OK;
+}
+
+template <typename T>
+qdg_status run(qdg_ensemble *e, long long step0, int nsteps) {
+  qdg::EnsArgs<T> a;
+  memset(&a, 0, sizeof(a));
+  a.m = e->d_m;
+  a.order = e->d_order;
+  a.n = e->n;
+  a.queue = e->d_queue;
+  a.psi = e->d_psi;
+  a.buf0 = reinterpret_cast<cplx<T> *>(e->d_buf0);
+  a.buf1 = reinterpret_cast<cplx<T> *>(e->d_buf1);
+  a.P0 = reinterpret_cast<cplx<T> *>(e->d_P0);
+  a.P1 = reinterpret_cast<cplx<T> *>(e->d_P1);
+  a.V = reinterpret_cast<const T *>(e->d_V);
+  a.mu = reinterpret_cast<const T *>(e->d_mu);
+  a.lasers = e->d_lasers;
+  a.coef = e->d_coef;
+  a.tw = reinterpret_cast<const cplx<T> *>(e->d_tw);
+  a.ktab = reinterpret_cast<const T *>(e->d_kt);
+  a.step0 = step0;
+  a.nsteps = nsteps;
+  a.diff = e->precision == QDG_PREC_MIXED ? 1 : 0;
+  a.terms = e->d_terms;
+  a.status = e->d_status;
+  ECK(cudaMemsetAsync(e->d_queue, 0, sizeof(int), e->stream));
+  void *k = (void *)qdg::ensemble_kernel<T>;
+  if (e->smem > 48 * 1024) ECK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smem));
+  void *args[] = {(void *)&a};
+  qdg::add_launches(1);
+  ECK(cudaLaunchKernel(k, dim3(e->grid), dim3(256), args, e->smem, e->stream));
+  return QDG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+qdg_status qdg_ensemble_create(const qdg_ensemble_member *members, int32_t n, double dt, const char *params,
+                               int32_t precision, qdg_ensemble **out) {
+  if (!members || n < 1 || !out) return efail(QDG_EINVAL, "bad arguments");
+  if (!(dt > 0)) return efail(QDG_EINVAL, "No time step defined");
+  if (precision != QDG_PREC_FP64 && precision != QDG_PREC_MIXED) return efail(QDG_EINVAL, "unknown precision");
+  *out = nullptr;
+  qdg_ensemble *e = new qdg_ensemble();
+  e->n = n;
+  e->precision = precision;
+  e->csize = precision == QDG_PREC_FP64 ? 16 : 8;
+  e->dt = dt;
+  std::map<std::string, std::string> kv;
+  parse_kv(params, kv);
+  const qdg_status s = precision == QDG_PREC_FP64 ? build<double>(e, members, kv) : build<float>(e, members, kv);
+  if (s != QDG_OK) {
+    free_ensemble(e);
+    return s;
+  }
+  *out = e;
+  return QDG_OK;
+}
+
+qdg_status qdg_ensemble_destroy(qdg_ensemble *e) {
+  if (!e) return QDG_OK;
+  if (e->stream) cudaStreamSynchronize(e->stream);
+  free_ensemble(e);
+  return QDG_OK;
+}
+
+qdg_status qdg_ensemble_upload(qdg_ensemble *e, const double *psi) {
+  if (!e || !psi) return efail(QDG_EINVAL, "null argument");
+  ECK(cudaMemcpyAsync(e->d_psi, psi, sizeof(cplx<double>) * e->total_pts, cudaMemcpyHostToDevice, e->stream));
+  ECK(cudaStreamSynchronize(e->stream));
+  return QDG_OK;
+}
+
+qdg_status qdg_ensemble_download(const qdg_ensemble *e, double *psi) {
+  if (!e || !psi) return efail(QDG_EINVAL, "null argument");
+  ECK(cudaMemcpyAsync(psi, e->d_psi, sizeof(cplx<double>) * e->total_pts, cudaMemcpyDeviceToHost, e->stream));
+  ECK(cudaStreamSynchronize(e->stream));
+  return QDG_OK;
+}
+
+qdg_status qdg_ensemble_run(qdg_ensemble *e, int64_t step0, int32_t nsteps, int64_t *terms_total) {
+  if (!e || nsteps < 0) return efail(QDG_EINVAL, "bad arguments");
+  std::vector<long long> before(e->n), after(e->n);
+  ECK(cudaMemcpy(before.data(), e->d_terms, sizeof(long long) * e->n, cudaMemcpyDeviceToHost));
+  const qdg_status s = e->precision == QDG_PREC_FP64 ? run<double>(e, step0, nsteps) : run<float>(e, step0, nsteps);
+  if (s != QDG_OK) return s;
+  ECK(cudaStreamSynchronize(e->stream));
+  ECK(cudaMemcpy(after.data(), e->d_terms, sizeof(long long) * e->n, cudaMemcpyDeviceToHost));
+  std::vector<int> st(e->n);
+  ECK(cudaMemcpy(st.data(), e->d_status, sizeof(int) * e->n, cudaMemcpyDeviceToHost));
+  long long tot = 0;
+  for (int i = 0; i < e->n; ++i) tot += after[i] - before[i];
+  if (terms_total) *terms_total = tot;
+  for (int i = 0; i < e->n; ++i)
+    if (st[i]) return efail(QDG_ENONFINITE, "Norm is not a number (ensemble member " + std::to_string(i) + ")");
+  return QDG_OK;
+}
+
+qdg_status qdg_ensemble_member_info(const qdg_ensemble *e, int32_t i, qdg_prop_info *info) {
+  if (!e || !info || i < 0 || i >= e->n) return efail(QDG_EINVAL, "bad arguments");
+  const qdg::EnsMember &m = e->hm[i];
+  info->kind = 1;
+  info->order = m.order;
+  info->scaling = std::abs(cd(0, -e->dt) / e->dt) / std::abs(cd(m.fac1.re, m.fac1.im));
+  info->offset_re = m.offset.re;
+  info->offset_im = m.offset.im;
+  info->exponent_re = 0;
+  info->exponent_im = -e->dt;
+  return QDG_OK;
+}
+
+}  // extern "C"

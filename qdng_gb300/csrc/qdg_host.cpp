@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 
 namespace qdg {
 namespace host {
@@ -158,6 +159,55 @@ std::vector<cd> expm_e0(int n, const std::vector<cd> &A, cd c) {
   std::vector<cd> v(n);
   for (int i = 0; i < n; ++i) v[i] = E[(size_t)i * n];
   return v;
+}
+
+std::string cheby_series(cd Emax, cd Emin, double dt, cd c0, bool imag,
+                         const std::map<std::string, std::string> &params, ChebySeries &out) {
+  auto has = [&](const char *k) { return params.count(k) > 0; };
+  auto getd = [&](const char *k) { return atof(params.at(k).c_str()); };
+  out = ChebySeries();
+  int order = 0;
+  if (has("order")) {
+    order = atoi(params.at("order").c_str());
+    if (order < 1) return "Chebychev recursion order invalid";
+  }
+  if (has("Emax")) Emax.real(getd("Emax"));
+  if (has("Emax_im")) Emax.imag(getd("Emax_im"));
+  if (has("Emin")) Emin.real(getd("Emin"));
+  if (has("Emin_im")) Emin.imag(getd("Emin_im"));
+  cd offset;
+  double scaling;
+  if (!imag) offset = cd((Emax + Emin).real() / 2, (Emax + Emin).imag());
+  else offset = Emin - std::abs(Emin) * 0.05;
+  if (offset.imag() != 0 || std::fabs(c0.imag()) == 0) scaling = std::abs(Emax - Emin) * 1.05;
+  else scaling = std::abs(Emax - Emin) / 2;
+  if (order <= 0) order = std::abs(int(20 * scaling * dt));
+  if (order < 10) order = 10;
+  if (has("scaling")) scaling = getd("scaling");
+  if (has("order")) order = atoi(params.at("order").c_str());
+  if (order < 3) return "Chebychev recursion must be at least 3";
+  std::vector<double> b;
+  int zeroes;
+  const double R = scaling * dt;
+  if (std::fabs(c0.imag()) != 0 && std::fabs(c0.real()) == 0) zeroes = bessel_j(order, R, b);
+  else if (std::fabs(c0.imag()) == 0 && std::fabs(c0.real()) != 0) zeroes = bessel_i_scaled(order, R, b);
+  else return "Chebychev propagator doesn't support mixed real/complex exponents";
+  order -= zeroes;
+  if (!has("order")) {
+    const double precission = 1e-32;  // BESSEL_DELTA (OCheby.h:10)
+    int i = 2;
+    while (i < order && std::fabs(b[i - 1] - b[i - 2]) > precission) i++;
+    order = i;
+  }
+  if (order > 0 && !imag && order <= int(scaling * dt)) return "Chebychev recursion order is to small";
+  out.order = order;
+  out.scaling = scaling;
+  out.offset = offset;
+  out.coeff.assign(order, 0.0);
+  out.coeff[0] = b[0];
+  for (int i = 1; i < order; ++i) out.coeff[i] = 2.0 * b[i];
+  if (has("prec")) out.prec = getd("prec");
+  return std::string();
 }
 
 }  // namespace host

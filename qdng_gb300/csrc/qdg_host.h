@@ -7,6 +7,8 @@
 #pragma once
 
 #include <complex>
+#include <map>
+#include <string>
 #include <vector>
 
 namespace qdg {
@@ -29,6 +31,19 @@ void sym_eig(int n, const std::vector<double> &a, std::vector<double> &w, std::v
 // v = exp(c A) e_0 for a small complex matrix A (row-major), the vector
 // OArnoldi::Propagate forms with zhseqr/zhsein/zgetri (OArnoldi.cpp:169-186).
 std::vector<cd> expm_e0(int n, const std::vector<cd> &A, cd c);
+
+// Series of OCheby::Init (src/qdlib/OCheby.cpp:358-493) for a Hamiltonian
+// with energy range [emin, emax] and exponent c0 (OPropagator::Exponent).
+struct ChebySeries {
+  int order = 0;
+  double scaling = 1.0;
+  cd offset = 0.0;
+  double prec = 1e-10;          // DEFAULT_PREC (OCheby.h:11)
+  std::vector<double> coeff;    // a_0 = J_0 (I_0), a_i = 2 J_i (2 I_i)
+};
+// Returns an empty string on success, else the reference's error message.
+std::string cheby_series(cd emax, cd emin, double dt, cd c0, bool imag,
+                         const std::map<std::string, std::string> &params, ChebySeries &out);
 
 }  // namespace host
 }  // namespace qdg

@@ -175,10 +175,72 @@ class Propagator:
         return np.array(rows), np.array(terms)
 
 
+class Ensemble:
+    """Batched independent wavepackets (qdg_ensemble_*): one persistent launch.
+
+    members: dicts with keys grid (operators.GridSystem), mass, V, and
+    optionally mu and laser (GridDipole x field)."""
+
+    def __init__(self, members, dt, params="", precision="mixed"):
+        self.lib = load()
+        self.members = members
+        self._keep = []
+        arr = (abi.EnsembleMember * len(members))()
+        self.sizes = []
+        for i, m in enumerate(members):
+            g = m["grid"]
+            e = arr[i]
+            e.grid = g.to_c()
+            for d, mass in enumerate(np.atleast_1d(m["mass"])):
+                e.mass[d] = float(mass)
+            V = np.ascontiguousarray(m["V"], dtype=np.float64).reshape(-1)
+            self._keep.append(V)
+            e.potential = V.ctypes.data_as(C.POINTER(C.c_double))
+            if m.get("mu") is not None and m.get("laser") is not None:
+                mu = np.ascontiguousarray(m["mu"], dtype=np.float64).reshape(-1)
+                las = np.ascontiguousarray(m["laser"], dtype=np.float64).reshape(-1)
+                self._keep += [mu, las]
+                e.dipole = mu.ctypes.data_as(C.POINTER(C.c_double))
+                e.laser = las.ctypes.data_as(C.POINTER(C.c_double))
+                e.laser_nt = las.size
+            self.sizes.append(g.npts)
+        h = C.c_void_p()
+        check(self.lib.qdg_ensemble_create(arr, len(members), dt, params.encode(), PRECISIONS[precision],
+                                           C.byref(h)))
+        self.h = h
+        self.offsets = np.concatenate([[0], np.cumsum(self.sizes)])
+
+    def close(self):
+        if getattr(self, "h", None) and not _exiting[0]:
+            self.lib.qdg_ensemble_destroy(self.h)
+        self.h = None
+
+    __del__ = close
+
+    def upload(self, psis):
+        a = np.ascontiguousarray(np.concatenate([np.asarray(p, dtype=np.complex128).reshape(-1) for p in psis]))
+        check(self.lib.qdg_ensemble_upload(self.h, _dp(a)))
+
+    def download(self):
+        out = np.empty(int(self.offsets[-1]), dtype=np.complex128)
+        check(self.lib.qdg_ensemble_download(self.h, _dp(out)))
+        return [out[self.offsets[i]:self.offsets[i + 1]] for i in range(len(self.sizes))]
+
+    def run(self, step0, nsteps):
+        t = C.c_int64(0)
+        check(self.lib.qdg_ensemble_run(self.h, step0, nsteps, C.byref(t)))
+        return t.value
+
+    def info(self, i):
+        inf = abi.PropInfo()
+        check(self.lib.qdg_ensemble_member_info(self.h, i, C.byref(inf)))
+        return dict(order=inf.order, scaling=inf.scaling, offset=complex(inf.offset_re, inf.offset_im))
+
+
 def kernel_launches():
     return load().qdg_kernel_launches()
 
 
 PASS_MODES = ["kinetic", "kin_acc", "h_apply", "cheby_first", "cheby_term", "gspo_kin", "cheby_step"]
 
-__all__ = ["Plan", "WaveFunction", "Propagator", "QDGError", "kernel_launches", "PASS_MODES"]
+__all__ = ["Plan", "WaveFunction", "Propagator", "Ensemble", "QDGError", "kernel_launches", "PASS_MODES"]

@@ -148,3 +148,74 @@ def cfg5_double_well(n=128):
     hp = op.HPlan(g, op.Sum([op.GridNablaSq([1836.0, 1836.0]), op.GridPotential(V)]))
     psi = np.exp(-((X - 2.0) ** 2 + Y ** 2) / 0.5).reshape(-1).astype(np.complex128)
     return hp, _normalize(hp, psi), dict(name="Cheby", params="", dt=20.0, steps=2000)
+
+
+# ----------------------------------------------------------------- ensemble
+ENS_1D_SIZES = [256, 384, 512, 768, 1024, 1536, 2048, 3072, 4096]
+ENS_2D_SIDES = [64, 96, 128, 192, 256]
+
+
+def cfg4_member(rng, kind, size, nt=5000, dt=10.0):
+    """One laser-driven Morse member (BASELINE configs[3]); 2-D members add a
+    harmonic y mode.  Box x in [1,10] (y in [-3,3]), mass 1728, dt 10."""
+    D = rng.uniform(0.05, 0.2)
+    a = rng.uniform(0.7, 1.3)
+    re = rng.uniform(1.5, 2.5)
+    E0 = rng.uniform(0.001, 0.02)
+    w = rng.uniform(0.005, 0.02)
+    m = 1728.0
+    if kind == 1:
+        g = op.GridSystem([size], [1.0], [10.0])
+        x = g.axes()[0]
+        V = D * (1 - np.exp(-a * (x - re))) ** 2
+        mu = x * np.exp(-x / 4)
+        sig = (m * a * np.sqrt(2 * D / m)) ** -0.5
+        psi = np.exp(-(x - re - 0.1) ** 2 / (2 * sig ** 2)).astype(np.complex128)
+        mass = [m]
+    else:
+        g = op.GridSystem([size, size], [1.0, -3.0], [10.0, 3.0])
+        X, Y = g.mesh()
+        ky = 0.01
+        V = D * (1 - np.exp(-a * (X - re))) ** 2 + 0.5 * ky * Y ** 2
+        mu = X * np.exp(-X / 4)
+        sig = (m * a * np.sqrt(2 * D / m)) ** -0.5
+        sy = (m * np.sqrt(ky / m)) ** -0.5
+        psi = np.exp(-(X - re - 0.1) ** 2 / (2 * sig ** 2) - Y ** 2 / (2 * sy ** 2)).astype(np.complex128)
+        mass = [m, m]
+    T = nt * dt
+    t = np.arange(nt) * dt
+    laser = E0 * np.sin(np.pi * t / T) ** 2 * np.cos(w * t)
+    psi = psi.reshape(-1)
+    psi /= np.sqrt((np.abs(psi) ** 2).sum() * np.prod(g.dx))
+    return dict(grid=g, mass=mass, V=V.reshape(-1), mu=mu.reshape(-1), laser=laser, psi=psi,
+                params=dict(D=D, a=a, re=re, E0=E0, w=w))
+
+
+def cfg4_ensemble(n=512, seed=4, frac_2d=0.25, sizes_1d=ENS_1D_SIZES, sides_2d=ENS_2D_SIDES, nt=5000):
+    """The seeded 512-member ensemble; 1-D/2-D split and sizes drawn uniformly."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        if rng.uniform() < frac_2d:
+            out.append(cfg4_member(rng, 2, int(rng.choice(sides_2d)), nt))
+        else:
+            out.append(cfg4_member(rng, 1, int(rng.choice(sizes_1d)), nt))
+    return out
+
+
+def member_hplan(mem):
+    """The member as a QDng operator tree: Sum(GridNablaSq, GridPotential, GridDipole)."""
+    return op.HPlan(mem["grid"], op.Sum([op.GridNablaSq(mem["mass"]), op.GridPotential(mem["V"]),
+                                         op.GridDipole(mem["mu"], mem["laser"])]))
+
+
+def lpt_partition(costs, nparts):
+    """Largest-processing-time-first assignment of independent members to ranks."""
+    order = sorted(range(len(costs)), key=lambda i: -costs[i])
+    loads = [0.0] * nparts
+    parts = [[] for _ in range(nparts)]
+    for i in order:
+        r = min(range(nparts), key=lambda k: loads[k])
+        parts[r].append(i)
+        loads[r] += costs[i]
+    return [sorted(p) for p in parts], loads

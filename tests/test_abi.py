@@ -39,12 +39,15 @@ def test_struct_layouts_match_c(tmp_path):
     src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "qdg.h"\n'
                    'int main(void){printf("%zu %zu %zu %zu %zu %zu %zu\\n", sizeof(qdg_grid), sizeof(qdg_hterm),'
                    ' sizeof(qdg_hplan_desc), sizeof(qdg_observables), sizeof(qdg_prop_info),'
-                   ' offsetof(qdg_hterm, mass), offsetof(qdg_hplan_desc, laser_data)); return 0;}\n')
+                   ' offsetof(qdg_hterm, mass), offsetof(qdg_hplan_desc, laser_data));'
+                   ' printf("%zu %zu\\n", sizeof(qdg_ensemble_member), offsetof(qdg_ensemble_member, laser_nt));'
+                   ' return 0;}\n')
     exe = tmp_path / "sizes"
     subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
     got = [int(v) for v in subprocess.check_output([str(exe)]).split()]
     want = [C.sizeof(abi.Grid), C.sizeof(abi.HTerm), C.sizeof(abi.HPlanDesc), C.sizeof(abi.Observables),
-            C.sizeof(abi.PropInfo), abi.HTerm.mass.offset, abi.HPlanDesc.laser_data.offset]
+            C.sizeof(abi.PropInfo), abi.HTerm.mass.offset, abi.HPlanDesc.laser_data.offset,
+            C.sizeof(abi.EnsembleMember), abi.EnsembleMember.laser_nt.offset]
     assert got == want
 
 
