@@ -162,6 +162,32 @@ def cpu_reference(hp, psi, run, steps, warmup, budget_s=None):
     return hp.size * n / dt, threads, n, dt
 
 
+def mixed_error(hp, psi, run, nsteps):
+    """Observables of the mixed-precision path against the FP64 path over
+    nsteps from the same start (the FP64 path equals the oracle to 1e-12):
+    largest error over the steps of the norm, each state population, <H>
+    and the autocorrelation <psi0|psi(t)> (populations and autocorrelation
+    relative to the norm, which bounds them; norm and <H> relative to their
+    values)."""
+    import numpy as np
+
+    from qdng_gb300 import engine
+    rows = {}
+    for prec in ("fp64", "mixed"):
+        plan = engine.Plan(hp, prec)
+        prop = engine.Propagator(plan, run["name"], run["params"], dt=run["dt"])
+        w, w0 = plan.wavefunction(psi), plan.wavefunction(psi)
+        rows[prec], _ = prop.propagate(w, w0, nsteps)
+    a, b = rows["mixed"], rows["fp64"]
+    S = hp.nstates
+    ac_a, ac_b = a[:, S + 2] + 1j * a[:, S + 3], b[:, S + 2] + 1j * b[:, S + 3]
+    return {"steps": nsteps,
+            "norm_rel": float(np.max(np.abs(a[:, 0] - b[:, 0]) / np.abs(b[:, 0]))),
+            "populations": float(np.max(np.abs(a[:, 1:S + 1] - b[:, 1:S + 1]) / b[:, :1])),
+            "energy_rel": float(np.max(np.abs(a[:, S + 1] - b[:, S + 1]) / np.abs(b[:, S + 1]))),
+            "autocorrelation": float(np.max(np.abs(ac_a - ac_b) / b[:, 0]))}
+
+
 def engine_arm(args, world, rank, local):
     import numpy as np
     import torch
@@ -280,6 +306,10 @@ def engine_arm(args, world, rank, local):
     e2e_s = reduce_max(e2e_s, world)
     e2e_val = hp.size * args.steps * world / e2e_s
 
+    err = None
+    if args.precision == "mixed" and rank == 0 and args.err_steps > 0:
+        err = mixed_error(hp, psi, run, args.err_steps)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         v, threads, n, dt = cpu_reference(hp, psi, run, steps=10 ** 6, warmup=1, budget_s=args.cpu_budget)
@@ -309,6 +339,7 @@ def engine_arm(args, world, rank, local):
         "per_term": term_rate,
         "pass_profile": per_mode,
         "step_phases_us_per_term": phases or None,
+        "error_vs_fp64": err,
         "clocks": clocks,
         "cpu_baseline": cpu,
     }
@@ -362,8 +393,15 @@ def ensemble_arm(args, world, rank, local):
         R.upload(psi0)
         E.run(0, args.steps)
         R.run(0, args.steps)
-        errs = [float(np.abs(a - b).max() / np.abs(b).max()) for a, b in zip(E.download(), R.download())]
-        err = {"max_rel_psi_error_vs_fp64": max(errs), "median": float(np.median(errs)), "steps": args.steps}
+        errs, acs, nrms = [], [], []
+        for p0, a, b in zip(psi0, E.download(), R.download()):
+            errs.append(float(np.abs(a - b).max() / np.abs(b).max()))
+            ac, ac_ref = np.vdot(p0, a), np.vdot(p0, b)
+            acs.append(float(abs(ac - ac_ref) / abs(ac_ref)))
+            n, n_ref = np.vdot(a, a).real, np.vdot(b, b).real
+            nrms.append(float(abs(n - n_ref) / n_ref))
+        err = {"max_rel_psi_error_vs_fp64": max(errs), "median": float(np.median(errs)),
+               "max_rel_autocorrelation_error": max(acs), "max_rel_norm_error": max(nrms), "steps": args.steps}
     bytes_io = int(sum(p.size for p in psi0) * 16)
     line = {
         "metric": "wavepackets/s (512 laser-driven members, 5000 steps each)",
@@ -427,6 +465,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--err-steps", type=int, default=400,
+                    help="steps of the mixed-vs-FP64 observable comparison (0: skip)")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="cfg2", choices=["cfg2", "ensemble"])

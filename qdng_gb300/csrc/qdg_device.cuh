@@ -128,6 +128,47 @@ template <typename T> __device__ __forceinline__ void dft16(cplx<T> *x, int sign
   for (int k = 0; k < 16; ++k) x[k] = y[k];
 }
 
+// Twiddles w^(r*k) and the R-point DFT of one Stockham item, in registers.
+template <typename T, int R>
+__device__ __forceinline__ void stage_butterfly(cplx<T> (&v)[R], int k, int step, int M,
+                                                const cplx<T> *__restrict__ tw, int sign) {
+  if (k) {
+#pragma unroll
+    for (int r = 1; r < R; ++r) {
+      cplx<T> w = tw[r * k * step];  // r*k*step < R*Ns*step = N
+      if (sign > 0) w.im = -w.im;
+      v[r] = cmul(v[r], w);
+    }
+  }
+  if (R == 2) {
+    const cplx<T> a = v[0];
+    v[0] = a + v[1];
+    v[1] = a - v[1];
+  } else if (R == 4) {
+    dft4(v[0], v[1], v[2], v[3], sign);
+  } else if (R == 8) {
+    dft8(v, sign);
+  } else if (R == 16) {
+    dft16(v, sign);
+  } else {
+    // direct R-point DFT with the table entries of the R-th roots of unity
+    cplx<T> y[R];
+#pragma unroll
+    for (int qq = 0; qq < R; ++qq) {
+      cplx<T> s = v[0];
+#pragma unroll
+      for (int r = 1; r < R; ++r) {
+        cplx<T> w = tw[((r * qq) % R) * M];
+        if (sign > 0) w.im = -w.im;
+        s = s + cmul(v[r], w);
+      }
+      y[qq] = s;
+    }
+#pragma unroll
+    for (int qq = 0; qq < R; ++qq) v[qq] = y[qq];
+  }
+}
+
 // One Stockham stage over `nlines` lines of length N stored line after line
 // in `in` (line stride N); result in `out`.  Items are spread over all
 // threads of the block.  tw[m] = exp(-2 pi i m / N); sign = -1 forward
@@ -162,45 +203,58 @@ __device__ __forceinline__ void stockham_stage(const cplx<T> *__restrict__ in, c
     cplx<T> v[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = src[j + r * M];
-    if (k) {
-#pragma unroll
-      for (int r = 1; r < R; ++r) {
-        cplx<T> w = tw[r * k * step];  // r*k*step < R*Ns*step = N
-        if (sign > 0) w.im = -w.im;
-        v[r] = cmul(v[r], w);
-      }
-    }
-    if (R == 2) {
-      const cplx<T> a = v[0];
-      v[0] = a + v[1];
-      v[1] = a - v[1];
-    } else if (R == 4) {
-      dft4(v[0], v[1], v[2], v[3], sign);
-    } else if (R == 8) {
-      dft8(v, sign);
-    } else if (R == 16) {
-      dft16(v, sign);
-    } else {
-      // direct R-point DFT with the table entries of the R-th roots of unity
-      cplx<T> y[R];
-#pragma unroll
-      for (int qq = 0; qq < R; ++qq) {
-        cplx<T> s = v[0];
-#pragma unroll
-        for (int r = 1; r < R; ++r) {
-          cplx<T> w = tw[((r * qq) % R) * M];
-          if (sign > 0) w.im = -w.im;
-          s = s + cmul(v[r], w);
-        }
-        y[qq] = s;
-      }
-#pragma unroll
-      for (int qq = 0; qq < R; ++qq) v[qq] = y[qq];
-    }
+    stage_butterfly<T, R>(v, k, step, M, tw, sign);
     cplx<T> *dst = out + line * N + q * Ns * R + k;
 #pragma unroll
     for (int r = 0; r < R; ++r) dst[r * Ns] = v[r];
   }
+}
+
+// The same stage with the element reads and writes as functors, load(idx)
+// and store(idx, value) with idx = line * N + position, so that a caller can
+// fuse a multiply into the loads of a stage or its point update into the
+// stores of the last one.
+template <typename T, int R, typename Load, typename Store>
+__device__ __forceinline__ void stockham_stage_io(Load load, Store store, int N, int nlines, int Ns,
+                                                  const cplx<T> *__restrict__ tw, int sign) {
+  const int M = N / R;
+  const int step = N / (Ns * R);
+  const int items = nlines * M;
+  const bool pow2 = ((M & (M - 1)) == 0) && ((Ns & (Ns - 1)) == 0);
+  const int lgM = __ffs(M) - 1, lgNs = __ffs(Ns) - 1;
+  for (int it = threadIdx.x; it < items; it += blockDim.x) {
+    int line, j, k, q;
+    if (pow2) {
+      line = it >> lgM;
+      j = it & (M - 1);
+      k = j & (Ns - 1);
+      q = j >> lgNs;
+    } else {
+      line = it / M;
+      j = it - line * M;
+      q = j / Ns;
+      k = j - q * Ns;
+    }
+    cplx<T> v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = load(line * N + j + r * M);
+    stage_butterfly<T, R>(v, k, step, M, tw, sign);
+    const int dst = line * N + q * Ns * R + k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) store(dst + r * Ns, v[r]);
+  }
+}
+
+// One functor stage of any radix of a plan.
+template <typename T, typename Load, typename Store>
+__device__ __forceinline__ void stage_any(int R, Load load, Store store, int N, int nlines, int Ns,
+                                          const cplx<T> *__restrict__ tw, int sign) {
+  if (R == 16) stockham_stage_io<T, 16>(load, store, N, nlines, Ns, tw, sign);
+  else if (R == 8) stockham_stage_io<T, 8>(load, store, N, nlines, Ns, tw, sign);
+  else if (R == 4) stockham_stage_io<T, 4>(load, store, N, nlines, Ns, tw, sign);
+  else if (R == 2) stockham_stage_io<T, 2>(load, store, N, nlines, Ns, tw, sign);
+  else if (R == 3) stockham_stage_io<T, 3>(load, store, N, nlines, Ns, tw, sign);
+  else stockham_stage_io<T, 5>(load, store, N, nlines, Ns, tw, sign);
 }
 
 // Full unnormalised FFT of `nlines` lines in shared memory.  Data starts in

@@ -41,6 +41,7 @@ struct EnsMember {
   long long laser_off;    // -1: no field
   int laser_nt;
   int has_dipole;
+  int fast;               // 1-D member kept in shared memory for the whole step
 };
 
 template <typename T>
@@ -150,6 +151,126 @@ __device__ double ens_points(const EnsArgs<T> &a, const EnsMember &m, const cplx
   return acc;
 }
 
+// Shared memory of the resident 1-D path for a line of N points: psi
+// (FP64), phi_{i-1}, phi_{i-2}, the two FFT buffers and V - mu E.
+template <typename T>
+__host__ __device__ inline size_t ens_fast_smem(int N) {
+  return (size_t)N * (sizeof(cplx<double>) + 4 * sizeof(cplx<T>) + sizeof(T));
+}
+
+// One step of a 1-D member that lives in shared memory for the whole step.
+// Per term: the forward FFT reads phi_{i-1} directly, the k^2 multiply is
+// fused into the loads of the first inverse stage and the point update
+// (H phi, the recurrence, the psi accumulation and the norm) into the stores
+// of the last inverse stage, so a term costs 2 x stages block barriers.
+template <typename T>
+__device__ void ens_step_1d(const EnsArgs<T> &a, const EnsMember &m, T field, unsigned char *smem_raw,
+                            double *red, long long &terms, int &status) {
+  const int N = m.n[0];
+  cplx<double> *ps = reinterpret_cast<cplx<double> *>(smem_raw);
+  cplx<T> *cur = reinterpret_cast<cplx<T> *>(ps + N);
+  cplx<T> *prev = cur + N;
+  cplx<T> *f0 = prev + N;
+  cplx<T> *f1 = f0 + N;
+  T *Vs = reinterpret_cast<T *>(f1 + N);
+  const cplx<T> *__restrict__ tw = a.tw + m.tw_off[0];
+  const T *__restrict__ kt = a.ktab + m.kt_off[0];
+  cplx<double> *__restrict__ gpsi = a.psi + m.off;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    T v = a.V[m.off + i];
+    if (m.has_dipole) v = v + field * a.mu[m.off + i];
+    Vs[i] = v;
+    const cplx<double> p = ld(gpsi + i);
+    ps[i] = p;
+    cur[i] = ccast<T>(p);
+  }
+  __syncthreads();
+  const RadixPlan &rp = m.rp[0];
+  const cplx<T> off = ccast<T>(m.offset);
+  const int nw = (blockDim.x + 31) >> 5;
+  double norm0 = 0.0, last = 0.0;
+  bool done = false;
+  int used = 2;
+  for (int it = 1; it < m.order && !done; ++it) {
+    const bool first = it == 1;
+    // forward transform of phi_{i-1}: cur -> f0 -> f1 -> ...
+    int Ns = 1;
+    cplx<T> *dst = f0;
+    const cplx<T> *src = cur;
+    for (int s = 0; s < rp.nstages; ++s) {
+      stage_any<T>(rp.radix[s], [&](int i) { return src[i]; }, [&](int i, const cplx<T> &v) { dst[i] = v; }, N, 1,
+                   Ns, tw, -1);
+      __syncthreads();
+      Ns *= rp.radix[s];
+      src = dst;
+      dst = dst == f0 ? f1 : f0;
+    }
+    // inverse transform; the last stage finishes the term point by point
+    const cplx<T> fac = ccast<T>(first ? m.fac1 : m.fac);
+    const double ai = a.coef[m.coef_off + it];
+    const double a0 = a.coef[m.coef_off];
+    double acc = 0.0;
+    auto point = [&](int i, const cplx<T> &tk) {
+      const cplx<T> x = cur[i];
+      const cplx<T> h = tk + cmulr(x, Vs[i]);
+      const cplx<T> bf = cmul(h - cmul(off, x), fac);
+      cplx<double> p = ps[i];
+      if (first) {
+        acc += cabs2(p);
+        prev[i] = bf;  // phi_1
+        const cplx<double> b = ccast<double>(bf);
+        p = mk(p.re * a0 + b.re * ai, p.im * a0 + b.im * ai);
+      } else {
+        const cplx<T> k2 = bf + prev[i];
+        prev[i] = k2;  // phi_i over phi_{i-2}
+        p.re += ai * (double)k2.re;
+        p.im += ai * (double)k2.im;
+        acc += cabs2(p);
+      }
+      ps[i] = p;
+    };
+    Ns = 1;
+    for (int s = 0; s < rp.nstages; ++s) {
+      const bool ks = s == 0, ls = s == rp.nstages - 1;
+      auto load = [&](int i) { return ks ? cmulr(src[i], kt[i]) : src[i]; };
+      if (ls) {
+        stage_any<T>(rp.radix[s], load, point, N, 1, Ns, tw, +1);
+      } else {
+        stage_any<T>(rp.radix[s], load, [&](int i, const cplx<T> &v) { dst[i] = v; }, N, 1, Ns, tw, +1);
+        __syncthreads();
+      }
+      Ns *= rp.radix[s];
+      src = dst;
+      dst = dst == f0 ? f1 : f0;
+    }
+    // deterministic block reduction: every thread sums the warp totals in order
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    double tot = 0.0;
+    for (int w = 0; w < nw; ++w) tot += red[w];
+    // phi_{i-1} <- phi_i (prev), phi_{i-2} <- phi_{i-1} (cur)
+    cplx<T> *tmp = cur;
+    cur = prev;
+    prev = tmp;
+    if (first) {
+      norm0 = last = tot;
+      if (!isfinite(norm0)) { done = true; status = 2; }
+      continue;
+    }
+    used = it + 1;
+    if (!isfinite(tot)) { done = true; status = 2; }
+    else {
+      const double ref = a.diff ? last : norm0;
+      if (fabs(ref - tot) / norm0 < m.prec && m.offset.im == 0.0) done = true;  // OCheby.cpp:179-182
+    }
+    last = tot;
+  }
+  for (int i = threadIdx.x; i < N; i += blockDim.x) st(gpsi + i, cmul(ps[i], m.ph));
+  __syncthreads();
+  terms += used;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) ensemble_kernel(EnsArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -171,6 +292,10 @@ __global__ void __launch_bounds__(256) ensemble_kernel(EnsArgs<T> a) {
       // E(step) of Laser::Get (src/qdlib/Laser.cpp:125-128); the dipole term is -mu E
       T field = (T)0;
       if (m.has_dipole && step >= 0 && step < m.laser_nt) field = (T)(-a.lasers[m.laser_off + step]);
+      if (m.nd == 1 && m.fast) {
+        ens_step_1d<T>(a, m, field, smem_raw, red, terms, status);
+        continue;
+      }
       for (long long p = threadIdx.x; p < m.npts; p += blockDim.x)
         st(a.buf0 + m.off + p, ccast<T>(ld(a.psi + m.off + p)));
       ens_kinetic<T>(a, m, a.buf0, smem);
@@ -355,6 +480,13 @@ qdg_status build(qdg_ensemble *e, const qdg_ensemble_member *mem, const std::map
       }
       m.lmax[d] = (int)std::max(1, std::min(64, 4096 / N));
       smem = std::max(smem, (size_t)N * (1 + 2 * (size_t)m.lmax[d]) * sizeof(cplx<T>));
+    }
+    if (m.nd == 1) {
+      const size_t fsm = qdg::ens_fast_smem<T>(m.n[0]);
+      if (fsm <= 216 * 1024) {
+        m.fast = 1;
+        smem = std::max(smem, fsm);
+      }
     }
     m.off = off;
     off += m.npts;
