@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define QDG_ABI_VERSION 1
+#define QDG_ABI_VERSION 2
 
 /* Limits of the reference: MAX_DIMS (src/math/typedefs.h:28),
  * QD_MAX_STATES (src/qdlib/WFMultistate.h:10). */
@@ -52,7 +52,9 @@ typedef enum qdg_status {
 typedef enum qdg_term_kind {
   QDG_TERM_KINETIC = 1,    /* OGridNablaSq: -1/(2m) Laplacian via FFT (src/qdlib/OGridNablaSq.cpp:28-111) */
   QDG_TERM_POTENTIAL = 2,  /* OGridPotential: V(x) psi (src/qdlib/OGridPotential.cpp:134-142) */
-  QDG_TERM_DIPOLE = 3      /* OGridDipole: -mu(x) E(t) psi (src/qdlib/OGridDipole.cpp:46-60) */
+  QDG_TERM_DIPOLE = 3,     /* OGridDipole: -mu(x) E(t) psi (src/qdlib/OGridDipole.cpp:46-60) */
+  QDG_TERM_NAC = 4         /* OGridNAC: sign/(2 mass) sum_d [f_d d/dx_d psi + d/dx_d (f_d psi)]
+                              (src/qdlib/OGridNAC.cpp:131-148), derivatives by FFT (OGridNabla.cpp:76-95) */
 } qdg_term_kind;
 
 typedef enum qdg_precision {
@@ -72,15 +74,20 @@ typedef struct qdg_grid {
 /* One operator of the Hamiltonian matrix H_{row,col}.
  * The matrix is a QDng "Multistate" of "Sum"s (src/qdlib/OMultistate.cpp:206-231,
  * src/qdlib/OSum.cpp:53-60); an off-diagonal term given at (row, col) is also
- * applied at (col, row) (hermitian pointer copy, OMultistate.cpp:122-132).
+ * applied at (col, row) (hermitian pointer copy, OMultistate.cpp:122-132)
+ * unless the matrix is non-hermitian (qdg_hplan_desc.nonhermitian, or terms
+ * given at both (i, j) and (j, i), OMultistate.cpp:52-53).
  * A single-state Hamiltonian is a plain Sum (nstates = 1). */
 typedef struct qdg_hterm {
   int32_t kind;                  /* qdg_term_kind */
   int32_t row, col;              /* matrix element; KINETIC must be diagonal */
-  int32_t grid;                  /* POTENTIAL/DIPOLE: index of the grid array in grid_data */
+  int32_t grid;                  /* POTENTIAL/DIPOLE: index of the grid array in grid_data;
+                                    NAC: index of f_0, with f_1 .. f_{ndims-1} following it */
   int32_t laser;                 /* DIPOLE: index of the field in laser_data */
   int32_t group;                 /* GSPO split member: 0 = "A" (full step), 1 = "B", ... (OGSPO.cpp:71-85) */
-  double mass[QDG_MAX_DIMS];     /* KINETIC: masses per dimension, all > 0 */
+  double mass[QDG_MAX_DIMS];     /* KINETIC: masses per dimension, all > 0;
+                                    NAC: mass[0] = the reduced mass (1 for N-D, OGridNAC.cpp:83-85) */
+  double sign;                   /* NAC: sign of the element (+1 or -1; 0 means the default +1) */
 } qdg_hterm;
 
 typedef struct qdg_hplan_desc {
@@ -93,6 +100,7 @@ typedef struct qdg_hplan_desc {
   int32_t nlasers;
   int32_t laser_nt;              /* samples per field; E(step) = laser[step] (Laser.cpp:125-128) */
   const double *laser_data;      /* nlasers * laser_nt doubles */
+  int32_t nonhermitian;          /* Multistate "nonhermitian" (OMultistate.cpp:83-85): no (col, row) copies */
 } qdg_hplan_desc;
 
 /* Per-step observables of QDng's Reporter (src/Reporter.cpp:65-154). */

@@ -284,9 +284,35 @@ struct System {
   std::vector<qdg_hterm> terms;
   std::vector<std::vector<double>> grids, lasers;
   int laser_nt = 0;
+  bool hermitian = true;                  /* OMultistate _hermitian (OMultistate.cpp:14,52-53,83-85) */
   std::vector<std::vector<double>> ktab;  /* per kinetic term: collective k-space table */
   FFTN fft;
 };
+
+/* Kspace::Init1Dddx (src/qdlib/Kspace.cpp:60-96) for dimension d, spread over
+ * the grid (OGridNabla::_InitDim, OGridNabla.cpp:172-180): k_d(p) * factor. */
+static void kspace_ddx(const System &s, int d, double factor, std::vector<double> &tab) {
+  long stride = 1;
+  for (int i = 0; i < d; ++i) stride *= s.g.n[i];
+  int Nx = s.g.n[d];
+  double dp = (2 * M_PI) / (s.g.xmax[d] - s.g.xmin[d] + s.dx[d]);
+  dp *= factor;
+  std::vector<double> k1(Nx);
+  if (Nx % 2 == 0) {
+    for (int i = 0; i < Nx / 2; ++i) {
+      k1[i] = double(i) * dp;
+      k1[Nx - i - 1] = -1 * double(i + 1) * dp;
+    }
+  } else {
+    k1[0] = 0;
+    for (int i = 1; i < (Nx + 1) / 2; ++i) {
+      k1[i] = double(i) * dp;
+      k1[Nx - i] = -1 * double(i) * dp;
+    }
+  }
+  tab.assign(s.npts, 0.0);
+  for (long p = 0; p < s.npts; ++p) tab[p] = k1[(p / stride) % Nx];
+}
 
 /* Kspace::Init1Dd2dx2 (src/qdlib/Kspace.cpp:22-50) summed over dims
  * (Diff::_InitKspace collective part, src/qdlib/Diff.cpp:119-139). */
@@ -321,8 +347,10 @@ static void kspace_table(const System &s, const double *mass, std::vector<double
 static double vec_max(const std::vector<double> &v) { double m = v[0]; for (double x : v) m = std::max(m, x); return m; }
 static double vec_min(const std::vector<double> &v) { double m = v[0]; for (double x : v) m = std::min(m, x); return m; }
 
-static bool term_at(const qdg_hterm &t, int i, int j) {
-  return (t.row == i && t.col == j) || (t.row != t.col && t.row == j && t.col == i);
+/* Element (i, j) of the matrix: the hermitian copy (OMultistate.cpp:122-132)
+ * puts an off-diagonal element at (j, i) too. */
+static bool term_at(const System &s, const qdg_hterm &t, int i, int j) {
+  return (t.row == i && t.col == j) || (s.hermitian && t.row != t.col && t.row == j && t.col == i);
 }
 
 /* Emax/Emin of one operator: OGridNablaSq.cpp:89-106, OGridPotential.cpp:124-132, OGridDipole.cpp:36-44. */
@@ -334,8 +362,15 @@ static cd term_emax(const System &s, const qdg_hterm &t) {
     return T;
   }
   if (t.kind == QDG_TERM_POTENTIAL) return vec_max(s.grids[t.grid]);
+  if (t.kind == QDG_TERM_NAC) {  /* OGridNAC::Emax (OGridNAC.cpp:105-115): dx of dim 0 */
+    double m = 0;
+    for (int d = 0; d < s.g.ndims; ++d) m += vec_max(s.grids[t.grid + d]);
+    return m * M_PI / t.mass[0] / s.dx[0];
+  }
   return vec_max(s.grids[t.grid]) * vec_max(s.lasers[t.laser]);
 }
+/* OGridNAC::Emin (OGridNAC.cpp:118-128) never adds the minima it computes and
+ * returns 0; that is kept. */
 static cd term_emin(const System &s, const qdg_hterm &t) {
   if (t.kind == QDG_TERM_POTENTIAL) return vec_min(s.grids[t.grid]);
   return 0.0;
@@ -348,12 +383,17 @@ static void erange(const System &s, cd &emax, cd &emin) {
     for (auto &t : s.terms) { emax += term_emax(s, t); emin += term_emin(s, t); }
     return;
   }
+  /* dsyev with uplo 'U' on the column-major matrix (LapackDiag.cpp:22-47)
+   * reads the elements (i, j), i <= j, only. */
   int S = s.S;
   std::vector<long double> mx(S * S, 0), mn(S * S, 0);
-  for (int i = 0; i < S; ++i) for (int j = 0; j < S; ++j) {
+  for (int i = 0; i < S; ++i) for (int j = i; j < S; ++j) {
     cd a = 0, b = 0; bool any = false;
-    for (auto &t : s.terms) if (term_at(t, i, j)) { a += term_emax(s, t); b += term_emin(s, t); any = true; }
-    if (any) { mx[i * S + j] = std::abs(a); mn[i * S + j] = std::abs(b); }
+    for (auto &t : s.terms) if (term_at(s, t, i, j)) { a += term_emax(s, t); b += term_emin(s, t); any = true; }
+    if (any) {
+      mx[i * S + j] = mx[j * S + i] = std::abs(a);
+      mn[i * S + j] = mn[j * S + i] = std::abs(b);
+    }
   }
   std::vector<long double> w, z;
   jacobi_eig(S, mx, w, z); emax = (double)w[S - 1];
@@ -363,6 +403,38 @@ static void erange(const System &s, cd &emax, cd &emin) {
 static double laser_at(const System &s, int l, long step) {
   if (step < 0 || step >= s.laser_nt) return 0.0;
   return s.lasers[l][step];
+}
+
+/* OGridNAC::Apply (OGridNAC.cpp:131-148) added to o: for every dimension d,
+ * f_d (c d/dx_d x) and c d/dx_d (f_d x), c = sign/(2 mass); each derivative is
+ * OGridNabla::Apply (OGridNabla.cpp:76-115): full FFT, times i k_d c / N
+ * (MultElementsComplexEq, codelets/MultElementsComplexEqCCDd.h), inverse FFT.
+ * The element's result is summed first and then added (Operator::ApplyAdd,
+ * Operator.h:307-316). */
+static void nac_apply(const System &s, const qdg_hterm &t, const cd *x, cd *o) {
+  const long N = s.npts;
+  const double sign = t.sign == 0 ? 1.0 : t.sign;
+  const double c = 0.5 * sign / t.mass[0];
+  std::vector<cd> b(N), acc(N, 0.0);
+  std::vector<double> k;
+  for (int d = 0; d < s.g.ndims; ++d) {
+    const double *f = s.grids[t.grid + d].data();
+    kspace_ddx(s, d, 1.0, k);
+    const double fac = c / double(N);
+    /* 1/2 f del psi */
+    for (long p = 0; p < N; ++p) b[p] = x[p];
+    s.fft.exec(b.data(), -1);
+    for (long p = 0; p < N; ++p) b[p] = b[p] * (k[p] * cd(0, 1)) * fac;
+    s.fft.exec(b.data(), +1);
+    for (long p = 0; p < N; ++p) acc[p] += b[p] * f[p];
+    /* 1/2 del f psi */
+    for (long p = 0; p < N; ++p) b[p] = x[p] * f[p];
+    s.fft.exec(b.data(), -1);
+    for (long p = 0; p < N; ++p) b[p] = b[p] * (k[p] * cd(0, 1)) * fac;
+    s.fft.exec(b.data(), +1);
+    for (long p = 0; p < N; ++p) acc[p] += b[p];
+  }
+  for (long p = 0; p < N; ++p) o[p] += acc[p];
 }
 
 /* H psi: OMultistate::Apply (OMultistate.cpp:206-231) over OSum::Apply/ApplyAdd
@@ -382,9 +454,11 @@ static void h_apply(const System &s, const cd *in, cd *out, long step) {
       for (size_t ti = 0; ti < s.terms.size(); ++ti) {
         const qdg_hterm &t = s.terms[ti];
         bool kin = t.kind == QDG_TERM_KINETIC;
-        if (term_at(t, i, j)) {
+        if (term_at(s, t, i, j)) {
           /* elementwise codelets are OpenMP loops in the reference (src/math/codelets) */
-          if (kin) {
+          if (t.kind == QDG_TERM_NAC) {
+            nac_apply(s, t, x, o);
+          } else if (kin) {
             cd *b = buf.data();
             #pragma omp parallel for schedule(static) if (N >= 8192)
             for (long p = 0; p < N; ++p) b[p] = x[p];
@@ -819,6 +893,10 @@ void *orc_system_create(const qdg_hplan_desc *d) {
     s->dx[i] = (d->grid.xmax[i] - d->grid.xmin[i]) / double(d->grid.n[i] - 1);
   }
   s->terms.assign(d->terms, d->terms + d->nterms);
+  s->hermitian = !d->nonhermitian;
+  for (auto &a : s->terms)
+    for (auto &b : s->terms)
+      if (a.row != a.col && a.row == b.col && a.col == b.row) s->hermitian = false;  /* OMultistate.cpp:52-53 */
   for (int i = 0; i < d->ngrids; ++i) s->grids.emplace_back(d->grid_data + i * s->npts, d->grid_data + (i + 1) * s->npts);
   s->laser_nt = d->laser_nt;
   for (int i = 0; i < d->nlasers; ++i) s->lasers.emplace_back(d->laser_data + (long)i * d->laser_nt, d->laser_data + (long)(i + 1) * d->laser_nt);

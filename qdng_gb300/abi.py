@@ -25,6 +25,7 @@ STATUS_NAMES = {
 TERM_KINETIC = 1
 TERM_POTENTIAL = 2
 TERM_DIPOLE = 3
+TERM_NAC = 4
 
 PREC_FP64 = 0
 PREC_MIXED = 1
@@ -48,6 +49,7 @@ class HTerm(C.Structure):
         ("laser", C.c_int32),
         ("group", C.c_int32),
         ("mass", C.c_double * QDG_MAX_DIMS),
+        ("sign", C.c_double),
     ]
 
 
@@ -62,6 +64,7 @@ class HPlanDesc(C.Structure):
         ("nlasers", C.c_int32),
         ("laser_nt", C.c_int32),
         ("laser_data", C.POINTER(C.c_double)),
+        ("nonhermitian", C.c_int32),
     ]
 
 

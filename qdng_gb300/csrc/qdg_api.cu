@@ -87,6 +87,14 @@ struct qdg_plan {
   std::vector<double> grids_h, lasers_h;
   int ngrids = 0, nlasers = 0, laser_nt = 0;
   cd emax = 0, emin = 0;
+  // OMultistate's hermitian copy of off-diagonal elements (OMultistate.cpp:122-132)
+  bool hermitian = true;
+  // OGridNAC elements as applied: (row, col) plus the hermitian copy
+  struct NacEntry { int row, col, grid; double c; };
+  std::vector<NacEntry> nac;
+  size_t nac_smem = 0;
+  int nac_per_sm = 1;
+  int nac_tw[QDG_MAX_DIMS] = {1, 1, 1, 1};
   // device
   void *d_grids = nullptr;      // bulk type
   double *d_lasers = nullptr;
@@ -212,18 +220,25 @@ cd term_emax(const qdg_plan *p, const qdg_hterm &t) {
     return T * (M_PI * M_PI / 2);
   }
   const double *g = p->grids_h.data() + (long long)t.grid * n;
+  if (t.kind == QDG_TERM_NAC) {  // OGridNAC::Emax (OGridNAC.cpp:105-115): dx of dimension 0
+    double m = 0;
+    for (int d = 0; d < p->nd; ++d) m += *std::max_element(g + d * n, g + (d + 1) * n);
+    return m * M_PI / t.mass[0] / p->dx[0];
+  }
   double gm = *std::max_element(g, g + n);
   if (t.kind == QDG_TERM_POTENTIAL) return gm;
   const double *l = p->lasers_h.data() + (long long)t.laser * p->laser_nt;
   return gm * *std::max_element(l, l + p->laser_nt);
 }
+// OGridNAC::Emin (OGridNAC.cpp:118-128) computes minima but never adds them:
+// it returns 0, and so does this.
 cd term_emin(const qdg_plan *p, const qdg_hterm &t) {
   if (t.kind != QDG_TERM_POTENTIAL) return 0.0;
   const double *g = p->grids_h.data() + (long long)t.grid * p->npts;
   return *std::min_element(g, g + p->npts);
 }
-bool term_at(const qdg_hterm &t, int i, int j) {
-  return (t.row == i && t.col == j) || (t.row != t.col && t.row == j && t.col == i);
+bool term_at(const qdg_plan *p, const qdg_hterm &t, int i, int j) {
+  return (t.row == i && t.col == j) || (p->hermitian && t.row != t.col && t.row == j && t.col == i);
 }
 
 // OSum::Emax/Emin (OSum.cpp:28-51) for one state; OMultistate::Emax/Emin
@@ -235,15 +250,21 @@ void compute_erange(qdg_plan *p) {
     p->emax = a; p->emin = b;
     return;
   }
+  // dsyev with uplo 'U' on the column-major matrix (LapackDiag.cpp:22-47)
+  // reads the elements (i, j), i <= j: the lower ones matter only through
+  // the hermitian copy.
   const int S = p->S;
   std::vector<double> mx(S * S, 0.0), mn(S * S, 0.0), w, z;
   for (int i = 0; i < S; ++i)
-    for (int j = 0; j < S; ++j) {
+    for (int j = i; j < S; ++j) {
       cd a = 0, b = 0;
       bool any = false;
       for (auto &t : p->terms)
-        if (term_at(t, i, j)) { a += term_emax(p, t); b += term_emin(p, t); any = true; }
-      if (any) { mx[i * S + j] = std::abs(a); mn[i * S + j] = std::abs(b); }
+        if (term_at(p, t, i, j)) { a += term_emax(p, t); b += term_emin(p, t); any = true; }
+      if (any) {
+        mx[i * S + j] = mx[j * S + i] = std::abs(a);
+        mn[i * S + j] = mn[j * S + i] = std::abs(b);
+      }
     }
   qdg::host::sym_eig(S, mx, w, z);
   p->emax = w[S - 1];
@@ -355,9 +376,47 @@ qdg_status prof_end(qdg_plan *p, size_t slot) {
 // (FFT, k^2, inverse FFT, potential matrix and epilogue).  Higher
 // dimensions: one launch computing T_d phi for all d, then one point-wise
 // launch that sums them, adds the potential matrix and runs the epilogue.
+// OGridNAC elements, after the kinetic pass: one launch per element and
+// dimension, each adding into T_0 phi of its row state.
+template <typename T>
+qdg_status run_nac(qdg_plan *p, const cplx<T> *phi, const Epi &e) {
+  for (const auto &ne : p->nac) {
+    for (int d = 0; d < p->nd; ++d) {
+      const DimInfo &di = p->dim[d];
+      qdg::NacArgs<T> a;
+      memset(&a, 0, sizeof(a));
+      const int TW = p->nac_tw[d];
+      a.N = di.n;
+      a.TW = TW;
+      if (d == 0) {
+        a.es = 1; a.ls = di.n; a.tiles_per_hi = 1; a.hi_stride = (long long)TW * di.n;
+      } else {
+        a.es = (int)di.stride; a.ls = 1; a.tiles_per_hi = (int)(di.stride / TW); a.hi_stride = di.stride * di.n;
+      }
+      a.ntiles = p->npts / ((long long)di.n * TW);
+      a.npts = p->npts;
+      a.rp = di.rp;
+      a.tw = reinterpret_cast<const cplx<T> *>(di.tw);
+      a.kfac = p->dk[d] * ne.c / (double)di.n;
+      a.phi = phi;
+      a.col = ne.col;
+      a.f = reinterpret_cast<const T *>(p->d_grids) + (long long)(ne.grid + d) * p->npts;
+      a.out = reinterpret_cast<cplx<T> *>(p->d_Pd[0]) + (long long)ne.row * p->npts;
+      a.done = e.done;
+      a.cs = e.cut.cs;
+      a.dyn = e.cut.dyn;
+      a.bufs[0] = reinterpret_cast<const cplx<T> *>(e.bufs[0]);
+      a.bufs[1] = reinterpret_cast<const cplx<T> *>(e.bufs[1]);
+      const int grid = (int)std::max<long long>(1, std::min<long long>(a.ntiles, (long long)p->nac_per_sm * p->sm_count));
+      CK(qdg::launch_nac<T>(a, grid, 256, p->nac_smem, p->stream));
+    }
+  }
+  return QDG_OK;
+}
+
 template <typename T>
 qdg_status run_h(qdg_plan *p, int final_mode, const cplx<T> *phi, const Epi &e) {
-  if (p->nd == 1) {
+  if (p->nd == 1 && p->nac.empty()) {
     qdg::PassArgs<T> a;
     memset(&a, 0, sizeof(a));
     fill_geometry<T>(p, 0, p->S, a);
@@ -407,6 +466,7 @@ qdg_status run_h(qdg_plan *p, int final_mode, const cplx<T> *phi, const Epi &e) 
   if (s != QDG_OK) return s;
   CK(qdg::launch_kin_all<T>(k, (int)std::min<long long>(items, p->kin_grid), 256, p->kin_smem, p->stream));
   if ((s = prof_end(p, slot)) != QDG_OK) return s;
+  if (!p->nac.empty() && (s = run_nac<T>(p, phi, e)) != QDG_OK) return s;
 
   qdg::CombArgs<T> c;
   memset(&c, 0, sizeof(c));
@@ -468,7 +528,7 @@ qdg_status upload_tables(qdg_plan *p) {
   CK(cudaMalloc(&p->d_grids, sizeof(T) * std::max<size_t>(1, g.size())));
   if (!g.empty()) CK(cudaMemcpy(p->d_grids, g.data(), sizeof(T) * g.size(), cudaMemcpyHostToDevice));
   CK(cudaMalloc(&p->d_P, sizeof(cplx<T>) * wf_elems(p)));
-  if (p->nd > 1) {
+  if (p->nd > 1 || !p->nac.empty()) {
     size_t smem = 0;
     long long items = 0;
     for (int d = 0; d < p->nd; ++d) {
@@ -481,6 +541,19 @@ qdg_status upload_tables(qdg_plan *p) {
     p->kin_smem = smem;
     const int per_sm = qdg::kin_all_max_blocks<T>(256, smem);
     p->kin_grid = (int)std::min<long long>(items, (long long)per_sm * p->sm_count);
+  }
+  if (!p->nac.empty()) {
+    // NAC tiles hold 2 TW lines twice (phi and f phi, ping-pong buffers)
+    size_t smem = 0;
+    for (int d = 0; d < p->nd; ++d) {
+      int tw = p->dim[d].TW_k;
+      while (tw > 1 && (size_t)p->dim[d].n * (1 + 4 * (size_t)tw) * sizeof(cplx<T>) > 200 * 1024) tw /= 2;
+      p->nac_tw[d] = tw;
+      smem = std::max(smem, (size_t)p->dim[d].n * (1 + 4 * (size_t)tw) * sizeof(cplx<T>));
+    }
+    if (smem > 227 * 1024) return fail(QDG_EUNSUPPORTED, "grid line too long for the shared-memory FFT");
+    p->nac_smem = smem;
+    p->nac_per_sm = qdg::nac_max_blocks<T>(256, smem);
   }
   {
     long long g = (p->npts + 255) / 256;
@@ -531,8 +604,8 @@ qdg_status build_couplings(const qdg_plan *p, F pick, qdg::Couplings &cp) {
   struct E { int row, col, gid, lid; };
   std::vector<E> es;
   for (auto &t : p->terms) {
-    if (t.kind == QDG_TERM_KINETIC || !pick(t)) continue;
-    const int nrep = t.row != t.col ? 2 : 1;
+    if (t.kind == QDG_TERM_KINETIC || t.kind == QDG_TERM_NAC || !pick(t)) continue;
+    const int nrep = (p->hermitian && t.row != t.col) ? 2 : 1;
     for (int r = 0; r < nrep; ++r)
       es.push_back({r ? t.col : t.row, r ? t.row : t.col, t.grid, t.kind == QDG_TERM_DIPOLE ? t.laser : -1});
   }
@@ -618,6 +691,7 @@ qdg_status step_setup(qdg_prop *P) {
   qdg_plan *p = P->plan;
   const char *env = getenv("QDG_CHEBY_MODE");
   if (env && strcmp(env, "graph") == 0) return QDG_OK;
+  if (!p->nac.empty()) return QDG_OK;  // NAC elements run as extra line passes (graph path)
   const size_t cs = p->csize;
   if (p->nd == 1) {
     P->step_tw1 = p->dim[0].TW_e;
@@ -974,6 +1048,9 @@ qdg_status gspo_init(qdg_prop *P) {
   for (auto &t : p->terms) ng = std::max(ng, t.group + 1);
   if (ng < 1) return fail(QDG_EINVAL, "GSPO is empty!");
   if (ng > QDG_MAX_GROUPS) return fail(QDG_EINVAL, "too many GSPO members");
+  for (auto &t : p->terms)  // OGSPO::Init takes ODSpace members only (OGSPO.cpp:71-85); OGridNAC is none
+    if (t.kind == QDG_TERM_NAC) return fail(QDG_EUNSUPPORTED, "GridNAC has no diagonal representation for GSPO");
+  if (!p->hermitian) return fail(QDG_EUNSUPPORTED, "GSPO members must be hermitian matrices");
   P->ngroups = ng;
   P->group_kinetic.assign(ng, 0);
   P->gcp_h.resize(ng);
@@ -1306,6 +1383,9 @@ qdg_status qdg_plan_create(const qdg_hplan_desc *desc, int32_t precision, qdg_pl
       if (t.row != t.col) { free_plan(p); return fail(QDG_EUNSUPPORTED, "kinetic operator off the diagonal"); }
       for (int d = 0; d < p->nd; ++d)
         if (!(t.mass[d] > 0)) { free_plan(p); return fail(QDG_EINVAL, "Zero mass defined"); }
+    } else if (t.kind == QDG_TERM_NAC) {
+      if (t.grid < 0 || t.grid + p->nd > p->ngrids || !desc->grid_data) { free_plan(p); return fail(QDG_EINVAL, "NACME grid index out of range"); }
+      if (!(t.mass[0] > 0)) { free_plan(p); return fail(QDG_EINVAL, "Zero mass defined"); }
     } else if (t.kind == QDG_TERM_POTENTIAL || t.kind == QDG_TERM_DIPOLE) {
       if (t.grid < 0 || t.grid >= p->ngrids || !desc->grid_data) { free_plan(p); return fail(QDG_EINVAL, "potential grid index out of range"); }
       if (t.kind == QDG_TERM_DIPOLE && (t.laser < 0 || t.laser >= p->nlasers || p->laser_nt < 1 || !desc->laser_data)) {
@@ -1316,6 +1396,18 @@ qdg_status qdg_plan_create(const qdg_hplan_desc *desc, int32_t precision, qdg_pl
   if (p->ngrids > 0) p->grids_h.assign(desc->grid_data, desc->grid_data + (long long)p->ngrids * p->npts);
   if (p->nlasers > 0) p->lasers_h.assign(desc->laser_data, desc->laser_data + (long long)p->nlasers * p->laser_nt);
   for (double v : p->grids_h) if (!std::isfinite(v)) { free_plan(p); return fail(QDG_EINVAL, "non-finite value in a potential grid"); }
+  // OMultistate: the "nonhermitian" parameter, or elements at both (i, j) and
+  // (j, i), switch the hermitian copy off (OMultistate.cpp:52-53,83-85)
+  p->hermitian = !desc->nonhermitian;
+  for (auto &a : p->terms)
+    for (auto &b : p->terms)
+      if (a.row != a.col && a.row == b.col && a.col == b.row) p->hermitian = false;
+  for (auto &t : p->terms) {
+    if (t.kind != QDG_TERM_NAC) continue;
+    const double c = 0.5 * (t.sign == 0 ? 1.0 : t.sign) / t.mass[0];  // PreFactor(0.5 sign / mass)
+    p->nac.push_back({t.row, t.col, t.grid, c});
+    if (p->hermitian && t.row != t.col) p->nac.push_back({t.col, t.row, t.grid, c});
+  }
   compute_erange(p);
   cudaDeviceProp prop;
   if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) { free_plan(p); return fail(QDG_ECUDA, "cudaGetDeviceProperties failed"); }

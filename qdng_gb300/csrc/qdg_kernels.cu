@@ -269,6 +269,84 @@ __global__ void __launch_bounds__(256) kin_all_kernel(KinArgs<T> a) {
   }
 }
 
+// ---------------------------------------------------------------- NAC pass
+// A tile of TW lines along d: phi lines and f phi lines are transformed
+// together (2 TW lines), multiplied by i k c / N, transformed back, and the
+// row state's T_0 phi gets f * (first half) + (second half).  Every point
+// belongs to one line of one tile, so the read-modify-write is race free;
+// the elements and dimensions of one H application are separate launches.
+template <typename T>
+__global__ void __launch_bounds__(256) nac_kernel(NacArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  if (a.done != nullptr && *a.done) return;
+  const cplx<T> *phi = (a.dyn ? a.bufs[(a.cs->i + 1) & 1] : a.phi) + (long long)a.col * a.npts;
+  const int N = a.N, TW = a.TW;
+  cplx<T> *tws = reinterpret_cast<cplx<T> *>(smem_raw);
+  cplx<T> *b0 = tws + N;
+  cplx<T> *b1 = b0 + (size_t)2 * TW * N;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) tws[i] = a.tw[i];
+  const int tileN = TW * N;
+  for (long long tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
+    const long long hi = tile / a.tiles_per_hi;
+    const long long base = hi * a.hi_stride + (tile - hi * a.tiles_per_hi) * TW;
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < tileN; idx += blockDim.x) {
+      int w, i;
+      tile_coord(idx, TW, N, a.es, w, i);
+      const long long g = base + (long long)w * a.ls + (long long)i * a.es;
+      const cplx<T> x = ld(phi + g);
+      b0[w * N + i] = x;
+      b0[(TW + w) * N + i] = cmulr(x, a.f[g]);
+    }
+    __syncthreads();
+    const int cur = fft_lines<T>(b0, b1, a.rp, 2 * TW, tws, -1);
+    cplx<T> *bc = cur ? b1 : b0;
+    for (int idx = threadIdx.x; idx < 2 * tileN; idx += blockDim.x) {
+      const int i = idx % N;
+      const int q = i < (N + 1) / 2 ? i : i - N;  // Kspace::Init1Dddx order, Nyquist negative
+      const T m = (T)(a.kfac * (double)q);
+      const cplx<T> v = bc[idx];
+      bc[idx] = mk(-v.im * m, v.re * m);
+    }
+    __syncthreads();
+    const int cur2 = fft_lines<T>(bc, cur ? b0 : b1, a.rp, 2 * TW, tws, +1);
+    const cplx<T> *res = cur2 ? (cur ? b0 : b1) : bc;
+    for (int idx = threadIdx.x; idx < tileN; idx += blockDim.x) {
+      int w, i;
+      tile_coord(idx, TW, N, a.es, w, i);
+      const long long g = base + (long long)w * a.ls + (long long)i * a.es;
+      const cplx<T> add = cmulr(res[w * N + i], a.f[g]) + res[(TW + w) * N + i];
+      st(a.out + g, ld(a.out + g) + add);
+    }
+  }
+}
+
+template <typename T>
+cudaError_t launch_nac(const NacArgs<T> &a, int grid, int block, size_t smem, cudaStream_t st) {
+  void *k = (void *)nac_kernel<T>;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  void *args[] = {(void *)&a};
+  COUNT_LAUNCH();
+  return cudaLaunchKernel(k, dim3(grid), dim3(block), args, smem, st);
+}
+
+template <typename T>
+int nac_max_blocks(int block, size_t smem) {
+  void *k = (void *)nac_kernel<T>;
+  if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, block, smem) != cudaSuccess) return 1;
+  return nb > 0 ? nb : 1;
+}
+
+template cudaError_t launch_nac<double>(const NacArgs<double> &, int, int, size_t, cudaStream_t);
+template cudaError_t launch_nac<float>(const NacArgs<float> &, int, int, size_t, cudaStream_t);
+template int nac_max_blocks<double>(int, size_t);
+template int nac_max_blocks<float>(int, size_t);
+
 // ------------------------------------------------------------ combine pass
 template <typename T, int MODE, int SS>
 __global__ void __launch_bounds__(256) combine_kernel(CombArgs<T> a) {

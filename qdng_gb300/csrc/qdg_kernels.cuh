@@ -144,6 +144,26 @@ struct KinArgs {
   int dyn;
 };
 
+// One OGridNAC element along one dimension d (src/qdlib/OGridNAC.cpp:131-148):
+// out += c [f_d d/dx_d phi + d/dx_d (f_d phi)], c = sign/(2 mass), added to
+// the kinetic result T_0 phi of the row state, which the combine pass reads.
+template <typename T>
+struct NacArgs {
+  int N, TW, es, ls, tiles_per_hi;
+  long long hi_stride, ntiles, npts;
+  RadixPlan rp;
+  const cplx<T> *tw;
+  double kfac;            // dk * c / N: the multiplier of line index q is i q kfac
+  const cplx<T> *phi;     // all states; the column state is read
+  int col;
+  const T *f;             // f_d, grid-shaped
+  cplx<T> *out;           // T_0 phi of the row state (read-modify-write)
+  const int *done;
+  const ChebyState *cs;
+  const cplx<T> *bufs[2];
+  int dyn;
+};
+
 // Point-wise finish of H phi: sum_d T_d phi + potential matrix, then the
 // epilogue (H apply output or the Chebyshev recurrence).
 template <typename T>
@@ -212,6 +232,10 @@ template <typename T>
 cudaError_t launch_kin_all(const KinArgs<T> &a, int grid, int block, size_t smem, cudaStream_t st);
 template <typename T>
 int kin_all_max_blocks(int block, size_t smem);
+template <typename T>
+cudaError_t launch_nac(const NacArgs<T> &a, int grid, int block, size_t smem, cudaStream_t st);
+template <typename T>
+int nac_max_blocks(int block, size_t smem);
 template <typename T>
 cudaError_t launch_combine(int mode, const CombArgs<T> &a, int grid, int block, cudaStream_t st);
 

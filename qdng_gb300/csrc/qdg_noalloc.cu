@@ -144,6 +144,14 @@ qdg_status qdg_h_apply_noalloc(const qdg_hplan_desc *desc, const double *psi_in,
   // potential-matrix list sorted by row (hermitian mirrors explicit)
   int er[qdg::kMaxCouplings], ec[qdg::kMaxCouplings], eg[qdg::kMaxCouplings], el[qdg::kMaxCouplings];
   int nent = 0;
+  // OMultistate's hermitian copy, off for "nonhermitian" or when elements sit
+  // at both (i, j) and (j, i) (OMultistate.cpp:52-53,83-85)
+  bool hermitian = !desc->nonhermitian;
+  for (int i = 0; i < desc->nterms; ++i)
+    for (int j = 0; j < desc->nterms; ++j) {
+      const qdg_hterm &a = desc->terms[i], &b = desc->terms[j];
+      if (a.row != a.col && a.row == b.col && a.col == b.row) hermitian = false;
+    }
   for (int i = 0; i < desc->nterms; ++i) {
     const qdg_hterm &h = desc->terms[i];
     if (h.row < 0 || h.col < 0 || h.row >= S || h.col >= S) return na_fail(QDG_EINVAL, "matrix element outside the states");
@@ -159,7 +167,7 @@ qdg_status qdg_h_apply_noalloc(const qdg_hplan_desc *desc, const double *psi_in,
     if (h.grid < 0 || h.grid >= desc->ngrids || !desc->grid_data) return na_fail(QDG_EINVAL, "potential grid index out of range");
     if (h.kind == QDG_TERM_DIPOLE && (h.laser < 0 || h.laser >= desc->nlasers || !desc->laser_data))
       return na_fail(QDG_EINVAL, "dipole operator without a laser field");
-    for (int r = 0; r < (h.row != h.col ? 2 : 1); ++r) {
+    for (int r = 0; r < (hermitian && h.row != h.col ? 2 : 1); ++r) {
       if (nent >= qdg::kMaxCouplings) return na_fail(QDG_EUNSUPPORTED, "too many potential/dipole matrix entries");
       er[nent] = r ? h.col : h.row;
       ec[nent] = r ? h.row : h.col;

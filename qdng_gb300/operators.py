@@ -6,8 +6,10 @@ attributes, and flatten the tree into the qdg_hplan_desc the C ABI takes:
 * ``GridNablaSq(mass=[...])``   -- src/qdlib/OGridNablaSq.cpp:28-58
 * ``GridPotential(values)``     -- src/qdlib/OGridPotential.cpp:26-109 (setzero/offset/scale)
 * ``GridDipole(mu, laser)``     -- src/qdlib/OGridDipole.cpp:18-60, Laser.cpp:125-128
+* ``GridNAC([f_0, ...], mass, sign)`` -- src/qdlib/OGridNAC.cpp:26-148 (first-derivative coupling)
 * ``Sum([...])``                -- src/qdlib/OSum.cpp:28-72
-* ``Multistate({(i, j): op})``  -- src/qdlib/OMultistate.cpp:100-241 (hermitian: (i,j) also acts at (j,i))
+* ``Multistate({(i, j): op})``  -- src/qdlib/OMultistate.cpp:100-241 (hermitian: (i,j) also acts at (j,i),
+  unless ``nonhermitian`` or both (i,j) and (j,i) are given, OMultistate.cpp:52-53,83-85)
 * ``DMultistate({(i, j): op})`` -- src/qdlib/ODMultistate.cpp:35-182 (GSPO members)
 
 Errors follow the reference's exceptions: ``EParamProblem`` for bad
@@ -159,6 +161,37 @@ class GridDipole(Operator):
         return [t]
 
 
+class GridNAC(Operator):
+    """Non-adiabatic first-derivative coupling (OGridNAC::Apply,
+    src/qdlib/OGridNAC.cpp:131-148):
+    sign/(2 mass) * sum_d [f_d d/dx_d psi + d/dx_d (f_d psi)].
+    ``nacme`` holds one coupling grid per dimension.  ``mass`` is used for
+    one-dimensional grids only; with more dimensions the reference keeps
+    mass = 1 and expects it folded into the coupling data (OGridNAC.cpp:83-85)."""
+
+    def __init__(self, nacme, mass=None, sign=1.0):
+        if isinstance(nacme, np.ndarray) and nacme.ndim == 1:
+            nacme = [nacme]
+        self.nacme = [np.array(f, dtype=np.float64).reshape(-1) for f in nacme]
+        if len(self.nacme) < 1:
+            raise EParamProblem("NAC got nonsense dims")
+        self.mass = 1.0 if mass is None else float(mass)
+        self.sign = float(sign)
+
+    def terms(self, row, col, group, ctx):
+        if len(self.nacme) != ctx.grid.ndims:
+            raise EIncompatible("NAC: Psi has different num of dims")
+        for f in self.nacme:
+            if f.size != ctx.grid.npts:
+                raise EIncompatible("GridNAC parameters are not compatible with wave function")
+        t = abi.HTerm()
+        t.kind, t.row, t.col, t.laser, t.group = abi.TERM_NAC, row, col, -1, group
+        t.grid = ctx.add_grids(self.nacme)
+        t.mass[0] = self.mass if ctx.grid.ndims == 1 else 1.0
+        t.sign = self.sign
+        return [t]
+
+
 class Sum(Operator):
     def __init__(self, ops):
         if len(ops) == 0:
@@ -173,24 +206,25 @@ class Sum(Operator):
 
 
 class Multistate(Operator):
-    """Operator matrix; an element given at (i, j), i != j, also acts at (j, i)."""
+    """Operator matrix.  An element given at (i, j), i != j, also acts at
+    (j, i), unless the matrix is non-hermitian: the ``nonhermitian``
+    parameter, or elements given at both (i, j) and (j, i)."""
 
-    def __init__(self, elements, nstates=None):
+    def __init__(self, elements, nstates=None, nonhermitian=False):
         self.elements = dict(elements)
         n = 1 + max(max(i, j) for (i, j) in self.elements)
         self.nstates = nstates or n
         if self.nstates < 1:
             raise EParamProblem("Multistate operator is empty")
+        both = any(i != j and (j, i) in self.elements for (i, j) in self.elements)
+        self.nonhermitian = bool(nonhermitian) or both
 
     def terms(self, row, col, group, ctx):
         out = []
-        seen = set()
         for (i, j), o in sorted(self.elements.items()):
-            key = (min(i, j), max(i, j))
-            if key in seen and i != j:
-                raise EParamProblem("off-diagonal element given twice")
-            seen.add(key)
             out += o.terms(i, j, group, ctx)
+        if self.nonhermitian:
+            ctx.nonhermitian = True
         return out
 
 
@@ -203,6 +237,7 @@ class _Ctx:
         self.grid = grid
         self.grids = []
         self.lasers = []
+        self.nonhermitian = False
 
     def add_grid(self, v):
         for i, g in enumerate(self.grids):
@@ -210,6 +245,12 @@ class _Ctx:
                 return i
         self.grids.append(v)
         return len(self.grids) - 1
+
+    def add_grids(self, vs):
+        """Consecutive grid slots (a coupling grid per dimension); returns the first."""
+        first = len(self.grids)
+        self.grids.extend(vs)
+        return first
 
     def add_laser(self, v):
         for i, g in enumerate(self.lasers):
@@ -243,6 +284,7 @@ class HPlan:
                 raise EParamProblem("Multistate operator can only use WFs with same number of states")
         self.nstates = nstates
         self.terms = terms
+        self.nonhermitian = ctx.nonhermitian
         npts = grid.npts
         self.grid_data = (np.concatenate(ctx.grids) if ctx.grids else np.zeros(1)).astype(np.float64)
         if ctx.lasers:
@@ -270,6 +312,7 @@ class HPlan:
         d.laser_nt = self.laser_nt
         self._ld = np.ascontiguousarray(self.laser_data)
         d.laser_data = self._ld.ctypes.data_as(C.POINTER(C.c_double))
+        d.nonhermitian = 1 if self.nonhermitian else 0
         self.desc = d
         self.npts = npts
 

@@ -150,6 +150,44 @@ def cfg5_double_well(n=128):
     return hp, _normalize(hp, psi), dict(name="Cheby", params="", dt=20.0, steps=2000)
 
 
+def nac_two_state(n=128, nd=1, paired=True):
+    """Two adiabatic harmonic states coupled by a first-derivative NAC
+    (OGridNAC, the Handbook's Multistate example: m0.1 with sign +1 and m1.0
+    with sign -1, which makes the matrix non-hermitian in QDng's sense and H
+    itself hermitian).  paired=False gives m0.1 alone (hermitian copy).
+    Returns (HPlan, psi0, run settings, coupling grids, NAC mass)."""
+    m = 2000.0
+    k = 0.01
+    if nd == 1:
+        g = op.GridSystem([n], [-6.0], [6.0])
+        X = g.axes()[0]
+        V0 = 0.5 * k * X ** 2
+        V1 = 0.5 * k * (X - 1.0) ** 2 + 0.02
+        f = [0.5 * np.exp(-X ** 2)]
+        T = op.GridNablaSq([m])
+        nac_mass = m
+        psi = np.exp(-(X + 0.5) ** 2 / (2 * (m * np.sqrt(k)) ** -1.0))
+    else:
+        g = op.GridSystem([n, n], [-5.0, -5.0], [5.0, 5.0])
+        X, Y = g.mesh()
+        V0 = 0.5 * k * (X ** 2 + Y ** 2)
+        V1 = 0.5 * k * ((X - 1.0) ** 2 + Y ** 2) + 0.02
+        # N-D: the reduced mass is folded into the coupling data (mass = 1)
+        f = [0.5 * np.exp(-X ** 2 - Y ** 2) / m, 0.2 * np.exp(-(X - 0.5) ** 2 - Y ** 2) / m]
+        T = op.GridNablaSq([m, m])
+        nac_mass = None
+        sig = (m * np.sqrt(k)) ** -0.5
+        psi = np.exp(-((X + 0.5) ** 2 + Y ** 2) / (2 * sig ** 2))
+    el = {(0, 0): op.Sum([T, op.GridPotential(V0)]), (1, 1): op.Sum([T, op.GridPotential(V1)]),
+          (0, 1): op.GridNAC(f, mass=nac_mass, sign=1.0)}
+    if paired:
+        el[(1, 0)] = op.GridNAC(f, mass=nac_mass, sign=-1.0)
+    hp = op.HPlan(g, op.Multistate(el))
+    psi = np.concatenate([psi.reshape(-1), np.zeros(g.npts)]).astype(np.complex128)
+    f = [fd.reshape(-1) for fd in f]
+    return hp, _normalize(hp, psi), dict(name="Cheby", params="", dt=10.0, steps=200), f, nac_mass
+
+
 # ----------------------------------------------------------------- ensemble
 ENS_1D_SIZES = [256, 384, 512, 768, 1024, 1536, 2048, 3072, 4096]
 ENS_2D_SIDES = [64, 96, 128, 192, 256]

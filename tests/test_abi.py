@@ -31,7 +31,7 @@ def test_exports_every_header_symbol(lib):
 
 
 def test_abi_version(lib):
-    assert lib.qdg_abi_version() == 1
+    assert lib.qdg_abi_version() == 2
 
 
 def test_struct_layouts_match_c(tmp_path):
@@ -40,6 +40,7 @@ def test_struct_layouts_match_c(tmp_path):
                    'int main(void){printf("%zu %zu %zu %zu %zu %zu %zu\\n", sizeof(qdg_grid), sizeof(qdg_hterm),'
                    ' sizeof(qdg_hplan_desc), sizeof(qdg_observables), sizeof(qdg_prop_info),'
                    ' offsetof(qdg_hterm, mass), offsetof(qdg_hplan_desc, laser_data));'
+                   ' printf("%zu %zu\\n", offsetof(qdg_hterm, sign), offsetof(qdg_hplan_desc, nonhermitian));'
                    ' printf("%zu %zu\\n", sizeof(qdg_ensemble_member), offsetof(qdg_ensemble_member, laser_nt));'
                    ' return 0;}\n')
     exe = tmp_path / "sizes"
@@ -47,6 +48,7 @@ def test_struct_layouts_match_c(tmp_path):
     got = [int(v) for v in subprocess.check_output([str(exe)]).split()]
     want = [C.sizeof(abi.Grid), C.sizeof(abi.HTerm), C.sizeof(abi.HPlanDesc), C.sizeof(abi.Observables),
             C.sizeof(abi.PropInfo), abi.HTerm.mass.offset, abi.HPlanDesc.laser_data.offset,
+            abi.HTerm.sign.offset, abi.HPlanDesc.nonhermitian.offset,
             C.sizeof(abi.EnsembleMember), abi.EnsembleMember.laser_nt.offset]
     assert got == want
 
@@ -103,3 +105,23 @@ def test_reference_parameter_errors():
 def test_potential_setzero_offset_scale():
     v = op.GridPotential(np.array([3.0, 1.0, 2.0]), setzero=True, offset=0.5, scale=2.0).values
     assert np.allclose(v, (np.array([3.0, 1.0, 2.0]) - 1.0 + 0.5) * 2.0)   # OGridPotential.cpp:56-76
+
+
+def test_nac_flattening_and_nonhermitian_flag():
+    """GridNAC takes one grid slot per dimension; elements at both (0,1) and
+    (1,0) make the Multistate non-hermitian (OMultistate.cpp:52-53)."""
+    g = op.GridSystem([8, 4], [0.0, 0.0], [1.0, 1.0])
+    f0, f1 = np.ones(32), 2 * np.ones(32)
+    V = op.GridPotential(np.zeros(32))
+    hp = op.HPlan(g, op.Multistate({(0, 0): V, (1, 1): V, (0, 1): op.GridNAC([f0, f1], mass=5.0, sign=-1)}))
+    t = [x for x in hp.terms if x.kind == abi.TERM_NAC][0]
+    assert (t.row, t.col, t.sign, t.mass[0]) == (0, 1, -1.0, 1.0)  # N-D: mass folded into f
+    np.testing.assert_array_equal(hp.grid_data[t.grid * 32:(t.grid + 2) * 32], np.concatenate([f0, f1]))
+    assert hp.desc.nonhermitian == 0
+    hp2 = op.HPlan(g, op.Multistate({(0, 0): V, (1, 1): V, (0, 1): op.GridNAC([f0, f1]),
+                                     (1, 0): op.GridNAC([f0, f1], sign=-1)}))
+    assert hp2.desc.nonhermitian == 1
+    g1 = op.GridSystem([8], [0.0], [1.0])
+    hp3 = op.HPlan(g1, op.Multistate({(0, 1): op.GridNAC([np.ones(8)], mass=5.0)}, nonhermitian=True))
+    t3 = hp3.terms[0]
+    assert t3.mass[0] == 5.0 and hp3.desc.nonhermitian == 1
