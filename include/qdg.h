@@ -258,8 +258,9 @@ qdg_status qdg_prop_phase_times(qdg_prop *prop, double ns[4]);
 #define QDG_NOALLOC_SCRATCH_BYTES (8 << 20)
 
 /* out = H(step) in, like qdg_h_apply, for callers that cannot allocate
- * device memory (code running during CUDA graph capture, frameworks whose
- * pool owns all device memory).  It calls no cudaMalloc/cudaFree: desc is a
+ * device memory (frameworks whose caching pool owns all device memory,
+ * plug-ins that must leave the process's allocation state alone, loops
+ * where the implicit device synchronisation of cudaMalloc is too costly).  It calls no cudaMalloc/cudaFree: desc is a
  * host struct whose grid_data and laser_data point to DEVICE arrays, psi_in
  * and psi_out are device arrays of nstates*npoints complex128, and all
  * scratch lives in one static device array of QDG_NOALLOC_SCRATCH_BYTES.

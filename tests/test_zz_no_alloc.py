@@ -1,7 +1,8 @@
 """qdg_h_apply_noalloc: H psi for callers that cannot allocate device memory.
 
-Callers running inside CUDA graph capture, or frameworks whose memory pool
-owns all device memory, cannot let a library call cudaMalloc.  This entry
+Frameworks whose memory pool owns all device memory, or plug-ins that must
+not change the process's allocation state, cannot let a library call
+cudaMalloc.  This entry
 point takes device arrays the caller owns and keeps its own scratch in a
 static device array of the library, so it must give the same H psi as the
 plan-based qdg_h_apply.  Collected last so that a failure here comes after
