@@ -289,8 +289,10 @@ int choose_tw(const qdg_plan *p, int d, int nsub) {
   return best;
 }
 
+// Twiddles plus two line-batch buffers of TW * nsub lines (padded layout).
 size_t pass_smem(const qdg_plan *p, int d, int TW, int nsub) {
-  return (size_t)p->dim[d].n * (1 + 2 * (size_t)TW * nsub) * p->csize;
+  const int n = p->dim[d].n;
+  return ((size_t)n + 2 * qdg::line_buf_elems(n, TW * nsub)) * p->csize;
 }
 
 template <typename T>
@@ -547,9 +549,11 @@ qdg_status upload_tables(qdg_plan *p) {
     size_t smem = 0;
     for (int d = 0; d < p->nd; ++d) {
       int tw = p->dim[d].TW_k;
-      while (tw > 1 && (size_t)p->dim[d].n * (1 + 4 * (size_t)tw) * sizeof(cplx<T>) > 200 * 1024) tw /= 2;
+      const int n = p->dim[d].n;
+      auto bytes = [&](int t) { return ((size_t)n + 2 * qdg::line_buf_elems(n, 2 * t)) * sizeof(cplx<T>); };
+      while (tw > 1 && bytes(tw) > 200 * 1024) tw /= 2;
       p->nac_tw[d] = tw;
-      smem = std::max(smem, (size_t)p->dim[d].n * (1 + 4 * (size_t)tw) * sizeof(cplx<T>));
+      smem = std::max(smem, bytes(tw));
     }
     if (smem > 227 * 1024) return fail(QDG_EUNSUPPORTED, "grid line too long for the shared-memory FFT");
     p->nac_smem = smem;
@@ -725,10 +729,10 @@ qdg_status step_setup(qdg_prop *P) {
     smem = 0;
     for (int d = 0; d < p->nd; ++d) {
       const long long n = p->dim[d].n;
-      long long cap = (long long)((budget / cs - n) / (2 * n));
+      long long cap = (long long)((budget / cs - n) / (2 * (size_t)qdg::lstride((int)n)));
       int lm = (int)std::max<long long>(1, std::min<long long>(std::min<long long>(chunk, cap), qdg::kMaxBatchLines));
       P->lmax[d] = lm;
-      smem = std::max(smem, (size_t)(n * (1 + 2 * (size_t)lm)) * cs);
+      smem = std::max(smem, ((size_t)n + 2 * qdg::line_buf_elems((int)n, lm)) * cs);
     }
     if (smem > 227 * 1024) return QDG_OK;
     if (qdg::cheby_step_max_blocks<T>(p->S, p->nd, 256, smem) >= per_sm) break;

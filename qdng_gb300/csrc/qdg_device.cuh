@@ -169,8 +169,21 @@ __device__ __forceinline__ void stage_butterfly(cplx<T> (&v)[R], int k, int step
   }
 }
 
-// One Stockham stage over `nlines` lines of length N stored line after line
-// in `in` (line stride N); result in `out`.  Items are spread over all
+// Shared-memory layout of a batch of lines: line l starts at l * lstride(N)
+// and element i of a line sits at lpos(i) = i + i/16.  The gap after every 16
+// elements spreads the stride-R stores of a Stockham stage with Ns = 1 (and
+// of radix-16 chains in general) over distinct banks; the odd line stride
+// does the same for accesses that walk across lines (the gather and scatter
+// of lines along dimensions other than 0, where consecutive threads take
+// consecutive lines so that the global accesses coalesce).
+__host__ __device__ __forceinline__ int lstride(int N) { return (N + (N >> 4)) | 1; }
+__device__ __forceinline__ int lpos(int i) { return i + (i >> 4); }
+__host__ __device__ __forceinline__ int lidx(int l, int i, int LS) { return l * LS + i + (i >> 4); }
+// Complex elements of a line-batch buffer of nlines lines of length N.
+__host__ __device__ __forceinline__ size_t line_buf_elems(int N, int nlines) { return (size_t)nlines * lstride(N); }
+
+// One Stockham stage over `nlines` lines of length N stored in the layout
+// above in `in`; result in `out`.  Items are spread over all
 // threads of the block.  tw[m] = exp(-2 pi i m / N); sign = -1 forward
 // (FFTW_FORWARD), +1 backward.  The Stockham autosort indexing follows the
 // classic formulation (Stockham 1966; Govindaraju et al., SC'08): item j
@@ -186,6 +199,7 @@ __device__ __forceinline__ void stockham_stage(const cplx<T> *__restrict__ in, c
   // powers of two (the usual case): shifts and masks instead of divisions
   const bool pow2 = ((M & (M - 1)) == 0) && ((Ns & (Ns - 1)) == 0);
   const int lgM = __ffs(M) - 1, lgNs = __ffs(Ns) - 1;
+  const int LS = lstride(N);
   for (int it = threadIdx.x; it < items; it += blockDim.x) {
     int line, j, k, q;
     if (pow2) {
@@ -199,14 +213,15 @@ __device__ __forceinline__ void stockham_stage(const cplx<T> *__restrict__ in, c
       q = j / Ns;
       k = j - q * Ns;
     }
-    const cplx<T> *src = in + line * N;
+    const cplx<T> *src = in + line * LS;
     cplx<T> v[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = src[j + r * M];
+    for (int r = 0; r < R; ++r) v[r] = src[lpos(j + r * M)];
     stage_butterfly<T, R>(v, k, step, M, tw, sign);
-    cplx<T> *dst = out + line * N + q * Ns * R + k;
+    cplx<T> *dst = out + line * LS;
+    const int o = q * Ns * R + k;
 #pragma unroll
-    for (int r = 0; r < R; ++r) dst[r * Ns] = v[r];
+    for (int r = 0; r < R; ++r) dst[lpos(o + r * Ns)] = v[r];
   }
 }
 
@@ -257,8 +272,9 @@ __device__ __forceinline__ void stage_any(int R, Load load, Store store, int N, 
   else stockham_stage_io<T, 5>(load, store, N, nlines, Ns, tw, sign);
 }
 
-// Full unnormalised FFT of `nlines` lines in shared memory.  Data starts in
-// buf0; returns the buffer index (0/1) that holds the result.  Every
+// Full unnormalised FFT of `nlines` lines in shared memory (layout above,
+// line_buf_elems(N, nlines) elements per buffer).  Data starts in buf0;
+// returns the buffer index (0/1) that holds the result.  Every
 // thread of the block must call it (it synchronises between stages).
 template <typename T>
 __device__ int fft_lines(cplx<T> *buf0, cplx<T> *buf1, const RadixPlan &rp, int nlines,

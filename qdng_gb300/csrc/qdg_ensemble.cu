@@ -76,9 +76,10 @@ __device__ void ens_kinetic(const EnsArgs<T> &a, const EnsMember &m, const cplx<
     const cplx<T> *tw = a.tw + m.tw_off[d];
     const T *kt = a.ktab + m.kt_off[d];
     cplx<T> *dst = (d == 0 ? a.P0 : a.P1) + m.off;
+    const int LS = lstride(N);
     cplx<T> *tws = smem;
     cplx<T> *b0 = tws + N;
-    cplx<T> *b1 = b0 + (size_t)m.lmax[d] * N;
+    cplx<T> *b1 = b0 + line_buf_elems(N, m.lmax[d]);
     __syncthreads();
     for (int i = threadIdx.x; i < N; i += blockDim.x) tws[i] = tw[i];
     for (long long l0 = 0; l0 < nl; l0 += m.lmax[d]) {
@@ -94,13 +95,16 @@ __device__ void ens_kinetic(const EnsArgs<T> &a, const EnsMember &m, const cplx<
         int w, i;
         if (stride == 1) { w = idx / N; i = idx - w * N; }
         else { i = idx / L; w = idx - i * L; }
-        b0[w * N + i] = ld(phi + m.off + lb[w] + (long long)i * stride);
+        b0[lidx(w, i, LS)] = ld(phi + m.off + lb[w] + (long long)i * stride);
       }
       __syncthreads();
       const int cur = fft_lines<T>(b0, b1, m.rp[d], L, tws, -1);
       cplx<T> *bc = cur ? b1 : b0;
       for (int w = 0; w < L; ++w)
-        for (int i = threadIdx.x; i < N; i += blockDim.x) bc[w * N + i] = cmulr(bc[w * N + i], kt[i]);
+        for (int i = threadIdx.x; i < N; i += blockDim.x) {
+          const int x = lidx(w, i, LS);
+          bc[x] = cmulr(bc[x], kt[i]);
+        }
       __syncthreads();
       const int cur2 = fft_lines<T>(bc, cur ? b0 : b1, m.rp[d], L, tws, +1);
       const cplx<T> *res = cur2 ? (cur ? b0 : b1) : bc;
@@ -108,7 +112,7 @@ __device__ void ens_kinetic(const EnsArgs<T> &a, const EnsMember &m, const cplx<
         int w, i;
         if (stride == 1) { w = idx / N; i = idx - w * N; }
         else { i = idx / L; w = idx - i * L; }
-        st(dst + lb[w] + (long long)i * stride, res[w * N + i]);
+        st(dst + lb[w] + (long long)i * stride, res[lidx(w, i, LS)]);
       }
     }
   }
@@ -152,10 +156,12 @@ __device__ double ens_points(const EnsArgs<T> &a, const EnsMember &m, const cplx
 }
 
 // Shared memory of the resident 1-D path for a line of N points: psi
-// (FP64), phi_{i-1}, phi_{i-2}, the two FFT buffers and V - mu E.
+// (FP64), phi_{i-1}, phi_{i-2}, the two FFT buffers (padded line layout)
+// and V - mu E.
 template <typename T>
 __host__ __device__ inline size_t ens_fast_smem(int N) {
-  return (size_t)N * (sizeof(cplx<double>) + 4 * sizeof(cplx<T>) + sizeof(T));
+  return (size_t)N * (sizeof(cplx<double>) + 2 * sizeof(cplx<T>) + sizeof(T)) +
+         2 * line_buf_elems(N, 1) * sizeof(cplx<T>);
 }
 
 // One step of a 1-D member that lives in shared memory for the whole step.
@@ -171,8 +177,8 @@ __device__ void ens_step_1d(const EnsArgs<T> &a, const EnsMember &m, T field, un
   cplx<T> *cur = reinterpret_cast<cplx<T> *>(ps + N);
   cplx<T> *prev = cur + N;
   cplx<T> *f0 = prev + N;
-  cplx<T> *f1 = f0 + N;
-  T *Vs = reinterpret_cast<T *>(f1 + N);
+  cplx<T> *f1 = f0 + line_buf_elems(N, 1);
+  T *Vs = reinterpret_cast<T *>(f1 + line_buf_elems(N, 1));
   const cplx<T> *__restrict__ tw = a.tw + m.tw_off[0];
   const T *__restrict__ kt = a.ktab + m.kt_off[0];
   cplx<double> *__restrict__ gpsi = a.psi + m.off;
@@ -198,8 +204,9 @@ __device__ void ens_step_1d(const EnsArgs<T> &a, const EnsMember &m, T field, un
     cplx<T> *dst = f0;
     const cplx<T> *src = cur;
     for (int s = 0; s < rp.nstages; ++s) {
-      stage_any<T>(rp.radix[s], [&](int i) { return src[i]; }, [&](int i, const cplx<T> &v) { dst[i] = v; }, N, 1,
-                   Ns, tw, -1);
+      const bool from_cur = s == 0;  // phi_{i-1} is stored unpadded
+      stage_any<T>(rp.radix[s], [&](int i) { return from_cur ? src[i] : src[lpos(i)]; },
+                   [&](int i, const cplx<T> &v) { dst[lpos(i)] = v; }, N, 1, Ns, tw, -1);
       __syncthreads();
       Ns *= rp.radix[s];
       src = dst;
@@ -232,11 +239,11 @@ __device__ void ens_step_1d(const EnsArgs<T> &a, const EnsMember &m, T field, un
     Ns = 1;
     for (int s = 0; s < rp.nstages; ++s) {
       const bool ks = s == 0, ls = s == rp.nstages - 1;
-      auto load = [&](int i) { return ks ? cmulr(src[i], kt[i]) : src[i]; };
+      auto load = [&](int i) { return ks ? cmulr(src[lpos(i)], kt[i]) : src[lpos(i)]; };
       if (ls) {
         stage_any<T>(rp.radix[s], load, point, N, 1, Ns, tw, +1);
       } else {
-        stage_any<T>(rp.radix[s], load, [&](int i, const cplx<T> &v) { dst[i] = v; }, N, 1, Ns, tw, +1);
+        stage_any<T>(rp.radix[s], load, [&](int i, const cplx<T> &v) { dst[lpos(i)] = v; }, N, 1, Ns, tw, +1);
         __syncthreads();
       }
       Ns *= rp.radix[s];
@@ -479,7 +486,7 @@ qdg_status build(qdg_ensemble *e, const qdg_ensemble_member *mem, const std::map
         kt.push_back((T)(kf * q * q));
       }
       m.lmax[d] = (int)std::max(1, std::min(64, 4096 / N));
-      smem = std::max(smem, (size_t)N * (1 + 2 * (size_t)m.lmax[d]) * sizeof(cplx<T>));
+      smem = std::max(smem, ((size_t)N + 2 * qdg::line_buf_elems(N, m.lmax[d])) * sizeof(cplx<T>));
     }
     if (m.nd == 1) {
       const size_t fsm = qdg::ens_fast_smem<T>(m.n[0]);

@@ -81,9 +81,10 @@ __global__ void __launch_bounds__(256) linepass_kernel(PassArgs<T> a) {
   const int TW = a.TW;
   const int nsub = a.nsub;
   const int L = TW * nsub;
+  const int LS = lstride(N);
   cplx<T> *tws = reinterpret_cast<cplx<T> *>(smem_raw);
   cplx<T> *b0 = tws + N;
-  cplx<T> *b1 = b0 + (size_t)L * N;
+  cplx<T> *b1 = b0 + line_buf_elems(N, L);
   for (int i = threadIdx.x; i < N; i += blockDim.x) tws[i] = a.tw[i];
   __syncthreads();
 
@@ -116,7 +117,7 @@ __global__ void __launch_bounds__(256) linepass_kernel(PassArgs<T> a) {
       int w, i;
       tile_coord(idx - sl * tileN, TW, N, a.es, w, i);
       const long long p = base + (long long)w * a.ls + (long long)i * a.es;
-      b0[(sl * TW + w) * N + i] = ld(phi + (long long)(s0 + sl) * npts + p);
+      b0[lidx(sl * TW + w, i, LS)] = ld(phi + (long long)(s0 + sl) * npts + p);
     }
     __syncthreads();
 
@@ -126,12 +127,13 @@ __global__ void __launch_bounds__(256) linepass_kernel(PassArgs<T> a) {
       const int l = idx / N;
       const int i = idx - l * N;
       const int s = s0 + l / TW;
+      const int x = lidx(l, i, LS);
       if (MODE == PM_GSPO_KIN) {
-        bc[idx] = cmul(bc[idx], a.gtab[(long long)s * N + i]);
+        bc[x] = cmul(bc[x], a.gtab[(long long)s * N + i]);
       } else {
         const int kq = min(i, N - i);
         const T f = (T)(a.kfac[s] * (double)kq * (double)kq);
-        bc[idx] = cmulr(bc[idx], f);
+        bc[x] = cmulr(bc[x], f);
       }
     }
     __syncthreads();
@@ -146,7 +148,7 @@ __global__ void __launch_bounds__(256) linepass_kernel(PassArgs<T> a) {
         tile_coord(idx - sl * tileN, TW, N, a.es, w, i);
         const long long p = base + (long long)w * a.ls + (long long)i * a.es;
         const long long g = (long long)(s0 + sl) * npts + p;
-        cplx<T> v = res[(sl * TW + w) * N + i];
+        cplx<T> v = res[lidx(sl * TW + w, i, LS)];
         if (MODE == PM_KIN_FIRST) st(a.P + g, v);
         else if (MODE == PM_KIN_ACC) st(a.P + g, ld(a.P + g) + v);
         else st(a.out + g, v);
@@ -163,7 +165,7 @@ __global__ void __launch_bounds__(256) linepass_kernel(PassArgs<T> a) {
         for (int s = 0; s < ((SS > 0) ? SS : kMaxStates); ++s) {
           if (s < S) {
             ph[s] = ld(phi + (long long)s * npts + p);
-            h[s] = res[(s * TW + w) * N + i];
+            h[s] = res[lidx(s * TW + w, i, LS)];
             if (a.multi_pass) h[s] = h[s] + ld(a.P + (long long)s * npts + p);
           }
         }
@@ -228,8 +230,9 @@ __global__ void __launch_bounds__(256) kin_all_kernel(KinArgs<T> a) {
     while (item >= a.item_start[d + 1]) ++d;
     const DimPass<T> &g = a.dp[d];
     const int N = g.N, TW = g.TW;
+    const int LS = lstride(N);
     cplx<T> *b0 = tws + N;
-    cplx<T> *b1 = b0 + (size_t)TW * N;
+    cplx<T> *b1 = b0 + line_buf_elems(N, TW);
     if (d != cur_dim) {
       __syncthreads();
       for (int i = threadIdx.x; i < N; i += blockDim.x) tws[i] = g.tw[i];
@@ -245,16 +248,17 @@ __global__ void __launch_bounds__(256) kin_all_kernel(KinArgs<T> a) {
     for (int idx = threadIdx.x; idx < tileN; idx += blockDim.x) {
       int w, i;
       tile_coord(idx, TW, N, g.es, w, i);
-      b0[w * N + i] = ld(src + base + (long long)w * g.ls + (long long)i * g.es);
+      b0[lidx(w, i, LS)] = ld(src + base + (long long)w * g.ls + (long long)i * g.es);
     }
     __syncthreads();
     const int cur = fft_lines<T>(b0, b1, g.rp, TW, tws, -1);
     cplx<T> *bc = cur ? b1 : b0;
     const double kf = g.kfac[s];
     for (int idx = threadIdx.x; idx < tileN; idx += blockDim.x) {
-      const int i = idx % N;
+      const int w = idx / N, i = idx - w * N;
       const int kq = min(i, N - i);
-      bc[idx] = cmulr(bc[idx], (T)(kf * (double)kq * (double)kq));
+      const int x = lidx(w, i, LS);
+      bc[x] = cmulr(bc[x], (T)(kf * (double)kq * (double)kq));
     }
     __syncthreads();
     const int cur2 = fft_lines<T>(bc, cur ? b0 : b1, g.rp, TW, tws, +1);
@@ -263,7 +267,7 @@ __global__ void __launch_bounds__(256) kin_all_kernel(KinArgs<T> a) {
     for (int idx = threadIdx.x; idx < tileN; idx += blockDim.x) {
       int w, i;
       tile_coord(idx, TW, N, g.es, w, i);
-      st(dst + base + (long long)w * g.ls + (long long)i * g.es, res[w * N + i]);
+      st(dst + base + (long long)w * g.ls + (long long)i * g.es, res[lidx(w, i, LS)]);
     }
     __syncthreads();
   }
@@ -281,9 +285,10 @@ __global__ void __launch_bounds__(256) nac_kernel(NacArgs<T> a) {
   if (a.done != nullptr && *a.done) return;
   const cplx<T> *phi = (a.dyn ? a.bufs[(a.cs->i + 1) & 1] : a.phi) + (long long)a.col * a.npts;
   const int N = a.N, TW = a.TW;
+  const int LS = lstride(N);
   cplx<T> *tws = reinterpret_cast<cplx<T> *>(smem_raw);
   cplx<T> *b0 = tws + N;
-  cplx<T> *b1 = b0 + (size_t)2 * TW * N;
+  cplx<T> *b1 = b0 + line_buf_elems(N, 2 * TW);
   for (int i = threadIdx.x; i < N; i += blockDim.x) tws[i] = a.tw[i];
   const int tileN = TW * N;
   for (long long tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
@@ -295,18 +300,19 @@ __global__ void __launch_bounds__(256) nac_kernel(NacArgs<T> a) {
       tile_coord(idx, TW, N, a.es, w, i);
       const long long g = base + (long long)w * a.ls + (long long)i * a.es;
       const cplx<T> x = ld(phi + g);
-      b0[w * N + i] = x;
-      b0[(TW + w) * N + i] = cmulr(x, a.f[g]);
+      b0[lidx(w, i, LS)] = x;
+      b0[lidx(TW + w, i, LS)] = cmulr(x, a.f[g]);
     }
     __syncthreads();
     const int cur = fft_lines<T>(b0, b1, a.rp, 2 * TW, tws, -1);
     cplx<T> *bc = cur ? b1 : b0;
     for (int idx = threadIdx.x; idx < 2 * tileN; idx += blockDim.x) {
-      const int i = idx % N;
+      const int l = idx / N, i = idx - l * N;
       const int q = i < (N + 1) / 2 ? i : i - N;  // Kspace::Init1Dddx order, Nyquist negative
       const T m = (T)(a.kfac * (double)q);
-      const cplx<T> v = bc[idx];
-      bc[idx] = mk(-v.im * m, v.re * m);
+      const int x = lidx(l, i, LS);
+      const cplx<T> v = bc[x];
+      bc[x] = mk(-v.im * m, v.re * m);
     }
     __syncthreads();
     const int cur2 = fft_lines<T>(bc, cur ? b0 : b1, a.rp, 2 * TW, tws, +1);
@@ -315,7 +321,7 @@ __global__ void __launch_bounds__(256) nac_kernel(NacArgs<T> a) {
       int w, i;
       tile_coord(idx, TW, N, a.es, w, i);
       const long long g = base + (long long)w * a.ls + (long long)i * a.es;
-      const cplx<T> add = cmulr(res[w * N + i], a.f[g]) + res[(TW + w) * N + i];
+      const cplx<T> add = cmulr(res[lidx(w, i, LS)], a.f[g]) + res[lidx(TW + w, i, LS)];
       st(a.out + g, ld(a.out + g) + add);
     }
   }

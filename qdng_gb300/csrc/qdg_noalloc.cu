@@ -1,9 +1,9 @@
 // qdg_noalloc.cu -- H psi without any device allocation.
 //
-// Some callers cannot allocate device memory: code that runs while a CUDA
-// graph is being captured, host frameworks that own all device memory
-// through their own pool, or plug-ins that must not change the process's
-// allocation state.  qdg_h_apply_noalloc() gives them H psi on arrays they
+// Some callers cannot allocate device memory: host frameworks that own all
+// device memory through their own caching pool, plug-ins that must not
+// change the process's allocation state, or time-step loops where the
+// implicit device synchronisation of cudaMalloc would stall the pipeline.  qdg_h_apply_noalloc() gives them H psi on arrays they
 // already own.  The scratch the kinetic passes need (the per-dimension parts
 // T_d psi, FFT twiddle tables, the potential-matrix list) lives in one
 // statically sized device array of this file, QDG_NOALLOC_SCRATCH_BYTES
@@ -232,7 +232,7 @@ qdg_status qdg_h_apply_noalloc(const qdg_hplan_desc *desc, const double *psi_in,
     a.tw = d_tw + t.tw_off[0];
     a.kfac = d_kfac;
     a.phi = in; a.out = out; a.cp = d_cp; a.coef = d_coef; a.grids = desc->grid_data;
-    const size_t smem = (size_t)g.n[0] * (1 + 2 * (size_t)S) * sizeof(cplx<double>);
+    const size_t smem = ((size_t)g.n[0] + 2 * qdg::line_buf_elems(g.n[0], S)) * sizeof(cplx<double>);
     if (smem > 227 * 1024) return na_fail(QDG_EUNSUPPORTED, "grid line too long for the shared-memory FFT");
     const int grid = (int)std::min<long long>(a.ntiles, 4LL * sms);
     if (qdg::launch_pass<double>(qdg::PM_HAPPLY, a, grid, 256, smem, st) != cudaSuccess)
@@ -259,7 +259,7 @@ qdg_status qdg_h_apply_noalloc(const qdg_hplan_desc *desc, const double *psi_in,
     dp.P = reinterpret_cast<cplx<double> *>(b + o_P + d * pbytes);
     k.item_start[d] = items;
     items += dp.ntiles * S;
-    smem = std::max(smem, (size_t)N * (1 + 2 * (size_t)TW) * sizeof(cplx<double>));
+    smem = std::max(smem, ((size_t)N + 2 * qdg::line_buf_elems(N, TW)) * sizeof(cplx<double>));
   }
   k.item_start[g.ndims] = items;
   if (smem > 227 * 1024) return na_fail(QDG_EUNSUPPORTED, "grid line too long for the shared-memory FFT");

@@ -130,8 +130,9 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
     l += cnt;
     const bool owner = d == 0;
     if (kind == PK_LAST && !owner) continue;
+    const int LS = lstride(N);
     cplx<T> *b0 = tws + N;
-    cplx<T> *b1 = b0 + (size_t)a.lmax[d] * N;
+    cplx<T> *b1 = b0 + line_buf_elems(N, a.lmax[d]);
     __syncthreads();
     if (d != cur_dim && kind != PK_LAST) {
       for (int i = threadIdx.x; i < N; i += blockDim.x) tws[i] = g.tw[i];
@@ -177,7 +178,7 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
           if (istr == 1) { w = idx / N; i = idx - w * N; }
           else { i = idx / L; w = idx - i * L; }
         }
-        sidx[u] = ok ? w * N + i : -1;
+        sidx[u] = ok ? lidx(w, i, LS) : -1;
         const long long p = lbase[w] + (long long)i * istr;
         pp[u] = p;
         if (!ok) continue;
@@ -259,7 +260,10 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
     cplx<T> *bc = cur ? b1 : b0;
     const T *__restrict__ kt = g.ktab + (long long)s * N;
     for (int w = 0; w < L; ++w)
-      for (int i = threadIdx.x; i < N; i += blockDim.x) bc[w * N + i] = cmulr(bc[w * N + i], __ldg(kt + i));
+      for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        const int x = lidx(w, i, LS);
+        bc[x] = cmulr(bc[x], __ldg(kt + i));
+      }
     __syncthreads();
     const int cur2 = fft_lines<T>(bc, cur ? b0 : b1, g.rp, L, tws, +1);
     const cplx<T> *res = cur2 ? (cur ? b0 : b1) : bc;
@@ -269,7 +273,7 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
       int w, i;
       if (istr == 1) { w = idx / N; i = idx - w * N; }
       else { i = idx / L; w = idx - i * L; }
-      st(dst + lbase[w] + (long long)i * istr, res[w * N + i]);
+      st(dst + lbase[w] + (long long)i * istr, res[lidx(w, i, LS)]);
     }
     if (tr) {
       const unsigned long long tg3 = gtimer();
@@ -332,9 +336,10 @@ __device__ void phase_lines(const StepArgs<T> &a, const cplx<T> *phi, cplx<T> *k
   const DimPass<T> &g = a.dp[0];
   const int N = g.N, TW = a.TW1;
   const int L = TW * S;
+  const int LS = lstride(N);
   cplx<T> *tws = smem;
   cplx<T> *b0 = tws + N;
-  cplx<T> *b1 = b0 + (size_t)L * N;
+  cplx<T> *b1 = b0 + line_buf_elems(N, L);
   const long long ntiles = a.npts / ((long long)N * TW);
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const long long base = tile * TW * N;
@@ -343,14 +348,15 @@ __device__ void phase_lines(const StepArgs<T> &a, const cplx<T> *phi, cplx<T> *k
     for (int idx = threadIdx.x; idx < L * N; idx += blockDim.x) {
       const int l = idx / N, i = idx - l * N;
       const int s = l / TW, w = l - s * TW;
-      b0[idx] = ldcg(phi + (long long)s * a.npts + base + (long long)w * N + i);
+      b0[lidx(l, i, LS)] = ldcg(phi + (long long)s * a.npts + base + (long long)w * N + i);
     }
     __syncthreads();
     const int cur = fft_lines<T>(b0, b1, g.rp, L, tws, -1);
     cplx<T> *bc = cur ? b1 : b0;
     for (int idx = threadIdx.x; idx < L * N; idx += blockDim.x) {
       const int l = idx / N, i = idx - l * N;
-      bc[idx] = cmulr(bc[idx], __ldg(g.ktab + (long long)(l / TW) * N + i));
+      const int x = lidx(l, i, LS);
+      bc[x] = cmulr(bc[x], __ldg(g.ktab + (long long)(l / TW) * N + i));
     }
     __syncthreads();
     const int cur2 = fft_lines<T>(bc, cur ? b0 : b1, g.rp, L, tws, +1);
@@ -363,7 +369,7 @@ __device__ void phase_lines(const StepArgs<T> &a, const cplx<T> *phi, cplx<T> *k
       for (int s = 0; s < SM; ++s)
         if (s < S) {
           ph[s] = ldcg(phi + (long long)s * a.npts + p);
-          h[s] = res[(s * TW + w) * N + i];
+          h[s] = res[lidx(s * TW + w, i, LS)];
         }
       point_term<T, SM, FIRST>(a, p, ph, h, kout, coeff_i, S, acc);
     }
