@@ -201,6 +201,20 @@ qdg_status qdg_prop_apply_host(qdg_prop *prop, qdg_wf *scratch, double *host_psi
 qdg_status qdg_prop_run(qdg_prop *prop, qdg_wf *psi, int64_t step0, int32_t nsteps,
                         int64_t *terms_total);
 
+/* Eigenstates by imaginary-time relaxation: ProgEigen::ImagTimeEF
+ * (src/ProgEigen.cpp:318-409) with OProjection (OProjection.cpp:133-149)
+ * and, with diag != 0, DiagBasis (ProgEigen.cpp:94-138).  prop must be an
+ * imaginary-time propagator (QDng builds it backward, ProgEigen.cpp:692-693).
+ * Every function starts from the normalised psi_init (host, nstates*npoints
+ * complex128) and is stepped, projected against the ones already found and
+ * normalised until |1 - <psi_old|psi>| <= convergence or maxsteps.  Outputs
+ * (host): e_raw[nef] = <psi_i|H|psi_i>, e_diag[nef] (eigenvalues of H in the
+ * basis, or e_raw without diag), steps[nef] (may be NULL), efs
+ * (nef * nstates*npoints complex128, may be NULL): the diagonalised basis. */
+qdg_status qdg_eigen_imag(qdg_prop *prop, const double *psi_init, int32_t nef, int32_t maxsteps,
+                          double convergence, int32_t diag, double *efs, double *e_raw, double *e_diag,
+                          int32_t *steps);
+
 /* ---- batched ensemble of independent wavepackets ------------------------ */
 
 /* One member: a single-state Hamiltonian Sum(GridNablaSq, GridPotential,

@@ -1341,6 +1341,115 @@ qdg_status prop_step(qdg_prop *P, cplx<double> *psi, long long step, int *used, 
   return prop_step_t<float>(P, psi, step, used, sync);
 }
 
+// <a|H|b> (all states, grid weights) with H applied at step 0 into the plan's scratch.
+qdg_status h_expec(qdg_plan *p, const cplx<double> *a, const cplx<double> *b, cd *out) {
+  std::vector<cd> d;
+  qdg_status s;
+  if (p->precision == QDG_PREC_FP64) {
+    cplx<double> *o = reinterpret_cast<cplx<double> *>(p->d_scratch);
+    if ((s = h_apply_bulk<double>(p, b, o, 0)) != QDG_OK) return s;
+    if ((s = dots<double, double>(p, a, o, d)) != QDG_OK) return s;
+  } else {
+    cplx<float> *o = reinterpret_cast<cplx<float> *>(p->d_scratch);
+    if ((s = h_apply_bulk<float>(p, b, o, 0)) != QDG_OK) return s;
+    if ((s = dots<double, float>(p, a, o, d)) != QDG_OK) return s;
+  }
+  *out = total(d);
+  return QDG_OK;
+}
+
+// ProgEigen::ImagTimeEF (src/ProgEigen.cpp:318-409): relax each function in
+// imaginary time from the same start, projecting out the functions already
+// found after every step (OProjection::Apply, OProjection.cpp:133-149),
+// normalising, until |1 - <psi_old|psi>| <= convergence; then DiagBasis
+// (ProgEigen.cpp:94-138) diagonalises H in the basis found.
+qdg_status eigen_imag(qdg_prop *P, const double *psi_init, int nef, int maxsteps, double conv, int diag,
+                      double *efs, double *e_raw, double *e_diag, int32_t *steps) {
+  qdg_plan *p = P->plan;
+  const long long n = wf_elems(p);
+  const size_t bytes = sizeof(cplx<double>) * (size_t)n;
+  std::vector<cplx<double> *> bufs;
+  auto cleanup = [&](qdg_status st) {
+    cudaStreamSynchronize(p->stream);
+    for (auto *b : bufs) cudaFree(b);
+    return st;
+  };
+  for (int i = 0; i < nef + 3; ++i) {  // nef functions, psi, old, init
+    cplx<double> *b = nullptr;
+    if (cudaMalloc(&b, bytes) != cudaSuccess) return cleanup(fail(QDG_ENOMEM, "device allocation failed"));
+    bufs.push_back(b);
+  }
+  cplx<double> *psi = bufs[nef], *old = bufs[nef + 1], *init = bufs[nef + 2];
+  qdg_status s;
+  std::vector<cd> d;
+#define ECHK(expr) do { if ((s = (expr)) != QDG_OK) return cleanup(s); } while (0)
+#define ECUDA(expr) do { if ((expr) != cudaSuccess) return cleanup(fail(QDG_ECUDA, #expr)); } while (0)
+  ECUDA(cudaMemcpyAsync(init, psi_init, bytes, cudaMemcpyHostToDevice, p->stream));
+  ECHK((dots<double, double>(p, init, init, d)));
+  const double n0 = std::sqrt(total(d).real());
+  if (!(n0 > 0) || !std::isfinite(n0)) return cleanup(fail(QDG_ENONFINITE, "Norm is not a number"));
+  ECUDA(qdg::launch_lincomb<double>(init, (const cplx<double> *)nullptr, cplx<double>{1.0 / n0, 0}, cplx<double>{0, 0}, n, p->stream));
+  for (int i = 0; i < nef; ++i) {
+    ECUDA(cudaMemcpyAsync(psi, init, bytes, cudaMemcpyDeviceToDevice, p->stream));
+    int st = 0;
+    double diff = 1;
+    while (st < maxsteps && diff > conv) {
+      ECUDA(cudaMemcpyAsync(old, psi, bytes, cudaMemcpyDeviceToDevice, p->stream));
+      int used = 0;
+      ECHK(prop_step(P, psi, st, &used, true));
+      if (i > 0) {
+        std::vector<cd> c(i);
+        for (int j = 0; j < i; ++j) {  // all overlaps against the propagated psi first
+          ECHK((dots<double, double>(p, bufs[j], psi, d)));
+          c[j] = total(d);
+        }
+        for (int j = 0; j < i; ++j)
+          ECUDA(qdg::launch_lincomb<double>(psi, bufs[j], cplx<double>{1, 0}, C(-c[j]), n, p->stream));
+      }
+      ECHK((dots<double, double>(p, psi, psi, d)));
+      const double nr = std::sqrt(total(d).real());
+      if (!std::isfinite(nr) || !(nr > 0)) return cleanup(fail(QDG_ENONFINITE, "Norm is not a number"));
+      ECUDA(qdg::launch_lincomb<double>(psi, (const cplx<double> *)nullptr, cplx<double>{1.0 / nr, 0}, cplx<double>{0, 0}, n, p->stream));
+      ECHK((dots<double, double>(p, old, psi, d)));
+      diff = std::abs(1.0 - total(d));
+      ++st;
+    }
+    ECUDA(cudaMemcpyAsync(bufs[i], psi, bytes, cudaMemcpyDeviceToDevice, p->stream));
+    cd e;
+    ECHK(h_expec(p, psi, psi, &e));
+    e_raw[i] = e.real();
+    if (steps) steps[i] = st;
+  }
+  if (diag) {
+    std::vector<double> Sm((size_t)nef * nef, 0.0), w, z;
+    for (int i = 0; i < nef; ++i) {
+      for (int j = 0; j < i; ++j) {
+        cd v;
+        ECHK(h_expec(p, bufs[i], bufs[j], &v));
+        Sm[(size_t)j * nef + i] = Sm[(size_t)i * nef + j] = v.real();
+      }
+      Sm[(size_t)i * nef + i] = e_raw[i];
+    }
+    qdg::host::sym_eig(nef, Sm, w, z);
+    for (int i = 0; i < nef; ++i) {
+      e_diag[i] = w[i];
+      if (!efs) continue;
+      ECUDA(qdg::launch_lincomb<double>(psi, bufs[0], cplx<double>{0, 0}, cplx<double>{z[(size_t)0 * nef + i], 0}, n, p->stream));
+      for (int j = 1; j < nef; ++j)
+        ECUDA(qdg::launch_lincomb<double>(psi, bufs[j], cplx<double>{1, 0}, cplx<double>{z[(size_t)j * nef + i], 0}, n, p->stream));
+      ECUDA(cudaMemcpyAsync(efs + 2 * (size_t)i * n, psi, bytes, cudaMemcpyDeviceToHost, p->stream));
+    }
+  } else {
+    for (int i = 0; i < nef; ++i) {
+      e_diag[i] = e_raw[i];
+      if (efs) ECUDA(cudaMemcpyAsync(efs + 2 * (size_t)i * n, bufs[i], bytes, cudaMemcpyDeviceToHost, p->stream));
+    }
+  }
+#undef ECHK
+#undef ECUDA
+  return cleanup(QDG_OK);
+}
+
 }  // namespace
 
 // ====================================================================== ABI
@@ -1685,6 +1794,14 @@ qdg_status qdg_prop_apply_host(qdg_prop *P, qdg_wf *scratch, double *host_psi, i
   }
   if (terms_used) *terms_used = used;
   return QDG_OK;
+}
+
+qdg_status qdg_eigen_imag(qdg_prop *P, const double *psi_init, int32_t nef, int32_t maxsteps, double convergence,
+                          int32_t diag, double *efs, double *e_raw, double *e_diag, int32_t *steps) {
+  if (!P || !psi_init || nef < 1 || maxsteps < 1 || !e_raw || !e_diag) return fail(QDG_EINVAL, "bad arguments");
+  if (!P->inited) return fail(QDG_EINVAL, "propagator not initialised");
+  if (!P->imag) return fail(QDG_EINVAL, "ImagTimeEF needs an imaginary-time propagator");
+  return eigen_imag(P, psi_init, nef, maxsteps, convergence, diag, efs, e_raw, e_diag, steps);
 }
 
 qdg_status qdg_prop_run(qdg_prop *P, qdg_wf *psi, int64_t step0, int32_t nsteps, int64_t *terms_total) {

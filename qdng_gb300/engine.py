@@ -159,6 +159,18 @@ class Propagator:
         check(self.lib.qdg_prop_phase_times(self.h, _dp(ns)))
         return dict(gather=ns[0], fft=ns[1], store=ns[2], barrier=ns[3])
 
+    def eigen_imag(self, psi_init, nef, maxsteps, conv, diag=True):
+        """ProgEigen::ImagTimeEF (+ DiagBasis): returns (efs [nef x size],
+        e_raw, e_diag, steps), the layout of the oracle's eigen_imag."""
+        n = self.plan.S * self.plan.npts
+        efs = np.zeros((nef, n), dtype=np.complex128)
+        e_raw, e_diag = np.zeros(nef), np.zeros(nef)
+        steps = np.zeros(nef, dtype=np.int32)
+        x = np.ascontiguousarray(psi_init, dtype=np.complex128).reshape(-1)
+        check(self.lib.qdg_eigen_imag(self.h, _dp(x), nef, maxsteps, conv, int(diag), _dp(efs), _dp(e_raw),
+                                      _dp(e_diag), steps.ctypes.data_as(C.c_void_p)))
+        return efs, e_raw, e_diag, steps
+
     def run(self, wf, step0, nsteps):
         tot = C.c_int64(0)
         check(self.lib.qdg_prop_run(self.h, wf.h, step0, nsteps, C.byref(tot)))
