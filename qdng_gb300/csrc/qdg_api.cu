@@ -135,7 +135,9 @@ struct qdg_wf {
 };
 
 struct qdg_prop {
-  qdg_plan *plan;
+  qdg_plan *plan;          // the plan the series runs on
+  qdg_plan *user = nullptr;  // the caller's plan (wave functions belong to it)
+  qdg_plan *twin = nullptr;  // owned FP64 copy of a mixed plan (imaginary-time Chebyshev)
   std::string name;
   int kind = 0;
   std::map<std::string, std::string> params;
@@ -1450,6 +1452,18 @@ qdg_status eigen_imag(qdg_prop *P, const double *psi_init, int nef, int maxsteps
   return cleanup(QDG_OK);
 }
 
+// A propagator on an FP64 twin of the caller's plan queues its work on the
+// caller's stream, so it stays ordered with the caller's other calls.
+void sync_twin(qdg_prop *P) {
+  if (!P->twin || P->twin->stream == P->user->stream) return;
+  if (P->twin->own_stream) {
+    cudaStreamSynchronize(P->twin->stream);
+    cudaStreamDestroy(P->twin->stream);
+    P->twin->own_stream = false;
+  }
+  P->twin->stream = P->user->stream;
+}
+
 }  // namespace
 
 // ====================================================================== ABI
@@ -1689,6 +1703,7 @@ qdg_status qdg_prop_create(qdg_plan *plan, const char *name, const char *params,
   if (!(dt != 0) || !std::isfinite(dt)) return fail(QDG_EINVAL, "No time step defined");
   qdg_prop *P = new qdg_prop();
   P->plan = plan;
+  P->user = plan;
   P->name = name;
   parse_params(params, P->params);
   P->dt = dt;
@@ -1709,6 +1724,30 @@ qdg_status qdg_prop_create(qdg_plan *plan, const char *name, const char *params,
     if (has(P, "err")) P->err = parse_d(P, "err");
     if (has(P, "conv")) P->conv = parse_d(P, "conv");
   }
+  if (P->kind == 1 && P->imag && plan->precision == QDG_PREC_MIXED) {
+    // The imaginary-time series (scaled I_n, OCheby.cpp:427-433) reaches the
+    // low states through cancellations of terms ~1/sqrt(2 pi R) down to
+    // e^{-R (1 - X)}; FP32 phi cannot carry that, so this propagator runs on
+    // an FP64 copy of the plan (same host data, the caller's stream).
+    qdg_hplan_desc d;
+    memset(&d, 0, sizeof(d));
+    d.grid = plan->grid;
+    d.nstates = plan->S;
+    d.nterms = (int32_t)plan->terms.size();
+    d.terms = plan->terms.data();
+    d.ngrids = plan->ngrids;
+    d.grid_data = plan->grids_h.empty() ? nullptr : plan->grids_h.data();
+    d.nlasers = plan->nlasers;
+    d.laser_nt = plan->laser_nt;
+    d.laser_data = plan->lasers_h.empty() ? nullptr : plan->lasers_h.data();
+    d.nonhermitian = plan->hermitian ? 0 : 1;
+    qdg_plan *tw = nullptr;
+    const qdg_status s = qdg_plan_create(&d, QDG_PREC_FP64, &tw);
+    if (s != QDG_OK) { delete P; return s; }
+    P->twin = tw;
+    P->plan = tw;
+    sync_twin(P);
+  }
   plan->children++;
   *out = P;
   return QDG_OK;
@@ -1716,7 +1755,7 @@ qdg_status qdg_prop_create(qdg_plan *plan, const char *name, const char *params,
 
 qdg_status qdg_prop_destroy(qdg_prop *P) {
   if (!P) return QDG_OK;
-  qdg_plan *plan = P->plan;
+  qdg_plan *plan = P->user;
   cudaStreamSynchronize(plan->stream);
   if (P->k0) cudaFree(P->k0);
   if (P->k1) cudaFree(P->k1);
@@ -1732,6 +1771,12 @@ qdg_status qdg_prop_destroy(qdg_prop *P) {
   for (auto v : P->lzb) if (v) cudaFree(v);
   if (P->kbuf) cudaFree(P->kbuf);
   if (P->kwide) cudaFree(P->kwide);
+  if (P->twin) {
+    if (P->twin->own_stream) cudaStreamDestroy(P->twin->stream);
+    P->twin->own_stream = false;
+    P->twin->stream = nullptr;
+    free_plan(P->twin);
+  }
   delete P;
   release_child(plan);
   return QDG_OK;
@@ -1768,7 +1813,8 @@ qdg_status qdg_prop_get_coeffs(const qdg_prop *P, double *coeffs, int32_t capaci
 }
 
 qdg_status qdg_prop_apply(qdg_prop *P, qdg_wf *psi, int64_t step, int32_t *terms_used) {
-  if (!P || !psi || psi->plan != P->plan) return fail(QDG_EINVAL, "bad arguments");
+  if (!P || !psi || psi->plan != P->user) return fail(QDG_EINVAL, "bad arguments");
+  sync_twin(P);
   if (!P->inited) return fail(QDG_EINVAL, "propagator not initialised");
   int used = 0;
   qdg_status s = prop_step(P, psi->d, step, &used, true);
@@ -1777,7 +1823,8 @@ qdg_status qdg_prop_apply(qdg_prop *P, qdg_wf *psi, int64_t step, int32_t *terms
 }
 
 qdg_status qdg_prop_apply_host(qdg_prop *P, qdg_wf *scratch, double *host_psi, int64_t step, int32_t *terms_used) {
-  if (!P || !scratch || !host_psi || scratch->plan != P->plan) return fail(QDG_EINVAL, "bad arguments");
+  if (!P || !scratch || !host_psi || scratch->plan != P->user) return fail(QDG_EINVAL, "bad arguments");
+  sync_twin(P);
   qdg_plan *p = P->plan;
   CK(cudaMemcpyAsync(scratch->d, host_psi, sizeof(cplx<double>) * wf_elems(p), cudaMemcpyHostToDevice, p->stream));
   int used = 0;
@@ -1805,7 +1852,8 @@ qdg_status qdg_eigen_imag(qdg_prop *P, const double *psi_init, int32_t nef, int3
 }
 
 qdg_status qdg_prop_run(qdg_prop *P, qdg_wf *psi, int64_t step0, int32_t nsteps, int64_t *terms_total) {
-  if (!P || !psi || psi->plan != P->plan || nsteps < 0) return fail(QDG_EINVAL, "bad arguments");
+  if (!P || !psi || psi->plan != P->user || nsteps < 0) return fail(QDG_EINVAL, "bad arguments");
+  sync_twin(P);
   if (!P->inited) return fail(QDG_EINVAL, "propagator not initialised");
   long long tot = 0, before = 0;
   if (P->kind == 1) {
