@@ -278,8 +278,12 @@ def engine_arm(args, world, rank, local):
             what = "kinetic line pass: read phi, write T_d phi"
             kname = f"kin_all_kernel ({modes[top]})"
         ach = per_launch / avg_s / 1e9
+        # DRAM bytes (read + write) of one step-kernel launch on this workload,
+        # from an ncu capture of the same command (dram__bytes_read.sum +
+        # dram__bytes_write.sum): the working set stays in L2
+        traffic = {"fp64": 5.79e6, "mixed": 3.75e6}[args.precision] if modes[top] == "cheby_step" else None
         roof = {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(ach / peak, 4), "traffic": None, "kernel": kname,
+                "frac": round(ach / peak, 4), "traffic": traffic, "kernel": kname,
                 "algorithmic_bytes_per_launch": int(per_launch), "bytes_note": what,
                 "avg_launch_us": round(avg_s * 1e6, 2), "peak_source": peak_src + " (MEASURED_PEAKS.json hbm_gbs)"}
     per_mode = {modes[i]: {"ms": round(float(prof_ms[i]), 3), "launches": int(prof_n[i])}
