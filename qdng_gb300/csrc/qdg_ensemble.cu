@@ -278,6 +278,164 @@ __device__ void ens_step_1d(const EnsArgs<T> &a, const EnsMember &m, T field, un
   terms += used;
 }
 
+// ---- double-float accumulation (mixed precision) --------------------------
+// GB300 runs FP64 at 1/64 of the FP32 rate, and in the resident path the
+// FP64 psi update and norm were ~40% of a term (ncu, one 4096-point member).
+// The mixed form therefore accumulates psi as an unevaluated sum hi + lo of
+// two FP32 numbers (error-free transformations of Dekker and Knuth; about
+// 48 significant bits, far below the FP32 error of the phi_n) and tracks
+// the series cut through the norm change of each term.  The explicit
+// round-to-nearest intrinsics keep the compiler from contracting the
+// transformations into FMAs.
+struct dfloat { float hi, lo; };
+
+__device__ __forceinline__ dfloat df_split(double x) {
+  dfloat r;
+  r.hi = (float)x;
+  r.lo = (float)(x - (double)r.hi);
+  return r;
+}
+
+// v += (ah + al) * x, with ah + al a split FP64 coefficient
+__device__ __forceinline__ void df_axpy(dfloat &v, float ah, float al, float x) {
+  const float p = __fmul_rn(ah, x);
+  const float e = fmaf(al, x, fmaf(ah, x, -p));       // exact low part of ah x, plus al x
+  const float s = __fadd_rn(v.hi, p);                  // two-sum of v.hi and p
+  const float bb = __fsub_rn(s, v.hi);
+  const float se = __fadd_rn(__fsub_rn(v.hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+  const float lo = __fadd_rn(v.lo, __fadd_rn(se, e));
+  const float h2 = __fadd_rn(s, lo);                    // renormalise
+  v.lo = __fsub_rn(lo, __fsub_rn(h2, s));
+  v.hi = h2;
+}
+
+// One step of a 1-D member in shared memory, mixed form: as ens_step_1d with
+// psi in double-float.  The cut uses the norm change of term i,
+// 2 Re<psi|a_i phi_i> + |a_i phi_i|^2 (summed in FP32 per thread, FP64 across
+// the block), which is what |psi|^2 - previous |psi|^2 measures; the
+// reference's first comparison (term 2 against the norm before the step)
+// becomes the change of term 2, which differs only for series that have
+// converged by term 2.
+__device__ void ens_step_1d_df(const EnsArgs<float> &a, const EnsMember &m, float field, unsigned char *smem_raw,
+                               double *red, long long &terms, int &status) {
+  typedef float T;
+  const int N = m.n[0];
+  dfloat *pre = reinterpret_cast<dfloat *>(smem_raw);   // psi real part
+  dfloat *pim = pre + N;                                 // psi imaginary part
+  cplx<T> *cur = reinterpret_cast<cplx<T> *>(pim + N);
+  cplx<T> *prev = cur + N;
+  cplx<T> *f0 = prev + N;
+  cplx<T> *f1 = f0 + line_buf_elems(N, 1);
+  T *Vs = reinterpret_cast<T *>(f1 + line_buf_elems(N, 1));
+  const cplx<T> *__restrict__ tw = a.tw + m.tw_off[0];
+  const T *__restrict__ kt = a.ktab + m.kt_off[0];
+  cplx<double> *__restrict__ gpsi = a.psi + m.off;
+  double n0 = 0.0;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    T v = a.V[m.off + i];
+    if (m.has_dipole) v = v + field * a.mu[m.off + i];
+    Vs[i] = v;
+    const cplx<double> p = ld(gpsi + i);
+    pre[i] = df_split(p.re);
+    pim[i] = df_split(p.im);
+    cur[i] = ccast<T>(p);
+    n0 += cabs2(p);
+  }
+  const int nw = (blockDim.x + 31) >> 5;
+  for (int o = 16; o > 0; o >>= 1) n0 += __shfl_down_sync(0xffffffffu, n0, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = n0;
+  __syncthreads();
+  double norm0 = 0.0;
+  for (int w = 0; w < nw; ++w) norm0 += red[w];
+  if (!isfinite(norm0)) status = 2;
+  const RadixPlan &rp = m.rp[0];
+  const cplx<T> off = ccast<T>(m.offset);
+  bool done = !isfinite(norm0);
+  int used = 2;
+  for (int it = 1; it < m.order && !done; ++it) {
+    const bool first = it == 1;
+    int Ns = 1;
+    cplx<T> *dst = f0;
+    const cplx<T> *src = cur;
+    for (int s = 0; s < rp.nstages; ++s) {
+      const bool from_cur = s == 0;
+      stage_any<T>(rp.radix[s], [&](int i) { return from_cur ? src[i] : src[lpos(i)]; },
+                   [&](int i, const cplx<T> &v) { dst[lpos(i)] = v; }, N, 1, Ns, tw, -1);
+      __syncthreads();
+      Ns *= rp.radix[s];
+      src = dst;
+      dst = dst == f0 ? f1 : f0;
+    }
+    const cplx<T> fac = ccast<T>(first ? m.fac1 : m.fac);
+    const double ai = a.coef[m.coef_off + it];
+    const float ai_h = (float)ai, ai_l = (float)(ai - (double)ai_h);
+    const double a0 = a.coef[m.coef_off];
+    const float a0_h = (float)a0, a0_l = (float)(a0 - (double)a0_h);
+    float dn = 0.0f;  // this thread's share of the norm change
+    auto point = [&](int i, const cplx<T> &tk) {
+      const cplx<T> x = cur[i];
+      const cplx<T> h = tk + cmulr(x, Vs[i]);
+      const cplx<T> bf = cmul(h - cmul(off, x), fac);
+      dfloat pr = pre[i], pi = pim[i];
+      if (first) {
+        prev[i] = bf;  // phi_1
+        // psi = a0 psi + a1 phi_1
+        dfloat qr = {0.0f, 0.0f}, qi = {0.0f, 0.0f};
+        df_axpy(qr, a0_h, a0_l, pr.hi);
+        df_axpy(qr, a0_h, a0_l, pr.lo);
+        df_axpy(qi, a0_h, a0_l, pi.hi);
+        df_axpy(qi, a0_h, a0_l, pi.lo);
+        df_axpy(qr, ai_h, ai_l, bf.re);
+        df_axpy(qi, ai_h, ai_l, bf.im);
+        pr = qr;
+        pi = qi;
+      } else {
+        const cplx<T> k2 = bf + prev[i];
+        prev[i] = k2;  // phi_i over phi_{i-2}
+        const float tr = ai_h * k2.re, ti = ai_h * k2.im;
+        dn = fmaf(2.0f * pr.hi + tr, tr, fmaf(2.0f * pi.hi + ti, ti, dn));
+        df_axpy(pr, ai_h, ai_l, k2.re);
+        df_axpy(pi, ai_h, ai_l, k2.im);
+      }
+      pre[i] = pr;
+      pim[i] = pi;
+    };
+    Ns = 1;
+    for (int s = 0; s < rp.nstages; ++s) {
+      const bool ks = s == 0, ls = s == rp.nstages - 1;
+      auto load = [&](int i) { return ks ? cmulr(src[lpos(i)], kt[i]) : src[lpos(i)]; };
+      if (ls) {
+        stage_any<T>(rp.radix[s], load, point, N, 1, Ns, tw, +1);
+      } else {
+        stage_any<T>(rp.radix[s], load, [&](int i, const cplx<T> &v) { dst[lpos(i)] = v; }, N, 1, Ns, tw, +1);
+        __syncthreads();
+      }
+      Ns *= rp.radix[s];
+      src = dst;
+      dst = dst == f0 ? f1 : f0;
+    }
+    double acc = (double)dn;
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    double delta = 0.0;
+    for (int w = 0; w < nw; ++w) delta += red[w];
+    cplx<T> *tmp = cur;
+    cur = prev;
+    prev = tmp;
+    if (first) continue;
+    used = it + 1;
+    if (!isfinite(delta)) { done = true; status = 2; }
+    else if (fabs(delta) / norm0 < m.prec && m.offset.im == 0.0) done = true;  // OCheby.cpp:179-182
+  }
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    const cplx<double> p = mk((double)pre[i].hi + (double)pre[i].lo, (double)pim[i].hi + (double)pim[i].lo);
+    st(gpsi + i, cmul(p, m.ph));
+  }
+  __syncthreads();
+  terms += used;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) ensemble_kernel(EnsArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -300,7 +458,8 @@ __global__ void __launch_bounds__(256) ensemble_kernel(EnsArgs<T> a) {
       T field = (T)0;
       if (m.has_dipole && step >= 0 && step < m.laser_nt) field = (T)(-a.lasers[m.laser_off + step]);
       if (m.nd == 1 && m.fast) {
-        ens_step_1d<T>(a, m, field, smem_raw, red, terms, status);
+        if constexpr (sizeof(T) == sizeof(float)) ens_step_1d_df(a, m, field, smem_raw, red, terms, status);
+        else ens_step_1d<T>(a, m, field, smem_raw, red, terms, status);
         continue;
       }
       for (long long p = threadIdx.x; p < m.npts; p += blockDim.x)
