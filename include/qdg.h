@@ -249,6 +249,12 @@ qdg_status qdg_ensemble_download(const qdg_ensemble *e, double *psi_all);
 qdg_status qdg_ensemble_run(qdg_ensemble *e, int64_t step0, int32_t nsteps, int64_t *terms_total);
 /* Series parameters of member i after create (order, scaling, offset). */
 qdg_status qdg_ensemble_member_info(const qdg_ensemble *e, int32_t i, qdg_prop_info *info);
+/* Schedule of the last qdg_ensemble_run: for every member its start and end
+ * on the GPU clock in ns relative to the launch's first start
+ * (start_end[2 i], start_end[2 i + 1]) and the block that ran it (block[i],
+ * may be NULL).  A tuning aid for the work-queue order; no counterpart in
+ * the reference. */
+qdg_status qdg_ensemble_timeline(const qdg_ensemble *e, int64_t *start_end, int32_t *block);
 
 /* ---- engine instrumentation (no counterpart in the reference) ---------- */
 

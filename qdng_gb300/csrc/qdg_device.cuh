@@ -128,14 +128,14 @@ template <typename T> __device__ __forceinline__ void dft16(cplx<T> *x, int sign
   for (int k = 0; k < 16; ++k) x[k] = y[k];
 }
 
-// Twiddles w^(r*k) and the R-point DFT of one Stockham item, in registers.
-template <typename T, int R>
-__device__ __forceinline__ void stage_butterfly(cplx<T> (&v)[R], int k, int step, int M,
-                                                const cplx<T> *__restrict__ tw, int sign) {
+// Twiddles w^(r*k) and the R-point DFT of one Stockham item, in registers;
+// twf(m) returns w^m = exp(-2 pi i m / N).
+template <typename T, int R, typename TwF>
+__device__ __forceinline__ void stage_butterfly_t(cplx<T> (&v)[R], int k, int step, int M, TwF twf, int sign) {
   if (k) {
 #pragma unroll
     for (int r = 1; r < R; ++r) {
-      cplx<T> w = tw[r * k * step];  // r*k*step < R*Ns*step = N
+      cplx<T> w = twf(r * k * step);  // r*k*step < R*Ns*step = N
       if (sign > 0) w.im = -w.im;
       v[r] = cmul(v[r], w);
     }
@@ -158,7 +158,7 @@ __device__ __forceinline__ void stage_butterfly(cplx<T> (&v)[R], int k, int step
       cplx<T> s = v[0];
 #pragma unroll
       for (int r = 1; r < R; ++r) {
-        cplx<T> w = tw[((r * qq) % R) * M];
+        cplx<T> w = twf(((r * qq) % R) * M);
         if (sign > 0) w.im = -w.im;
         s = s + cmul(v[r], w);
       }
@@ -167,6 +167,12 @@ __device__ __forceinline__ void stage_butterfly(cplx<T> (&v)[R], int k, int step
 #pragma unroll
     for (int qq = 0; qq < R; ++qq) v[qq] = y[qq];
   }
+}
+
+template <typename T, int R>
+__device__ __forceinline__ void stage_butterfly(cplx<T> (&v)[R], int k, int step, int M,
+                                                const cplx<T> *__restrict__ tw, int sign) {
+  stage_butterfly_t<T, R>(v, k, step, M, [tw](int m) { return tw[m]; }, sign);
 }
 
 // Shared-memory layout of a batch of lines: line l starts at l * lstride(N)
@@ -229,9 +235,9 @@ __device__ __forceinline__ void stockham_stage(const cplx<T> *__restrict__ in, c
 // and store(idx, value) with idx = line * N + position, so that a caller can
 // fuse a multiply into the loads of a stage or its point update into the
 // stores of the last one.
-template <typename T, int R, typename Load, typename Store>
-__device__ __forceinline__ void stockham_stage_io(Load load, Store store, int N, int nlines, int Ns,
-                                                  const cplx<T> *__restrict__ tw, int sign) {
+template <typename T, int R, typename Load, typename Store, typename TwF>
+__device__ __forceinline__ void stockham_stage_io(Load load, Store store, int N, int nlines, int Ns, TwF twf,
+                                                  int sign) {
   const int M = N / R;
   const int step = N / (Ns * R);
   const int items = nlines * M;
@@ -253,23 +259,23 @@ __device__ __forceinline__ void stockham_stage_io(Load load, Store store, int N,
     cplx<T> v[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = load(line * N + j + r * M);
-    stage_butterfly<T, R>(v, k, step, M, tw, sign);
+    stage_butterfly_t<T, R>(v, k, step, M, twf, sign);
     const int dst = line * N + q * Ns * R + k;
 #pragma unroll
     for (int r = 0; r < R; ++r) store(dst + r * Ns, v[r]);
   }
 }
 
-// One functor stage of any radix of a plan.
-template <typename T, typename Load, typename Store>
-__device__ __forceinline__ void stage_any(int R, Load load, Store store, int N, int nlines, int Ns,
-                                          const cplx<T> *__restrict__ tw, int sign) {
-  if (R == 16) stockham_stage_io<T, 16>(load, store, N, nlines, Ns, tw, sign);
-  else if (R == 8) stockham_stage_io<T, 8>(load, store, N, nlines, Ns, tw, sign);
-  else if (R == 4) stockham_stage_io<T, 4>(load, store, N, nlines, Ns, tw, sign);
-  else if (R == 2) stockham_stage_io<T, 2>(load, store, N, nlines, Ns, tw, sign);
-  else if (R == 3) stockham_stage_io<T, 3>(load, store, N, nlines, Ns, tw, sign);
-  else stockham_stage_io<T, 5>(load, store, N, nlines, Ns, tw, sign);
+// One functor stage of any radix of a plan; twf(m) returns w^m.
+template <typename T, typename Load, typename Store, typename TwF>
+__device__ __forceinline__ void stage_any(int R, Load load, Store store, int N, int nlines, int Ns, TwF twf,
+                                          int sign) {
+  if (R == 16) stockham_stage_io<T, 16>(load, store, N, nlines, Ns, twf, sign);
+  else if (R == 8) stockham_stage_io<T, 8>(load, store, N, nlines, Ns, twf, sign);
+  else if (R == 4) stockham_stage_io<T, 4>(load, store, N, nlines, Ns, twf, sign);
+  else if (R == 2) stockham_stage_io<T, 2>(load, store, N, nlines, Ns, twf, sign);
+  else if (R == 3) stockham_stage_io<T, 3>(load, store, N, nlines, Ns, twf, sign);
+  else stockham_stage_io<T, 5>(load, store, N, nlines, Ns, twf, sign);
 }
 
 // Full unnormalised FFT of `nlines` lines in shared memory (layout above,

@@ -42,7 +42,11 @@ struct EnsMember {
   int laser_nt;
   int has_dipole;
   int fast;               // 1-D member kept in shared memory for the whole step
+  double kf;              // k^2 multiplier of dimension 0: dk^2 / (2 m) / N
 };
+
+// psi of the mixed form as an unevaluated sum hi + lo of two FP32 numbers
+struct dfloat { float hi, lo; };
 
 template <typename T>
 struct EnsArgs {
@@ -63,7 +67,15 @@ struct EnsArgs {
   int diff;               // mixed precision: differential series cut
   long long *terms;       // per member, accumulated
   int *status;            // per member: 2 = non-finite norm
+  dfloat *dfr, *dfi;      // mixed form: psi in double-float during a step (members off the resident path)
+  unsigned long long *tl; // per member: start, end (GPU clock, ns) and block of the last run
 };
+
+__device__ __forceinline__ unsigned long long ens_clock() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 
 // T_d phi for every dimension of member m: lines in batches of lmax[d].
 template <typename T>
@@ -156,12 +168,21 @@ __device__ double ens_points(const EnsArgs<T> &a, const EnsMember &m, const cplx
 }
 
 // Shared memory of the resident 1-D path for a line of N points: psi
-// (FP64), phi_{i-1}, phi_{i-2}, the two FFT buffers (padded line layout)
-// and V - mu E.
+// (FP64 or double-float), phi_{i-1}, phi_{i-2}, the two FFT buffers (padded
+// line layout), the twiddles as two tables (w^m = W[m / 64] w[m % 64]) and
+// V - mu E.
+__host__ __device__ inline int ens_tw_hi(int N) { return (N + 63) / 64; }
 template <typename T>
 __host__ __device__ inline size_t ens_fast_smem(int N) {
   return (size_t)N * (sizeof(cplx<double>) + 2 * sizeof(cplx<T>) + sizeof(T)) +
-         2 * line_buf_elems(N, 1) * sizeof(cplx<T>);
+         (2 * line_buf_elems(N, 1) + 64 + ens_tw_hi(N)) * sizeof(cplx<T>);
+}
+
+// Fills the two twiddle tables from the N-entry table tw of the line.
+template <typename T>
+__device__ __forceinline__ void ens_load_twiddles(const cplx<T> *__restrict__ tw, int N, cplx<T> *twl, cplx<T> *twh) {
+  for (int i = threadIdx.x; i < 64; i += blockDim.x) twl[i] = tw[i < N ? i : 0];
+  for (int j = threadIdx.x; j < ens_tw_hi(N); j += blockDim.x) twh[j] = tw[64 * j];
 }
 
 // One step of a 1-D member that lives in shared memory for the whole step.
@@ -178,9 +199,12 @@ __device__ void ens_step_1d(const EnsArgs<T> &a, const EnsMember &m, T field, un
   cplx<T> *prev = cur + N;
   cplx<T> *f0 = prev + N;
   cplx<T> *f1 = f0 + line_buf_elems(N, 1);
-  T *Vs = reinterpret_cast<T *>(f1 + line_buf_elems(N, 1));
-  const cplx<T> *__restrict__ tw = a.tw + m.tw_off[0];
-  const T *__restrict__ kt = a.ktab + m.kt_off[0];
+  cplx<T> *twl = f1 + line_buf_elems(N, 1);
+  cplx<T> *twh = twl + 64;
+  T *Vs = reinterpret_cast<T *>(twh + ens_tw_hi(N));
+  ens_load_twiddles<T>(a.tw + m.tw_off[0], N, twl, twh);
+  auto tw = [&](int q) { return cmul(twh[q >> 6], twl[q & 63]); };
+  const T kfT = (T)m.kf;
   cplx<double> *__restrict__ gpsi = a.psi + m.off;
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
     T v = a.V[m.off + i];
@@ -239,7 +263,11 @@ __device__ void ens_step_1d(const EnsArgs<T> &a, const EnsMember &m, T field, un
     Ns = 1;
     for (int s = 0; s < rp.nstages; ++s) {
       const bool ks = s == 0, ls = s == rp.nstages - 1;
-      auto load = [&](int i) { return ks ? cmulr(src[lpos(i)], kt[i]) : src[lpos(i)]; };
+      auto load = [&](int i) {
+        if (!ks) return src[lpos(i)];
+        const int q = min(i, N - i);
+        return cmulr(src[lpos(i)], kfT * (T)(q * q));
+      };
       if (ls) {
         stage_any<T>(rp.radix[s], load, point, N, 1, Ns, tw, +1);
       } else {
@@ -287,8 +315,6 @@ __device__ void ens_step_1d(const EnsArgs<T> &a, const EnsMember &m, T field, un
 // the series cut through the norm change of each term.  The explicit
 // round-to-nearest intrinsics keep the compiler from contracting the
 // transformations into FMAs.
-struct dfloat { float hi, lo; };
-
 __device__ __forceinline__ dfloat df_split(double x) {
   dfloat r;
   r.hi = (float)x;
@@ -326,9 +352,12 @@ __device__ void ens_step_1d_df(const EnsArgs<float> &a, const EnsMember &m, floa
   cplx<T> *prev = cur + N;
   cplx<T> *f0 = prev + N;
   cplx<T> *f1 = f0 + line_buf_elems(N, 1);
-  T *Vs = reinterpret_cast<T *>(f1 + line_buf_elems(N, 1));
-  const cplx<T> *__restrict__ tw = a.tw + m.tw_off[0];
-  const T *__restrict__ kt = a.ktab + m.kt_off[0];
+  cplx<T> *twl = f1 + line_buf_elems(N, 1);
+  cplx<T> *twh = twl + 64;
+  T *Vs = reinterpret_cast<T *>(twh + ens_tw_hi(N));
+  ens_load_twiddles<T>(a.tw + m.tw_off[0], N, twl, twh);
+  auto tw = [&](int q) { return cmul(twh[q >> 6], twl[q & 63]); };
+  const T kfT = (T)m.kf;
   cplx<double> *__restrict__ gpsi = a.psi + m.off;
   double n0 = 0.0;
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
@@ -403,7 +432,11 @@ __device__ void ens_step_1d_df(const EnsArgs<float> &a, const EnsMember &m, floa
     Ns = 1;
     for (int s = 0; s < rp.nstages; ++s) {
       const bool ks = s == 0, ls = s == rp.nstages - 1;
-      auto load = [&](int i) { return ks ? cmulr(src[lpos(i)], kt[i]) : src[lpos(i)]; };
+      auto load = [&](int i) {
+        if (!ks) return src[lpos(i)];
+        const int q = min(i, N - i);
+        return cmulr(src[lpos(i)], kfT * (T)(q * q));
+      };
       if (ls) {
         stage_any<T>(rp.radix[s], load, point, N, 1, Ns, tw, +1);
       } else {
@@ -436,6 +469,107 @@ __device__ void ens_step_1d_df(const EnsArgs<float> &a, const EnsMember &m, floa
   terms += used;
 }
 
+// Sum over the block of one double per thread, returned to every thread.
+__device__ __forceinline__ double block_sum_all(double v, double *red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  const int nw = (blockDim.x + 31) >> 5;
+  for (int w = 0; w < nw; ++w) t += red[w];
+  return t;
+}
+
+// Point work of one term for members off the resident path, mixed form:
+// psi in double-float (global), the norm change of the term per thread.
+template <bool FIRST>
+__device__ float ens_points_df(const EnsArgs<float> &a, const EnsMember &m, const cplx<float> *phi,
+                               cplx<float> *kout, float a0h, float a0l, float aih, float ail, float field) {
+  typedef float T;
+  float dn = 0.0f;
+  const cplx<T> off = ccast<T>(m.offset);
+  const cplx<T> fac = ccast<T>(FIRST ? m.fac1 : m.fac);
+  for (long long p = threadIdx.x; p < m.npts; p += blockDim.x) {
+    const long long g = m.off + p;
+    const cplx<T> x = ld(phi + g);
+    cplx<T> h = ld(a.P0 + g);
+    if (m.nd > 1) h = h + ld(a.P1 + g);
+    T v = a.V[g];
+    if (m.has_dipole) v = v + field * a.mu[g];
+    h = h + cmulr(x, v);
+    const cplx<T> bf = cmul(h - cmul(off, x), fac);
+    dfloat pr = a.dfr[g], pi = a.dfi[g];
+    if (FIRST) {
+      st(kout + g, bf);
+      dfloat qr = {0.0f, 0.0f}, qi = {0.0f, 0.0f};
+      df_axpy(qr, a0h, a0l, pr.hi);
+      df_axpy(qr, a0h, a0l, pr.lo);
+      df_axpy(qi, a0h, a0l, pi.hi);
+      df_axpy(qi, a0h, a0l, pi.lo);
+      df_axpy(qr, aih, ail, bf.re);
+      df_axpy(qi, aih, ail, bf.im);
+      pr = qr;
+      pi = qi;
+    } else {
+      const cplx<T> k2 = bf + ld(kout + g);
+      st(kout + g, k2);
+      const float tr = aih * k2.re, ti = aih * k2.im;
+      dn = fmaf(2.0f * pr.hi + tr, tr, fmaf(2.0f * pi.hi + ti, ti, dn));
+      df_axpy(pr, aih, ail, k2.re);
+      df_axpy(pi, aih, ail, k2.im);
+    }
+    a.dfr[g] = pr;
+    a.dfi[g] = pi;
+  }
+  return dn;
+}
+
+// One step of a member off the resident path, mixed form (see ens_step_1d_df
+// for the series cut).
+__device__ void ens_step_df(const EnsArgs<float> &a, const EnsMember &m, float field, cplx<float> *smem,
+                            double *red, long long &terms, int &status) {
+  cplx<double> *__restrict__ psi = a.psi + m.off;
+  double n0 = 0.0;
+  for (long long p = threadIdx.x; p < m.npts; p += blockDim.x) {
+    const cplx<double> ps = ld(psi + p);
+    a.dfr[m.off + p] = df_split(ps.re);
+    a.dfi[m.off + p] = df_split(ps.im);
+    st(a.buf0 + m.off + p, ccast<float>(ps));
+    n0 += cabs2(ps);
+  }
+  const double norm0 = block_sum_all(n0, red);
+  bool done = !isfinite(norm0);
+  if (done) status = 2;
+  const double a0 = a.coef[m.coef_off], a1 = a.coef[m.coef_off + 1];
+  const float a0h = (float)a0, a0l = (float)(a0 - (double)a0h);
+  const float a1h = (float)a1, a1l = (float)(a1 - (double)a1h);
+  int used = 2;
+  if (!done) {
+    ens_kinetic<float>(a, m, a.buf0, smem);
+    ens_points_df<true>(a, m, a.buf0, a.buf1, a0h, a0l, a1h, a1l, field);
+  }
+  // phi_{i-1} in buf[(i+1)&1], phi_{i-2} in buf[i&1] (overwritten by phi_i)
+  for (int i = 2; i < m.order && !done; ++i) {
+    cplx<float> *phi = (i & 1) ? a.buf0 : a.buf1;
+    cplx<float> *kout = (i & 1) ? a.buf1 : a.buf0;
+    ens_kinetic<float>(a, m, phi, smem);
+    const double ai = a.coef[m.coef_off + i];
+    const float aih = (float)ai, ail = (float)(ai - (double)aih);
+    const double delta = block_sum_all((double)ens_points_df<false>(a, m, phi, kout, 0.f, 0.f, aih, ail, field), red);
+    used = i + 1;
+    if (!isfinite(delta)) { done = true; status = 2; }
+    else if (fabs(delta) / norm0 < m.prec && m.offset.im == 0.0) done = true;  // OCheby.cpp:179-182
+  }
+  __syncthreads();
+  for (long long p = threadIdx.x; p < m.npts; p += blockDim.x) {
+    const dfloat pr = a.dfr[m.off + p], pi = a.dfi[m.off + p];
+    st(psi + p, cmul(mk((double)pr.hi + (double)pr.lo, (double)pi.hi + (double)pi.lo), m.ph));
+  }
+  __syncthreads();
+  terms += used;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) ensemble_kernel(EnsArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -450,6 +584,7 @@ __global__ void __launch_bounds__(256) ensemble_kernel(EnsArgs<T> a) {
     if (cur >= a.n) return;
     const int mi = a.order[cur];
     const EnsMember m = a.m[mi];
+    if (threadIdx.x == 0) { a.tl[3 * mi] = ens_clock(); a.tl[3 * mi + 2] = blockIdx.x; }
     long long terms = 0;
     int status = 0;
     for (int k = 0; k < a.nsteps; ++k) {
@@ -460,6 +595,10 @@ __global__ void __launch_bounds__(256) ensemble_kernel(EnsArgs<T> a) {
       if (m.nd == 1 && m.fast) {
         if constexpr (sizeof(T) == sizeof(float)) ens_step_1d_df(a, m, field, smem_raw, red, terms, status);
         else ens_step_1d<T>(a, m, field, smem_raw, red, terms, status);
+        continue;
+      }
+      if constexpr (sizeof(T) == sizeof(float)) {
+        ens_step_df(a, m, field, smem, red, terms, status);
         continue;
       }
       for (long long p = threadIdx.x; p < m.npts; p += blockDim.x)
@@ -497,6 +636,7 @@ __global__ void __launch_bounds__(256) ensemble_kernel(EnsArgs<T> a) {
     if (threadIdx.x == 0) {
       a.terms[mi] += terms;
       if (status) a.status[mi] = status;
+      a.tl[3 * mi + 1] = ens_clock();
     }
   }
 }
@@ -530,6 +670,8 @@ struct qdg_ensemble {
   long long *d_terms = nullptr;
   cplx<double> *d_psi = nullptr;
   void *d_buf0 = nullptr, *d_buf1 = nullptr, *d_P0 = nullptr, *d_P1 = nullptr;
+  void *d_dfr = nullptr, *d_dfi = nullptr;  // mixed form: double-float psi of a step
+  unsigned long long *d_tl = nullptr;       // per member start, end, block of the last run
   void *d_V = nullptr, *d_mu = nullptr, *d_tw = nullptr, *d_kt = nullptr;
   double *d_lasers = nullptr, *d_coef = nullptr;
   size_t smem = 0;
@@ -589,12 +731,16 @@ qdg_status upload_vec(void **dst, const std::vector<T> &v) {
 
 void free_ensemble(qdg_ensemble *e) {
   void *ps[] = {e->d_m, e->d_order, e->d_queue, e->d_status, e->d_terms, e->d_psi, e->d_buf0, e->d_buf1, e->d_P0,
-                e->d_P1, e->d_V, e->d_mu, e->d_tw, e->d_kt, e->d_lasers, e->d_coef};
+                e->d_P1, e->d_V, e->d_mu, e->d_tw, e->d_kt, e->d_lasers, e->d_coef, e->d_dfr, e->d_dfi, e->d_tl};
   for (void *p : ps)
     if (p) cudaFree(p);
   if (e->stream) cudaStreamDestroy(e->stream);
   delete e;
 }
+
+// Time per point and term of a member off the resident path relative to one
+// on it (one block each, measured on GB300 over the workload's sizes).
+constexpr double kOffResidentCost = 2.0;
 
 template <typename T>
 qdg_status build(qdg_ensemble *e, const qdg_ensemble_member *mem, const std::map<std::string, std::string> &params) {
@@ -640,6 +786,7 @@ qdg_status build(qdg_ensemble *e, const qdg_ensemble_member *mem, const std::map
       m.tw_off[d] = tw_at[N];
       m.kt_off[d] = (long long)kt.size();
       const double kf = dk[d] * dk[d] / (2.0 * x.mass[d]) / N;
+      if (d == 0) m.kf = kf;
       for (int i = 0; i < N; ++i) {
         const double q = std::min(i, N - i);
         kt.push_back((T)(kf * q * q));
@@ -687,7 +834,12 @@ qdg_status build(qdg_ensemble *e, const qdg_ensemble_member *mem, const std::map
     m.fac.re = f.real(); m.fac.im = f.imag();
     m.ph.re = ph.real(); m.ph.im = ph.imag();
     m.prec = cs.prec;
-    cost[k] = (double)m.npts * std::log2((double)m.npts + 1) * cs.order;
+    // LPT cost: the series needs about R = scaling dt terms (J_n(R) is
+    // negligible beyond R + O(R^{1/3})), each about npts log npts of work;
+    // members off the resident path run slower per point (global memory)
+    const double R = cs.scaling * e->dt;
+    const double est = std::min<double>(cs.order, R + 4.0 * std::cbrt(R) + 10.0);
+    cost[k] = (double)m.npts * std::log2((double)m.npts + 1) * est * (m.fast ? 1.0 : kOffResidentCost);
     e->hm.push_back(m);
   }
   e->total_pts = off;
@@ -711,12 +863,18 @@ qdg_status build(qdg_ensemble *e, const qdg_ensemble_member *mem, const std::map
   ECK(cudaMemset(e->d_psi, 0, sizeof(cplx<double>) * pts));
   ECK(cudaMalloc(&e->d_buf0, sizeof(cplx<T>) * pts));
   ECK(cudaMalloc(&e->d_buf1, sizeof(cplx<T>) * pts));
+  if (sizeof(T) == sizeof(float)) {
+    ECK(cudaMalloc(&e->d_dfr, sizeof(qdg::dfloat) * pts));
+    ECK(cudaMalloc(&e->d_dfi, sizeof(qdg::dfloat) * pts));
+  }
   ECK(cudaMalloc(&e->d_P0, sizeof(cplx<T>) * pts));
   ECK(cudaMalloc(&e->d_P1, sizeof(cplx<T>) * pts));
   ECK(cudaMalloc(&e->d_queue, sizeof(int)));
   ECK(cudaMalloc(&e->d_status, sizeof(int) * n));
   ECK(cudaMemset(e->d_status, 0, sizeof(int) * n));
   ECK(cudaMalloc(&e->d_terms, sizeof(long long) * n));
+  ECK(cudaMalloc(&e->d_tl, sizeof(unsigned long long) * 3 * n));
+  ECK(cudaMemset(e->d_tl, 0, sizeof(unsigned long long) * 3 * n));
   ECK(cudaMemset(e->d_terms, 0, sizeof(long long) * n));
   const int occ = qdg::ensemble_occupancy<T>(smem);
   if (occ <= 0) return efail(QDG_EUNSUPPORTED, "ensemble kernel cannot be resident");
@@ -752,6 +910,9 @@ qdg_status run(qdg_ensemble *e, long long step0, int nsteps) {
   a.diff = e->precision == QDG_PREC_MIXED ? 1 : 0;
   a.terms = e->d_terms;
   a.status = e->d_status;
+  a.dfr = reinterpret_cast<qdg::dfloat *>(e->d_dfr);
+  a.tl = e->d_tl;
+  a.dfi = reinterpret_cast<qdg::dfloat *>(e->d_dfi);
   ECK(cudaMemsetAsync(e->d_queue, 0, sizeof(int), e->stream));
   void *k = (void *)qdg::ensemble_kernel<T>;
   if (e->smem > 48 * 1024) ECK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smem));
@@ -823,6 +984,20 @@ qdg_status qdg_ensemble_run(qdg_ensemble *e, int64_t step0, int32_t nsteps, int6
   if (terms_total) *terms_total = tot;
   for (int i = 0; i < e->n; ++i)
     if (st[i]) return efail(QDG_ENONFINITE, "Norm is not a number (ensemble member " + std::to_string(i) + ")");
+  return QDG_OK;
+}
+
+qdg_status qdg_ensemble_timeline(const qdg_ensemble *e, int64_t *start_end, int32_t *block) {
+  if (!e || !start_end) return efail(QDG_EINVAL, "null argument");
+  std::vector<unsigned long long> t(3 * (size_t)e->n);
+  ECK(cudaMemcpy(t.data(), e->d_tl, sizeof(unsigned long long) * t.size(), cudaMemcpyDeviceToHost));
+  unsigned long long t0 = ~0ULL;
+  for (int i = 0; i < e->n; ++i) t0 = std::min(t0, t[3 * i]);
+  for (int i = 0; i < e->n; ++i) {
+    start_end[2 * i] = (int64_t)(t[3 * i] - t0);
+    start_end[2 * i + 1] = (int64_t)(t[3 * i + 1] - t0);
+    if (block) block[i] = (int32_t)t[3 * i + 2];
+  }
   return QDG_OK;
 }
 

@@ -243,6 +243,14 @@ class Ensemble:
         check(self.lib.qdg_ensemble_run(self.h, step0, nsteps, C.byref(t)))
         return t.value
 
+    def timeline(self):
+        """(start, end) in ns of every member in the last run, and the block that ran it."""
+        n = len(self.members)
+        se = np.zeros(2 * n, dtype=np.int64)
+        blk = np.zeros(n, dtype=np.int32)
+        check(self.lib.qdg_ensemble_timeline(self.h, se.ctypes.data_as(C.c_void_p), blk.ctypes.data_as(C.c_void_p)))
+        return se.reshape(-1, 2), blk
+
     def info(self, i):
         inf = abi.PropInfo()
         check(self.lib.qdg_ensemble_member_info(self.h, i, C.byref(inf)))
