@@ -104,12 +104,28 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def workload(precision):
+WORKLOADS = {
+    # name: (builder, description, coupling grids C, dipole grids D)
+    "cfg2": ("cfg2_two_state", "cfg2 two-state 2-D Chebyshev, 256x256 grid x 2 states, dt=5 a.u.", 1, 0),
+    "cfg1": ("cfg1_morse", "cfg1 1-D Morse Chebyshev, 1024 points, dt=10 a.u.", 0, 0),
+    "cfg3": ("cfg3_anharmonic", "cfg3 3-D anharmonic Chebyshev, 128^3 grid, dt=10 a.u.", 0, 0),
+    "cfg5sil": ("cfg5_double_well", "cfg5 2-D double well, 128x128, real-time SIL (Krylov 16), dt=20 a.u.", 0, 0),
+    "cfg5arnoldi": ("cfg5_double_well", "cfg5 2-D double well, 128x128, real-time Arnoldi (Krylov 16), dt=20 a.u.",
+                    0, 0),
+}
+
+
+def workload(precision, name="cfg2"):
     from tests import cases
-    hp, psi, run = cases.cfg2_two_state(n=256)
-    cfg = {"workload": "cfg2 two-state 2-D Chebyshev, 256x256 grid x 2 states, dt=5 a.u.",
-           "grid": [256, 256], "states": 2, "dt": 5.0, "precision": precision,
-           "l2": "flushed between timed steps (512 MB write)"}
+    builder, desc, C, D = WORKLOADS[name]
+    hp, psi, run = getattr(cases, builder)()
+    if name == "cfg5sil":
+        run = dict(run, name="SIL", params="order=16")
+    elif name == "cfg5arnoldi":
+        run = dict(run, name="Arnoldi", params="order=16")
+    cfg = {"workload": desc, "grid": list(hp.grid.n), "states": hp.nstates, "dt": run["dt"],
+           "propagator": run["name"], "precision": precision,
+           "l2": "flushed between timed steps (512 MB write)", "C": C, "D": D}
     return hp, psi, run, cfg
 
 
@@ -195,7 +211,7 @@ def engine_arm(args, world, rank, local):
     from qdng_gb300 import build, engine
 
     build.build()
-    hp, psi, run, cfg = workload(args.precision)
+    hp, psi, run, cfg = workload(args.precision, args.workload)
     torch.cuda.set_device(0)
     stream = torch.cuda.Stream()
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -256,8 +272,7 @@ def engine_arm(args, world, rank, local):
     modes = engine.PASS_MODES
     top = int(np.argmax(prof_ms[:len(modes)]))
     npts, S = hp.npts, hp.nstates
-    C = 1  # distinct off-diagonal coupling grids (V12)
-    D = 0
+    C, D = cfg.pop("C"), cfg.pop("D")  # distinct off-diagonal coupling and dipole grids
     peak, peak_src = read_peak()
     roof = None
     if prof_n[top] > 0:
@@ -318,11 +333,11 @@ def engine_arm(args, world, rank, local):
     if rank == 0 and world == 1 and not args.no_cpu:
         v, threads, n, dt = cpu_reference(hp, psi, run, steps=10 ** 6, warmup=1, budget_s=args.cpu_budget)
         cpu = {"value": round(v, 1), "unit": "grid-pt*steps/s", "cores": threads, "kind": "port",
-               "sample": f"{n} Chebyshev steps of the same 256x256x2 workload in {dt:.1f} s "
-                         f"(oracle restatement of OCheby, OpenMP FFT lines)"}
+               "sample": f"{n} {run['name']} steps of the same workload in {dt:.1f} s "
+                         f"(oracle restatement of the QDng propagator, OpenMP FFT lines)"}
 
     line = {
-        "metric": "grid-pt*steps/s (Chebyshev, 256^2 x 2 states)",
+        "metric": "grid-pt*steps/s" + (" (Chebyshev, 256^2 x 2 states)" if args.workload == "cfg2" else ""),
         "value": round(value, 1),
         "unit": "grid-pt*steps/s",
         "n_gpus": world,
@@ -436,10 +451,11 @@ def ensemble_arm(args, world, rank, local):
 def reference_arm(args, world, rank):
     if rank != 0:
         return
-    hp, psi, run, cfg = workload("fp64")
+    hp, psi, run, cfg = workload("fp64", args.workload if args.workload != "ensemble" else "cfg2")
+    cfg.pop("C"), cfg.pop("D")
     v, threads, n, dt = cpu_reference(hp, psi, run, steps=args.steps, warmup=args.warmup)
     line = {
-        "metric": "grid-pt*steps/s (Chebyshev, 256^2 x 2 states)",
+        "metric": "grid-pt*steps/s" + (" (Chebyshev, 256^2 x 2 states)" if cfg["workload"].startswith("cfg2") else ""),
         "value": round(v, 1),
         "unit": "grid-pt*steps/s",
         "n_gpus": world,
@@ -454,9 +470,9 @@ def reference_arm(args, world, rank):
         "config": dict(cfg, l2="n/a (host)"),
         "impl": "reference",
         "cpu_baseline": {"value": round(v, 1), "unit": "grid-pt*steps/s", "cores": threads, "kind": "port",
-                         "sample": f"{n} Chebyshev steps of the 256x256x2 workload on {threads} host threads "
+                         "sample": f"{n} {run['name']} steps of the workload on {threads} host threads "
                                    "(QDng is not buildable here: FFTW/LAPACK/SLATEC/protobuf missing; "
-                                   "the oracle restatement of OCheby stands in)"},
+                                   "the oracle restatement of the propagator stands in)"},
         "e2e": {"value": round(v, 1), "unit": "grid-pt*steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -473,7 +489,7 @@ def main():
                     help="steps of the mixed-vs-FP64 observable comparison (0: skip)")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "ensemble"])
+    ap.add_argument("--workload", default="cfg2", choices=list(WORKLOADS) + ["ensemble"])
     ap.add_argument("--members", type=int, default=512)
     args = ap.parse_args()
     if args.warmup < 3:
