@@ -1724,11 +1724,19 @@ qdg_status qdg_prop_create(qdg_plan *plan, const char *name, const char *params,
     if (has(P, "err")) P->err = parse_d(P, "err");
     if (has(P, "conv")) P->conv = parse_d(P, "conv");
   }
-  if (P->kind == 1 && P->imag && plan->precision == QDG_PREC_MIXED) {
-    // The imaginary-time series (scaled I_n, OCheby.cpp:427-433) reaches the
-    // low states through cancellations of terms ~1/sqrt(2 pi R) down to
-    // e^{-R (1 - X)}; FP32 phi cannot carry that, so this propagator runs on
-    // an FP64 copy of the plan (same host data, the caller's stream).
+  // Propagators that FP32 H phi cannot carry run on an FP64 copy of a mixed
+  // plan (same host data, the caller's stream):
+  // * imaginary-time Chebyshev: its scaled-I_n series (OCheby.cpp:427-433)
+  //   reaches the low states through cancellations of terms ~1/sqrt(2 pi R)
+  //   down to e^{-R (1 - X)}, far below FP32 resolution;
+  // * Lanczos / Arnoldi: each new basis vector is (H q - alpha q - beta q')/beta,
+  //   so the FP32 error of H q (~1e-7 of the spectral range) is amplified by
+  //   range/beta, and the energies it perturbs turn into a phase error that
+  //   grows with the propagation time (6e-4 in the autocorrelation after
+  //   2000 a.u. on the 128^2 double well).  The parameter krylov_fp32=1 keeps
+  //   the FP32 basis (about 1.2x faster there).
+  const bool krylov_twin = P->kind >= 3 && !(has(P, "krylov_fp32") && atoi(P->params["krylov_fp32"].c_str()) != 0);
+  if (plan->precision == QDG_PREC_MIXED && ((P->kind == 1 && P->imag) || krylov_twin)) {
     qdg_hplan_desc d;
     memset(&d, 0, sizeof(d));
     d.grid = plan->grid;
