@@ -180,6 +180,10 @@ struct qdg_prop {
   int kord = 20, aorder = 0;
   double err = 1e-12, conv = 1e-12;
   std::vector<void *> lzb;
+  double *d_ks = nullptr;   // Lanczos scalars on the device: alpha, beta, |psi|, order reached
+  double *h_ks = nullptr;   // pinned copy read by the host after the step
+  int *h_kdone = nullptr;
+  int *d_kdone = nullptr;   // [0]: stop the step's remaining kernels, [1]: error estimate reached
   void *kbuf = nullptr;
   void *kwide = nullptr;  // FP64 copy of one basis vector (mixed precision)
 };
@@ -1170,6 +1174,10 @@ qdg_status krylov_alloc(qdg_prop *P) {
   P->lzb.assign(P->kord + 1, nullptr);
   for (auto &v : P->lzb) CK(cudaMalloc(&v, sizeof(cplx<T>) * wf_elems(p)));
   CK(cudaMalloc(&P->kbuf, sizeof(cplx<T>) * wf_elems(p)));
+  CK(cudaMalloc(&P->d_ks, sizeof(double) * (2 * (size_t)P->kord + 2)));
+  CK(cudaMalloc(&P->d_kdone, 2 * sizeof(int)));
+  CK(cudaMallocHost(&P->h_ks, sizeof(double) * (2 * (size_t)P->kord + 2)));
+  CK(cudaMallocHost(&P->h_kdone, sizeof(int)));
   if (sizeof(T) != sizeof(double)) CK(cudaMalloc(&P->kwide, sizeof(cplx<double>) * wf_elems(p)));
   return QDG_OK;
 }
@@ -1182,72 +1190,143 @@ qdg_status hq(qdg_prop *P, const cplx<T> *q, cplx<T> *out, long long step) {
 }
 
 // OSIL::BuildLZB / DiagLZB (src/qdlib/OSIL.cpp:83-185), FP64 scalars.
+// The Lanczos recursion runs with its scalars on the device: every dot
+// product is finished by a one-thread kernel into P->d_ks (in the order the
+// host used to sum it), the basis updates read their coefficient from there,
+// and the reference's error estimate sets a flag that turns the remaining
+// kernels of the step into no-ops.  The host reads alpha, beta and the order
+// once per step for the tridiagonal eigenproblem.
+// The recursion of one step as a fixed sequence of launches (captured once
+// in a CUDA graph per psi buffer); results land in the pinned P->h_ks.
 template <typename T>
-qdg_status sil_step(qdg_prop *P, cplx<double> *psi, long long step, int *used) {
+qdg_status sil_body(qdg_prop *P, cplx<double> *psi) {
   qdg_plan *p = P->plan;
   const long long n = wf_elems(p);
   const int order = P->kord;
   std::vector<cplx<T> *> L(order);
   for (int i = 0; i < order; ++i) L[i] = reinterpret_cast<cplx<T> *>(P->lzb[i]);
   cplx<T> *buf0 = reinterpret_cast<cplx<T> *>(P->kbuf);
-  std::vector<double> alpha(order, 0.0), beta(order, 0.0);
-  std::vector<cd> d;
+  double *ks = P->d_ks;
+  int *done = P->d_kdone;
+  const int grid = dots_grid(p);
+  double w = 1.0;
+  for (int d = 0; d < p->nd; ++d) w *= p->dx[d];
+  auto finish = [&](int mode, int slot, int it) {
+    qdg::KsFinish f;
+    f.grid = grid; f.S = p->S; f.mode = mode; f.slot = slot; f.order = order; f.w = w;
+    f.it = it; f.dt = P->dt; f.tol = P->err;
+    return qdg::launch_ks_finish(p->d_partials, f, ks, done, p->stream);
+  };
+  Epi e;
+  e.done = done;
+  auto hq_if = [&](const cplx<T> *q, cplx<T> *out) {
+    e.out = out;
+    return run_h<T>(p, qdg::PM_HAPPLY, q, e);
+  };
   qdg_status s;
-  CK(qdg::launch_set_coefs(p->d_coef, p->d_cp, p->d_lasers, p->laser_nt, step, p->stream));
-  if ((s = dots<double, double>(p, psi, psi, d)) != QDG_OK) return s;
-  const double psinorm = std::sqrt(total(d).real());
+  CK(cudaMemsetAsync(ks, 0, sizeof(double) * (2 * order + 2), p->stream));
+  CK(cudaMemsetAsync(done, 0, 2 * sizeof(int), p->stream));
+  CK(qdg::launch_dots_if<double, double>(psi, psi, p->S, p->npts, p->d_partials, grid, done, p->stream));
+  CK(finish(qdg::KS_PSN, 2 * order, 0));
   CK(qdg::launch_convert<T>(L[0], psi, n, p->stream));
-  if ((s = hq<T>(P, L[0], buf0, step)) != QDG_OK) return s;
-  if ((s = dots<T, T>(p, L[0], buf0, d)) != QDG_OK) return s;
-  alpha[0] = total(d).real();
+  if ((s = hq_if(L[0], buf0)) != QDG_OK) return s;
+  CK(qdg::launch_dots_if<T, T>(L[0], buf0, p->S, p->npts, p->d_partials, grid, done, p->stream));
+  CK(finish(qdg::KS_ALPHA, 0, 0));
   CK(cudaMemcpyAsync(L[1], buf0, sizeof(cplx<T>) * n, cudaMemcpyDeviceToDevice, p->stream));
-  CK(qdg::launch_lincomb<T>(L[1], L[0], cplx<double>{1.0, 0.0}, cplx<double>{-alpha[0], 0.0}, n, p->stream));
-  if ((s = dots<T, T>(p, L[1], L[1], d)) != QDG_OK) return s;
-  beta[0] = std::sqrt(total(d).real());
-  CK(qdg::launch_lincomb<T>(L[1], (const cplx<T> *)nullptr, cplx<double>{1.0 / beta[0], 0.0}, cplx<double>{0, 0}, n, p->stream));
-  int convorder = 2, it;
-  for (it = 2; it < order; ++it) {
-    double err = std::pow(P->dt, it - 2) * beta[0];
-    for (int i = 1; i < it - 2; ++i) err *= beta[i] / double(i);
-    err = std::fabs(err);
-    convorder++;
-    if ((s = hq<T>(P, L[it - 1], L[it], step)) != QDG_OK) return s;
-    if ((s = dots<T, T>(p, L[it - 1], L[it], d)) != QDG_OK) return s;
-    alpha[it - 1] = total(d).real();
-    CK(qdg::launch_lincomb<T>(L[it], L[it - 1], cplx<double>{1, 0}, cplx<double>{-alpha[it - 1], 0}, n, p->stream));
-    CK(qdg::launch_lincomb<T>(L[it], L[it - 2], cplx<double>{1, 0}, cplx<double>{-beta[it - 2], 0}, n, p->stream));
-    if ((s = dots<T, T>(p, L[it], L[it], d)) != QDG_OK) return s;
-    beta[it - 1] = std::sqrt(total(d).real());
-    CK(qdg::launch_lincomb<T>(L[it], (const cplx<T> *)nullptr, cplx<double>{1.0 / beta[it - 1], 0}, cplx<double>{0, 0}, n, p->stream));
-    if (err < P->err * psinorm) break;
+  CK(qdg::launch_ks_lincomb<T>(L[1], L[0], ks, 0, n, done, p->stream));
+  CK(qdg::launch_dots_if<T, T>(L[1], L[1], p->S, p->npts, p->d_partials, grid, done, p->stream));
+  CK(finish(qdg::KS_BETA, order + 0, 0));
+  CK(qdg::launch_ks_lincomb<T>(L[1], (const cplx<T> *)nullptr, ks, order + 0, n, done, p->stream));
+  for (int it = 2; it < order; ++it) {
+    if ((s = hq_if(L[it - 1], L[it])) != QDG_OK) return s;
+    CK(qdg::launch_dots_if<T, T>(L[it - 1], L[it], p->S, p->npts, p->d_partials, grid, done, p->stream));
+    CK(finish(qdg::KS_ALPHA, it - 1, it));
+    CK(qdg::launch_ks_lincomb<T>(L[it], L[it - 1], ks, it - 1, n, done, p->stream));
+    CK(qdg::launch_ks_lincomb<T>(L[it], L[it - 2], ks, order + it - 2, n, done, p->stream));
+    CK(qdg::launch_dots_if<T, T>(L[it], L[it], p->S, p->npts, p->d_partials, grid, done, p->stream));
+    CK(finish(qdg::KS_BETA, order + it - 1, it));
+    CK(qdg::launch_ks_lincomb<T>(L[it], (const cplx<T> *)nullptr, ks, order + it - 1, n, done, p->stream));
+    CK(qdg::launch_ks_commit(done, p->stream));
   }
-  if (it == order) {  // alpha of the last vector (the break case recomputes an identical value)
-    if ((s = hq<T>(P, L[it - 1], buf0, step)) != QDG_OK) return s;
-    if ((s = dots<T, T>(p, L[it - 1], buf0, d)) != QDG_OK) return s;
-    alpha[it - 1] = total(d).real();
+  // alpha of the last vector when the recursion ran to the full order
+  if ((s = hq_if(L[order - 1], buf0)) != QDG_OK) return s;
+  CK(qdg::launch_dots_if<T, T>(L[order - 1], buf0, p->S, p->npts, p->d_partials, grid, done, p->stream));
+  CK(finish(qdg::KS_ALPHA, order - 1, order));
+  CK(cudaMemcpyAsync(P->h_ks, ks, sizeof(double) * (2 * order + 2), cudaMemcpyDeviceToHost, p->stream));
+  CK(cudaMemcpyAsync(P->h_kdone, done, sizeof(int), cudaMemcpyDeviceToHost, p->stream));
+  return QDG_OK;
+}
+
+template <typename T>
+qdg_status sil_enqueue(qdg_prop *P, cplx<double> *psi) {
+  qdg_plan *p = P->plan;
+  if (p->profiling || !P->graphs_ok) return sil_body<T>(P, psi);
+  if (!P->graph || P->graph_psi != psi || P->graph_stream != p->stream) {
+    if (P->graph) { cudaGraphExecDestroy(P->graph); P->graph = nullptr; }
+    cudaGraph_t g = nullptr;
+    const long long l0 = qdg::launch_counter();
+    CK(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeRelaxed));
+    qdg_status s = sil_body<T>(P, psi);
+    cudaError_t ce = cudaStreamEndCapture(p->stream, &g);
+    const long long l1 = qdg::launch_counter();
+    qdg::add_launches(-(l1 - l0));
+    if (s != QDG_OK) { if (g) cudaGraphDestroy(g); return s; }
+    if (ce != cudaSuccess || cudaGraphInstantiate(&P->graph, g, 0) != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+      P->graphs_ok = false;
+      P->graph = nullptr;
+      return sil_body<T>(P, psi);
+    }
+    cudaGraphDestroy(g);
+    P->graph_launches = l1 - l0;
+    P->graph_psi = psi;
+    P->graph_stream = p->stream;
   }
+  CK(cudaGraphLaunch(P->graph, p->stream));
+  qdg::add_launches(P->graph_launches);
+  return QDG_OK;
+}
+
+// OSIL::BuildLZB / DiagLZB (src/qdlib/OSIL.cpp:83-185), FP64 scalars.
+// The Lanczos recursion runs with its scalars on the device: every dot
+// product is finished by a one-thread kernel into P->d_ks (in the order the
+// host used to sum it), the basis updates read their coefficient from there,
+// and the reference's error estimate sets a flag that turns the remaining
+// kernels of the step into no-ops.  The host reads alpha, beta and the order
+// once per step for the tridiagonal eigenproblem.
+template <typename T>
+qdg_status sil_step(qdg_prop *P, cplx<double> *psi, long long step, int *used) {
+  qdg_plan *p = P->plan;
+  const long long n = wf_elems(p);
+  const int order = P->kord;
+  if (order > qdg::kMaxKrylov) return fail(QDG_EUNSUPPORTED, "Krylov order above 64");
+  CK(qdg::launch_set_coefs(p->d_coef, p->d_cp, p->d_lasers, p->laser_nt, step, p->stream));
+  qdg_status s = sil_enqueue<T>(P, psi);
+  if (s != QDG_OK) return s;
+  CK(cudaStreamSynchronize(p->stream));
+  const double *hks = P->h_ks;
+  const int convorder = *P->h_kdone ? (int)hks[2 * order + 1] : order;
+  if (!std::isfinite(hks[2 * order])) return fail(QDG_ENONFINITE, "Norm is not a number");
   // Z exp(c0 Lambda) Z^T e0 of the full order x order tridiagonal matrix (LapackDiag dstev)
-  std::vector<double> Tm((size_t)order * order, 0.0), w, z;
-  for (int i = 0; i < order; ++i) Tm[(size_t)i * order + i] = alpha[i];
-  for (int i = 0; i + 1 < order; ++i) { Tm[(size_t)i * order + i + 1] = beta[i]; Tm[(size_t)(i + 1) * order + i] = beta[i]; }
-  qdg::host::sym_eig(order, Tm, w, z);
-  std::vector<cd> vect(order);
+  std::vector<double> Tm((size_t)order * order, 0.0), wv, z;
+  for (int i = 0; i < order; ++i) Tm[(size_t)i * order + i] = hks[i];
+  for (int i = 0; i + 1 < order; ++i) {
+    Tm[(size_t)i * order + i + 1] = hks[order + i];
+    Tm[(size_t)(i + 1) * order + i] = hks[order + i];
+  }
+  qdg::host::sym_eig(order, Tm, wv, z);
+  // psi = vect[0] psi + sum_i vect[i] q_i, accumulated in FP64
+  qdg::KCombine<T> kc;
+  memset(&kc, 0, sizeof(kc));
+  kc.m = convorder;
   for (int i = 0; i < order; ++i) {
     cd acc = 0;
-    for (int k = 0; k < order; ++k) acc += z[(size_t)i * order + k] * z[k] * std::exp(P->c0 * w[k]);
-    vect[i] = acc;
+    for (int k = 0; k < order; ++k) acc += z[(size_t)i * order + k] * z[k] * std::exp(P->c0 * wv[k]);
+    if (i < convorder) kc.c[i] = C(acc);
+    kc.q[i] = reinterpret_cast<const cplx<T> *>(P->lzb[i]);
   }
-  // psi = vect[0] psi + sum_i vect[i] q_i, accumulated in FP64
-  CK(qdg::launch_lincomb<double>(psi, (const cplx<double> *)nullptr, C(vect[0]), cplx<double>{0, 0}, n, p->stream));
-  for (int i = 1; i < convorder; ++i) {
-    if (sizeof(T) == sizeof(double)) {
-      CK(qdg::launch_lincomb<double>(psi, reinterpret_cast<const cplx<double> *>(L[i]), cplx<double>{1, 0}, C(vect[i]), n, p->stream));
-    } else {
-      cplx<double> *wide = reinterpret_cast<cplx<double> *>(P->kwide);
-      CK(qdg::launch_widen<T>(wide, L[i], n, p->stream));
-      CK(qdg::launch_lincomb<double>(psi, wide, cplx<double>{1, 0}, C(vect[i]), n, p->stream));
-    }
-  }
+  CK(qdg::launch_kcombine<T>(psi, kc, n, p->stream));
   if (used) *used = convorder;
   return QDG_OK;
 }
@@ -1778,6 +1857,10 @@ qdg_status qdg_prop_destroy(qdg_prop *P) {
   for (auto v : P->gcoef_d) if (v) cudaFree(v);
   for (auto v : P->lzb) if (v) cudaFree(v);
   if (P->kbuf) cudaFree(P->kbuf);
+  if (P->d_ks) cudaFree(P->d_ks);
+  if (P->d_kdone) cudaFree(P->d_kdone);
+  if (P->h_ks) cudaFreeHost(P->h_ks);
+  if (P->h_kdone) cudaFreeHost(P->h_kdone);
   if (P->kwide) cudaFree(P->kwide);
   if (P->twin) {
     if (P->twin->own_stream) cudaStreamDestroy(P->twin->stream);

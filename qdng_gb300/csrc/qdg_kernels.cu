@@ -636,8 +636,10 @@ template cudaError_t launch_lincomb<float>(cplx<float> *, const cplx<float> *, c
 
 // Per-state sum conj(a) b, FP64 accumulation, fixed reduction order.
 template <typename T, typename U>
-__global__ void dots_kernel(const cplx<T> *a, const cplx<U> *b, int S, long long npts, double *partials) {
+__global__ void dots_kernel(const cplx<T> *a, const cplx<U> *b, int S, long long npts, double *partials,
+                            const int *done) {
   __shared__ double red[32];
+  if (done != nullptr && *done) return;
   for (int s = 0; s < S; ++s) {
     double re = 0, im = 0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npts;
@@ -658,10 +660,110 @@ __global__ void dots_kernel(const cplx<T> *a, const cplx<U> *b, int S, long long
 template <typename T, typename U>
 cudaError_t launch_dots(const cplx<T> *a, const cplx<U> *b, int S, long long npts, double *partials, int grid,
                         cudaStream_t st) {
-  dots_kernel<T, U><<<grid, 256, 0, st>>>(a, b, S, npts, partials);
+  dots_kernel<T, U><<<grid, 256, 0, st>>>(a, b, S, npts, partials, nullptr);
   COUNT_LAUNCH();
   return cudaGetLastError();
 }
+template <typename T, typename U>
+cudaError_t launch_dots_if(const cplx<T> *a, const cplx<U> *b, int S, long long npts, double *partials, int grid,
+                           const int *done, cudaStream_t st) {
+  dots_kernel<T, U><<<grid, 256, 0, st>>>(a, b, S, npts, partials, done);
+  COUNT_LAUNCH();
+  return cudaGetLastError();
+}
+template cudaError_t launch_dots_if<double, double>(const cplx<double> *, const cplx<double> *, int, long long,
+                                                    double *, int, const int *, cudaStream_t);
+template cudaError_t launch_dots_if<float, float>(const cplx<float> *, const cplx<float> *, int, long long, double *,
+                                                  int, const int *, cudaStream_t);
+
+// Partial sums -> scalar, summed in the order of the host's dot products
+// (blocks outer, states inner; states weighted, then added in order).
+__global__ void ks_finish_kernel(const double *partials, KsFinish f, double *ks, int *done) {
+  if (threadIdx.x != 0 || *done) return;
+  double re[kMaxStates], im[kMaxStates];
+  for (int s = 0; s < f.S; ++s) re[s] = im[s] = 0.0;
+  for (int b = 0; b < f.grid; ++b)
+    for (int s = 0; s < f.S; ++s) {
+      re[s] += partials[(b * f.S + s) * 2];
+      im[s] += partials[(b * f.S + s) * 2 + 1];
+    }
+  double tr = 0.0;
+  for (int s = 0; s < f.S; ++s) tr += re[s] * f.w;
+  if (f.mode == KS_ALPHA) {
+    ks[f.slot] = tr;
+    return;
+  }
+  const double v = sqrt(tr);
+  ks[f.slot] = v;
+  if (f.mode != KS_BETA || f.it < 2) return;
+  // OSIL::BuildLZB error estimate (src/qdlib/OSIL.cpp:106-112), tested after the iteration
+  const double *beta = ks + f.order;
+  double err = pow(f.dt, (double)(f.it - 2)) * beta[0];
+  for (int i = 1; i < f.it - 2; ++i) err *= beta[i] / double(i);
+  err = fabs(err);
+  if (err < f.tol * ks[2 * f.order]) {  // ks[2 order] = |psi|
+    done[1] = 1;                          // stop after this iteration's normalisation
+    ks[2 * f.order + 1] = (double)(f.it + 1);
+  }
+}
+
+__global__ void ks_commit_kernel(int *done) {
+  if (threadIdx.x == 0 && done[1]) done[0] = 1;
+}
+template <typename T>
+__global__ void kcombine_kernel(cplx<double> *psi, KCombine<T> k, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    // the arithmetic of the sequence of lincomb launches it replaces
+    cplx<double> r = dmul(ld(psi + i), k.c[0]);
+    for (int j = 1; j < k.m; ++j) r = dmul(r, cplx<double>{1.0, 0.0}) + dmul(ccast<double>(ld(k.q[j] + i)), k.c[j]);
+    st(psi + i, r);
+  }
+}
+template <typename T>
+cudaError_t launch_kcombine(cplx<double> *psi, const KCombine<T> &k, long long n, cudaStream_t st) {
+  kcombine_kernel<T><<<ew_grid(n), 256, 0, st>>>(psi, k, n);
+  COUNT_LAUNCH();
+  return cudaGetLastError();
+}
+template cudaError_t launch_kcombine<double>(cplx<double> *, const KCombine<double> &, long long, cudaStream_t);
+template cudaError_t launch_kcombine<float>(cplx<double> *, const KCombine<float> &, long long, cudaStream_t);
+
+cudaError_t launch_ks_commit(int *done, cudaStream_t st) {
+  ks_commit_kernel<<<1, 32, 0, st>>>(done);
+  COUNT_LAUNCH();
+  return cudaGetLastError();
+}
+cudaError_t launch_ks_finish(const double *partials, const KsFinish &f, double *ks, int *done, cudaStream_t st) {
+  ks_finish_kernel<<<1, 32, 0, st>>>(partials, f, ks, done);
+  COUNT_LAUNCH();
+  return cudaGetLastError();
+}
+
+template <typename T>
+__global__ void ks_lincomb_kernel(cplx<T> *y, const cplx<T> *x, const double *ks, int idx, long long n,
+                                  const int *done) {
+  if (*done) return;
+  // the arithmetic of lincomb_kernel with a = 1, b = -s (or a = 1/s, no x)
+  const double sc = ks[idx];
+  const cplx<double> a = x ? cplx<double>{1.0, 0.0} : cplx<double>{1.0 / sc, 0.0};
+  const cplx<double> b = cplx<double>{-sc, 0.0};
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    cplx<double> r = dmul(ccast<double>(ld(y + i)), a);
+    if (x) r = r + dmul(ccast<double>(ld(x + i)), b);
+    st(y + i, ccast<T>(r));
+  }
+}
+template <typename T>
+cudaError_t launch_ks_lincomb(cplx<T> *y, const cplx<T> *x, const double *ks, int idx, long long n, const int *done,
+                              cudaStream_t st) {
+  ks_lincomb_kernel<T><<<ew_grid(n), 256, 0, st>>>(y, x, ks, idx, n, done);
+  COUNT_LAUNCH();
+  return cudaGetLastError();
+}
+template cudaError_t launch_ks_lincomb<double>(cplx<double> *, const cplx<double> *, const double *, int, long long,
+                                               const int *, cudaStream_t);
+template cudaError_t launch_ks_lincomb<float>(cplx<float> *, const cplx<float> *, const double *, int, long long,
+                                              const int *, cudaStream_t);
 template cudaError_t launch_dots<double, double>(const cplx<double> *, const cplx<double> *, int, long long, double *,
                                                  int, cudaStream_t);
 template cudaError_t launch_dots<float, float>(const cplx<float> *, const cplx<float> *, int, long long, double *,

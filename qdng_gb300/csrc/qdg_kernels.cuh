@@ -285,4 +285,35 @@ template <typename T>
 cudaError_t launch_lincomb(cplx<T> *y, const cplx<T> *x, cplx<double> a, cplx<double> b, long long n,
                            cudaStream_t st);
 
+// ---- Lanczos with its scalars on the device (no host round trip per
+// iteration).  ks holds alpha[order], beta[order], then KS_PSN (the norm of
+// psi) and KS_CONV (the order reached); *done stops every later kernel.
+enum KsMode { KS_ALPHA = 0, KS_BETA = 1, KS_PSN = 2 };
+struct KsFinish {
+  int grid, S, mode, slot, order;
+  double w;        // grid weight prod dx
+  int it;          // KS_BETA: Lanczos iteration (convergence test for it >= 2)
+  double dt, tol;  // error estimate dt^(it-2) beta_0 prod beta_i / i < tol * |psi|
+};
+template <typename T, typename U>
+cudaError_t launch_dots_if(const cplx<T> *a, const cplx<U> *b, int S, long long npts, double *partials, int grid,
+                           const int *done, cudaStream_t st);
+cudaError_t launch_ks_finish(const double *partials, const KsFinish &f, double *ks, int *done, cudaStream_t st);
+// done[0] = done[1]: the error estimate of an iteration stops the kernels after it
+cudaError_t launch_ks_commit(int *done, cudaStream_t st);
+// psi = c[0] psi + sum_{i=1}^{m-1} c[i] q_i in FP64, term by term in that order
+constexpr int kMaxKrylov = 64;
+template <typename T>
+struct KCombine {
+  const cplx<T> *q[kMaxKrylov];
+  cplx<double> c[kMaxKrylov];
+  int m;
+};
+template <typename T>
+cudaError_t launch_kcombine(cplx<double> *psi, const KCombine<T> &k, long long n, cudaStream_t st);
+// y -= ks[idx] x (x != null) or y *= 1 / ks[idx] (x == null), skipped once *done
+template <typename T>
+cudaError_t launch_ks_lincomb(cplx<T> *y, const cplx<T> *x, const double *ks, int idx, long long n, const int *done,
+                              cudaStream_t st);
+
 }  // namespace qdg
