@@ -487,7 +487,8 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default=None, choices=["fp64", "mixed"],
+                    help="default: fp64 (the drop-in path); mixed for the ensemble workload")
     ap.add_argument("--err-steps", type=int, default=400,
                     help="steps of the mixed-vs-FP64 observable comparison (0: skip)")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
@@ -497,6 +498,8 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.precision is None:
+        args.precision = "mixed" if args.workload == "ensemble" else "fp64"
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
         reference_arm(args, world, rank)
