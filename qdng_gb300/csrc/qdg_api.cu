@@ -801,7 +801,9 @@ qdg_status cheby_step_persistent(qdg_prop *P, cplx<double> *psi, long long step)
   a.partials = p->d_partials;
   a.cs = P->d_cs;
   a.bar = p->d_bar;
-  a.trace = p->profiling ? 1 : 0;
+  // phase timing of one block (block 0 unless QDG_TRACE_BLOCK names another)
+  const char *tb = getenv("QDG_TRACE_BLOCK");
+  a.trace = p->profiling ? 1 + (tb ? std::max(0, std::min(atoi(tb), P->step_grid - 1)) : 0) : 0;
   size_t slot = 0;
   qdg_status s = prof_begin<T>(p, 6, &slot);
   if (s != QDG_OK) return s;

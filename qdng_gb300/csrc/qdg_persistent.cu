@@ -60,7 +60,7 @@ __device__ bool grid_sync(GridBarrier *b) {
       }
     }
     __threadfence();
-    ok = atomicAdd(&b->err, 0) == 0;
+    ok = *(volatile int *)&b->err == 0;
   }
   __syncthreads();
   return ok != 0;
@@ -97,7 +97,7 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
                             const cplx<T> *__restrict__ phim2, cplx<T> *__restrict__ phout,
                             cplx<T> *const *Pprev, cplx<T> *const *Pnext, double coeff_i, double &acc,
                             cplx<T> *smem, unsigned long long *tp = nullptr) {
-  const bool tr = tp != nullptr && blockIdx.x == 0 && threadIdx.x == 0;
+  const bool tr = tp != nullptr && threadIdx.x == 0;
   constexpr int UNR = (sizeof(T) == 8 || SM > 2) ? 1 : 2;
   constexpr int RE = kMaxRowEntries;
   const long long npts = a.npts;
@@ -390,7 +390,7 @@ __global__ void __launch_bounds__(256, OCC) cheby_step_kernel(StepArgs<T> a) {
   const long long n = a.npts * a.S;
   const long long gtid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const long long gstride = (long long)gridDim.x * blockDim.x;
-  const bool tr = a.trace && blockIdx.x == 0 && threadIdx.x == 0;
+  const bool tr = a.trace && blockIdx.x == (unsigned)(a.trace - 1) && threadIdx.x == 0;
   unsigned long long tp[4] = {0, 0, 0, 0};
   unsigned long long *tpi = tp;  // gather, FFT + multiply, store (inside the phase), barrier
 
@@ -493,9 +493,9 @@ __global__ void __launch_bounds__(256, OCC) cheby_step_kernel(StepArgs<T> a) {
     a.cs->total += used;
     a.cs->status = status;
     a.cs->norm0 = norm0;
-    if (a.trace)
-      for (int k = 0; k < 4; ++k) a.cs->t_phase[k] += tp[k];
   }
+  if (tr)
+    for (int k = 0; k < 4; ++k) a.cs->t_phase[k] += tp[k];
 }
 
 template <typename T, int ND, int OCC>
