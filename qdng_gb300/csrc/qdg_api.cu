@@ -1176,9 +1176,13 @@ qdg_status krylov_alloc(qdg_prop *P) {
   P->lzb.assign(P->kord + 1, nullptr);
   for (auto &v : P->lzb) CK(cudaMalloc(&v, sizeof(cplx<T>) * wf_elems(p)));
   CK(cudaMalloc(&P->kbuf, sizeof(cplx<T>) * wf_elems(p)));
-  CK(cudaMalloc(&P->d_ks, sizeof(double) * (2 * (size_t)P->kord + 2)));
-  CK(cudaMalloc(&P->d_kdone, 2 * sizeof(int)));
-  CK(cudaMallocHost(&P->h_ks, sizeof(double) * (2 * (size_t)P->kord + 2)));
+  // Krylov scalars: Lanczos alpha, beta, |psi|, order (2 m + 2); Arnoldi H (2 m^2) and |psi|
+  const size_t nks = std::max<size_t>(2 * (size_t)P->kord + 2, 2 * (size_t)P->kord * P->kord + 1);
+  CK(cudaMalloc(&P->d_ks, sizeof(double) * nks));
+  CK(cudaMalloc(&P->d_kdone, 3 * sizeof(int)));  // stop flags [0], [1]; Arnoldi order [2]
+  const int o0[3] = {0, 0, P->kord};             // the reference starts at the full order
+  CK(cudaMemcpy(P->d_kdone, o0, sizeof(o0), cudaMemcpyHostToDevice));
+  CK(cudaMallocHost(&P->h_ks, sizeof(double) * nks));
   CK(cudaMallocHost(&P->h_kdone, sizeof(int)));
   if (sizeof(T) != sizeof(double)) CK(cudaMalloc(&P->kwide, sizeof(cplx<double>) * wf_elems(p)));
   return QDG_OK;
@@ -1335,60 +1339,128 @@ qdg_status sil_step(qdg_prop *P, cplx<double> *psi, long long step, int *used) {
 
 // OArnoldi::BuildLZB / DiagLZB / Propagate (src/qdlib/OArnoldi.cpp:86-199):
 // modified Gram-Schmidt in the reference order, FP64 scalars.
+// The Arnoldi recursion of one step as a fixed launch sequence with its
+// scalars on the device (captured once in a CUDA graph per psi buffer);
+// H, |psi| and the order land in the pinned P->h_ks / P->h_kdone.
+template <typename T>
+qdg_status arnoldi_body(qdg_prop *P, cplx<double> *psi) {
+  qdg_plan *p = P->plan;
+  const long long n = wf_elems(p);
+  const int m = P->kord;
+  std::vector<cplx<T> *> L(m);
+  for (int i = 0; i < m; ++i) L[i] = reinterpret_cast<cplx<T> *>(P->lzb[i]);
+  cplx<T> *buf0 = reinterpret_cast<cplx<T> *>(P->kbuf);
+  cplx<T> *last = reinterpret_cast<cplx<T> *>(P->lzb[m]);  // spare basis slot
+  double *ks = P->d_ks;
+  int *done = P->d_kdone;
+  int *ia = P->d_kdone + 2;
+  const int grid = dots_grid(p);
+  qdg::KaArgs ka;
+  ka.grid = grid; ka.S = p->S; ka.m = m; ka.w = 1.0; ka.dt = P->dt; ka.conv = P->conv;
+  for (int d = 0; d < p->nd; ++d) ka.w *= p->dx[d];
+  Epi e;
+  e.done = done;
+  auto hq_if = [&](const cplx<T> *q, cplx<T> *out) {
+    e.out = out;
+    return run_h<T>(p, qdg::PM_HAPPLY, q, e);
+  };
+  qdg_status s;
+  CK(cudaMemsetAsync(ks, 0, sizeof(double) * (2 * (size_t)m * m + 1), p->stream));
+  CK(cudaMemsetAsync(done, 0, 2 * sizeof(int), p->stream));
+  CK(qdg::launch_dots_if<double, double>(psi, psi, p->S, p->npts, p->d_partials, grid, done, p->stream));
+  CK(qdg::launch_ka_finish(p->d_partials, ka, qdg::KA_PSN, 0, 0, ks, ia, done, p->stream));
+  CK(qdg::launch_convert<T>(L[0], psi, n, p->stream));
+  for (int it = 1; it < m; ++it) {
+    if ((s = hq_if(L[it - 1], buf0)) != QDG_OK) return s;
+    for (int j = 0; j <= it - 1; ++j) {  // modified Gram-Schmidt
+      CK(qdg::launch_dots_if<T, T>(L[j], buf0, p->S, p->npts, p->d_partials, grid, done, p->stream));
+      CK(qdg::launch_ka_finish(p->d_partials, ka, qdg::KA_H, j, it - 1, ks, ia, done, p->stream));
+      CK(qdg::launch_ka_lincomb<T>(buf0, L[j], ks, m, j, it - 1, n, done, p->stream));
+    }
+    CK(qdg::launch_dots_if<T, T>(buf0, buf0, p->S, p->npts, p->d_partials, grid, done, p->stream));
+    CK(qdg::launch_ka_finish(p->d_partials, ka, qdg::KA_NORM, it, it - 1, ks, ia, done, p->stream));
+    CK(qdg::launch_ks_lincomb<T>(buf0, (const cplx<T> *)nullptr, ks, 2 * (it * m + it - 1), n, done, p->stream));
+    CK(qdg::launch_ka_commit<T>(L[it], buf0, n, it, ia, done, p->stream));
+  }
+  // last column H[j][order-1] from H q_{order-1}
+  qdg::KaBasis<T> kb;
+  memset(&kb, 0, sizeof(kb));
+  for (int i = 0; i < m; ++i) kb.q[i] = L[i];
+  CK(qdg::launch_ka_select<T>(last, kb, ia, n, p->stream));
+  e.done = nullptr;
+  if ((s = hq_if(last, buf0)) != QDG_OK) return s;
+  for (int j = 0; j < m; ++j) {
+    CK(qdg::launch_dots_lt<T>(L[j], buf0, p->S, p->npts, p->d_partials, grid, ia, j, p->stream));
+    CK(qdg::launch_ka_finish(p->d_partials, ka, qdg::KA_LAST, j, 0, ks, ia, done, p->stream));
+  }
+  CK(cudaMemcpyAsync(P->h_ks, ks, sizeof(double) * (2 * (size_t)m * m + 1), cudaMemcpyDeviceToHost, p->stream));
+  CK(cudaMemcpyAsync(P->h_kdone, ia, sizeof(int), cudaMemcpyDeviceToHost, p->stream));
+  return QDG_OK;
+}
+
+template <typename T>
+qdg_status arnoldi_enqueue(qdg_prop *P, cplx<double> *psi) {
+  qdg_plan *p = P->plan;
+  if (p->profiling || !P->graphs_ok) return arnoldi_body<T>(P, psi);
+  if (!P->graph || P->graph_psi != psi || P->graph_stream != p->stream) {
+    if (P->graph) { cudaGraphExecDestroy(P->graph); P->graph = nullptr; }
+    cudaGraph_t g = nullptr;
+    const long long l0 = qdg::launch_counter();
+    CK(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeRelaxed));
+    qdg_status s = arnoldi_body<T>(P, psi);
+    cudaError_t ce = cudaStreamEndCapture(p->stream, &g);
+    const long long l1 = qdg::launch_counter();
+    qdg::add_launches(-(l1 - l0));
+    if (s != QDG_OK) { if (g) cudaGraphDestroy(g); return s; }
+    if (ce != cudaSuccess || cudaGraphInstantiate(&P->graph, g, 0) != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+      P->graphs_ok = false;
+      P->graph = nullptr;
+      return arnoldi_body<T>(P, psi);
+    }
+    cudaGraphDestroy(g);
+    P->graph_launches = l1 - l0;
+    P->graph_psi = psi;
+    P->graph_stream = p->stream;
+  }
+  CK(cudaGraphLaunch(P->graph, p->stream));
+  qdg::add_launches(P->graph_launches);
+  return QDG_OK;
+}
+
+// OArnoldi::BuildLZB / DiagLZB / Propagate (src/qdlib/OArnoldi.cpp:86-199):
+// modified Gram-Schmidt in the reference order, FP64 scalars, the
+// reference's order kept across steps.  Each dot product is finished on the
+// device into H, the Gram-Schmidt updates read their coefficients there,
+// and the underrun / error tests set flags that turn the remaining kernels
+// of the step into no-ops; the host reads H once per step.
 template <typename T>
 qdg_status arnoldi_step(qdg_prop *P, cplx<double> *psi, long long step, int *used) {
   qdg_plan *p = P->plan;
   const long long n = wf_elems(p);
-  const int maxorder = P->kord;
-  if (P->aorder == 0) P->aorder = maxorder;
-  std::vector<cplx<T> *> L(maxorder);
-  for (int i = 0; i < maxorder; ++i) L[i] = reinterpret_cast<cplx<T> *>(P->lzb[i]);
-  cplx<T> *buf0 = reinterpret_cast<cplx<T> *>(P->kbuf);
-  std::vector<cd> tHA((size_t)maxorder * maxorder, 0.0), d;
-  qdg_status s;
+  const int m = P->kord;
+  if (m > qdg::kMaxKrylov) return fail(QDG_EUNSUPPORTED, "Krylov order above 64");
   CK(qdg::launch_set_coefs(p->d_coef, p->d_cp, p->d_lasers, p->laser_nt, step, p->stream));
-  if ((s = dots<double, double>(p, psi, psi, d)) != QDG_OK) return s;
-  const double PsiNorm = std::sqrt(total(d).real());
-  CK(qdg::launch_convert<T>(L[0], psi, n, p->stream));
-  for (int it = 1; it < maxorder; ++it) {
-    if ((s = hq<T>(P, L[it - 1], buf0, step)) != QDG_OK) return s;
-    for (int j = 0; j <= it - 1; ++j) {
-      if ((s = dots<T, T>(p, L[j], buf0, d)) != QDG_OK) return s;
-      const cd h = total(d);
-      tHA[(size_t)j * maxorder + it - 1] = h;
-      CK(qdg::launch_lincomb<T>(buf0, L[j], cplx<double>{1, 0}, C(-h), n, p->stream));
-    }
-    if ((s = dots<T, T>(p, buf0, buf0, d)) != QDG_OK) return s;
-    const double nrm = std::sqrt(total(d).real());
-    if (nrm < 1e-11) break;  // ARNOLDI_UNDERRUN (OArnoldi.h:12)
-    tHA[(size_t)it * maxorder + it - 1] = nrm;
-    CK(qdg::launch_lincomb<T>(buf0, (const cplx<T> *)nullptr, cplx<double>{1.0 / nrm, 0}, cplx<double>{0, 0}, n, p->stream));
-    CK(cudaMemcpyAsync(L[it], buf0, sizeof(cplx<T>) * n, cudaMemcpyDeviceToDevice, p->stream));
-    P->aorder = it + 1;
-    cd err = std::pow(P->dt, it - 2) * tHA[(size_t)1 * maxorder + 0] * PsiNorm;
-    for (int i = 1; i < it - 2; ++i) err *= tHA[(size_t)(i + 1) * maxorder + i] / double(i);
-    if (std::abs(err) < P->conv) break;
-  }
-  const int order = P->aorder;
-  if ((s = hq<T>(P, L[order - 1], buf0, step)) != QDG_OK) return s;
-  for (int j = 0; j < order; ++j) {
-    if ((s = dots<T, T>(p, L[j], buf0, d)) != QDG_OK) return s;
-    tHA[(size_t)j * maxorder + order - 1] = total(d);
-  }
+  qdg_status s = arnoldi_enqueue<T>(P, psi);
+  if (s != QDG_OK) return s;
+  CK(cudaStreamSynchronize(p->stream));
+  const double *H = P->h_ks;
+  const int order = *P->h_kdone;
+  P->aorder = order;
+  if (!std::isfinite(H[2 * m * m])) return fail(QDG_ENONFINITE, "Norm is not a number");
   std::vector<cd> HA((size_t)order * order);
   for (int i = 0; i < order; ++i)
-    for (int j = 0; j < order; ++j) HA[(size_t)i * order + j] = tHA[(size_t)i * maxorder + j];
+    for (int j = 0; j < order; ++j) HA[(size_t)i * order + j] = cd(H[2 * (i * m + j)], H[2 * (i * m + j) + 1]);
   std::vector<cd> vect = qdg::host::expm_e0(order, HA, P->c0);
-  CK(qdg::launch_lincomb<double>(psi, (const cplx<double> *)nullptr, C(vect[0]), cplx<double>{0, 0}, n, p->stream));
-  for (int i = 1; i < order; ++i) {
-    if (sizeof(T) == sizeof(double)) {
-      CK(qdg::launch_lincomb<double>(psi, reinterpret_cast<const cplx<double> *>(L[i]), cplx<double>{1, 0}, C(vect[i]), n, p->stream));
-    } else {
-      cplx<double> *wide = reinterpret_cast<cplx<double> *>(P->kwide);
-      CK(qdg::launch_widen<T>(wide, L[i], n, p->stream));
-      CK(qdg::launch_lincomb<double>(psi, wide, cplx<double>{1, 0}, C(vect[i]), n, p->stream));
-    }
+  qdg::KCombine<T> kc;
+  memset(&kc, 0, sizeof(kc));
+  kc.m = order;
+  for (int i = 0; i < order; ++i) {
+    kc.c[i] = C(vect[i]);
+    kc.q[i] = reinterpret_cast<const cplx<T> *>(P->lzb[i]);
   }
+  CK(qdg::launch_kcombine<T>(psi, kc, n, p->stream));
   if (used) *used = order;
   return QDG_OK;
 }

@@ -636,10 +636,9 @@ template cudaError_t launch_lincomb<float>(cplx<float> *, const cplx<float> *, c
 
 // Per-state sum conj(a) b, FP64 accumulation, fixed reduction order.
 template <typename T, typename U>
-__global__ void dots_kernel(const cplx<T> *a, const cplx<U> *b, int S, long long npts, double *partials,
-                            const int *done) {
+__device__ __forceinline__ void dots_body(const cplx<T> *a, const cplx<U> *b, int S, long long npts,
+                                          double *partials) {
   __shared__ double red[32];
-  if (done != nullptr && *done) return;
   for (int s = 0; s < S; ++s) {
     double re = 0, im = 0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npts;
@@ -656,6 +655,12 @@ __global__ void dots_kernel(const cplx<T> *a, const cplx<U> *b, int S, long long
       partials[((long long)blockIdx.x * S + s) * 2 + 1] = ti;
     }
   }
+}
+template <typename T, typename U>
+__global__ void dots_kernel(const cplx<T> *a, const cplx<U> *b, int S, long long npts, double *partials,
+                            const int *done) {
+  if (done != nullptr && *done) return;
+  dots_body<T, U>(a, b, S, npts, partials);
 }
 template <typename T, typename U>
 cudaError_t launch_dots(const cplx<T> *a, const cplx<U> *b, int S, long long npts, double *partials, int grid,
@@ -710,6 +715,141 @@ __global__ void ks_finish_kernel(const double *partials, KsFinish f, double *ks,
 __global__ void ks_commit_kernel(int *done) {
   if (threadIdx.x == 0 && done[1]) done[0] = 1;
 }
+__global__ void ka_finish_kernel(const double *partials, KaArgs a, int op, int j, int col, double *ks, int *ia,
+                                 int *done) {
+  if (threadIdx.x != 0) return;
+  if (op != KA_LAST && *done) return;
+  if (op == KA_LAST && j >= ia[0]) return;
+  double re[kMaxStates], im[kMaxStates];
+  for (int s = 0; s < a.S; ++s) re[s] = im[s] = 0.0;
+  for (int b = 0; b < a.grid; ++b)
+    for (int s = 0; s < a.S; ++s) {
+      re[s] += partials[(b * a.S + s) * 2];
+      im[s] += partials[(b * a.S + s) * 2 + 1];
+    }
+  double tr = 0.0, ti = 0.0;
+  for (int s = 0; s < a.S; ++s) { tr += re[s] * a.w; ti += im[s] * a.w; }
+  const int m = a.m;
+  double *H = ks;
+  if (op == KA_PSN) { ks[2 * m * m] = sqrt(tr); return; }
+  if (op == KA_H) { H[2 * (j * m + col)] = tr; H[2 * (j * m + col) + 1] = ti; return; }
+  if (op == KA_LAST) {
+    const int c = ia[0] - 1;
+    H[2 * (j * m + c)] = tr; H[2 * (j * m + c) + 1] = ti;
+    return;
+  }
+  // KA_NORM for iteration it = col + 1 (OArnoldi::BuildLZB, src/qdlib/OArnoldi.cpp:111-136)
+  const int it = col + 1;
+  const double nrm = sqrt(tr);
+  if (nrm < 1e-11) {  // ARNOLDI_UNDERRUN (OArnoldi.h:12): stop before this vector
+    done[0] = 1;
+    return;
+  }
+  H[2 * (it * m + it - 1)] = nrm;
+  H[2 * (it * m + it - 1) + 1] = 0.0;
+  // err = dt^(it-2) H[1][0] |psi| prod H[i+1][i] / i, complex
+  double er = pow(a.dt, (double)(it - 2)) * H[2 * m] * ks[2 * m * m];
+  double ei = pow(a.dt, (double)(it - 2)) * H[2 * m + 1] * ks[2 * m * m];
+  for (int i = 1; i < it - 2; ++i) {
+    const double hr = H[2 * ((i + 1) * m + i)] / double(i), hi = H[2 * ((i + 1) * m + i) + 1] / double(i);
+    const double nr = er * hr - ei * hi, ni = er * hi + ei * hr;
+    er = nr;
+    ei = ni;
+  }
+  if (hypot(er, ei) < a.conv) done[1] = 1;  // after this iteration's vector is stored
+}
+cudaError_t launch_ka_finish(const double *partials, const KaArgs &a, int op, int j, int col, double *ks, int *ia,
+                             int *done, cudaStream_t st) {
+  ka_finish_kernel<<<1, 32, 0, st>>>(partials, a, op, j, col, ks, ia, done);
+  COUNT_LAUNCH();
+  return cudaGetLastError();
+}
+
+template <typename T>
+__global__ void ka_lincomb_kernel(cplx<T> *y, const cplx<T> *x, const double *ks, int m, int j, int col, long long n,
+                                  const int *done) {
+  if (*done) return;
+  const cplx<double> a = cplx<double>{1.0, 0.0};
+  const cplx<double> b = cplx<double>{-ks[2 * (j * m + col)], -ks[2 * (j * m + col) + 1]};
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    cplx<double> r = dmul(ccast<double>(ld(y + i)), a);
+    r = r + dmul(ccast<double>(ld(x + i)), b);
+    st(y + i, ccast<T>(r));
+  }
+}
+template <typename T>
+cudaError_t launch_ka_lincomb(cplx<T> *y, const cplx<T> *x, const double *ks, int m, int j, int col, long long n,
+                              const int *done, cudaStream_t st) {
+  ka_lincomb_kernel<T><<<ew_grid(n), 256, 0, st>>>(y, x, ks, m, j, col, n, done);
+  COUNT_LAUNCH();
+  return cudaGetLastError();
+}
+template cudaError_t launch_ka_lincomb<double>(cplx<double> *, const cplx<double> *, const double *, int, int, int,
+                                               long long, const int *, cudaStream_t);
+template cudaError_t launch_ka_lincomb<float>(cplx<float> *, const cplx<float> *, const double *, int, int, int,
+                                              long long, const int *, cudaStream_t);
+
+// The commit reads done[0] as set before this iteration; its own error test
+// (done[1]) takes effect for the kernels after it.
+template <typename T>
+__global__ void ka_commit_kernel(cplx<T> *q, const cplx<T> *buf, long long n, int it, int *ia, int *done) {
+  if (*(volatile int *)done) return;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    q[i] = buf[i];
+}
+__global__ void ka_order_kernel(int it, int *ia, int *done) {
+  if (threadIdx.x != 0 || done[0]) return;
+  ia[0] = it + 1;
+  if (done[1]) done[0] = 1;
+}
+template <typename T>
+cudaError_t launch_ka_commit(cplx<T> *q, const cplx<T> *buf, long long n, int it, int *ia, int *done, cudaStream_t st) {
+  ka_commit_kernel<T><<<ew_grid(n), 256, 0, st>>>(q, buf, n, it, ia, done);
+  ka_order_kernel<<<1, 32, 0, st>>>(it, ia, done);
+  COUNT_LAUNCH();
+  COUNT_LAUNCH();
+  return cudaGetLastError();
+}
+template cudaError_t launch_ka_commit<double>(cplx<double> *, const cplx<double> *, long long, int, int *, int *,
+                                              cudaStream_t);
+template cudaError_t launch_ka_commit<float>(cplx<float> *, const cplx<float> *, long long, int, int *, int *,
+                                             cudaStream_t);
+
+template <typename T>
+__global__ void ka_select_kernel(cplx<T> *dst, KaBasis<T> b, const int *ia, long long n) {
+  const cplx<T> *src = b.q[ia[0] - 1];
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+template <typename T>
+cudaError_t launch_ka_select(cplx<T> *dst, const KaBasis<T> &b, const int *ia, long long n, cudaStream_t st) {
+  ka_select_kernel<T><<<ew_grid(n), 256, 0, st>>>(dst, b, ia, n);
+  COUNT_LAUNCH();
+  return cudaGetLastError();
+}
+template cudaError_t launch_ka_select<double>(cplx<double> *, const KaBasis<double> &, const int *, long long,
+                                              cudaStream_t);
+template cudaError_t launch_ka_select<float>(cplx<float> *, const KaBasis<float> &, const int *, long long,
+                                             cudaStream_t);
+
+template <typename T>
+__global__ void dots_lt_kernel(const cplx<T> *a, const cplx<T> *b, int S, long long npts, double *partials,
+                               const int *ia, int j) {
+  if (j >= ia[0]) return;
+  dots_body<T, T>(a, b, S, npts, partials);
+}
+template <typename T>
+cudaError_t launch_dots_lt(const cplx<T> *a, const cplx<T> *b, int S, long long npts, double *partials, int grid,
+                           const int *ia, int j, cudaStream_t st) {
+  dots_lt_kernel<T><<<grid, 256, 0, st>>>(a, b, S, npts, partials, ia, j);
+  COUNT_LAUNCH();
+  return cudaGetLastError();
+}
+template cudaError_t launch_dots_lt<double>(const cplx<double> *, const cplx<double> *, int, long long, double *, int,
+                                            const int *, int, cudaStream_t);
+template cudaError_t launch_dots_lt<float>(const cplx<float> *, const cplx<float> *, int, long long, double *, int,
+                                           const int *, int, cudaStream_t);
+
 template <typename T>
 __global__ void kcombine_kernel(cplx<double> *psi, KCombine<T> k, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {

@@ -301,6 +301,37 @@ cudaError_t launch_dots_if(const cplx<T> *a, const cplx<U> *b, int S, long long 
 cudaError_t launch_ks_finish(const double *partials, const KsFinish &f, double *ks, int *done, cudaStream_t st);
 // done[0] = done[1]: the error estimate of an iteration stops the kernels after it
 cudaError_t launch_ks_commit(int *done, cudaStream_t st);
+// ---- Arnoldi with its scalars on the device.  ks holds the Hessenberg
+// matrix H (m x m complex, row-major, re/im interleaved), then |psi|;
+// ia[0] is the order reached (kept across steps, like the reference's
+// _order), done[0]/done[1] as for the Lanczos flags.
+struct KaArgs {
+  int grid, S, m;
+  double w, dt, conv;
+};
+enum KaOp { KA_H = 0, KA_NORM = 1, KA_PSN = 2, KA_LAST = 3 };
+// finish a dot product into H[j][col] (KA_H), the subdiagonal with the
+// underrun and error tests (KA_NORM, it = col + 1), |psi| (KA_PSN), or the
+// last column H[j][order-1] (KA_LAST, skipped for j >= order)
+cudaError_t launch_ka_finish(const double *partials, const KaArgs &a, int op, int j, int col, double *ks, int *ia,
+                             int *done, cudaStream_t st);
+// y -= H[j][col] x (complex coefficient), skipped once *done
+template <typename T>
+cudaError_t launch_ka_lincomb(cplx<T> *y, const cplx<T> *x, const double *ks, int m, int j, int col, long long n,
+                              const int *done, cudaStream_t st);
+// after the normalisation of iteration it: q_it = buf, order = it + 1, done[0] |= done[1]
+template <typename T>
+cudaError_t launch_ka_commit(cplx<T> *q, const cplx<T> *buf, long long n, int it, int *ia, int *done, cudaStream_t st);
+// dst = q_{order-1} (the basis vector the last column is built from)
+template <typename T>
+struct KaBasis { const cplx<T> *q[64]; };
+template <typename T>
+cudaError_t launch_ka_select(cplx<T> *dst, const KaBasis<T> &b, const int *ia, long long n, cudaStream_t st);
+// dot products guarded by j < order (the last column)
+template <typename T>
+cudaError_t launch_dots_lt(const cplx<T> *a, const cplx<T> *b, int S, long long npts, double *partials, int grid,
+                           const int *ia, int j, cudaStream_t st);
+
 // psi = c[0] psi + sum_{i=1}^{m-1} c[i] q_i in FP64, term by term in that order
 constexpr int kMaxKrylov = 64;
 template <typename T>
