@@ -350,7 +350,9 @@ def engine_arm(args, world, rank, local):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+        # the FP64 path keeps psi and the reductions in FP64 and runs phi, H phi
+        # and the FFTs of the multi-dimensional step in double-float (2 x f32)
+        "dtype": ("f64+df32" if hp.grid.ndims > 1 else "f64") if args.precision == "fp64" else "f32+f64",
         "data": "synthetic (seeded analytic potentials and Gaussian start, BASELINE configs[1])",
         "config": dict(cfg, parallelism="replicas" if world > 1 else "single",
                        cheby_order=info["order"]),

@@ -55,6 +55,8 @@ struct DimInfo {
   void *tw;           // n twiddles (cplx<T>)
   double *kfac;       // [S] dk^2/(2m)/n for H passes
   void *ktab;         // [S][n] kfac[s] * min(i, n-i)^2 in the bulk type
+  void *twdf = nullptr;  // FP64 plans: twiddles and k^2 multipliers in double-float
+  void *ktdf = nullptr;
   int TW_k, TW_e;     // lines per tile: kinetic-only passes, coupled epilogue pass
 };
 
@@ -97,6 +99,7 @@ struct qdg_plan {
   int nac_tw[QDG_MAX_DIMS] = {1, 1, 1, 1};
   // device
   void *d_grids = nullptr;      // bulk type
+  void *d_grids_df = nullptr;   // FP64 plans: the grids in double-float
   double *d_lasers = nullptr;
   DimInfo dim[QDG_MAX_DIMS];
   qdg::Couplings cp_h;           // all potential/dipole entries of H
@@ -529,12 +532,34 @@ qdg_status upload_tables(qdg_plan *p) {
       }
     CK(cudaMalloc(&di.ktab, sizeof(T) * kt.size()));
     CK(cudaMemcpy(di.ktab, kt.data(), sizeof(T) * kt.size(), cudaMemcpyHostToDevice));
+    if (sizeof(T) == sizeof(double)) {
+      // double-float copies for the FFTs of the FP64 step kernel
+      std::vector<qdg::cplx<qdg::dfl>> twd(n);
+      for (int m = 0; m < n; ++m) {
+        const long double ang = -2.0L * pi * (long double)m / (long double)n;
+        const long double c = cosl(ang), sn = sinl(ang);
+        twd[m].re = qdg::dfl((float)c, (float)(c - (long double)(float)c));
+        twd[m].im = qdg::dfl((float)sn, (float)(sn - (long double)(float)sn));
+      }
+      std::vector<qdg::dfl> ktd(kt.size());
+      for (size_t i = 0; i < kt.size(); ++i) ktd[i] = qdg::dfl((double)kt[i]);
+      CK(cudaMalloc(&di.twdf, sizeof(qdg::cplx<qdg::dfl>) * n));
+      CK(cudaMemcpy(di.twdf, twd.data(), sizeof(qdg::cplx<qdg::dfl>) * n, cudaMemcpyHostToDevice));
+      CK(cudaMalloc(&di.ktdf, sizeof(qdg::dfl) * ktd.size()));
+      CK(cudaMemcpy(di.ktdf, ktd.data(), sizeof(qdg::dfl) * ktd.size(), cudaMemcpyHostToDevice));
+    }
   }
   // grids in the bulk type
   std::vector<T> g(p->grids_h.size());
   for (size_t i = 0; i < g.size(); ++i) g[i] = (T)p->grids_h[i];
   CK(cudaMalloc(&p->d_grids, sizeof(T) * std::max<size_t>(1, g.size())));
   if (!g.empty()) CK(cudaMemcpy(p->d_grids, g.data(), sizeof(T) * g.size(), cudaMemcpyHostToDevice));
+  if (sizeof(T) == sizeof(double)) {
+    std::vector<qdg::dfl> gd(p->grids_h.size());
+    for (size_t i = 0; i < gd.size(); ++i) gd[i] = qdg::dfl(p->grids_h[i]);
+    CK(cudaMalloc(&p->d_grids_df, sizeof(qdg::dfl) * std::max<size_t>(1, gd.size())));
+    if (!gd.empty()) CK(cudaMemcpy(p->d_grids_df, gd.data(), sizeof(qdg::dfl) * gd.size(), cudaMemcpyHostToDevice));
+  }
   CK(cudaMalloc(&p->d_P, sizeof(cplx<T>) * wf_elems(p)));
   if (p->nd > 1 || !p->nac.empty()) {
     size_t smem = 0;
@@ -580,8 +605,11 @@ void free_plan(qdg_plan *p) {
     if (p->dim[d].tw) cudaFree(p->dim[d].tw);
     if (p->dim[d].kfac) cudaFree(p->dim[d].kfac);
     if (p->dim[d].ktab) cudaFree(p->dim[d].ktab);
+    if (p->dim[d].twdf) cudaFree(p->dim[d].twdf);
+    if (p->dim[d].ktdf) cudaFree(p->dim[d].ktdf);
   }
   if (p->d_grids) cudaFree(p->d_grids);
+  if (p->d_grids_df) cudaFree(p->d_grids_df);
   if (p->d_lasers) cudaFree(p->d_lasers);
   if (p->d_cp) cudaFree(p->d_cp);
   if (p->d_coef) cudaFree(p->d_coef);
@@ -769,6 +797,8 @@ qdg_status cheby_step_persistent(qdg_prop *P, cplx<double> *psi, long long step)
     dp.hi_stride = g.hi_stride; dp.ntiles = g.ntiles; dp.rp = g.rp; dp.tw = g.tw; dp.kfac = g.kfac;
     dp.P = reinterpret_cast<cplx<T> *>(p->d_Pd[d]);
     dp.ktab = reinterpret_cast<const T *>(p->dim[d].ktab);
+    dp.twdf = reinterpret_cast<const cplx<qdg::dfl> *>(p->dim[d].twdf);
+    dp.ktdf = reinterpret_cast<const qdg::dfl *>(p->dim[d].ktdf);
     a.item_start[d] = items;
     items += g.ntiles * p->S;
   }
@@ -787,6 +817,7 @@ qdg_status cheby_step_persistent(qdg_prop *P, cplx<double> *psi, long long step)
   a.cp = p->d_cp;
   a.coef = p->d_coef;
   a.grids = reinterpret_cast<const T *>(p->d_grids);
+  a.gdf = reinterpret_cast<const qdg::dfl *>(p->d_grids_df);
   const cd ex = P->c0 / P->dt;
   a.offset = C(P->offset);
   a.fac1 = C(ex / P->scaling);

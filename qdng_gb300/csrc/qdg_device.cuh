@@ -13,6 +13,80 @@ namespace qdg {
 
 template <typename T> struct cplx { T re, im; };
 
+// ---- double-float: an unevaluated sum hi + lo of two FP32 numbers ---------
+// GB300 executes FP64 at 1/64 of the FP32 rate.  The FFTs of the FP64 path
+// run in this type: about 48 significant bits (error-free transformations:
+// Knuth's TwoSum, Dekker/FMA products; the addition is the "sloppy" form,
+// whose error is bounded by ~2^-47 of the operands' magnitude, which is what
+// a normwise FFT error bound needs).  The round-to-nearest intrinsics keep
+// the compiler from contracting the transformations.
+struct dfl {
+  float hi, lo;
+  __host__ __device__ constexpr dfl() : hi(0.0f), lo(0.0f) {}
+  __host__ __device__ constexpr dfl(float h, float l) : hi(h), lo(l) {}
+  __host__ __device__ constexpr dfl(double x) : hi((float)x), lo((float)(x - (double)(float)x)) {}
+  __host__ __device__ constexpr dfl(int x) : hi((float)x), lo(0.0f) {}
+};
+__device__ __forceinline__ dfl df_fast(float s, float e) {  // |s| >= |e|
+  const float h = __fadd_rn(s, e);
+  return dfl(h, __fsub_rn(e, __fsub_rn(h, s)));
+}
+__device__ __forceinline__ dfl operator+(dfl a, dfl b) {
+  const float s = __fadd_rn(a.hi, b.hi);
+  const float bb = __fsub_rn(s, a.hi);
+  float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+  e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+  return df_fast(s, e);
+}
+__device__ __forceinline__ dfl operator-(dfl a) { return dfl(-a.hi, -a.lo); }
+__device__ __forceinline__ dfl operator-(dfl a, dfl b) { return a + (-b); }
+__device__ __forceinline__ dfl operator*(dfl a, dfl b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return df_fast(p, e);
+}
+__device__ __forceinline__ double df_to_double(dfl a) { return (double)a.hi + (double)a.lo; }
+__device__ __forceinline__ dfl df_from_double(double x) {
+  const float h = __double2float_rn(x);
+  return dfl(h, __double2float_rn(x - (double)h));
+}
+
+// Bulk-type helpers for float and double-float (the step kernel's phi, T_d phi
+// and potential values).
+__device__ __forceinline__ double b2d(float x) { return (double)x; }
+__device__ __forceinline__ double b2d(dfl x) { return df_to_double(x); }
+__device__ __forceinline__ float fma_b(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ dfl fma_b(dfl a, dfl b, dfl c) { return a * b + c; }
+template <typename B> __device__ __forceinline__ B d2b(double x);
+template <> __device__ __forceinline__ float d2b<float>(double x) { return (float)x; }
+template <> __device__ __forceinline__ dfl d2b<dfl>(double x) { return df_from_double(x); }
+__device__ __forceinline__ float ldg_b(const float *p) { return __ldg(p); }
+__device__ __forceinline__ dfl ldg_b(const dfl *p) {
+  const float2 v = __ldg(reinterpret_cast<const float2 *>(p));
+  return dfl(v.x, v.y);
+}
+__device__ __forceinline__ cplx<dfl> ldcg(const cplx<dfl> *p) {
+  const float4 v = __ldcg(reinterpret_cast<const float4 *>(p));
+  return cplx<dfl>{dfl(v.x, v.y), dfl(v.z, v.w)};
+}
+__device__ __forceinline__ void st(cplx<dfl> *p, cplx<dfl> c) {
+  *reinterpret_cast<float4 *>(p) = make_float4(c.re.hi, c.re.lo, c.im.hi, c.im.lo);
+}
+
+// Arithmetic type of the FFTs: double-float for the FP64 path, float for FP32.
+template <typename T> struct FftType { typedef T type; };
+template <> struct FftType<double> { typedef dfl type; };
+template <typename F, typename T> __device__ __forceinline__ cplx<F> to_fft(cplx<T> v) {
+  if constexpr (sizeof(F) == sizeof(T) && sizeof(T) == sizeof(float)) return v;
+  else return cplx<F>{df_from_double(v.re), df_from_double(v.im)};
+}
+template <typename T, typename F> __device__ __forceinline__ cplx<T> from_fft(cplx<F> v) {
+  if constexpr (sizeof(F) == sizeof(T) && sizeof(T) == sizeof(float)) return v;
+  else return cplx<T>{df_to_double(v.re), df_to_double(v.im)};
+}
+
 template <typename T> struct vec2;
 template <> struct vec2<double> { typedef double2 type; };
 template <> struct vec2<float> { typedef float2 type; };

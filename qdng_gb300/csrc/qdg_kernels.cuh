@@ -126,6 +126,8 @@ struct DimPass {
   const double *kfac;   // [S] dk^2/(2m)/N
   cplx<T> *P;           // T_d phi output (state stride npts)
   const T *ktab;        // [S][N] kinetic multipliers kfac[s] * min(i, N-i)^2 (precomputed)
+  const cplx<dfl> *twdf;  // FP64 path: twiddles and multipliers in double-float (the FFT type)
+  const dfl *ktdf;
 };
 
 // T_d phi for every dimension d in one launch (the kinetic operator is a sum
@@ -212,6 +214,7 @@ struct StepArgs {
   const Couplings *cp;
   const double *coef;
   const T *grids;
+  const dfl *gdf;            // FP64 path: the grids in double-float (the phases' bulk type)
   cplx<double> offset, fac1, fac, ph;  // offset, exp/scaling, 2 exp/scaling, exp(c0 offset)
   const double *a;           // real series coefficients a_i (J_0, 2 J_i / I_0, 2 I_i)
   int order;

@@ -98,6 +98,13 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
                             cplx<T> *const *Pprev, cplx<T> *const *Pnext, double coeff_i, double &acc,
                             cplx<T> *smem, unsigned long long *tp = nullptr) {
   const bool tr = tp != nullptr && threadIdx.x == 0;
+  // Bulk arithmetic (phi, T_d phi, potentials, FFTs): double-float for the
+  // FP64 path, float for the mixed one; psi and its norm stay FP64.
+  typedef typename FftType<T>::type FT;
+  typedef FT B;
+  const cplx<B> *phim1b = reinterpret_cast<const cplx<B> *>(phim1);
+  const cplx<B> *phim2b = reinterpret_cast<const cplx<B> *>(phim2);
+  cplx<B> *phoutb = reinterpret_cast<cplx<B> *>(phout);
   constexpr int UNR = (sizeof(T) == 8 || SM > 2) ? 1 : 2;
   constexpr int RE = kMaxRowEntries;
   const long long npts = a.npts;
@@ -106,13 +113,15 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
   const long long end = total * (blockIdx.x + 1) / G;
   long long l = total * blockIdx.x / G;
   int cur_dim = -1;
-  cplx<T> *tws = smem;
+  cplx<FT> *tws = reinterpret_cast<cplx<FT> *>(smem);  // same size as cplx<T>
   __shared__ long long lbase[kMaxBatchLines];
-  const cplx<T> off = ccast<T>(a.offset);
-  const cplx<T> fac = ccast<T>(kind == PK_FIRST ? a.fac1 : a.fac);
+  const cplx<B> off = {d2b<B>(a.offset.re), d2b<B>(a.offset.im)};
+  const cplx<double> facd = kind == PK_FIRST ? a.fac1 : a.fac;
+  const cplx<B> fac = {d2b<B>(facd.re), d2b<B>(facd.im)};
   const bool off_real = a.offset.im == 0.0;
-  const bool fac_imag = (kind == PK_FIRST ? a.fac1.re : a.fac.re) == 0.0;
-  const T *__restrict__ grids = a.grids;
+  const bool fac_imag = facd.re == 0.0;
+  const B *__restrict__ grids = sizeof(T) == sizeof(double) ? reinterpret_cast<const B *>(a.gdf)
+                                                            : reinterpret_cast<const B *>(a.grids);
   while (l < end) {
     int d = 0;
     while (l >= a.line_start[d + 1]) ++d;
@@ -131,11 +140,14 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
     const bool owner = d == 0;
     if (kind == PK_LAST && !owner) continue;
     const int LS = lstride(N);
-    cplx<T> *b0 = tws + N;
-    cplx<T> *b1 = b0 + line_buf_elems(N, a.lmax[d]);
+    cplx<FT> *b0 = tws + N;
+    cplx<FT> *b1 = b0 + line_buf_elems(N, a.lmax[d]);
     __syncthreads();
     if (d != cur_dim && kind != PK_LAST) {
-      for (int i = threadIdx.x; i < N; i += blockDim.x) tws[i] = g.tw[i];
+      for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        if constexpr (sizeof(T) == sizeof(double)) tws[i] = g.twdf[i];
+        else tws[i] = g.tw[i];
+      }
       cur_dim = d;
     }
     // first point of each line of the batch (one 64-bit division per line)
@@ -149,14 +161,14 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
     const int e0 = a.cp->rs[s];
     const int ne = a.cp->rs[s + 1] - e0;
     int ecol[RE], egid[RE];
-    T ecoef[RE];
+    B ecoef[RE];
     bool unit_coef = true;  // only static potentials (coefficient 1) in this row
 #pragma unroll
     for (int k = 0; k < RE; ++k) {
       ecol[k] = k < ne ? a.cp->col[e0 + k] : 0;
       egid[k] = k < ne ? a.cp->gid[e0 + k] : 0;
-      ecoef[k] = k < ne ? (T)a.coef[e0 + k] : (T)0;
-      if (k < ne && ecoef[k] != (T)1) unit_coef = false;
+      ecoef[k] = d2b<B>(k < ne ? a.coef[e0 + k] : 0.0);
+      if (k < ne && a.coef[e0 + k] != 1.0) unit_coef = false;
     }
     const long long so = (long long)s * npts;
     const int tot = L * N;
@@ -164,10 +176,10 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
     for (int base = threadIdx.x; base < tot; base += UNR * blockDim.x) {
       long long pp[UNR];
       int sidx[UNR];
-      cplx<T> v[UNR];
+      cplx<B> v[UNR];
       // ---- gather
-      cplx<T> hP[UNR], pm[UNR][SM], km2[UNR];
-      T vg[UNR][RE];
+      cplx<B> hP[UNR], pm[UNR][SM], km2[UNR];
+      B vg[UNR][RE];
       cplx<double> ps[UNR];
 #pragma unroll
       for (int u = 0; u < UNR; ++u) {
@@ -182,17 +194,17 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
         const long long p = lbase[w] + (long long)i * istr;
         pp[u] = p;
         if (!ok) continue;
-        if (kind == PK_START) { v[u] = ldcg(phim1 + so + p); continue; }
-        cplx<T> h = ldcg(Pprev[0] + so + p);
+        if (kind == PK_START) { v[u] = ldcg(phim1b + so + p); continue; }
+        cplx<B> h = ldcg(reinterpret_cast<const cplx<B> *>(Pprev[0]) + so + p);
 #pragma unroll
-        for (int dd = 1; dd < ND; ++dd) h = h + ldcg(Pprev[dd] + so + p);
+        for (int dd = 1; dd < ND; ++dd) h = h + ldcg(reinterpret_cast<const cplx<B> *>(Pprev[dd]) + so + p);
         hP[u] = h;
 #pragma unroll
         for (int j = 0; j < SM; ++j)
-          if (j < a.S) pm[u][j] = ldcg(phim1 + (long long)j * npts + p);
+          if (j < a.S) pm[u][j] = ldcg(phim1b + (long long)j * npts + p);
 #pragma unroll
-        for (int k = 0; k < RE; ++k) vg[u][k] = k < ne ? __ldg(grids + (long long)egid[k] * npts + p) : (T)0;
-        if (kind != PK_FIRST) km2[u] = ldcg(phim2 + so + p);
+        for (int k = 0; k < RE; ++k) vg[u][k] = k < ne ? ldg_b(grids + (long long)egid[k] * npts + p) : B(0);
+        if (kind != PK_FIRST) km2[u] = ldcg(phim2b + so + p);
         if (owner) ps[u] = ldcg(a.psi + so + p);
       }
       // ---- compute and scatter
@@ -200,51 +212,51 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
       for (int u = 0; u < UNR; ++u) {
         if (sidx[u] < 0) continue;
         if (kind != PK_START) {
-          cplx<T> h = hP[u];
-          cplx<T> self = pm[u][0];
+          cplx<B> h = hP[u];
+          cplx<B> self = pm[u][0];
 #pragma unroll
           for (int j = 1; j < SM; ++j)
             if (j == s) self = pm[u][j];
 #pragma unroll
           for (int k = 0; k < RE; ++k) {
             if (k < ne) {
-              cplx<T> x = pm[u][0];
+              cplx<B> x = pm[u][0];
 #pragma unroll
               for (int j = 1; j < SM; ++j)
                 if (j == ecol[k]) x = pm[u][j];
-              const T vv = unit_coef ? vg[u][k] : ecoef[k] * vg[u][k];
-              h.re = fma(x.re, vv, h.re);
-              h.im = fma(x.im, vv, h.im);
+              const B vv = unit_coef ? vg[u][k] : ecoef[k] * vg[u][k];
+              h.re = fma_b(x.re, vv, h.re);
+              h.im = fma_b(x.im, vv, h.im);
             }
           }
           // (h - offset phi) * factor; a real offset and a purely imaginary
           // factor (real-time propagation) need half the multiplications
-          cplx<T> hm;
+          cplx<B> hm;
           if (off_real) {
-            hm.re = fma(-off.re, self.re, h.re);
-            hm.im = fma(-off.re, self.im, h.im);
+            hm.re = fma_b(-off.re, self.re, h.re);
+            hm.im = fma_b(-off.re, self.im, h.im);
           } else {
             hm = h - cmul(off, self);
           }
-          const cplx<T> bf = fac_imag ? mk(-fac.im * hm.im, fac.im * hm.re) : cmul(hm, fac);
+          const cplx<B> bf = fac_imag ? mk(-fac.im * hm.im, fac.im * hm.re) : cmul(hm, fac);
           const long long gidx = so + pp[u];
           if (kind == PK_FIRST) {
             v[u] = bf;
             if (owner) {
               const cplx<double> p0 = ps[u];
               acc += cabs2(p0);
-              st(phout + gidx, bf);
-              const cplx<double> b = ccast<double>(bf);
+              st(phoutb + gidx, bf);
+              const cplx<double> b = {b2d(bf.re), b2d(bf.im)};
               st(a.psi + gidx, mk(fma(b.re, a.a[1], p0.re * a.a[0]), fma(b.im, a.a[1], p0.im * a.a[0])));
             }
           } else {
-            const cplx<T> k2 = a.imag ? bf - km2[u] : bf + km2[u];
+            const cplx<B> k2 = a.imag ? bf - km2[u] : bf + km2[u];
             v[u] = k2;
             if (owner) {
-              st(phout + gidx, k2);
+              st(phoutb + gidx, k2);
               cplx<double> p0 = ps[u];
-              p0.re = fma(coeff_i, (double)k2.re, p0.re);
-              p0.im = fma(coeff_i, (double)k2.im, p0.im);
+              p0.re = fma(coeff_i, b2d(k2.re), p0.re);
+              p0.im = fma(coeff_i, b2d(k2.im), p0.im);
               st(a.psi + gidx, p0);
               acc = fma(p0.re, p0.re, fma(p0.im, p0.im, acc));
             }
@@ -256,19 +268,19 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
     if (kind == PK_LAST) continue;
     __syncthreads();
     unsigned long long tg1 = tr ? gtimer() : 0;
-    const int cur = fft_lines<T>(b0, b1, g.rp, L, tws, -1);
-    cplx<T> *bc = cur ? b1 : b0;
-    const T *__restrict__ kt = g.ktab + (long long)s * N;
+    const int cur = fft_lines<FT>(b0, b1, g.rp, L, tws, -1);
+    cplx<FT> *bc = cur ? b1 : b0;
     for (int w = 0; w < L; ++w)
       for (int i = threadIdx.x; i < N; i += blockDim.x) {
         const int x = lidx(w, i, LS);
-        bc[x] = cmulr(bc[x], __ldg(kt + i));
+        if constexpr (sizeof(T) == sizeof(double)) bc[x] = cmulr(bc[x], g.ktdf[(long long)s * N + i]);
+        else bc[x] = cmulr(bc[x], __ldg(g.ktab + (long long)s * N + i));
       }
     __syncthreads();
-    const int cur2 = fft_lines<T>(bc, cur ? b0 : b1, g.rp, L, tws, +1);
-    const cplx<T> *res = cur2 ? (cur ? b0 : b1) : bc;
+    const int cur2 = fft_lines<FT>(bc, cur ? b0 : b1, g.rp, L, tws, +1);
+    const cplx<FT> *res = cur2 ? (cur ? b0 : b1) : bc;
     unsigned long long tg2 = tr ? gtimer() : 0;
-    cplx<T> *dst = Pnext[d] + so;
+    cplx<B> *dst = reinterpret_cast<cplx<B> *>(Pnext[d]) + so;
     for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
       int w, i;
       if (istr == 1) { w = idx / N; i = idx - w * N; }
@@ -394,8 +406,13 @@ __global__ void __launch_bounds__(256, OCC) cheby_step_kernel(StepArgs<T> a) {
   unsigned long long tp[4] = {0, 0, 0, 0};
   unsigned long long *tpi = tp;  // gather, FFT + multiply, store (inside the phase), barrier
 
-  // phi_0 = psi (OCheby: ket0->FastCopy(*Psi))
-  for (long long i = gtid; i < n; i += gstride) st(a.buf[0] + i, ccast<T>(ld(a.psi + i)));
+  // phi_0 = psi (OCheby: ket0->FastCopy(*Psi)), in the bulk type of the phases
+  typedef typename FftType<T>::type B;
+  for (long long i = gtid; i < n; i += gstride) {
+    const cplx<double> p = ld(a.psi + i);
+    if (ND == 1) st(a.buf[0] + i, ccast<T>(p));
+    else st(reinterpret_cast<cplx<B> *>(a.buf[0]) + i, cplx<B>{d2b<B>(p.re), d2b<B>(p.im)});
+  }
   if (!grid_sync(a.bar)) return;
 
   double acc = 0.0, t;
