@@ -27,6 +27,10 @@ struct dfl {
   __host__ __device__ constexpr dfl(double x) : hi((float)x), lo((float)(x - (double)(float)x)) {}
   __host__ __device__ constexpr dfl(int x) : hi((float)x), lo(0.0f) {}
 };
+// A complex double-float is 16 bytes, like a complex double; aligned so that
+// shared-memory and global accesses move it with one 128-bit instruction.
+template <> struct __align__(16) cplx<dfl> { dfl re, im; };
+
 __device__ __forceinline__ dfl df_fast(float s, float e) {  // |s| >= |e|
   const float h = __fadd_rn(s, e);
   return dfl(h, __fsub_rn(e, __fsub_rn(h, s)));
