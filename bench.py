@@ -299,7 +299,7 @@ def engine_arm(args, world, rank, local):
         # DRAM bytes (read + write) of one step-kernel launch on this workload,
         # from an ncu capture of the same command (dram__bytes_read.sum +
         # dram__bytes_write.sum): the working set stays in L2
-        traffic = {"fp64": 5.49e6, "mixed": 3.75e6}[args.precision] if modes[top] == "cheby_step" else None
+        traffic = {"fp64": 5.31e6, "mixed": 3.75e6}[args.precision] if modes[top] == "cheby_step" else None
         roof = {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(ach / peak, 4), "traffic": traffic, "kernel": kname,
                 "algorithmic_bytes_per_launch": int(per_launch), "bytes_note": what,
