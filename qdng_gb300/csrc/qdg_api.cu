@@ -730,6 +730,11 @@ qdg_status step_setup(qdg_prop *P) {
   const char *env = getenv("QDG_CHEBY_MODE");
   if (env && strcmp(env, "graph") == 0) return QDG_OK;
   if (!p->nac.empty()) return QDG_OK;  // NAC elements run as extra line passes (graph path)
+  // The multi-dimensional step kernel computes the FP64 path's bulk in
+  // double-float (~48 bits).  Imaginary-time series reach the low states
+  // through cancellations of terms ~1/sqrt(2 pi R) down to e^{-R(1-X)}, which
+  // need the last bits of binary64: they take the graph path (binary64).
+  if (P->imag && p->precision == QDG_PREC_FP64 && p->nd > 1) return QDG_OK;
   const size_t cs = p->csize;
   if (p->nd == 1) {
     P->step_tw1 = p->dim[0].TW_e;
