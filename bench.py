@@ -107,6 +107,7 @@ class ClockSampler:
 WORKLOADS = {
     # name: (builder, description, coupling grids C, dipole grids D)
     "cfg2": ("cfg2_two_state", "cfg2 two-state 2-D Chebyshev, 256x256 grid x 2 states, dt=5 a.u.", 1, 0),
+    "cfg2gspo": ("cfg2_two_state", "cfg2 two-state 2-D GSPO, 256x256 grid x 2 states, dt=5 a.u.", 1, 0),
     "cfg1": ("cfg1_morse", "cfg1 1-D Morse Chebyshev, 1024 points, dt=10 a.u.", 0, 0),
     "cfg3": ("cfg3_anharmonic", "cfg3 3-D anharmonic Chebyshev, 128^3 grid, dt=10 a.u.", 0, 0),
     "cfg5sil": ("cfg5_double_well", "cfg5 2-D double well, 128x128, real-time SIL (Krylov 16), dt=20 a.u.", 0, 0),
@@ -118,7 +119,7 @@ WORKLOADS = {
 def workload(precision, name="cfg2"):
     from tests import cases
     builder, desc, C, D = WORKLOADS[name]
-    hp, psi, run = getattr(cases, builder)()
+    hp, psi, run = getattr(cases, builder)(gspo=True) if name == "cfg2gspo" else getattr(cases, builder)()
     # a mixed plan runs Krylov propagators on its FP64 copy unless the FP32
     # basis is asked for; the mixed bench line measures the FP32 basis
     fp32 = " krylov_fp32=1" if precision == "mixed" else ""
@@ -291,6 +292,10 @@ def engine_arm(args, world, rank, local):
             per_launch = term_bytes(npts, S, C, D, args.precision)
             what = "one Chebyshev term: read phi_(n-1), phi_(n-2), psi, potentials; write phi_n, psi"
             kname = "combine_kernel (cheby_term)"
+        elif modes[top] == "gspo_kin":
+            per_launch = npts * S * 2 * 16
+            what = "GSPO kinetic pass along one dimension: read psi, write exp(c T_d) psi (complex128)"
+            kname = "linepass_kernel (gspo_kin)"
         else:
             per_launch = npts * S * 2 * (16 if args.precision == "fp64" else 8)
             what = "kinetic line pass: read phi, write T_d phi"

@@ -9,6 +9,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 namespace qdg {
 
 template <typename T> struct cplx { T re, im; };
@@ -83,11 +85,11 @@ __device__ __forceinline__ void st(cplx<dfl> *p, cplx<dfl> c) {
 template <typename T> struct FftType { typedef T type; };
 template <> struct FftType<double> { typedef dfl type; };
 template <typename F, typename T> __device__ __forceinline__ cplx<F> to_fft(cplx<T> v) {
-  if constexpr (sizeof(F) == sizeof(T) && sizeof(T) == sizeof(float)) return v;
+  if constexpr (std::is_same<F, T>::value) return v;
   else return cplx<F>{df_from_double(v.re), df_from_double(v.im)};
 }
 template <typename T, typename F> __device__ __forceinline__ cplx<T> from_fft(cplx<F> v) {
-  if constexpr (sizeof(F) == sizeof(T) && sizeof(T) == sizeof(float)) return v;
+  if constexpr (std::is_same<F, T>::value) return v;
   else return cplx<T>{df_to_double(v.re), df_to_double(v.im)};
 }
 
