@@ -179,6 +179,8 @@ struct qdg_prop {
   std::vector<qdg::Couplings *> gcp_d;
   std::vector<double *> gcoef_d;
   std::vector<std::vector<void *>> gtab;  // [group][dim] S*n exp tables
+  std::vector<int> gdyn;                  // [group] member has a time-dependent (dipole) term
+  std::vector<void *> gU;                 // [group] precomputed per-point exp(c M(x)) of static members
   // Krylov
   int kord = 20, aorder = 0;
   double err = 1e-12, conv = 1e-12;
@@ -1105,6 +1107,10 @@ qdg_status gspo_init(qdg_prop *P) {
   P->gcp_d.assign(ng, nullptr);
   P->gcoef_d.assign(ng, nullptr);
   P->gtab.assign(ng, std::vector<void *>(p->nd, nullptr));
+  P->gdyn.assign(ng, 0);
+  P->gU.assign(ng, nullptr);
+  for (auto &t : p->terms)
+    if (t.kind == QDG_TERM_DIPOLE) P->gdyn[t.group] = 1;
   for (int g = 0; g < ng; ++g) {
     bool any = false, kin = false, pot = false;
     for (auto &t : p->terms)
@@ -1175,6 +1181,23 @@ qdg_status gspo_member(qdg_prop *P, int g, cplx<T> *x, long long step) {
       qdg_status s = launch_one<T>(p, qdg::PM_GSPO_KIN, d, a, nullptr);
       if (s != QDG_OK) return s;
     }
+  } else if (!P->gdyn[g]) {
+    // static member (OGSPO::InitExp computes its exponential once, OGSPO.cpp:30-52)
+    if (!P->gU[g]) {
+      const int kU = p->S == 2 ? 3 : p->S;
+      CK(cudaMalloc(&P->gU[g], sizeof(cplx<double>) * kU * (size_t)p->npts));
+      CK(qdg::launch_set_coefs(P->gcoef_d[g], P->gcp_d[g], p->d_lasers, p->laser_nt, step, p->stream));
+      double *g64 = nullptr;  // the grids in binary64 (a mixed plan keeps FP32 copies)
+      const size_t gb = sizeof(double) * std::max<size_t>(1, p->grids_h.size());
+      CK(cudaMalloc(&g64, gb));
+      if (!p->grids_h.empty())
+        CK(cudaMemcpyAsync(g64, p->grids_h.data(), sizeof(double) * p->grids_h.size(), cudaMemcpyHostToDevice, p->stream));
+      CK(qdg::launch_gspo_umat(reinterpret_cast<cplx<double> *>(P->gU[g]), p->S, p->npts, P->gcp_d[g], P->gcoef_d[g],
+                               g64, C(P->c0 * sf), p->stream));
+      CK(cudaStreamSynchronize(p->stream));
+      cudaFree(g64);
+    }
+    CK(qdg::launch_gspo_apply<T>(x, p->S, p->npts, reinterpret_cast<const cplx<double> *>(P->gU[g]), p->stream));
   } else {
     CK(qdg::launch_set_coefs(P->gcoef_d[g], P->gcp_d[g], p->d_lasers, p->laser_nt, step, p->stream));
     CK(qdg::launch_gspo_potential<T>(x, p->S, p->npts, P->gcp_d[g], P->gcoef_d[g],
@@ -1965,6 +1988,7 @@ qdg_status qdg_prop_destroy(qdg_prop *P) {
   for (auto &g : P->gtab) for (auto v : g) if (v) cudaFree(v);
   for (auto v : P->gcp_d) if (v) cudaFree(v);
   for (auto v : P->gcoef_d) if (v) cudaFree(v);
+  for (auto v : P->gU) if (v) cudaFree(v);
   for (auto v : P->lzb) if (v) cudaFree(v);
   if (P->kbuf) cudaFree(P->kbuf);
   if (P->d_ks) cudaFree(P->d_ks);

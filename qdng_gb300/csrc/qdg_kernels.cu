@@ -964,6 +964,74 @@ __global__ void gspo_potential_kernel(cplx<T> *psi, int S, long long npts, const
   }
 }
 
+// The same exponent as gspo_potential_kernel, stored instead of applied.
+__global__ void gspo_umat_kernel(cplx<double> *U, int S, long long npts, const Couplings *cp, const double *coef,
+                                 const double *grids, cplx<double> c) {
+  const int kU = S == 2 ? 3 : S;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npts; p += (long long)gridDim.x * blockDim.x) {
+    double m[kMaxStates * kMaxStates];
+    for (int i = 0; i < S * S; ++i) m[i] = 0;
+    for (int e = 0; e < cp->ne; ++e) m[cp->row[e] * S + cp->col[e]] += coef[e] * grids[(long long)cp->gid[e] * npts + p];
+    cplx<double> *u = U + (long long)kU * p;
+    if (S == 2 && (m[1] != 0.0 || m[2] != 0.0)) {
+      const double a = m[0], d = m[3], b = m[1];
+      const double mm = 0.5 * (a + d), h = 0.5 * (a - d);
+      const double r = sqrt(h * h + b * b);
+      const cplx<double> em = cexpd(mk(c.re * mm, c.im * mm));
+      const cplx<double> z = mk(c.re * r, c.im * r);
+      const cplx<double> ep = cexpd(z), en = cexpd(mk(-z.re, -z.im));
+      const cplx<double> ch = mk(0.5 * (ep.re + en.re), 0.5 * (ep.im + en.im));
+      cplx<double> shr;  // sinh(z)/r
+      if (r * sqrt(c.re * c.re + c.im * c.im) < 1e-4) {
+        const cplx<double> z2 = dmul(z, z);
+        shr = dmul(c, mk(1.0 + z2.re / 6.0, z2.im / 6.0));
+      } else {
+        shr = mk(0.5 * (ep.re - en.re) / r, 0.5 * (ep.im - en.im) / r);
+      }
+      // em [ch I + shr (M - m I)], (M - m I) = [[h, b], [b, -h]]
+      u[0] = dmul(em, ch + mk(shr.re * h, shr.im * h));
+      u[1] = dmul(em, mk(shr.re * b, shr.im * b));
+      u[2] = dmul(em, ch - mk(shr.re * h, shr.im * h));
+    } else if (S == 2) {
+      u[0] = cexpd(mk(c.re * m[0], c.im * m[0]));
+      u[1] = mk(0.0, 0.0);
+      u[2] = cexpd(mk(c.re * m[3], c.im * m[3]));
+    } else {
+      for (int s = 0; s < S; ++s) u[s] = cexpd(mk(c.re * m[s * S + s], c.im * m[s * S + s]));
+    }
+  }
+}
+cudaError_t launch_gspo_umat(cplx<double> *U, int S, long long npts, const Couplings *cp, const double *coef,
+                             const double *grids, cplx<double> c, cudaStream_t st) {
+  gspo_umat_kernel<<<ew_grid(npts), 256, 0, st>>>(U, S, npts, cp, coef, grids, c);
+  COUNT_LAUNCH();
+  return cudaGetLastError();
+}
+
+template <typename T>
+__global__ void gspo_apply_kernel(cplx<T> *psi, int S, long long npts, const cplx<double> *U) {
+  const int kU = S == 2 ? 3 : S;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npts; p += (long long)gridDim.x * blockDim.x) {
+    const cplx<double> *u = U + (long long)kU * p;
+    if (S == 2) {
+      const cplx<double> x0 = ccast<double>(ld(psi + p)), x1 = ccast<double>(ld(psi + npts + p));
+      st(psi + p, ccast<T>(dmul(u[0], x0) + dmul(u[1], x1)));
+      st(psi + npts + p, ccast<T>(dmul(u[1], x0) + dmul(u[2], x1)));
+    } else {
+      for (int s = 0; s < S; ++s)
+        st(psi + s * npts + p, ccast<T>(dmul(u[s], ccast<double>(ld(psi + s * npts + p)))));
+    }
+  }
+}
+template <typename T>
+cudaError_t launch_gspo_apply(cplx<T> *psi, int S, long long npts, const cplx<double> *U, cudaStream_t st) {
+  gspo_apply_kernel<T><<<ew_grid(npts), 256, 0, st>>>(psi, S, npts, U);
+  COUNT_LAUNCH();
+  return cudaGetLastError();
+}
+template cudaError_t launch_gspo_apply<double>(cplx<double> *, int, long long, const cplx<double> *, cudaStream_t);
+template cudaError_t launch_gspo_apply<float>(cplx<float> *, int, long long, const cplx<double> *, cudaStream_t);
+
 template <typename T>
 cudaError_t launch_gspo_potential(cplx<T> *psi, int S, long long npts, const Couplings *cp, const double *coef,
                                   const T *grids, cplx<double> c, cudaStream_t st) {

@@ -279,6 +279,13 @@ cudaError_t launch_dots(const cplx<T> *a, const cplx<U> *b, int S, long long npt
 // GSPO potential member: psi <- exp(c * M(x)) psi per grid point, where
 // M(x) = sum coef_e grid_e(x) over the member's entries (ODMultistate with
 // TransformMSD per-point diagonalisation, ODMultistate.cpp:115-182).
+// Time-independent potential members: the per-point propagator
+// exp(c M(x)) once (S = 2: u00, u01 = u10, u11; otherwise the S diagonal
+// factors), then a per-point matrix-vector product each half step.
+cudaError_t launch_gspo_umat(cplx<double> *U, int S, long long npts, const Couplings *cp, const double *coef,
+                             const double *grids, cplx<double> c, cudaStream_t st);
+template <typename T>
+cudaError_t launch_gspo_apply(cplx<T> *psi, int S, long long npts, const cplx<double> *U, cudaStream_t st);
 template <typename T>
 cudaError_t launch_gspo_potential(cplx<T> *psi, int S, long long npts, const Couplings *cp, const double *coef,
                                   const T *grids, cplx<double> c, cudaStream_t st);
