@@ -1,6 +1,6 @@
 """Benchmark: QDng Chebyshev propagation of the 256x256 two-state grid.
 
-Workload (benchmark configs[1], Chebyshev part): 2-D two-state
+Workload (the reference's two-state 2-D benchmark, Chebyshev part): 2-D two-state
 diabatic model, 256 x 256 grid on [-4,4]^2, masses (1836, 3672), harmonic
 surfaces with k = 0.02, Gaussian coupling V12 = 0.01 exp(-(x-0.5)^2 - y^2),
 displaced Gaussian start on state 1, dt = 5 a.u.  One "step" is one
@@ -358,7 +358,7 @@ def engine_arm(args, world, rank, local):
         # the FP64 path keeps psi and the reductions in FP64 and runs phi, H phi
         # and the FFTs of the multi-dimensional step in double-float (2 x f32)
         "dtype": ("f64+df32" if hp.grid.ndims > 1 else "f64") if args.precision == "fp64" else "f32+f64",
-        "data": "synthetic (seeded analytic potentials and Gaussian start, BASELINE configs[1])",
+        "data": "synthetic (seeded analytic potentials and Gaussian start)",
         "config": dict(cfg, parallelism="replicas" if world > 1 else "single",
                        cheby_order=info["order"]),
         "e2e": {"value": round(e2e_val, 1), "unit": "grid-pt*steps/s",
@@ -377,7 +377,7 @@ def engine_arm(args, world, rank, local):
 
 
 def ensemble_arm(args, world, rank, local):
-    """BASELINE configs[3]: 512 laser-driven members, one persistent launch per
+    """Ensemble of 512 laser-driven members, one persistent launch per
     call; wavepackets/s = members x (steps / 5000) / time."""
     import numpy as np
     import torch
@@ -444,7 +444,7 @@ def ensemble_arm(args, world, rank, local):
         "scaling": "strong",
         "vs_baseline": None,
         "dtype": "f64" if args.precision == "fp64" else "f32+f64",
-        "data": "synthetic (seeded Morse members, BASELINE configs[3])",
+        "data": "synthetic (seeded Morse members)",
         "config": {"workload": "cfg4 ensemble: 512 members, 1-D 256-4096 / 2-D 64^2-256^2, dt=10, mass 1728",
                    "precision": args.precision, "l2": "members larger than L2 in total (not flushed)",
                    "terms_per_step_total": terms / args.steps},
@@ -476,7 +476,7 @@ def reference_arm(args, world, rank):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
-        "data": "synthetic (seeded analytic potentials and Gaussian start, BASELINE configs[1])",
+        "data": "synthetic (seeded analytic potentials and Gaussian start)",
         "config": dict(cfg, l2="n/a (host)"),
         "impl": "reference",
         "cpu_baseline": {"value": round(v, 1), "unit": "grid-pt*steps/s", "cores": threads, "kind": "port",

@@ -194,7 +194,7 @@ ENS_2D_SIDES = [64, 96, 128, 192, 256]
 
 
 def cfg4_member(rng, kind, size, nt=5000, dt=10.0):
-    """One laser-driven Morse member (BASELINE configs[3]); 2-D members add a
+    """One laser-driven Morse member of the 512-member ensemble; 2-D members add a
     harmonic y mode.  Box x in [1,10] (y in [-3,3]), mass 1728, dt 10."""
     D = rng.uniform(0.05, 0.2)
     a = rng.uniform(0.7, 1.3)
