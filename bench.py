@@ -301,10 +301,15 @@ def engine_arm(args, world, rank, local):
             what = "kinetic line pass: read phi, write T_d phi"
             kname = f"kin_all_kernel ({modes[top]})"
         ach = per_launch / avg_s / 1e9
-        # DRAM bytes (read + write) of one step-kernel launch on this workload,
-        # from an ncu capture of the same command (dram__bytes_read.sum +
-        # dram__bytes_write.sum): the working set stays in L2
-        traffic = {"fp64": 5.31e6, "mixed": 3.75e6}[args.precision] if modes[top] == "cheby_step" else None
+        # DRAM bytes (read + write) of one launch of the dominant kernel, from
+        # an ncu capture of the same command (dram__bytes_read.sum +
+        # dram__bytes_write.sum); only the 256^2 x 2 workloads were captured
+        # (their working set stays in L2), the others report null
+        traffic = None
+        if args.workload == "cfg2" and modes[top] == "cheby_step":
+            traffic = {"fp64": 5.31e6, "mixed": 3.75e6}[args.precision]
+        elif args.workload == "cfg2gspo" and modes[top] == "gspo_kin":
+            traffic = 2.21e6
         roof = {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(ach / peak, 4), "traffic": traffic, "kernel": kname,
                 "algorithmic_bytes_per_launch": int(per_launch), "bytes_note": what,

@@ -681,17 +681,47 @@ template cudaError_t launch_dots_if<double, double>(const cplx<double> *, const 
 template cudaError_t launch_dots_if<float, float>(const cplx<float> *, const cplx<float> *, int, long long, double *,
                                                   int, const int *, cudaStream_t);
 
+// Per-state sums of the dots kernels' block partials (layout
+// [block][state][re, im]) in the order of the host's dot products: blocks
+// outer, states inner, each state's sum accumulated block by block.  The
+// block's threads stage the partials in shared memory (independent loads in
+// flight together); thread 0 then adds them in that order, so re/im (valid in
+// thread 0) are bit-identical to the host's sums.  Every thread of the block
+// calls this.
+__device__ __forceinline__ void sum_partials(const double *partials, int grid, int S, double *re, double *im) {
+  constexpr int kChunk = 1024;  // even: an (re, im) pair never straddles two chunks
+  __shared__ double buf[kChunk];
+  for (int s = 0; s < S; ++s) re[s] = im[s] = 0.0;
+  const int n = 2 * grid * S;
+  for (int c = 0; c < n; c += kChunk) {
+    const int m = min(kChunk, n - c);
+    for (int i = threadIdx.x; i < m; i += blockDim.x) buf[i] = __ldcg(partials + c + i);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      if (S == 1) {
+        double r = re[0], q = im[0];
+        for (int i = 0; i < m; i += 2) { r += buf[i]; q += buf[i + 1]; }
+        re[0] = r;
+        im[0] = q;
+      } else {
+        for (int i = 0; i < m; i += 2) {
+          const int s = ((c + i) >> 1) % S;
+          re[s] += buf[i];
+          im[s] += buf[i + 1];
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // Partial sums -> scalar, summed in the order of the host's dot products
 // (blocks outer, states inner; states weighted, then added in order).
 __global__ void ks_finish_kernel(const double *partials, KsFinish f, double *ks, int *done) {
-  if (threadIdx.x != 0 || *done) return;
+  if (*done) return;  // same value for every thread: nothing in the kernel writes done[0]
   double re[kMaxStates], im[kMaxStates];
-  for (int s = 0; s < f.S; ++s) re[s] = im[s] = 0.0;
-  for (int b = 0; b < f.grid; ++b)
-    for (int s = 0; s < f.S; ++s) {
-      re[s] += partials[(b * f.S + s) * 2];
-      im[s] += partials[(b * f.S + s) * 2 + 1];
-    }
+  sum_partials(partials, f.grid, f.S, re, im);
+  if (threadIdx.x != 0) return;
   double tr = 0.0;
   for (int s = 0; s < f.S; ++s) tr += re[s] * f.w;
   if (f.mode == KS_ALPHA) {
@@ -717,16 +747,13 @@ __global__ void ks_commit_kernel(int *done) {
 }
 __global__ void ka_finish_kernel(const double *partials, KaArgs a, int op, int j, int col, double *ks, int *ia,
                                  int *done) {
-  if (threadIdx.x != 0) return;
+  // both exits are the same for every thread: done[0] and ia[0] are written
+  // below by thread 0 only after every thread has read them
   if (op != KA_LAST && *done) return;
   if (op == KA_LAST && j >= ia[0]) return;
   double re[kMaxStates], im[kMaxStates];
-  for (int s = 0; s < a.S; ++s) re[s] = im[s] = 0.0;
-  for (int b = 0; b < a.grid; ++b)
-    for (int s = 0; s < a.S; ++s) {
-      re[s] += partials[(b * a.S + s) * 2];
-      im[s] += partials[(b * a.S + s) * 2 + 1];
-    }
+  sum_partials(partials, a.grid, a.S, re, im);
+  if (threadIdx.x != 0) return;
   double tr = 0.0, ti = 0.0;
   for (int s = 0; s < a.S; ++s) { tr += re[s] * a.w; ti += im[s] * a.w; }
   const int m = a.m;
