@@ -758,7 +758,11 @@ qdg_status step_setup(qdg_prop *P) {
     total += (p->npts / p->dim[d].n) * p->S;
   }
   P->line_start[p->nd] = total;
-  const size_t budget = 112 * 1024;  // shared memory per block for the line buffers
+  // shared memory per block for the line buffers: a kernel that fits one
+  // block per SM anyway (its registers) takes most of the SM's 228 KB, so
+  // large grids transform more lines per batch; otherwise two blocks fit
+  const size_t budget =
+      qdg::cheby_step_max_blocks<T>(p->S, p->nd, 256, 16 * 1024) == 1 ? 200 * 1024 : 112 * 1024;
   int grid = 0;
   size_t smem = 0;
   for (int iter = 0, per_sm = 0; iter < 3; ++iter) {
