@@ -303,11 +303,14 @@ def engine_arm(args, world, rank, local):
         ach = per_launch / avg_s / 1e9
         # DRAM bytes (read + write) of one launch of the dominant kernel, from
         # an ncu capture of the same command (dram__bytes_read.sum +
-        # dram__bytes_write.sum); only the 256^2 x 2 workloads were captured
-        # (their working set stays in L2), the others report null
+        # dram__bytes_write.sum); the 256^2 x 2 working set stays in L2, the
+        # 128^3 step re-reads its inputs once per dimension; workloads not
+        # captured report null
         traffic = None
         if args.workload == "cfg2" and modes[top] == "cheby_step":
             traffic = {"fp64": 5.31e6, "mixed": 3.75e6}[args.precision]
+        elif args.workload == "cfg3" and modes[top] == "cheby_step" and args.precision == "fp64":
+            traffic = 1.652e10
         elif args.workload == "cfg2gspo" and modes[top] == "gspo_kin":
             traffic = 2.21e6
         roof = {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
