@@ -289,9 +289,8 @@ qdg_status qdg_prop_phase_times(qdg_prop *prop, double ns[4]);
  * queued on cuda_stream (NULL: the legacy default stream) without
  * synchronising.  Every call shares the scratch array: calls whose kernels
  * overlap on the GPU race, so serialise them on one stream.  The first call
- * on a device looks up the array's address with that device current; make
- * it before any stream capture.  This entry point has no counterpart in the
- * reference. */
+ * on a device looks up the array's address with that device current.  This
+ * entry point has no counterpart in the reference. */
 qdg_status qdg_h_apply_noalloc(const qdg_hplan_desc *desc, const double *psi_in, double *psi_out,
                                int64_t step, void *cuda_stream);
 

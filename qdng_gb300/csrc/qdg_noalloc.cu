@@ -14,7 +14,7 @@
 // calls whose kernels overlap on the GPU (different streams, or other
 // threads) race on it; serialise them on one stream.  The first call on a
 // device looks up the array's device address (cudaGetSymbolAddress) with
-// that device current; make that first call before any stream capture.
+// that device current.
 #include <cuda_runtime.h>
 
 #include <cmath>
