@@ -3,7 +3,8 @@
  *
  * This is the drop-in boundary for QDng's time-stepping hot path. A QDng
  * operator module (a C++ OPropagator subclass built against the QDng
- * headers) walks its Hamiltonian tree once in
+ * headers; qdng_module/OGPUCheby.cpp in this repository) walks its
+ * Hamiltonian tree once in
  * Init(WaveFunction*), fills a qdg_hplan_desc and then calls the entry
  * points below once per time step from Apply(WaveFunction*).
  *
@@ -57,9 +58,20 @@ typedef enum qdg_term_kind {
                               (src/qdlib/OGridNAC.cpp:131-148), derivatives by FFT (OGridNabla.cpp:76-95) */
 } qdg_term_kind;
 
+/* Arithmetic of a plan.  FP64 is the drop-in form: every value (psi, phi_n,
+ * H phi, the FFTs, potentials, coefficients and reductions) is IEEE binary64,
+ * as in the reference.  MIXED keeps H phi, phi_n and the FFTs in FP32 and
+ * the series coefficients, the psi accumulator, norms, energies, overlaps
+ * and Krylov scalars in binary64.  DF64 is binary64 except for the
+ * Chebyshev step of grids with two or more dimensions, whose phi_n, H phi,
+ * potential values and FFTs are double-float (an unevaluated sum of two
+ * FP32 numbers: about 48 significant bits and the FP32 exponent range;
+ * wave-function values below ~1e-38 of the scale are lost), with psi and
+ * the reductions binary64. */
 typedef enum qdg_precision {
-  QDG_PREC_FP64 = 0,       /* IEEE binary64 everywhere (the drop-in path) */
-  QDG_PREC_MIXED = 1       /* FP32 H*phi bulk, FP64 coefficients, psi accumulator and reductions */
+  QDG_PREC_FP64 = 0,
+  QDG_PREC_MIXED = 1,
+  QDG_PREC_DF64 = 2
 } qdg_precision;
 
 /* Grid description: QDng GridSystem (src/qdlib/GridSystem.cpp:195-215).
@@ -270,6 +282,13 @@ qdg_status qdg_profile_read(qdg_plan *plan, double ms[8], int64_t launches[8]);
  * ns spent by block 0 in its own kinetic work, waiting at the barrier after
  * it, in its own point work, and waiting at the norm barrier; resets them. */
 qdg_status qdg_prop_phase_times(qdg_prop *prop, double ns[4]);
+/* Failure-path test aid: the next persistent step kernel launched for this
+ * plan finds its grid barrier's arrival count preset so that no arrival
+ * completes it.  Every block then waits out its bounded spin, raises the
+ * barrier's error flag and leaves; the step returns QDG_ETIMEOUT, the
+ * barrier is reset, and psi must be restored by the caller (the step was
+ * cut short).  No device wait is unbounded and nothing faults. */
+qdg_status qdg_plan_inject_barrier_stall(qdg_plan *plan);
 
 /* ---- H psi without device allocation ------------------------------------ */
 

@@ -17,19 +17,37 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = None
 
 
-def build(force=False):
-    """Compile liborc.so with the committed Makefile (g++, OpenMP, no fast-math)."""
-    so = os.path.join(_HERE, "liborc.so")
+# Builds of the same source: the parity oracle ("", -O2, IEEE arithmetic)
+# and two timed CPU baselines ("o3": -O3 -funroll-loops; "fast": also
+# -ffast-math, QDng's configure default for optimised builds).
+VARIANTS = {"": "liborc.so", "o3": "liborc_o3.so", "fast": "liborc_fast.so"}
+
+
+def build(force=False, variant=""):
+    """Compile the oracle libraries with the committed Makefile (g++, OpenMP)."""
+    so = os.path.join(_HERE, VARIANTS[variant])
     src = os.path.join(_HERE, "qdng_oracle.cpp")
     if force or not os.path.exists(so) or os.path.getmtime(so) < os.path.getmtime(src):
-        subprocess.check_call(["make", "-s", "-C", _HERE])
+        subprocess.check_call(["make", "-s", "-C", _HERE, VARIANTS[variant]])
     return so
+
+
+def use_variant(variant):
+    """Load a timed-baseline build instead of the parity oracle (before the
+    first call; bench.py's CPU legs only)."""
+    global _LIB, _VARIANT
+    if _LIB is not None and _VARIANT != variant:
+        raise RuntimeError("the oracle library is already loaded")
+    _VARIANT = variant
+
+
+_VARIANT = ""
 
 
 def lib():
     global _LIB
     if _LIB is None:
-        L = C.CDLL(build())
+        L = C.CDLL(build(variant=_VARIANT))
         vp, dp = C.c_void_p, C.POINTER(C.c_double)
         L.orc_last_error.restype = C.c_char_p
         L.orc_num_threads.argtypes = [C.c_int]

@@ -29,6 +29,7 @@ TERM_NAC = 4
 
 PREC_FP64 = 0
 PREC_MIXED = 1
+PREC_DF64 = 2
 
 
 class Grid(C.Structure):
@@ -135,6 +136,7 @@ SIGNATURES = [
     ("qdg_profile_enable", _i32, [_vp, _i32]),
     ("qdg_profile_read", _i32, [_vp, _dp, C.POINTER(_i64)]),
     ("qdg_prop_phase_times", _i32, [_vp, _dp]),
+    ("qdg_plan_inject_barrier_stall", _i32, [_vp]),
     ("qdg_h_apply_noalloc", _i32, [C.POINTER(HPlanDesc), _dp, _dp, _i64, _vp]),
     ("qdg_ensemble_create", _i32, [C.POINTER(EnsembleMember), _i32, C.c_double, C.c_char_p, _i32, C.POINTER(_vp)]),
     ("qdg_ensemble_destroy", _i32, [_vp]),

@@ -55,7 +55,7 @@ struct DimInfo {
   void *tw;           // n twiddles (cplx<T>)
   double *kfac;       // [S] dk^2/(2m)/n for H passes
   void *ktab;         // [S][n] kfac[s] * min(i, n-i)^2 in the bulk type
-  void *twdf = nullptr;  // FP64 plans: twiddles and k^2 multipliers in double-float
+  void *twdf = nullptr;  // DF64 plans: twiddles and k^2 multipliers in double-float
   void *ktdf = nullptr;
   int TW_k, TW_e;     // lines per tile: kinetic-only passes, coupled epilogue pass
 };
@@ -99,7 +99,7 @@ struct qdg_plan {
   int nac_tw[QDG_MAX_DIMS] = {1, 1, 1, 1};
   // device
   void *d_grids = nullptr;      // bulk type
-  void *d_grids_df = nullptr;   // FP64 plans: the grids in double-float
+  void *d_grids_df = nullptr;   // DF64 plans: the grids in double-float
   double *d_lasers = nullptr;
   DimInfo dim[QDG_MAX_DIMS];
   qdg::Couplings cp_h;           // all potential/dipole entries of H
@@ -199,6 +199,10 @@ template <typename T> struct Bulk;
 
 long long wf_elems(const qdg_plan *p) { return p->npts * p->S; }
 
+// Plans whose storage type is binary64 (FP64 and DF64 forms); mixed plans
+// store FP32.
+bool is64(const qdg_plan *p) { return p->precision != QDG_PREC_MIXED; }
+
 double parse_d(const qdg_prop *p, const char *k) { return atof(p->params.at(k).c_str()); }
 bool has(const qdg_prop *p, const char *k) { return p->params.count(k) > 0; }
 
@@ -288,7 +292,7 @@ int choose_tw(const qdg_plan *p, int d, int nsub) {
   const DimInfo &di = p->dim[d];
   const long long lines = p->npts / di.n;
   const long long limit = (d == 0) ? lines : di.stride;  // TW must divide this
-  const int target_elems = p->precision == QDG_PREC_FP64 ? 2048 : 4096;
+  const int target_elems = is64(p) ? 2048 : 4096;
   int best = 1;
   for (int tw = 2; tw <= 32; tw *= 2) {
     if (limit % tw) break;
@@ -534,8 +538,8 @@ qdg_status upload_tables(qdg_plan *p) {
       }
     CK(cudaMalloc(&di.ktab, sizeof(T) * kt.size()));
     CK(cudaMemcpy(di.ktab, kt.data(), sizeof(T) * kt.size(), cudaMemcpyHostToDevice));
-    if (sizeof(T) == sizeof(double)) {
-      // double-float copies for the FFTs of the FP64 step kernel
+    if (p->precision == QDG_PREC_DF64) {
+      // double-float copies for the FFTs of the DF64 step kernel
       std::vector<qdg::cplx<qdg::dfl>> twd(n);
       for (int m = 0; m < n; ++m) {
         const long double ang = -2.0L * pi * (long double)m / (long double)n;
@@ -556,7 +560,7 @@ qdg_status upload_tables(qdg_plan *p) {
   for (size_t i = 0; i < g.size(); ++i) g[i] = (T)p->grids_h[i];
   CK(cudaMalloc(&p->d_grids, sizeof(T) * std::max<size_t>(1, g.size())));
   if (!g.empty()) CK(cudaMemcpy(p->d_grids, g.data(), sizeof(T) * g.size(), cudaMemcpyHostToDevice));
-  if (sizeof(T) == sizeof(double)) {
+  if (p->precision == QDG_PREC_DF64) {
     std::vector<qdg::dfl> gd(p->grids_h.size());
     for (size_t i = 0; i < gd.size(); ++i) gd[i] = qdg::dfl(p->grids_h[i]);
     CK(cudaMalloc(&p->d_grids_df, sizeof(qdg::dfl) * std::max<size_t>(1, gd.size())));
@@ -726,23 +730,30 @@ qdg_status h_apply_bulk(qdg_plan *p, const cplx<double> *psi, cplx<T> *out, long
 // ------------------------------------------------------------ Chebyshev
 // Persistent step kernel configuration (cooperative launch: every block
 // resident).  step_grid stays 0 when the kernel cannot be made resident.
+int step_bulk(const qdg_plan *p) {
+  return p->precision == QDG_PREC_MIXED ? qdg::BULK_F32 : p->precision == QDG_PREC_DF64 ? qdg::BULK_DF64 : qdg::BULK_F64;
+}
+
 template <typename T>
 qdg_status step_setup(qdg_prop *P) {
   qdg_plan *p = P->plan;
-  const char *env = getenv("QDG_CHEBY_MODE");
-  if (env && strcmp(env, "graph") == 0) return QDG_OK;
+  // "path=graph" among the propagator parameters selects the multi-launch
+  // graph form of the step (a cross-check of the persistent kernel)
+  if (has(P, "path") && P->params.at("path") == "graph") return QDG_OK;
   if (!p->nac.empty()) return QDG_OK;  // NAC elements run as extra line passes (graph path)
-  // The multi-dimensional step kernel computes the FP64 path's bulk in
-  // double-float (~48 bits).  Imaginary-time series reach the low states
-  // through cancellations of terms ~1/sqrt(2 pi R) down to e^{-R(1-X)}, which
-  // need the last bits of binary64: they take the graph path (binary64).
-  if (P->imag && p->precision == QDG_PREC_FP64 && p->nd > 1) return QDG_OK;
+  // The DF64 form's multi-dimensional step kernel computes its bulk in
+  // double-float (~48 bits, FP32 exponent range).  Imaginary-time series
+  // reach the low states through cancellations of terms ~1/sqrt(2 pi R) down
+  // to e^{-R(1-X)}, which need the last bits of binary64: they take the graph
+  // path (binary64).
+  if (P->imag && p->precision == QDG_PREC_DF64 && p->nd > 1) return QDG_OK;
+  const int bulk = step_bulk(p);
   const size_t cs = p->csize;
   if (p->nd == 1) {
     P->step_tw1 = p->dim[0].TW_e;
     const size_t smem = pass_smem(p, 0, P->step_tw1, p->S);
     if (smem > 227 * 1024) return QDG_OK;
-    const int per_sm = qdg::cheby_step_max_blocks<T>(p->S, p->nd, 256, smem);
+    const int per_sm = qdg::cheby_step_max_blocks(bulk, p->S, p->nd, 256, smem);
     if (per_sm <= 0) return QDG_OK;
     long long want = p->npts / ((long long)p->dim[0].n * P->step_tw1);
     want = std::min<long long>(want, (long long)per_sm * p->sm_count);
@@ -762,12 +773,12 @@ qdg_status step_setup(qdg_prop *P) {
   // block per SM anyway (its registers) takes most of the SM's 228 KB, so
   // large grids transform more lines per batch; otherwise two blocks fit
   const size_t budget =
-      qdg::cheby_step_max_blocks<T>(p->S, p->nd, 256, 16 * 1024) == 1 ? 200 * 1024 : 112 * 1024;
+      qdg::cheby_step_max_blocks(bulk, p->S, p->nd, 256, 16 * 1024) == 1 ? 200 * 1024 : 112 * 1024;
   int grid = 0;
   size_t smem = 0;
   for (int iter = 0, per_sm = 0; iter < 3; ++iter) {
     const size_t probe = iter == 0 ? 16 * 1024 : smem;
-    per_sm = qdg::cheby_step_max_blocks<T>(p->S, p->nd, 256, probe);
+    per_sm = qdg::cheby_step_max_blocks(bulk, p->S, p->nd, 256, probe);
     if (per_sm <= 0) return QDG_OK;
     grid = (int)std::min<long long>((long long)per_sm * p->sm_count, std::min<long long>(total, p->max_parts));
     const long long chunk = (total + grid - 1) / grid;
@@ -780,9 +791,9 @@ qdg_status step_setup(qdg_prop *P) {
       smem = std::max(smem, ((size_t)n + 2 * qdg::line_buf_elems((int)n, lm)) * cs);
     }
     if (smem > 227 * 1024) return QDG_OK;
-    if (qdg::cheby_step_max_blocks<T>(p->S, p->nd, 256, smem) >= per_sm) break;
+    if (qdg::cheby_step_max_blocks(bulk, p->S, p->nd, 256, smem) >= per_sm) break;
   }
-  const int per_sm = qdg::cheby_step_max_blocks<T>(p->S, p->nd, 256, smem);
+  const int per_sm = qdg::cheby_step_max_blocks(bulk, p->S, p->nd, 256, smem);
   if (per_sm <= 0) return QDG_OK;
   P->step_grid = std::min(grid, per_sm * p->sm_count);
   P->step_smem = smem;
@@ -795,6 +806,7 @@ qdg_status cheby_step_persistent(qdg_prop *P, cplx<double> *psi, long long step)
   CK(qdg::launch_set_coefs(p->d_coef, p->d_cp, p->d_lasers, p->laser_nt, step, p->stream));
   qdg::StepArgs<T> a;
   memset(&a, 0, sizeof(a));
+  a.bulk = step_bulk(p);
   a.nd = p->nd;
   a.S = p->S;
   a.npts = p->npts;
@@ -879,7 +891,7 @@ qdg_status cheby_init(qdg_prop *P) {
     CK(cudaMalloc(&P->d_a, sizeof(double) * P->order));
     CK(cudaMemcpy(P->d_a, P->coeff.data(), sizeof(double) * P->order, cudaMemcpyHostToDevice));
   }
-  qdg_status ps = p->precision == QDG_PREC_FP64 ? step_setup<double>(P) : step_setup<float>(P);
+  qdg_status ps = is64(p) ? step_setup<double>(P) : step_setup<float>(P);
   if (ps != QDG_OK) return ps;
   CK(cudaMallocHost(&P->h_cs, sizeof(qdg::ChebyState)));
   return QDG_OK;
@@ -1143,7 +1155,7 @@ qdg_status gspo_init(qdg_prop *P) {
             tab[(size_t)t.row * n + i] = std::exp(z) / (long double)n;
           }
         }
-        if (p->precision == QDG_PREC_FP64) {
+        if (is64(p)) {
           std::vector<cplx<double>> h(tab.size());
           for (size_t i = 0; i < tab.size(); ++i) { h[i].re = (double)tab[i].real(); h[i].im = (double)tab[i].imag(); }
           CK(cudaMalloc(&P->gtab[g][d], sizeof(cplx<double>) * h.size()));
@@ -1166,7 +1178,7 @@ qdg_status gspo_init(qdg_prop *P) {
       CK(cudaMalloc(&P->gcoef_d[g], sizeof(double) * qdg::kMaxCouplings));
     }
   }
-  if (p->precision != QDG_PREC_FP64) CK(cudaMalloc(&P->k0, p->csize * wf_elems(p)));
+  if (!is64(p)) CK(cudaMalloc(&P->k0, p->csize * wf_elems(p)));
   return QDG_OK;
 }
 
@@ -1555,7 +1567,7 @@ qdg_status prop_step_t(qdg_prop *P, cplx<double> *psi, long long step, int *used
 }
 
 qdg_status prop_step(qdg_prop *P, cplx<double> *psi, long long step, int *used, bool sync) {
-  if (P->plan->precision == QDG_PREC_FP64) return prop_step_t<double>(P, psi, step, used, sync);
+  if (is64(P->plan)) return prop_step_t<double>(P, psi, step, used, sync);
   return prop_step_t<float>(P, psi, step, used, sync);
 }
 
@@ -1563,7 +1575,7 @@ qdg_status prop_step(qdg_prop *P, cplx<double> *psi, long long step, int *used, 
 qdg_status h_expec(qdg_plan *p, const cplx<double> *a, const cplx<double> *b, cd *out) {
   std::vector<cd> d;
   qdg_status s;
-  if (p->precision == QDG_PREC_FP64) {
+  if (is64(p)) {
     cplx<double> *o = reinterpret_cast<cplx<double> *>(p->d_scratch);
     if ((s = h_apply_bulk<double>(p, b, o, 0)) != QDG_OK) return s;
     if ((s = dots<double, double>(p, a, o, d)) != QDG_OK) return s;
@@ -1691,7 +1703,8 @@ int32_t qdg_abi_version(void) { return QDG_ABI_VERSION; }
 qdg_status qdg_plan_create(const qdg_hplan_desc *desc, int32_t precision, qdg_plan **out) {
   if (!desc || !out) return fail(QDG_EINVAL, "null argument");
   *out = nullptr;
-  if (precision != QDG_PREC_FP64 && precision != QDG_PREC_MIXED) return fail(QDG_EINVAL, "unknown precision");
+  if (precision != QDG_PREC_FP64 && precision != QDG_PREC_MIXED && precision != QDG_PREC_DF64)
+    return fail(QDG_EINVAL, "unknown precision");
   const qdg_grid &g = desc->grid;
   if (g.ndims < 1 || g.ndims > QDG_MAX_DIMS) return fail(QDG_EINVAL, "invalid number of grid dimensions");
   if (desc->nstates < 1 || desc->nstates > qdg::kMaxStates) return fail(QDG_EUNSUPPORTED, "number of states outside 1..8");
@@ -1703,7 +1716,7 @@ qdg_status qdg_plan_create(const qdg_hplan_desc *desc, int32_t precision, qdg_pl
   p->S = desc->nstates;
   p->nd = g.ndims;
   p->precision = precision;
-  p->csize = precision == QDG_PREC_FP64 ? sizeof(cplx<double>) : sizeof(cplx<float>);
+  p->csize = is64(p) ? sizeof(cplx<double>) : sizeof(cplx<float>);
   long long stride = 1;
   for (int d = 0; d < g.ndims; ++d) {
     if (g.n[d] < 2) { free_plan(p); return fail(QDG_EINVAL, "Zero points grid defined"); }
@@ -1780,7 +1793,7 @@ qdg_status qdg_plan_create(const qdg_hplan_desc *desc, int32_t precision, qdg_pl
       cudaMemset(p->d_bar, 0, sizeof(qdg::GridBarrier)) != cudaSuccess ||
       cudaMallocHost(&p->h_bar, sizeof(qdg::GridBarrier)) != cudaSuccess)
     return cleanup(fail(QDG_ENOMEM, "device allocation failed"));
-  s = precision == QDG_PREC_FP64 ? upload_tables<double>(p) : upload_tables<float>(p);
+  s = is64(p) ? upload_tables<double>(p) : upload_tables<float>(p);
   if (s != QDG_OK) return cleanup(s);
   *out = p;
   return QDG_OK;
@@ -1869,7 +1882,7 @@ qdg_status qdg_h_apply(qdg_plan *plan, const qdg_wf *in, qdg_wf *out, int64_t st
   if (!plan || !in || !out || in->plan != plan || out->plan != plan) return fail(QDG_EINVAL, "bad arguments");
   if (in == out) return fail(QDG_EINVAL, "H apply needs distinct input and output");
   qdg_status s;
-  if (plan->precision == QDG_PREC_FP64) {
+  if (is64(plan)) {
     s = h_apply_bulk<double>(plan, in->d, out->d, step);
   } else {
     cplx<float> *o = reinterpret_cast<cplx<float> *>(plan->d_scratch);
@@ -1892,7 +1905,7 @@ qdg_status qdg_observables_compute(qdg_plan *plan, const qdg_wf *psi, const qdg_
   for (int i = 0; i < plan->S; ++i) { out->pops[i] = d[i].real(); n2 += d[i].real(); }
   out->norm2 = n2;
   if (!std::isfinite(n2)) return fail(QDG_ENONFINITE, "Norm is not a number");
-  if (plan->precision == QDG_PREC_FP64) {
+  if (is64(plan)) {
     cplx<double> *o = reinterpret_cast<cplx<double> *>(plan->d_scratch);
     if ((s = h_apply_bulk<double>(plan, psi->d, o, step)) != QDG_OK) return s;
     if ((s = dots<double, double>(plan, psi->d, o, d)) != QDG_OK) return s;
@@ -2017,7 +2030,7 @@ qdg_status qdg_prop_init(qdg_prop *P) {
   qdg_status s;
   if (P->kind == 1) s = cheby_init(P);
   else if (P->kind == 2) s = gspo_init(P);
-  else s = P->plan->precision == QDG_PREC_FP64 ? krylov_alloc<double>(P) : krylov_alloc<float>(P);
+  else s = is64(P->plan) ? krylov_alloc<double>(P) : krylov_alloc<float>(P);
   if (s == QDG_OK) P->inited = true;
   return s;
 }
@@ -2069,6 +2082,17 @@ qdg_status qdg_prop_apply_host(qdg_prop *P, qdg_wf *scratch, double *host_psi, i
     if (P->h_cs->status == QDG_ENONFINITE) return fail(QDG_ENONFINITE, "Norm is not a number");
   }
   if (terms_used) *terms_used = used;
+  return QDG_OK;
+}
+
+qdg_status qdg_plan_inject_barrier_stall(qdg_plan *plan) {
+  if (!plan || !plan->d_bar) return fail(QDG_EINVAL, "bad arguments");
+  CK(cudaStreamSynchronize(plan->stream));
+  // an arrival count no block index can complete (arrived == gridDim.x - 1
+  // never holds), so every block runs into its spin limit
+  qdg::GridBarrier b{};
+  b.count = 0x80000000u;
+  CK(cudaMemcpy(plan->d_bar, &b, sizeof(b), cudaMemcpyHostToDevice));
   return QDG_OK;
 }
 

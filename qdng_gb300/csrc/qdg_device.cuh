@@ -59,15 +59,19 @@ __device__ __forceinline__ dfl df_from_double(double x) {
   return dfl(h, __double2float_rn(x - (double)h));
 }
 
-// Bulk-type helpers for float and double-float (the step kernel's phi, T_d phi
-// and potential values).
+// Bulk-type helpers for float, double and double-float (the step kernel's
+// phi, T_d phi and potential values).
 __device__ __forceinline__ double b2d(float x) { return (double)x; }
+__device__ __forceinline__ double b2d(double x) { return x; }
+__device__ __forceinline__ double fma_b(double a, double b, double c) { return fma(a, b, c); }
 __device__ __forceinline__ double b2d(dfl x) { return df_to_double(x); }
 __device__ __forceinline__ float fma_b(float a, float b, float c) { return fmaf(a, b, c); }
 __device__ __forceinline__ dfl fma_b(dfl a, dfl b, dfl c) { return a * b + c; }
 template <typename B> __device__ __forceinline__ B d2b(double x);
 template <> __device__ __forceinline__ float d2b<float>(double x) { return (float)x; }
 template <> __device__ __forceinline__ dfl d2b<dfl>(double x) { return df_from_double(x); }
+template <> __device__ __forceinline__ double d2b<double>(double x) { return x; }
+__device__ __forceinline__ double ldg_b(const double *p) { return __ldg(p); }
 __device__ __forceinline__ float ldg_b(const float *p) { return __ldg(p); }
 __device__ __forceinline__ dfl ldg_b(const dfl *p) {
   const float2 v = __ldg(reinterpret_cast<const float2 *>(p));
@@ -381,6 +385,199 @@ __device__ int fft_lines(cplx<T> *buf0, cplx<T> *buf1, const RadixPlan &rp, int 
     Ns *= R;
   }
   return cur;
+}
+
+// ---- transforms with the direction known at compile time ----------------
+// SIGN = -1: forward (FFTW_FORWARD, exp(-2 pi i nk/N)); +1: backward.  With
+// the direction a template constant the +-1 factors of the butterflies fold
+// into additions and subtractions: on GB300 every binary64 operation costs
+// 1/64 of an FP32 one, so none is spent on a sign.
+template <int SIGN, typename T> __device__ __forceinline__ cplx<T> rot90s(cplx<T> a) {
+  if constexpr (SIGN < 0) return mk(a.im, -a.re);
+  else return mk(-a.im, a.re);
+}
+template <int SIGN, typename T>
+__device__ __forceinline__ void dft4s(cplx<T> &x0, cplx<T> &x1, cplx<T> &x2, cplx<T> &x3) {
+  const cplx<T> a0 = x0 + x2, a1 = x0 - x2, a2 = x1 + x3, a3 = rot90s<SIGN>(x1 - x3);
+  x0 = a0 + a2; x2 = a0 - a2; x1 = a1 + a3; x3 = a1 - a3;
+}
+// a * exp(SIGN 2 pi i m/16); m is a constant after unrolling.
+template <int SIGN, typename T> __device__ __forceinline__ cplx<T> tw16s(cplx<T> a, int m) {
+  const T c = (T)QDG_COS_PI8, sn = (T)QDG_SIN_PI8, h = (T)QDG_SQRT1_2;
+  if constexpr (SIGN < 0) {
+    switch (m) {
+      case 0: return a;
+      case 1: return mk(c * a.re + sn * a.im, c * a.im - sn * a.re);
+      case 2: return mk(h * (a.re + a.im), h * (a.im - a.re));
+      case 3: return mk(sn * a.re + c * a.im, sn * a.im - c * a.re);
+      case 4: return mk(a.im, -a.re);
+      case 6: return mk(h * (a.im - a.re), -(h * (a.re + a.im)));
+      case 9: return mk(-(c * a.re + sn * a.im), sn * a.re - c * a.im);
+    }
+  } else {
+    switch (m) {
+      case 0: return a;
+      case 1: return mk(c * a.re - sn * a.im, c * a.im + sn * a.re);
+      case 2: return mk(h * (a.re - a.im), h * (a.im + a.re));
+      case 3: return mk(sn * a.re - c * a.im, sn * a.im + c * a.re);
+      case 4: return mk(-a.im, a.re);
+      case 6: return mk(-(h * (a.re + a.im)), h * (a.re - a.im));
+      case 9: return mk(sn * a.im - c * a.re, -(c * a.im + sn * a.re));
+    }
+  }
+  return a;
+}
+template <int SIGN, typename T> __device__ __forceinline__ void dft8s(cplx<T> *x) {
+  dft4s<SIGN>(x[0], x[2], x[4], x[6]);
+  dft4s<SIGN>(x[1], x[3], x[5], x[7]);
+  cplx<T> y[8];
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) {
+    const cplx<T> a0 = x[2 * k1];
+    const cplx<T> a1 = tw16s<SIGN>(x[2 * k1 + 1], 2 * k1);
+    y[k1] = a0 + a1;
+    y[k1 + 4] = a0 - a1;
+  }
+#pragma unroll
+  for (int k = 0; k < 8; ++k) x[k] = y[k];
+}
+template <int SIGN, typename T> __device__ __forceinline__ void dft16s(cplx<T> *x) {
+#pragma unroll
+  for (int n2 = 0; n2 < 4; ++n2) dft4s<SIGN>(x[n2], x[4 + n2], x[8 + n2], x[12 + n2]);
+  cplx<T> y[16];
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) {
+    cplx<T> b0 = x[4 * k1 + 0];
+    cplx<T> b1 = tw16s<SIGN>(x[4 * k1 + 1], k1);
+    cplx<T> b2 = tw16s<SIGN>(x[4 * k1 + 2], 2 * k1);
+    cplx<T> b3 = tw16s<SIGN>(x[4 * k1 + 3], 3 * k1);
+    dft4s<SIGN>(b0, b1, b2, b3);
+    y[k1] = b0; y[k1 + 4] = b1; y[k1 + 8] = b2; y[k1 + 12] = b3;
+  }
+#pragma unroll
+  for (int k = 0; k < 16; ++k) x[k] = y[k];
+}
+// a * w (SIGN < 0) or a * conj(w) (SIGN > 0), w from the forward table
+template <int SIGN, typename T> __device__ __forceinline__ cplx<T> twmul(cplx<T> a, cplx<T> w) {
+  if constexpr (SIGN < 0) return mk(a.re * w.re - a.im * w.im, a.re * w.im + a.im * w.re);
+  else return mk(a.re * w.re + a.im * w.im, a.im * w.re - a.re * w.im);
+}
+// Stage twiddles w^(r k step) and the R-point DFT of one Stockham item;
+// twf(m) returns exp(-2 pi i m/N).
+template <typename T, int R, int SIGN, typename TwF>
+__device__ __forceinline__ void butterfly_s(cplx<T> (&v)[R], int k, int step, int M, TwF twf) {
+  if (k) {
+#pragma unroll
+    for (int r = 1; r < R; ++r) v[r] = twmul<SIGN>(v[r], twf(r * k * step));
+  }
+  if constexpr (R == 2) {
+    const cplx<T> a = v[0];
+    v[0] = a + v[1];
+    v[1] = a - v[1];
+  } else if constexpr (R == 4) {
+    dft4s<SIGN>(v[0], v[1], v[2], v[3]);
+  } else if constexpr (R == 8) {
+    dft8s<SIGN>(v);
+  } else if constexpr (R == 16) {
+    dft16s<SIGN>(v);
+  } else {
+    cplx<T> y[R];
+#pragma unroll
+    for (int qq = 0; qq < R; ++qq) {
+      cplx<T> s = v[0];
+#pragma unroll
+      for (int r = 1; r < R; ++r) s = s + twmul<SIGN>(v[r], twf(((r * qq) % R) * M));
+      y[qq] = s;
+    }
+#pragma unroll
+    for (int qq = 0; qq < R; ++qq) v[qq] = y[qq];
+  }
+}
+
+// One Stockham stage of `nlines` lines read from the padded shared-memory
+// layout `in`; outputs go to store(line, position, value).  lfast: items
+// are spread with the line index fastest (consecutive threads take the same
+// position of consecutive lines, so a global store along a strided
+// dimension coalesces); otherwise the position within a line is fastest.
+template <typename T, int R, int SIGN, typename Store, typename TwF>
+__device__ __forceinline__ void stage_s(const cplx<T> *__restrict__ in, Store store, int N, int nlines, int Ns,
+                                        bool lfast, TwF twf) {
+  const int M = N / R;
+  const int step = N / (Ns * R);
+  const int items = nlines * M;
+  const bool pow2 = ((M & (M - 1)) == 0) && ((Ns & (Ns - 1)) == 0);
+  const int lgM = __ffs(M) - 1, lgNs = __ffs(Ns) - 1;
+  const int LS = lstride(N);
+  for (int it = threadIdx.x; it < items; it += blockDim.x) {
+    int line, j;
+    if (lfast) { j = it / nlines; line = it - j * nlines; }
+    else if (pow2) { line = it >> lgM; j = it & (M - 1); }
+    else { line = it / M; j = it - line * M; }
+    int q, k;
+    if (pow2) { q = j >> lgNs; k = j & (Ns - 1); }
+    else { q = j / Ns; k = j - q * Ns; }
+    const cplx<T> *src = in + line * LS;
+    cplx<T> v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = src[lpos(j + r * M)];
+    butterfly_s<T, R, SIGN>(v, k, step, M, twf);
+    const int o = q * Ns * R + k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) store(line, o + r * Ns, v[r]);
+  }
+}
+
+template <typename T, int SIGN, typename Store, typename TwF>
+__device__ __forceinline__ void stage_s_any(int R, const cplx<T> *__restrict__ in, Store store, int N, int nlines,
+                                            int Ns, bool lfast, TwF twf) {
+  if (R == 16) stage_s<T, 16, SIGN>(in, store, N, nlines, Ns, lfast, twf);
+  else if (R == 8) stage_s<T, 8, SIGN>(in, store, N, nlines, Ns, lfast, twf);
+  else if (R == 4) stage_s<T, 4, SIGN>(in, store, N, nlines, Ns, lfast, twf);
+  else if (R == 2) stage_s<T, 2, SIGN>(in, store, N, nlines, Ns, lfast, twf);
+  else if (R == 3) stage_s<T, 3, SIGN>(in, store, N, nlines, Ns, lfast, twf);
+  else stage_s<T, 5, SIGN>(in, store, N, nlines, Ns, lfast, twf);
+}
+
+// T_d of a batch of lines held in shared memory: forward FFT, the kinetic
+// multiplier applied by the last forward stage (kmul(line, k-index, value)),
+// inverse FFT whose last stage hands its outputs to out(line, position,
+// value).  Data start in b0; b1 is the second ping-pong buffer.  Every
+// thread of the block calls it; it synchronises between stages but not
+// after the last one.
+template <typename T, typename KMul, typename Out>
+__device__ __forceinline__ void kinetic_lines(cplx<T> *b0, cplx<T> *b1, const RadixPlan &rp, int nlines,
+                                              const cplx<T> *tw, KMul kmul, Out out, bool lfast_out) {
+  cplx<T> *bb[2] = {b0, b1};
+  const int N = rp.n, LS = lstride(N);
+  auto twf = [tw](int m) { return tw[m]; };
+  int cur = 0, Ns = 1;
+  for (int s = 0; s < rp.nstages; ++s) {
+    cplx<T> *dst = bb[cur ^ 1];
+    if (s + 1 < rp.nstages) {
+      stage_s_any<T, -1>(rp.radix[s], bb[cur], [dst, LS](int l, int i, cplx<T> v) { dst[lidx(l, i, LS)] = v; },
+                         N, nlines, Ns, false, twf);
+    } else {
+      stage_s_any<T, -1>(rp.radix[s], bb[cur],
+                         [dst, LS, kmul](int l, int i, cplx<T> v) { dst[lidx(l, i, LS)] = kmul(l, i, v); }, N,
+                         nlines, Ns, false, twf);
+    }
+    __syncthreads();
+    cur ^= 1;
+    Ns *= rp.radix[s];
+  }
+  Ns = 1;
+  for (int s = 0; s < rp.nstages; ++s) {
+    cplx<T> *dst = bb[cur ^ 1];
+    if (s + 1 < rp.nstages) {
+      stage_s_any<T, 1>(rp.radix[s], bb[cur], [dst, LS](int l, int i, cplx<T> v) { dst[lidx(l, i, LS)] = v; }, N,
+                        nlines, Ns, false, twf);
+      __syncthreads();
+    } else {
+      stage_s_any<T, 1>(rp.radix[s], bb[cur], out, N, nlines, Ns, lfast_out, twf);
+    }
+    cur ^= 1;
+    Ns *= rp.radix[s];
+  }
 }
 
 // Point (w, i) of a tile of TW lines from a flat index: consecutive indices

@@ -198,9 +198,16 @@ struct GridBarrier {
 // Polls of a barrier flag before a block gives up (~0.3 s with back-off).
 static const unsigned int kBarrierSpinLimit = 1u << 22;
 
-// One Chebyshev step in one cooperative launch (qdg_persistent.cu).
+// Arithmetic of the persistent step kernel's bulk (phi, T_d phi, potential
+// values, FFTs) on grids of two or more dimensions: FP32 (mixed form),
+// binary64 (the drop-in form) or double-float (DF64 form).
+enum StepBulk { BULK_F32 = 0, BULK_F64 = 1, BULK_DF64 = 2 };
+
+// One Chebyshev step in one cooperative launch (qdg_step.cuh, launched by
+// qdg_persistent.cu).
 template <typename T>
 struct StepArgs {
+  int bulk;                  // StepBulk
   int nd, S;
   long long npts;
   DimPass<T> dp[4];          // kinetic passes (P_d outputs); dp[0] also the 1-D line geometry
@@ -226,8 +233,7 @@ struct StepArgs {
   int trace;                 // record phase times in cs->t_phase
 };
 
-template <typename T>
-int cheby_step_max_blocks(int S, int nd, int block, size_t smem);
+int cheby_step_max_blocks(int bulk, int S, int nd, int block, size_t smem);
 template <typename T>
 cudaError_t launch_cheby_step(const StepArgs<T> &a, int grid, int block, size_t smem, cudaStream_t st);
 

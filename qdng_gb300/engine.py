@@ -12,7 +12,7 @@ import numpy as np
 from . import abi
 from ._lib import QDGError, check, load
 
-PRECISIONS = {"fp64": abi.PREC_FP64, "mixed": abi.PREC_MIXED}
+PRECISIONS = {"fp64": abi.PREC_FP64, "mixed": abi.PREC_MIXED, "df64": abi.PREC_DF64}
 
 # At interpreter exit the CUDA runtime may already be torn down; handles are
 # then left to process teardown instead of being released one by one.
@@ -61,6 +61,11 @@ class Plan:
         n = np.zeros(8, dtype=np.int64)
         check(self.lib.qdg_profile_read(self.h, _dp(ms), n.ctypes.data_as(C.POINTER(C.c_int64))))
         return ms, n
+
+    def inject_barrier_stall(self):
+        """Failure-path test aid: the next persistent step kernel's grid
+        barrier cannot complete, so the step returns QDG_ETIMEOUT."""
+        check(self.lib.qdg_plan_inject_barrier_stall(self.h))
 
     def wavefunction(self, psi=None):
         w = WaveFunction(self)

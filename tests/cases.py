@@ -150,6 +150,12 @@ def cfg5_double_well(n=128):
     return hp, _normalize(hp, psi), dict(name="Cheby", params="", dt=20.0, steps=2000)
 
 
+def superposition(hp, funcs):
+    """Normalised equal-weight superposition of the given wave functions
+    (the start of the double-well Krylov propagation: its 8 relaxed states)."""
+    return _normalize(hp, np.sum(np.asarray(funcs, dtype=np.complex128), axis=0))
+
+
 def nac_two_state(n=128, nd=1, paired=True):
     """Two adiabatic harmonic states coupled by a first-derivative NAC
     (OGridNAC, the Handbook's Multistate example: m0.1 with sign +1 and m1.0

@@ -1,0 +1,130 @@
+"""GPU parity at the full sizes of the benchmark workloads.
+
+The engine (through the C ABI) against the CPU oracle on the 1-D Morse
+line (1024 points, 500 steps), the 256 x 256 two-state grid (Chebyshev and
+GSPO, 100 steps), the 128^3 anharmonic grid (3 steps), the 128 x 128 double
+well (8-state imaginary-time relaxation, then SIL and Arnoldi on the
+equal-weight superposition of the relaxed states) and one member of each
+size class of the laser-driven ensemble.  The binary64 forms are held to
+1e-12 relative on norm and autocorrelation (Arnoldi 1e-11: its Hessenberg
+exponential is evaluated by a different small-matrix method), with the
+Chebyshev term counts compared first.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests import cases
+from tests.test_gpu_parity import _assert_parity, _run_both, rel
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def eng():
+    from qdng_gb300 import build, engine
+    build.build()
+    return engine
+
+
+def _ac(obs, S):
+    return obs[:, 2 + S] + 1j * obs[:, 3 + S]
+
+
+def test_cfg1_morse_500_steps(eng):
+    hp, psi, run = cases.cfg1_morse()
+    _assert_parity(hp, *_run_both(eng, hp, psi, run, 500))
+
+
+@pytest.fixture(scope="module")
+def cfg2_oracle():
+    hp, psi, run = cases.cfg2_two_state()
+    S = O.System(hp)
+    Q = O.Propagator(S, run["name"], run["params"], dt=run["dt"])
+    x = psi.copy()
+    obs, terms = Q.propagate(x, psi.copy(), 100)
+    return hp, psi, run, obs, terms, x
+
+
+def _engine_run(eng, hp, psi, run, nsteps, precision):
+    plan = eng.Plan(hp, precision)
+    P = eng.Propagator(plan, run["name"], run["params"], dt=run["dt"])
+    w, w0 = plan.wavefunction(psi), plan.wavefunction(psi)
+    obs, terms = P.propagate(w, w0, nsteps)
+    return obs, terms, w.download()
+
+
+def test_cfg2_cheby_fp64_100_steps(eng, cfg2_oracle):
+    hp, psi, run, obs_o, terms_o, x = cfg2_oracle
+    obs_g, terms_g, xg = _engine_run(eng, hp, psi, run, 100, "fp64")
+    _assert_parity(hp, obs_o, terms_o, x, obs_g, terms_g, xg)
+
+
+def test_cfg2_cheby_df64_100_steps(eng, cfg2_oracle):
+    """The double-float form (phi, H phi and the FFTs as two FP32 numbers)
+    against the binary64 oracle over 100 steps: the series has the same
+    terms, and the observables stay within 1e-11."""
+    hp, psi, run, obs_o, terms_o, x = cfg2_oracle
+    obs_g, terms_g, xg = _engine_run(eng, hp, psi, run, 100, "df64")
+    S = hp.nstates
+    err_n = np.abs(obs_g[:, 0] - obs_o[:, 0]).max() / np.abs(obs_o[:, 0]).max()
+    err_ac = np.abs(_ac(obs_g, S) - _ac(obs_o, S)).max() / np.abs(_ac(obs_o, S)).max()
+    print(f"df64 cfg2 100 steps: norm {err_n:.3g} autocorrelation {err_ac:.3g} psi {rel(xg, x):.3g}")
+    assert list(terms_g) == list(terms_o)
+    assert err_n <= 1e-11 and err_ac <= 1e-11
+
+
+def test_cfg2_gspo_100_steps(eng):
+    hp, psi, run = cases.cfg2_two_state(gspo=True)
+    _assert_parity(hp, *_run_both(eng, hp, psi, run, 100), check_terms=False)
+
+
+def test_cfg3_full_grid_3_steps(eng):
+    hp, psi, run = cases.cfg3_anharmonic()
+    _assert_parity(hp, *_run_both(eng, hp, psi, run, 3))
+
+
+def test_cfg5_eigenstates_then_krylov(eng):
+    """128 x 128 double well: 8 functions relaxed in imaginary time with
+    projection and basis diagonalisation (ProgEigen::ImagTimeEF + DiagBasis;
+    a fixed 16 steps per function, so both sides take the same steps), then
+    50 SIL and 50 Arnoldi steps (Krylov 16, dt = 20) of the normalised
+    equal-weight superposition of the 8 functions."""
+    hp, psi, run = cases.cfg5_double_well()
+    nef, steps = 8, 16
+    S = O.System(hp)
+    Q = O.Propagator(S, "Cheby", "", dt=run["dt"], imaginary_time=True, backward=True)
+    efs_o, raw_o, diag_o, steps_o = Q.eigen_imag(psi, nef, steps, -1.0, diag=True)
+    plan = eng.Plan(hp, "fp64")
+    P = eng.Propagator(plan, "Cheby", "", dt=run["dt"], imaginary_time=True, backward=True)
+    efs, raw, diag, steps_g = P.eigen_imag(psi, nef, steps, -1.0, diag=True)
+    assert list(steps_g) == list(steps_o)
+    np.testing.assert_allclose(raw, raw_o, rtol=1e-10)
+    np.testing.assert_allclose(diag, diag_o, rtol=1e-10)
+    sup = cases.superposition(hp, efs_o)
+    for name, rtol in (("SIL", 1e-12), ("Arnoldi", 1e-11)):
+        r = dict(name=name, params="order=16", dt=run["dt"])
+        _assert_parity(hp, *_run_both(eng, hp, sup, r, 50), rtol=rtol, check_terms=(name == "SIL"))
+
+
+def test_cfg4_member_size_classes(eng):
+    """One member of every size class of the ensemble (1-D 256 ... 4096
+    points, 2-D 64^2 ... 256^2), one binary64 step in one ensemble launch,
+    each against its own oracle propagation."""
+    rng = np.random.default_rng(21)
+    ens = [cases.cfg4_member(rng, 1, n, nt=4) for n in cases.ENS_1D_SIZES]
+    ens += [cases.cfg4_member(rng, 2, n, nt=4) for n in cases.ENS_2D_SIDES]
+    E = eng.Ensemble(ens, dt=10.0, precision="fp64")
+    E.upload([m["psi"] for m in ens])
+    E.run(0, 1)
+    out = E.download()
+    for i, m in enumerate(ens):
+        Sm = O.System(cases.member_hplan(m))
+        Pm = O.Propagator(Sm, "Cheby", "", dt=10.0)
+        x = m["psi"].copy()
+        Pm.apply(x, 0)
+        assert E.info(i)["order"] == Pm.info()["order"]
+        p0 = m["psi"]
+        err_psi = rel(out[i], x)
+        err_ac = abs(np.vdot(p0, out[i]) - np.vdot(p0, x)) / abs(np.vdot(p0, x))
+        assert err_psi < 1e-12 and err_ac < 1e-12, (m["grid"].n, err_psi, err_ac)

@@ -246,7 +246,7 @@ def test_apply_host_matches_device(eng, fixtures):
 
 
 @pytest.mark.parametrize("case", ["2d", "1d"])
-def test_persistent_and_graph_steps_agree(eng, fixtures, monkeypatch, case):
+def test_persistent_and_graph_steps_agree(eng, fixtures, case):
     """The persistent step kernel, the conditional-graph term loop and the
     kernel-by-kernel launches (profiling mode) give the same terms and wave
     functions to rounding (the persistent kernel applies the common phase
@@ -257,9 +257,7 @@ def test_persistent_and_graph_steps_agree(eng, fixtures, monkeypatch, case):
         hp, psi, run = cases.tgplms(fixtures)
     plan = eng.Plan(hp, "fp64")
     P1 = eng.Propagator(plan, run["name"], run["params"], dt=run["dt"])
-    monkeypatch.setenv("QDG_CHEBY_MODE", "graph")
-    P2 = eng.Propagator(plan, run["name"], run["params"], dt=run["dt"])
-    monkeypatch.delenv("QDG_CHEBY_MODE")
+    P2 = eng.Propagator(plan, run["name"], run["params"] + " path=graph", dt=run["dt"])
     w1, w2, w3 = plan.wavefunction(psi), plan.wavefunction(psi), plan.wavefunction(psi)
     t1 = [P1.apply(w1, s) for s in range(4)]
     t2 = [P2.apply(w2, s) for s in range(4)]
