@@ -487,13 +487,35 @@ static void h_apply(const System &s, const cd *in, cd *out, long step) {
   }
 }
 
+/* Compensated (Neumaier) summation for the oracle's reductions.  QDng sums
+ * with OpenMP reductions whose order depends on the thread count, so the
+ * reference has no fixed summation order; the oracle sums to within one
+ * rounding of the exact value instead (a plain serial sum over the 2M points
+ * of a 128^3 grid is off by ~1e-12 relative), which makes its norms a
+ * reference for any summation order. */
+struct CSum {
+  double s = 0, c = 0;
+  void add(double x) {
+    const double t = s + x;
+    if (std::fabs(s) >= std::fabs(x)) c += (s - t) + x;
+    else c += (x - t) + s;
+    s = t;
+  }
+  double get() const { return s + c; }
+};
+
 /* WFGridCartesian::operator* summed over states (WFGridCartesian.cpp:62-117,
  * WFMultistate.cpp:200-222): <a|b> * prod dx. */
 static cd dot(const System &s, const cd *a, const cd *b) {
   cd tot = 0;
   for (int st = 0; st < s.S; ++st) {
-    cd c = 0;
-    for (long p = 0; p < s.npts; ++p) c += std::conj(a[st * s.npts + p]) * b[st * s.npts + p];
+    CSum re, im;
+    for (long p = 0; p < s.npts; ++p) {
+      const cd v = std::conj(a[st * s.npts + p]) * b[st * s.npts + p];
+      re.add(v.real());
+      im.add(v.imag());
+    }
+    cd c(re.get(), im.get());
     for (int d = 0; d < s.g.ndims; ++d) c *= s.dx[d];
     tot += c;
   }
@@ -574,9 +596,9 @@ static int cheby_init(Prop &p) {
 }
 
 static double raw_norm(long n, const cd *x) {  /* OCheby::raw_norm, OCheby.cpp:64-90 */
-  double nrm = 0;
-  for (long j = 0; j < n; ++j) nrm += (std::conj(x[j]) * x[j]).real();
-  return nrm;
+  CSum nrm;
+  for (long j = 0; j < n; ++j) nrm.add((std::conj(x[j]) * x[j]).real());
+  return nrm.get();
 }
 
 /* OCheby::real_time_step / imag_time_step (OCheby.cpp:92-297). */
@@ -600,7 +622,7 @@ static int cheby_step(Prop &p, cd *psi, long step) {
   cd exp2 = 2.0 * ex;
   int used = 2;
   for (int i = 2; i < p.order; ++i) {
-    double accnorm = 0;
+    CSum acc;
     cd coeff = p.coeff[i] * ph;
     h_apply(s, k1, bf, step);
     for (long j = 0; j < n; ++j) {
@@ -609,8 +631,9 @@ static int cheby_step(Prop &p, cd *psi, long step) {
       k2[j] = p.imag ? bf[j] - k0[j] : bf[j] + k0[j];
       k0[j] = k2[j];
       psi[j] += k2[j] * coeff;
-      accnorm = accnorm + (std::conj(psi[j]) * psi[j]).real();
+      acc.add((std::conj(psi[j]) * psi[j]).real());
     }
+    const double accnorm = acc.get();
     used = i + 1;
     if (!p.imag) {
       double nconv = std::fabs(norm0 - accnorm) / norm0;
@@ -927,8 +950,9 @@ int orc_observables(void *sp, const double *psi_, const double *psi0_, long step
   out[0] = nrm * nrm;
   System one = s;  /* per-state norms with the single-state product */
   for (int st = 0; st < s.S; ++st) {
-    cd c = 0;
-    for (long p = 0; p < N; ++p) c += std::conj(psi[st * N + p]) * psi[st * N + p];
+    CSum re;
+    for (long p = 0; p < N; ++p) re.add(std::norm(psi[st * N + p]));
+    cd c(re.get(), 0.0);
     for (int d = 0; d < s.g.ndims; ++d) c *= s.dx[d];
     double n1 = std::sqrt(c.real());
     out[1 + st] = n1 * n1;

@@ -89,14 +89,21 @@ def test_cfg5_eigenstates_then_krylov(eng):
     projection and basis diagonalisation (ProgEigen::ImagTimeEF + DiagBasis;
     a fixed 16 steps per function, so both sides take the same steps), then
     50 SIL and 50 Arnoldi steps (Krylov 16, dt = 20) of the normalised
-    equal-weight superposition of the 8 functions."""
+    equal-weight superposition of the 8 functions.
+
+    The relaxation steps use dt = 2.  The imaginary-time series carries the
+    factor e^{-R} (scaled I_n coefficients, R = scaling * dt) and reaches it
+    by cancelling terms of size ~1/sqrt(2 pi R): with dt = 20 (R = 42) the
+    result lies below the rounding of its terms, so any two binary64
+    implementations (two FFT radix orders of the oracle, say) differ by
+    O(1) after one step; at dt = 2 (R = 4.2) they agree to ~1e-14."""
     hp, psi, run = cases.cfg5_double_well()
-    nef, steps = 8, 16
+    nef, steps, dt_imag = 8, 16, 2.0
     S = O.System(hp)
-    Q = O.Propagator(S, "Cheby", "", dt=run["dt"], imaginary_time=True, backward=True)
+    Q = O.Propagator(S, "Cheby", "", dt=dt_imag, imaginary_time=True, backward=True)
     efs_o, raw_o, diag_o, steps_o = Q.eigen_imag(psi, nef, steps, -1.0, diag=True)
     plan = eng.Plan(hp, "fp64")
-    P = eng.Propagator(plan, "Cheby", "", dt=run["dt"], imaginary_time=True, backward=True)
+    P = eng.Propagator(plan, "Cheby", "", dt=dt_imag, imaginary_time=True, backward=True)
     efs, raw, diag, steps_g = P.eigen_imag(psi, nef, steps, -1.0, diag=True)
     assert list(steps_g) == list(steps_o)
     np.testing.assert_allclose(raw, raw_o, rtol=1e-10)
