@@ -25,6 +25,37 @@
 
 namespace qdg {
 
+// The point work of a term: (h - offset x) times the series factor, with
+// the offset and the factor each carried as a rounded value plus its
+// rounding residual.  Binary64 needs the residual of the factor only (the
+// product offset x is rounded per point); FP32 needs both.  Multiplying
+// every point by a rounded constant would scale or shift the series
+// argument coherently: a phase error that grows with every time step.
+template <typename T>
+struct SeriesK {
+  cplx<T> oh, ol, fh, fl;
+  __device__ __forceinline__ cplx<T> operator()(cplx<T> h, cplx<T> x) const {
+    cplx<T> hm;
+    if constexpr (sizeof(T) == sizeof(double)) {
+      hm = h - cmul(oh, x);
+    } else {
+      hm.re = fma(-oh.re, x.re, fma(oh.im, x.im, fma(-ol.re, x.re, fma(ol.im, x.im, h.re))));
+      hm.im = fma(-oh.re, x.im, fma(-oh.im, x.re, fma(-ol.re, x.im, fma(-ol.im, x.re, h.im))));
+    }
+    const T sre = hm.re * fl.re - hm.im * fl.im, sim = hm.re * fl.im + hm.im * fl.re;
+    return mk<T>(fma(hm.re, fh.re, fma(-hm.im, fh.im, sre)), fma(hm.re, fh.im, fma(hm.im, fh.re, sim)));
+  }
+};
+template <typename T>
+__device__ __forceinline__ SeriesK<T> series_k(cplx<double> off, cplx<double> fac, cplx<double> lo) {
+  SeriesK<T> k;
+  k.oh = ccast<T>(off);
+  k.ol = mk<T>((T)(off.re - (double)k.oh.re), (T)(off.im - (double)k.oh.im));
+  k.fh = ccast<T>(fac);
+  k.fl = mk<T>((T)((fac.re - (double)k.fh.re) + lo.re), (T)((fac.im - (double)k.fh.im) + lo.im));
+  return k;
+}
+
 struct EnsMember {
   int nd;
   int n[2];
@@ -37,6 +68,7 @@ struct EnsMember {
   int order;
   long long coef_off;     // series coefficients a_i
   cplx<double> offset, fac1, fac, ph;
+  cplx<double> fac1_lo, fac_lo;  // rounding residuals of fac1, fac (exact factor = fac + fac_lo)
   double prec;
   long long laser_off;    // -1: no field
   int laser_nt;
@@ -136,8 +168,7 @@ template <typename T, bool FIRST>
 __device__ double ens_points(const EnsArgs<T> &a, const EnsMember &m, const cplx<T> *phi, cplx<T> *kout,
                              double ai, T field) {
   double acc = 0.0;
-  const cplx<T> off = ccast<T>(m.offset);
-  const cplx<T> fac = ccast<T>(FIRST ? m.fac1 : m.fac);
+  const SeriesK<T> sk = series_k<T>(m.offset, FIRST ? m.fac1 : m.fac, FIRST ? m.fac1_lo : m.fac_lo);
   for (long long p = threadIdx.x; p < m.npts; p += blockDim.x) {
     const long long g = m.off + p;
     const cplx<T> x = ld(phi + g);
@@ -146,7 +177,7 @@ __device__ double ens_points(const EnsArgs<T> &a, const EnsMember &m, const cplx
     T v = a.V[g];
     if (m.has_dipole) v = v + field * a.mu[g];
     h = h + cmulr(x, v);
-    const cplx<T> bf = cmul(h - cmul(off, x), fac);
+    const cplx<T> bf = sk(h, x);
     if (FIRST) {
       const cplx<double> ps = ld(a.psi + g);
       acc += cabs2(ps);
@@ -216,7 +247,6 @@ __device__ void ens_step_1d(const EnsArgs<T> &a, const EnsMember &m, T field, un
   }
   __syncthreads();
   const RadixPlan &rp = m.rp[0];
-  const cplx<T> off = ccast<T>(m.offset);
   const int nw = (blockDim.x + 31) >> 5;
   double norm0 = 0.0, last = 0.0;
   bool done = false;
@@ -237,14 +267,14 @@ __device__ void ens_step_1d(const EnsArgs<T> &a, const EnsMember &m, T field, un
       dst = dst == f0 ? f1 : f0;
     }
     // inverse transform; the last stage finishes the term point by point
-    const cplx<T> fac = ccast<T>(first ? m.fac1 : m.fac);
+    const SeriesK<T> sk = series_k<T>(m.offset, first ? m.fac1 : m.fac, first ? m.fac1_lo : m.fac_lo);
     const double ai = a.coef[m.coef_off + it];
     const double a0 = a.coef[m.coef_off];
     double acc = 0.0;
     auto point = [&](int i, const cplx<T> &tk) {
       const cplx<T> x = cur[i];
       const cplx<T> h = tk + cmulr(x, Vs[i]);
-      const cplx<T> bf = cmul(h - cmul(off, x), fac);
+      const cplx<T> bf = sk(h, x);
       cplx<double> p = ps[i];
       if (first) {
         acc += cabs2(p);
@@ -378,7 +408,6 @@ __device__ void ens_step_1d_df(const EnsArgs<float> &a, const EnsMember &m, floa
   for (int w = 0; w < nw; ++w) norm0 += red[w];
   if (!isfinite(norm0)) status = 2;
   const RadixPlan &rp = m.rp[0];
-  const cplx<T> off = ccast<T>(m.offset);
   bool done = !isfinite(norm0);
   int used = 2;
   for (int it = 1; it < m.order && !done; ++it) {
@@ -395,7 +424,7 @@ __device__ void ens_step_1d_df(const EnsArgs<float> &a, const EnsMember &m, floa
       src = dst;
       dst = dst == f0 ? f1 : f0;
     }
-    const cplx<T> fac = ccast<T>(first ? m.fac1 : m.fac);
+    const SeriesK<T> sk = series_k<T>(m.offset, first ? m.fac1 : m.fac, first ? m.fac1_lo : m.fac_lo);
     const double ai = a.coef[m.coef_off + it];
     const float ai_h = (float)ai, ai_l = (float)(ai - (double)ai_h);
     const double a0 = a.coef[m.coef_off];
@@ -404,7 +433,7 @@ __device__ void ens_step_1d_df(const EnsArgs<float> &a, const EnsMember &m, floa
     auto point = [&](int i, const cplx<T> &tk) {
       const cplx<T> x = cur[i];
       const cplx<T> h = tk + cmulr(x, Vs[i]);
-      const cplx<T> bf = cmul(h - cmul(off, x), fac);
+      const cplx<T> bf = sk(h, x);
       dfloat pr = pre[i], pi = pim[i];
       if (first) {
         prev[i] = bf;  // phi_1
@@ -488,8 +517,7 @@ __device__ float ens_points_df(const EnsArgs<float> &a, const EnsMember &m, cons
                                cplx<float> *kout, float a0h, float a0l, float aih, float ail, float field) {
   typedef float T;
   float dn = 0.0f;
-  const cplx<T> off = ccast<T>(m.offset);
-  const cplx<T> fac = ccast<T>(FIRST ? m.fac1 : m.fac);
+  const SeriesK<T> sk = series_k<T>(m.offset, FIRST ? m.fac1 : m.fac, FIRST ? m.fac1_lo : m.fac_lo);
   for (long long p = threadIdx.x; p < m.npts; p += blockDim.x) {
     const long long g = m.off + p;
     const cplx<T> x = ld(phi + g);
@@ -498,7 +526,7 @@ __device__ float ens_points_df(const EnsArgs<float> &a, const EnsMember &m, cons
     T v = a.V[g];
     if (m.has_dipole) v = v + field * a.mu[g];
     h = h + cmulr(x, v);
-    const cplx<T> bf = cmul(h - cmul(off, x), fac);
+    const cplx<T> bf = sk(h, x);
     dfloat pr = a.dfr[g], pi = a.dfi[g];
     if (FIRST) {
       st(kout + g, bf);
@@ -832,6 +860,12 @@ qdg_status build(qdg_ensemble *e, const qdg_ensemble_member *mem, const std::map
     const cd f1 = ex / cs.scaling, f = 2.0 * ex / cs.scaling, ph = std::exp(c0 * cs.offset);
     m.fac1.re = f1.real(); m.fac1.im = f1.imag();
     m.fac.re = f.real(); m.fac.im = f.imag();
+    {  // residuals of the rounded factors, from a long double evaluation
+      const std::complex<long double> exl((long double)c0.real() / e->dt, (long double)c0.imag() / e->dt);
+      const std::complex<long double> l1 = exl / (long double)cs.scaling, l2 = 2.0L * exl / (long double)cs.scaling;
+      m.fac1_lo.re = (double)(l1.real() - (long double)m.fac1.re); m.fac1_lo.im = (double)(l1.imag() - (long double)m.fac1.im);
+      m.fac_lo.re = (double)(l2.real() - (long double)m.fac.re); m.fac_lo.im = (double)(l2.imag() - (long double)m.fac.im);
+    }
     m.ph.re = ph.real(); m.ph.im = ph.imag();
     m.prec = cs.prec;
     // LPT cost: the series needs about R = scaling dt terms (J_n(R) is

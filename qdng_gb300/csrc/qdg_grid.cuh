@@ -38,7 +38,7 @@ __device__ __forceinline__ bool grid_sync(GridBarrier *b) {
           atomicExch(&b->err, 1);
           break;
         }
-        if (spins > 512) __nanosleep(32);  // tight spin first, back off later
+        if (spins > (1u << 14)) __nanosleep(64);  // tight spin first (a term is ~10-100 us), back off later
       }
     }
     __threadfence();
@@ -54,11 +54,16 @@ __device__ __forceinline__ unsigned long long gtimer() {
   return t;
 }
 
-// Sum of the per-block partials, same order in every block; valid on thread 0.
-__device__ __forceinline__ double sum_partials(const double *partials, double *red) {
+// Sum of the per-block partials by the first warp, in the same fixed order
+// in every block (strided lane sums, then a shuffle tree), so every block
+// takes the same series-cut decision; valid on thread 0, no block barrier.
+__device__ __forceinline__ double sum_partials(const double *partials, double *) {
   double v = 0.0;
-  for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) v += __ldcg(partials + i);
-  return block_sum(v, red);
+  if (threadIdx.x < 32) {
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += 32) v += __ldcg(partials + i);
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  }
+  return v;
 }
 
 }  // namespace qdg

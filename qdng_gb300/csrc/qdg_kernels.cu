@@ -27,6 +27,16 @@ void add_launches(long long n) { g_launches.fetch_add(n); }
 
 __device__ __forceinline__ cplx<double> dmul(cplx<double> a, cplx<double> b) { return cmul(a, b); }
 
+// x (hi + lo) for a factor carried beyond binary64 (lo: the rounding residual
+// of hi): the small part is added inside the fused products, so the result is
+// not scaled by hi's rounding.  Multiplying every term of a Chebyshev series
+// by the rounded factor 2 exp/scaling would scale the series argument by
+// (1 + d), a phase error that grows with every time step.
+__device__ __forceinline__ cplx<double> dmul2(cplx<double> x, cplx<double> hi, cplx<double> lo) {
+  const double sre = x.re * lo.re - x.im * lo.im, sim = x.re * lo.im + x.im * lo.re;
+  return mk(fma(x.re, hi.re, fma(-x.im, hi.im, sre)), fma(x.re, hi.im, fma(x.im, hi.re, sim)));
+}
+
 
 // Block-level end of a Chebyshev term: store this block's norm partial, and
 // let the last block to arrive sum all partials in block order and apply the
@@ -190,7 +200,7 @@ __global__ void __launch_bounds__(256) linepass_kernel(PassArgs<T> a) {
           } else {
             const cplx<double> hd = ccast<double>(h[s]);
             const cplx<double> pd = ccast<double>(ph[s]);
-            const cplx<double> bf = dmul(hd - dmul(a.offset, pd), a.fac);
+            const cplx<double> bf = dmul2(hd - dmul(a.offset, pd), a.fac, a.fac_lo);
             if (MODE == PM_CHEBY_FIRST) {
               const cplx<double> ps = ld(a.psi + g);
               acc += cabs2(ps);
@@ -403,7 +413,7 @@ __global__ void __launch_bounds__(256) combine_kernel(CombArgs<T> a) {
       if (MODE == PM_HAPPLY) {
         st(a.out + g, h[s]);
       } else {
-        const cplx<double> bf = dmul(ccast<double>(h[s]) - dmul(a.offset, ccast<double>(ph[s])), a.fac);
+        const cplx<double> bf = dmul2(ccast<double>(h[s]) - dmul(a.offset, ccast<double>(ph[s])), a.fac, a.fac_lo);
         if (MODE == PM_CHEBY_FIRST) {
           const cplx<double> ps = ld(a.psi + g);
           acc += cabs2(ps);

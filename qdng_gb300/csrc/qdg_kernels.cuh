@@ -105,6 +105,7 @@ struct PassArgs {
   // Chebyshev scalars (FP64)
   cplx<double> offset;     // energy offset (OCheby::_offset)
   cplx<double> fac;        // _exp/_scaling (first) or 2*_exp/_scaling (terms)
+  cplx<double> fac_lo;     // fac's rounding residual: the exact factor is fac + fac_lo
   cplx<double> c0p, c1p;   // coeff[0], coeff[1] times exp(c0*offset)
   cplx<double> coeff;      // coeff[i] times exp(c0*offset)
   int imag;                // imaginary-time recursion (minus sign, OCheby.cpp:276)
@@ -180,7 +181,7 @@ struct CombArgs {
   const Couplings *cp;
   const double *coef;
   const T *grids;
-  cplx<double> offset, fac, c0p, c1p, coeff;
+  cplx<double> offset, fac, fac_lo, c0p, c1p, coeff;  // fac_lo: rounding residual of fac
   int imag;
   double *partials;
   ChebyCut cut;
@@ -231,6 +232,13 @@ struct StepArgs {
   ChebyState *cs;
   GridBarrier *bar;
   int trace;                 // record phase times in cs->t_phase
+  // pre-scaled point work: dp[].ktab / ktdf hold f T_d, sgrids the scaled
+  // potential grids over the entries of scp (lid: the plan entry whose field
+  // coefficient applies, or -1), -f offset applied per point as soff_hi + soff_lo
+  int scaled, scaled_rt;
+  double soff_hi, soff_lo;
+  const Couplings *scp;
+  const void *sgrids;
 };
 
 int cheby_step_max_blocks(int bulk, int S, int nd, int block, size_t smem);

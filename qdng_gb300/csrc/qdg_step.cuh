@@ -67,6 +67,29 @@ __device__ __forceinline__ const FT *step_grids(const StepArgs<T> &a) {
   else return reinterpret_cast<const FT *>(a.grids);
 }
 
+// -f offset as the bulk type: binary64 and FP32 keep the rounded value and
+// its residual (part 1), double-float carries both in one number (part 1 is
+// zero).
+template <typename B>
+__device__ __forceinline__ B soff_part(double hi, double lo, int part) {
+  if constexpr (std::is_same<B, double>::value) return part == 0 ? hi : lo;
+  else if constexpr (std::is_same<B, dfl>::value) {
+    if (part) return dfl(0.0f, 0.0f);
+    const float h = __double2float_rn(hi);
+    return dfl(h, __double2float_rn((hi - (double)h) + lo));
+  } else {
+    const float h = __double2float_rn(hi);
+    return part == 0 ? h : __double2float_rn((hi - (double)h) + lo);
+  }
+}
+// h + (hi + lo) x, the residual first so that the rounded hi does not act
+// coherently on every point.
+template <typename B>
+__device__ __forceinline__ cplx<B> add_soff(cplx<B> h, cplx<B> x, B hi, B lo) {
+  if constexpr (std::is_same<B, dfl>::value) return mk(fma_b(hi, x.re, h.re), fma_b(hi, x.im, h.im));
+  else return mk(fma(hi, x.re, fma(lo, x.re, h.re)), fma(hi, x.im, fma(lo, x.im, h.im)));
+}
+
 // Kinetic transforms of phi_i (computed on load) for every dimension;
 // results go to Pnext.  PK_LAST only finishes phi_i and psi (row lines).
 // Loads of UNR points per thread are issued before any use or store, so the
@@ -81,7 +104,9 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
   const cplx<B> *phim1b = reinterpret_cast<const cplx<B> *>(phim1);
   const cplx<B> *phim2b = reinterpret_cast<const cplx<B> *>(phim2);
   cplx<B> *phoutb = reinterpret_cast<cplx<B> *>(phout);
-  constexpr int UNR = (sizeof(T) == 8 || SM > 2) ? 1 : 2;
+  // points gathered per thread and iteration (loads in flight); the binary64
+  // bulk is bound by its arithmetic and takes more to keep the FP64 pipe fed
+  constexpr int UNR = SM > 2 ? 1 : std::is_same<FT, double>::value ? 3 : 2;
   constexpr int RE = kMaxRowEntries;
   const long long npts = a.npts;
   const long long total = a.line_start[ND];
@@ -96,7 +121,14 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
   const cplx<B> fac = {d2b<B>(facd.re), d2b<B>(facd.im)};
   const bool off_real = a.offset.im == 0.0;
   const bool fac_imag = facd.re == 0.0;
-  const B *__restrict__ grids = step_grids<T, FT>(a);
+  // pre-scaled point work: H' = f (H - offset) from the scaled tables, then
+  // phi_i = (i) H' phi_{i-1} +- phi_{i-2}; otherwise the factor and the offset
+  // are applied per point
+  const bool scaled = a.scaled != 0;
+  const bool srt = a.scaled_rt != 0;
+  const Couplings *__restrict__ cpx = scaled ? a.scp : a.cp;
+  const B *__restrict__ grids = scaled ? reinterpret_cast<const B *>(a.sgrids) : step_grids<T, FT>(a);
+  const B soh = soff_part<B>(a.soff_hi, a.soff_lo, 0), sol = soff_part<B>(a.soff_hi, a.soff_lo, 1);
   while (l < end) {
     int d = 0;
     while (l >= a.line_start[d + 1]) ++d;
@@ -131,17 +163,20 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
     __syncthreads();
     const int istr = (int)stride;  // element stride of a line (< 2^31 points per dimension block)
     // potential-matrix entries of row s
-    const int e0 = a.cp->rs[s];
-    const int ne = a.cp->rs[s + 1] - e0;
+    const int e0 = cpx->rs[s];
+    const int ne = cpx->rs[s + 1] - e0;
     int ecol[RE], egid[RE];
     B ecoef[RE];
     bool unit_coef = true;  // only static potentials (coefficient 1) in this row
 #pragma unroll
     for (int k = 0; k < RE; ++k) {
-      ecol[k] = k < ne ? a.cp->col[e0 + k] : 0;
-      egid[k] = k < ne ? a.cp->gid[e0 + k] : 0;
-      ecoef[k] = d2b<B>(k < ne ? a.coef[e0 + k] : 0.0);
-      if (k < ne && a.coef[e0 + k] != 1.0) unit_coef = false;
+      ecol[k] = k < ne ? cpx->col[e0 + k] : 0;
+      egid[k] = k < ne ? cpx->gid[e0 + k] : 0;
+      // the field coefficient of the entry (scaled entries name the plan entry, -1: static)
+      const int ci = k >= ne ? -1 : scaled ? cpx->lid[e0 + k] : e0 + k;
+      const double c = ci >= 0 ? a.coef[ci] : (k < ne ? 1.0 : 0.0);
+      ecoef[k] = d2b<B>(c);
+      if (k < ne && c != 1.0) unit_coef = false;
     }
     const long long so = (long long)s * npts;
     const int tot = L * N;
@@ -202,16 +237,23 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
               h.im = fma_b(x.im, vv, h.im);
             }
           }
-          // (h - offset phi) * factor; a real offset and a purely imaginary
-          // factor (real-time propagation) need half the multiplications
-          cplx<B> hm;
-          if (off_real) {
-            hm.re = fma_b(-off.re, self.re, h.re);
-            hm.im = fma_b(-off.re, self.im, h.im);
+          cplx<B> bf;
+          if (scaled) {
+            h = add_soff(h, self, soh, sol);
+            bf = srt ? mk(-h.im, h.re) : h;
+            if (kind == PK_FIRST) bf = cmulr(bf, d2b<B>(0.5));
           } else {
-            hm = h - cmul(off, self);
+            // (h - offset phi) * factor; a real offset and a purely imaginary
+            // factor (real-time propagation) need half the multiplications
+            cplx<B> hm;
+            if (off_real) {
+              hm.re = fma_b(-off.re, self.re, h.re);
+              hm.im = fma_b(-off.re, self.im, h.im);
+            } else {
+              hm = h - cmul(off, self);
+            }
+            bf = fac_imag ? mk(-fac.im * hm.im, fac.im * hm.re) : cmul(hm, fac);
           }
-          const cplx<B> bf = fac_imag ? mk(-fac.im * hm.im, fac.im * hm.re) : cmul(hm, fac);
           const long long gidx = so + pp[u];
           if (kind == PK_FIRST) {
             v[u] = bf;
@@ -259,14 +301,23 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
 }
 
 // Point work of one term at point p for all states: H phi from the kinetic
-// parts h[] and the potential matrix, then the recurrence.
+// parts h[] and the potential matrix, then the recurrence.  Pre-scaled: h[]
+// is already f T phi, the scaled entries carry f V, and -f offset is added
+// as a value plus its residual, so no rounded constant multiplies every
+// point coherently (that would scale or shift the series argument: a phase
+// error growing with every step).
 template <typename T, int SM, bool FIRST>
 __device__ __forceinline__ void point_term(const StepArgs<T> &a, long long p, const cplx<T> *ph, cplx<T> *h,
                                            cplx<T> *kout, double coeff_i, int S, double &acc) {
-  const int ne = a.cp->ne;
+  const bool scaled = a.scaled != 0;
+  const Couplings *cpx = scaled ? a.scp : a.cp;
+  const T *grids = scaled ? reinterpret_cast<const T *>(a.sgrids) : a.grids;
+  const int ne = cpx->ne;
   for (int e = 0; e < ne; ++e) {
-    const int r = a.cp->row[e], c = a.cp->col[e];
-    const T v = (T)(a.coef[e]) * a.grids[(long long)a.cp->gid[e] * a.npts + p];
+    const int r = cpx->row[e], c = cpx->col[e];
+    const int ci = scaled ? cpx->lid[e] : e;
+    const T gv = grids[(long long)cpx->gid[e] * a.npts + p];
+    const T v = ci >= 0 ? (T)(a.coef[ci]) * gv : gv;
 #pragma unroll
     for (int s = 0; s < SM; ++s)
       if (s == r) {
@@ -280,6 +331,29 @@ __device__ __forceinline__ void point_term(const StepArgs<T> &a, long long p, co
   for (int s = 0; s < SM; ++s) {
     if (s >= S) break;
     const long long g = (long long)s * a.npts + p;
+    if (scaled) {
+      const cplx<T> hs = add_soff<T>(h[s], ph[s], soff_part<T>(a.soff_hi, a.soff_lo, 0),
+                                     soff_part<T>(a.soff_hi, a.soff_lo, 1));
+      cplx<T> bf = a.scaled_rt ? mk(-hs.im, hs.re) : hs;
+      if (FIRST) {
+        bf = cmulr(bf, (T)0.5);
+        const cplx<double> ps = ldcg(a.psi + g);
+        acc += cabs2(ps);
+        st(kout + g, bf);
+        const cplx<double> b = ccast<double>(bf);
+        st(a.psi + g, mk(ps.re * a.a[0] + b.re * a.a[1], ps.im * a.a[0] + b.im * a.a[1]));
+      } else {
+        const cplx<T> km2 = ldcg(kout + g);
+        const cplx<T> k2 = a.imag ? bf - km2 : bf + km2;
+        st(kout + g, k2);
+        cplx<double> ps = ldcg(a.psi + g);
+        ps.re += coeff_i * (double)k2.re;
+        ps.im += coeff_i * (double)k2.im;
+        st(a.psi + g, ps);
+        acc += cabs2(ps);
+      }
+      continue;
+    }
     if (FIRST) {
       const cplx<T> bf = cmul(h[s] - cmul(off, ph[s]), ccast<T>(a.fac1));
       const cplx<double> ps = ldcg(a.psi + g);
