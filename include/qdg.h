@@ -3,10 +3,9 @@
  *
  * This is the drop-in boundary for QDng's time-stepping hot path. A QDng
  * operator module (a C++ OPropagator subclass built against the QDng
- * headers; qdng_module/OGPUCheby.cpp in this repository) walks its
- * Hamiltonian tree once in
- * Init(WaveFunction*), fills a qdg_hplan_desc and then calls the entry
- * points below once per time step from Apply(WaveFunction*).
+ * headers; qdng_module/OGPUProp.h in this repository) walks its Hamiltonian
+ * tree once in Init(WaveFunction*), fills a qdg_hplan_desc and then calls
+ * the entry points below once per time step from Apply(WaveFunction*).
  *
  * Plain C: fixed-width integers, doubles and opaque handles, no exceptions,
  * integer status codes.  Complex arrays are interleaved (re, im) doubles,
@@ -27,7 +26,7 @@
 extern "C" {
 #endif
 
-#define QDG_ABI_VERSION 2
+#define QDG_ABI_VERSION 3
 
 /* Limits of the reference: MAX_DIMS (src/math/typedefs.h:28),
  * QD_MAX_STATES (src/qdlib/WFMultistate.h:10). */
@@ -207,6 +206,13 @@ qdg_status qdg_prop_apply(qdg_prop *prop, qdg_wf *psi, int64_t step, int32_t *te
  * host psi stays authoritative, upload before and download after). */
 qdg_status qdg_prop_apply_host(qdg_prop *prop, qdg_wf *scratch, double *host_psi,
                                int64_t step, int32_t *terms_used);
+
+/* The same drop-in step with the wave function as one host block per state
+ * (state_psi[s]: npoints complex128 values of state s), the layout of QDng's
+ * WFMultistate (src/qdlib/WFMultistate.cpp:89-140): no gather into one
+ * buffer on the host. */
+qdg_status qdg_prop_apply_host_states(qdg_prop *prop, qdg_wf *scratch, double *const *state_psi,
+                                      int64_t step, int32_t *terms_used);
 
 /* `nsteps` consecutive steps on device starting at clock step `step0`
  * (ProgPropa.cpp:317-327 without the per-step report). */

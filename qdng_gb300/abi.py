@@ -129,6 +129,7 @@ SIGNATURES = [
     ("qdg_prop_get_coeffs", _i32, [_vp, _dp, _i32]),
     ("qdg_prop_apply", _i32, [_vp, _vp, _i64, C.POINTER(_i32)]),
     ("qdg_prop_apply_host", _i32, [_vp, _vp, _dp, _i64, C.POINTER(_i32)]),
+    ("qdg_prop_apply_host_states", _i32, [_vp, _vp, C.POINTER(_dp), _i64, C.POINTER(_i32)]),
     ("qdg_prop_run", _i32, [_vp, _vp, _i64, _i32, C.POINTER(_i64)]),
     ("qdg_ensemble_timeline", _i32, [_vp, _vp, _vp]),
     ("qdg_eigen_imag", _i32, [_vp, _vp, _i32, _i32, C.c_double, _i32, _vp, _vp, _vp, _vp]),

@@ -2202,25 +2202,44 @@ qdg_status qdg_prop_apply(qdg_prop *P, qdg_wf *psi, int64_t step, int32_t *terms
   return s;
 }
 
-qdg_status qdg_prop_apply_host(qdg_prop *P, qdg_wf *scratch, double *host_psi, int64_t step, int32_t *terms_used) {
-  if (!P || !scratch || !host_psi || scratch->plan != P->user) return fail(QDG_EINVAL, "bad arguments");
+// The host-psi step: every state block copied in, one step, copied back.
+// states[s] points to state s's npoints complex128 values.
+qdg_status apply_host_states(qdg_prop *P, qdg_wf *scratch, double *const *states, long long step, int32_t *terms_used) {
   sync_twin(P);
   qdg_plan *p = P->plan;
-  CK(cudaMemcpyAsync(scratch->d, host_psi, sizeof(cplx<double>) * wf_elems(p), cudaMemcpyHostToDevice, p->stream));
+  const size_t sb = sizeof(cplx<double>) * (size_t)p->npts;
+  for (int st = 0; st < p->S; ++st)
+    CK(cudaMemcpyAsync(scratch->d + (size_t)st * p->npts, states[st], sb, cudaMemcpyHostToDevice, p->stream));
   int used = 0;
   qdg_status s = prop_step(P, scratch->d, step, &used, false);
   if (s != QDG_OK) return s;
-  CK(cudaMemcpyAsync(host_psi, scratch->d, sizeof(cplx<double>) * wf_elems(p), cudaMemcpyDeviceToHost, p->stream));
+  for (int st = 0; st < p->S; ++st)
+    CK(cudaMemcpyAsync(states[st], scratch->d + (size_t)st * p->npts, sb, cudaMemcpyDeviceToHost, p->stream));
   if (P->kind == 1) CK(cudaMemcpyAsync(P->h_cs, P->d_cs, sizeof(qdg::ChebyState), cudaMemcpyDeviceToHost, p->stream));
   CK(cudaStreamSynchronize(p->stream));
   if (P->kind == 1) {
     used = P->h_cs->terms;
     count_body_launches(P, used, 1);
-    if (P->step_grid > 0) { qdg_status sb = check_barrier(p); if (sb != QDG_OK) return sb; }
+    if (P->step_grid > 0) { qdg_status sb2 = check_barrier(p); if (sb2 != QDG_OK) return sb2; }
     if (P->h_cs->status == QDG_ENONFINITE) return fail(QDG_ENONFINITE, "Norm is not a number");
   }
   if (terms_used) *terms_used = used;
   return QDG_OK;
+}
+
+qdg_status qdg_prop_apply_host(qdg_prop *P, qdg_wf *scratch, double *host_psi, int64_t step, int32_t *terms_used) {
+  if (!P || !scratch || !host_psi || scratch->plan != P->user) return fail(QDG_EINVAL, "bad arguments");
+  std::vector<double *> states(P->user->S);
+  for (int st = 0; st < P->user->S; ++st) states[st] = host_psi + 2 * (size_t)st * P->user->npts;
+  return apply_host_states(P, scratch, states.data(), step, terms_used);
+}
+
+qdg_status qdg_prop_apply_host_states(qdg_prop *P, qdg_wf *scratch, double *const *state_psi, int64_t step,
+                                      int32_t *terms_used) {
+  if (!P || !scratch || !state_psi || scratch->plan != P->user) return fail(QDG_EINVAL, "bad arguments");
+  for (int st = 0; st < P->user->S; ++st)
+    if (!state_psi[st]) return fail(QDG_EINVAL, "null state block");
+  return apply_host_states(P, scratch, state_psi, step, terms_used);
 }
 
 qdg_status qdg_plan_inject_barrier_stall(qdg_plan *plan) {

@@ -157,6 +157,16 @@ class Propagator:
         check(self.lib.qdg_prop_apply_host(self.h, scratch.h, _dp(psi), step, C.byref(used)))
         return used.value
 
+    def apply_host_states(self, scratch, states, step):
+        """The drop-in call with one host block per state (QDng's WFMultistate
+        layout): each complex128 array is updated in place."""
+        for a in states:
+            assert a.dtype == np.complex128 and a.flags.c_contiguous
+        ptrs = (C.POINTER(C.c_double) * len(states))(*[_dp(a) for a in states])
+        used = C.c_int32(0)
+        check(self.lib.qdg_prop_apply_host_states(self.h, scratch.h, ptrs, step, C.byref(used)))
+        return used.value
+
     def phase_times(self):
         """ns spent by block 0 of the persistent step kernel while profiling: loading and
         finishing phi (gather), the shared-memory FFTs, storing T_d phi, waiting at the barrier."""

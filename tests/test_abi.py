@@ -31,7 +31,7 @@ def test_exports_every_header_symbol(lib):
 
 
 def test_abi_version(lib):
-    assert lib.qdg_abi_version() == 2
+    assert lib.qdg_abi_version() == 3
 
 
 def test_struct_layouts_match_c(tmp_path):

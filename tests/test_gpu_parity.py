@@ -245,6 +245,21 @@ def test_apply_host_matches_device(eng, fixtures):
     assert np.array_equal(w.download(), host)
 
 
+def test_apply_host_states_matches_device(eng):
+    """The per-state host-block drop-in call (QDng's WFMultistate layout)
+    gives the device step's result."""
+    hp, psi, run = cases.cfg2_two_state(n=64)
+    plan = eng.Plan(hp, "fp64")
+    P1 = eng.Propagator(plan, run["name"], run["params"], dt=run["dt"])
+    P2 = eng.Propagator(plan, run["name"], run["params"], dt=run["dt"])
+    w = plan.wavefunction(psi)
+    scratch = plan.wavefunction()
+    states = [psi[s * hp.npts:(s + 1) * hp.npts].copy() for s in range(hp.nstates)]
+    for step in range(3):
+        assert P1.apply(w, step) == P2.apply_host_states(scratch, states, step)
+    assert np.array_equal(w.download(), np.concatenate(states))
+
+
 @pytest.mark.parametrize("case", ["2d", "1d"])
 def test_persistent_and_graph_steps_agree(eng, fixtures, case):
     """The persistent step kernel, the conditional-graph term loop and the
