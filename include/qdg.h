@@ -296,6 +296,28 @@ qdg_status qdg_prop_phase_times(qdg_prop *prop, double ns[4]);
  * cut short).  No device wait is unbounded and nothing faults. */
 qdg_status qdg_plan_inject_barrier_stall(qdg_plan *plan);
 
+/* ---- FFT schedules (the FFTW planning/wisdom counterpart) --------------- */
+
+/* The line transforms of a plan (context 0) or of an ensemble member
+ * (context 1) of line length n and precision (a qdg_precision) use a radix
+ * order and, in the persistent step kernel, a number of lines per batch.
+ * They come from the autotuner's table, fft_schedules.txt next to the
+ * library (or the file QDG_FFT_SCHEDULES names), written by
+ * qdng_gb300/autotune.py after timing the candidates on the GPU; sizes
+ * without an entry use the greedy order (largest radices first).  This is
+ * the role of FFTW's planning and wisdom in the reference
+ * (src/fft/FFTGlobal.cpp:26-84, src/fft/fft.cpp:98-122).
+ * _set installs an override for plans and ensembles created afterwards in
+ * this process (radices from {2, 3, 4, 5, 8, 16} whose product is n; lines
+ * 0 = automatic, up to 64); _get returns the schedule a new plan would use;
+ * _reset drops the overrides and, with use_table = 0, ignores the table
+ * too (greedy orders). */
+qdg_status qdg_fft_schedule_set(int32_t context, int32_t n, int32_t precision, const int32_t *radices,
+                                int32_t nstages, int32_t lines);
+qdg_status qdg_fft_schedule_get(int32_t context, int32_t n, int32_t precision, int32_t *radices,
+                                int32_t *nstages, int32_t *lines);
+qdg_status qdg_fft_schedule_reset(int32_t use_table);
+
 /* ---- H psi without device allocation ------------------------------------ */
 
 /* Bytes of the library's static device scratch used by qdg_h_apply_noalloc

@@ -139,6 +139,9 @@ SIGNATURES = [
     ("qdg_prop_phase_times", _i32, [_vp, _dp]),
     ("qdg_plan_inject_barrier_stall", _i32, [_vp]),
     ("qdg_h_apply_noalloc", _i32, [C.POINTER(HPlanDesc), _dp, _dp, _i64, _vp]),
+    ("qdg_fft_schedule_set", _i32, [_i32, _i32, _i32, C.POINTER(_i32), _i32, _i32]),
+    ("qdg_fft_schedule_get", _i32, [_i32, _i32, _i32, C.POINTER(_i32), C.POINTER(_i32), C.POINTER(_i32)]),
+    ("qdg_fft_schedule_reset", _i32, [_i32]),
     ("qdg_ensemble_create", _i32, [C.POINTER(EnsembleMember), _i32, C.c_double, C.c_char_p, _i32, C.POINTER(_vp)]),
     ("qdg_ensemble_destroy", _i32, [_vp]),
     ("qdg_ensemble_upload", _i32, [_vp, _dp]),

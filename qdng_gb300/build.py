@@ -17,7 +17,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libqdg.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["qdg_kernels.cu", "qdg_persistent.cu", "qdg_api.cu", "qdg_noalloc.cu", "qdg_ensemble.cu",
-           "qdg_host.cpp",
+           "qdg_host.cpp", "qdg_schedule.cpp",
            # the persistent Chebyshev step kernel, one unit per bulk type and grid rank
            "qdg_step_f64_1.cu", "qdg_step_f64_2.cu", "qdg_step_f64_34.cu", "qdg_step_df_2.cu",
            "qdg_step_df_34.cu", "qdg_step_f32_1.cu", "qdg_step_f32_2.cu", "qdg_step_f32_34.cu"]
@@ -66,7 +66,7 @@ def build(force=False, verbose=False):
             sys.stderr.write(log)
     objs = [o for o, _ in results]
     tmp = LIB + ".tmp"
-    cmd = [nvcc(), "-shared"] + ARCH + objs + ["-o", tmp, "-lcudart"]
+    cmd = [nvcc(), "-shared"] + ARCH + objs + ["-o", tmp, "-lcudart", "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -60,21 +60,6 @@ struct DimInfo {
   int TW_k, TW_e;     // lines per tile: kinetic-only passes, coupled epilogue pass
 };
 
-// Largest radices first: 16-point DFTs in registers halve the shared-memory
-// stages of a radix-4 plan (256 = 16 x 16, 1024 = 16 x 16 x 4, 384 = 16 x 8 x 3).
-bool radix_plan(int n, qdg::RadixPlan &rp) {
-  rp.n = n; rp.nstages = 0;
-  int m = n;
-  while (m % 16 == 0) { rp.radix[rp.nstages++] = 16; m /= 16; }
-  if (m % 8 == 0) { rp.radix[rp.nstages++] = 8; m /= 8; }
-  if (m % 4 == 0) { rp.radix[rp.nstages++] = 4; m /= 4; }
-  if (m % 2 == 0) { rp.radix[rp.nstages++] = 2; m /= 2; }
-  while (m % 3 == 0) { rp.radix[rp.nstages++] = 3; m /= 3; }
-  while (m % 5 == 0) { rp.radix[rp.nstages++] = 5; m /= 5; }
-  if (rp.nstages > 16) return false;
-  return m == 1;
-}
-
 }  // namespace
 
 struct qdg_plan {
@@ -795,6 +780,8 @@ qdg_status step_setup(qdg_prop *P) {
       const long long n = p->dim[d].n;
       long long cap = (long long)((budget / cs - n) / (2 * (size_t)qdg::lstride((int)n)));
       int lm = (int)std::max<long long>(1, std::min<long long>(std::min<long long>(chunk, cap), qdg::kMaxBatchLines));
+      const int tuned = qdg::schedule_lines(qdg::SCHED_PLAN, (int)n, p->precision);
+      if (tuned > 0) lm = std::min(lm, tuned);
       P->lmax[d] = lm;
       smem = std::max(smem, ((size_t)n + 2 * qdg::line_buf_elems((int)n, lm)) * cs);
     }
@@ -1860,7 +1847,12 @@ qdg_status qdg_plan_create(const qdg_hplan_desc *desc, int32_t precision, qdg_pl
     p->dk[d] = (2 * M_PI) / (g.xmax[d] - g.xmin[d] + p->dx[d]);        // Kspace::Dk
     p->dim[d].n = g.n[d];
     p->dim[d].stride = stride;
-    if (!radix_plan(g.n[d], p->dim[d].rp)) { free_plan(p); return fail(QDG_EUNSUPPORTED, "grid size must be 2^a 3^b 5^c"); }
+    // the autotuner's schedule for this line length, else the greedy order
+    // (largest radices first: 256 = 16 x 16, 1024 = 16 x 16 x 4, 384 = 16 x 8 x 3)
+    if (!qdg::schedule_radix(qdg::SCHED_PLAN, g.n[d], precision, p->dim[d].rp)) {
+      free_plan(p);
+      return fail(QDG_EUNSUPPORTED, "grid size must be 2^a 3^b 5^c");
+    }
     stride *= g.n[d];
   }
   p->npts = stride;

@@ -11,6 +11,8 @@
 
 #include <type_traits>
 
+#include "qdg_schedule.h"
+
 namespace qdg {
 
 template <typename T> struct cplx { T re, im; };
@@ -134,12 +136,6 @@ template <typename T> __device__ __forceinline__ void st(cplx<T> *p, cplx<T> c) 
   *reinterpret_cast<V *>(p) = v;
 }
 
-// Radix plan of one line length: N = prod radix[i], radices in {16, 8, 4, 2, 3, 5}.
-struct RadixPlan {
-  int n;
-  int nstages;
-  int radix[16];
-};
 
 // ---- small DFTs in registers ---------------------------------------------
 // Constants of the 8th and 16th roots of unity (mathematical values).

@@ -720,19 +720,6 @@ qdg_status efail(qdg_status s, const std::string &m) {
     if (e_ != cudaSuccess) return efail(QDG_ECUDA, std::string(#__VA_ARGS__) + ": " + cudaGetErrorString(e_)); \
   } while (0)
 
-bool radix_plan_e(int n, qdg::RadixPlan &rp) {
-  rp.n = n;
-  rp.nstages = 0;
-  int m = n;
-  while (m % 16 == 0) { rp.radix[rp.nstages++] = 16; m /= 16; }
-  if (m % 8 == 0) { rp.radix[rp.nstages++] = 8; m /= 8; }
-  if (m % 4 == 0) { rp.radix[rp.nstages++] = 4; m /= 4; }
-  if (m % 2 == 0) { rp.radix[rp.nstages++] = 2; m /= 2; }
-  while (m % 3 == 0) { rp.radix[rp.nstages++] = 3; m /= 3; }
-  while (m % 5 == 0) { rp.radix[rp.nstages++] = 5; m /= 5; }
-  return m == 1 && rp.nstages <= 16;
-}
-
 void parse_kv(const char *s, std::map<std::string, std::string> &out) {
   if (!s) return;
   std::string str(s);
@@ -794,7 +781,8 @@ qdg_status build(qdg_ensemble *e, const qdg_ensemble_member *mem, const std::map
       const int N = x.grid.n[d];
       if (N < 2 || !(x.grid.xmax[d] > x.grid.xmin[d])) return efail(QDG_EINVAL, "invalid member grid");
       if (!(x.mass[d] > 0)) return efail(QDG_EINVAL, "Zero mass defined");
-      if (!radix_plan_e(N, m.rp[d])) return efail(QDG_EUNSUPPORTED, "grid size must be 2^a 3^b 5^c");
+      if (!qdg::schedule_radix(qdg::SCHED_ENSEMBLE, N, e->precision, m.rp[d]))
+        return efail(QDG_EUNSUPPORTED, "grid size must be 2^a 3^b 5^c");
       m.n[d] = N;
       m.npts *= N;
       dx[d] = (x.grid.xmax[d] - x.grid.xmin[d]) / double(N - 1);
