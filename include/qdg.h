@@ -336,7 +336,9 @@ qdg_status qdg_fft_schedule_reset(int32_t use_table);
  * queued on cuda_stream (NULL: the legacy default stream) without
  * synchronising.  Every call shares the scratch array: calls whose kernels
  * overlap on the GPU race, so serialise them on one stream.  The first call
- * on a device looks up the array's address with that device current.  This
+ * on a device looks up the array's address with that device current and
+ * keeps it; a cudaDeviceReset ends the context that holds the array, so a
+ * process that resets a device must not call this entry point on it again.  This
  * entry point has no counterpart in the reference. */
 qdg_status qdg_h_apply_noalloc(const qdg_hplan_desc *desc, const double *psi_in, double *psi_out,
                                int64_t step, void *cuda_stream);

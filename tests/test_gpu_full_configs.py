@@ -88,15 +88,22 @@ def test_cfg5_eigenstates_then_krylov(eng):
     """128 x 128 double well: 8 functions relaxed in imaginary time with
     projection and basis diagonalisation (ProgEigen::ImagTimeEF + DiagBasis;
     a fixed 16 steps per function, so both sides take the same steps), then
-    50 SIL and 50 Arnoldi steps (Krylov 16, dt = 20) of the normalised
-    equal-weight superposition of the 8 functions.
+    50 SIL and 50 Arnoldi steps (Krylov 16) of the normalised equal-weight
+    superposition of the 8 functions.
 
     The relaxation steps use dt = 2.  The imaginary-time series carries the
     factor e^{-R} (scaled I_n coefficients, R = scaling * dt) and reaches it
     by cancelling terms of size ~1/sqrt(2 pi R): with dt = 20 (R = 42) the
     result lies below the rounding of its terms, so any two binary64
     implementations (two FFT radix orders of the oracle, say) differ by
-    O(1) after one step; at dt = 2 (R = 4.2) they agree to ~1e-14."""
+    O(1) after one step; at dt = 2 (R = 4.2) they agree to ~1e-14.
+
+    The Krylov steps use dt = 5.  At dt = 20 a Krylov space of 16 does not
+    converge for this state (all 16 vectors are used every step and the
+    error estimate stays above its tolerance): the truncation error is not
+    unitary and amplifies rounding, so two binary64 builds of the oracle
+    differ by 4e-8 after 5 steps and 4e-4 after 50.  At dt = 5 the space
+    converges with 14-15 vectors and they agree to 1e-14 over 50 steps."""
     hp, psi, run = cases.cfg5_double_well()
     nef, steps, dt_imag = 8, 16, 2.0
     S = O.System(hp)
@@ -110,7 +117,7 @@ def test_cfg5_eigenstates_then_krylov(eng):
     np.testing.assert_allclose(diag, diag_o, rtol=1e-10)
     sup = cases.superposition(hp, efs_o)
     for name, rtol in (("SIL", 1e-12), ("Arnoldi", 1e-11)):
-        r = dict(name=name, params="order=16", dt=run["dt"])
+        r = dict(name=name, params="order=16", dt=5.0)
         _assert_parity(hp, *_run_both(eng, hp, sup, r, 50), rtol=rtol, check_terms=(name == "SIL"))
 
 

@@ -38,6 +38,32 @@ def _case_1d():
     return op.HPlan(g, op.Sum([op.GridNablaSq([1728.0]), op.GridPotential(0.1 * (1 - np.exp(-(x - 2))) ** 2)]))
 
 
+def _case_3d():
+    g = op.GridSystem([16, 8, 12], [-4.0, -3.0, -5.0], [4.0, 3.0, 5.0])
+    Q = g.mesh()
+    V = 0.01 * Q[0] ** 2 + 0.02 * Q[1] ** 2 + 0.015 * Q[2] ** 2 + 0.001 * Q[0] * Q[1] * Q[2]
+    return op.HPlan(g, op.Sum([op.GridNablaSq([1836.0, 900.0, 2000.0]), op.GridPotential(V)]))
+
+
+def _case_three_states(nonhermitian=False):
+    """Three states with off-diagonal potentials and a dipole coupling; with
+    nonhermitian=True the (j, i) elements are not mirrored."""
+    g = op.GridSystem([48, 40], [-4.0, -4.0], [4.0, 4.0])
+    X, Y = g.mesh()
+    T = op.GridNablaSq([1500.0, 2500.0])
+    mu = 0.2 * X * np.exp(-0.1 * Y ** 2)
+    laser = 0.03 * np.cos(0.2 * np.arange(10))
+    el = {(0, 0): op.Sum([T, op.GridPotential(0.01 * (X ** 2 + Y ** 2))]),
+          (1, 1): op.Sum([T, op.GridPotential(0.01 * ((X - 1) ** 2 + Y ** 2) + 0.02)]),
+          (2, 2): op.Sum([T, op.GridPotential(0.012 * (X ** 2 + (Y - 0.5) ** 2) + 0.04)]),
+          (0, 1): op.GridPotential(0.005 * np.exp(-X ** 2 - Y ** 2)),
+          (1, 2): op.GridDipole(mu, laser),
+          (0, 2): op.GridPotential(0.002 * np.exp(-(X - 0.5) ** 2))}
+    if nonhermitian:
+        el[(1, 0)] = op.GridPotential(0.003 * np.exp(-(Y - 0.3) ** 2))
+    return op.HPlan(g, op.Multistate(el, nonhermitian=nonhermitian))
+
+
 def _noalloc_apply(lib, hp, psi, step, torch):
     dev = torch.device("cuda")
     grids = torch.from_numpy(np.ascontiguousarray(hp.grid_data)).to(dev)
@@ -57,7 +83,9 @@ def _noalloc_apply(lib, hp, psi, step, torch):
     return y.cpu().numpy().view(np.complex128).copy()
 
 
-@pytest.mark.parametrize("builder", [_case_2d, _case_1d])
+@pytest.mark.parametrize("builder", [_case_2d, _case_1d, _case_3d, _case_three_states,
+                                     lambda: _case_three_states(nonhermitian=True)],
+                         ids=["2d", "1d", "3d", "three-states", "three-states-nonhermitian"])
 def test_noalloc_matches_plan_h_apply(builder):
     torch = pytest.importorskip("torch")
     from qdng_gb300 import build, engine
@@ -67,7 +95,10 @@ def test_noalloc_matches_plan_h_apply(builder):
     hp = builder()
     plan = engine.Plan(hp, "fp64")
     rng = np.random.default_rng(11)
-    for call, step in enumerate([3, 7]):  # two calls in a row, different inputs and field steps
+    # calls in a row with different inputs and field steps, including steps
+    # before the first and past the last field sample (the field is zero there)
+    nt = hp.desc.laser_nt
+    for call, step in enumerate([3, 7, -1, max(nt, 1)]):
         psi = rng.normal(size=hp.size) + 1j * rng.normal(size=hp.size)
         a, b = plan.wavefunction(psi), plan.wavefunction()
         plan.h_apply(a, b, step)
