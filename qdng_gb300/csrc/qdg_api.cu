@@ -161,6 +161,9 @@ struct qdg_prop {
   // multiplied by the series factor f once, -f offset per point as a value
   // and its rounding residual (scaled_setup)
   int scaled = 0, scaled_rt = 0;
+  int scaled_ne = 0;                   // entries of the scaled potential matrix
+  int cluster = 0;                     // 1-D single line on a cluster of 8 blocks (qdg_step_cluster.cu)
+  qdg::RadixPlan crp;                  // its M = N/8-point transforms
   double soff_hi = 0, soff_lo = 0;
   void *sk[QDG_MAX_DIMS] = {nullptr, nullptr, nullptr, nullptr};  // [S][N_d] f kfac k^2 (step bulk type)
   void *sgrids = nullptr;              // [S + extra][npts] (step bulk type)
@@ -902,12 +905,58 @@ qdg_status scaled_setup(qdg_prop *P) {
   P->soff_lo = (double)(so - (long double)P->soff_hi);
   P->scaled = 1;
   P->scaled_rt = rt ? 1 : 0;
+  P->scaled_ne = sc.ne;
   return QDG_OK;
+}
+
+// One line of a 1-D single-state grid with only a static potential goes to
+// the cluster kernel when N = 8 M with M a multiple of 8 (the exchange
+// splits the M columns evenly over the 8 blocks).
+void cluster_setup(qdg_prop *P) {
+  qdg_plan *p = P->plan;
+  if (!P->scaled || p->nd != 1 || p->S != 1 || P->scaled_ne != 1) return;
+  if (has(P, "cluster") && atoi(P->params.at("cluster").c_str()) == 0) return;
+  const int N = p->dim[0].n;
+  if (N % 64 != 0 || N < 512 || N > 8192) return;
+  if (!qdg::schedule_radix(qdg::SCHED_PLAN, N / 8, p->precision, P->crp)) return;
+  P->cluster = 1;
+}
+
+template <typename T>
+qdg_status cheby_step_cluster(qdg_prop *P, cplx<double> *psi) {
+  qdg_plan *p = P->plan;
+  qdg::ClusterStepArgs<T> a;
+  memset(&a, 0, sizeof(a));
+  a.N = p->dim[0].n;
+  a.M = a.N / 8;
+  a.rp = P->crp;
+  a.twN = reinterpret_cast<const cplx<T> *>(p->dim[0].tw);
+  a.ktab = reinterpret_cast<const T *>(P->sk[0]);
+  a.V = reinterpret_cast<const T *>(P->sgrids);
+  a.psi = psi;
+  a.psi_out = psi;
+  a.soff_hi = P->soff_hi;
+  a.soff_lo = P->soff_lo;
+  a.rt = P->scaled_rt;
+  a.a = P->d_a;
+  a.order = P->order;
+  a.prec = P->prec;
+  a.imag = P->imag ? 1 : 0;
+  a.offim0 = P->offset.imag() == 0 ? 1 : 0;
+  a.diff = p->precision == QDG_PREC_MIXED ? 1 : 0;
+  a.ph = C(std::exp(P->c0 * P->offset));
+  a.cs = P->d_cs;
+  size_t slot = 0;
+  qdg_status s = prof_begin<T>(p, 6, &slot);
+  if (s != QDG_OK) return s;
+  CK(qdg::launch_cheby_step_cluster<T>(a, p->stream));
+  return prof_end(p, slot);
 }
 
 template <typename T>
 qdg_status cheby_step_persistent(qdg_prop *P, cplx<double> *psi, long long step) {
   qdg_plan *p = P->plan;
+  if (P->cluster) return cheby_step_cluster<T>(P, psi);
   CK(qdg::launch_set_coefs(p->d_coef, p->d_cp, p->d_lasers, p->laser_nt, step, p->stream));
   qdg::StepArgs<T> a;
   memset(&a, 0, sizeof(a));
@@ -1006,6 +1055,7 @@ qdg_status cheby_init(qdg_prop *P) {
   if (ps != QDG_OK) return ps;
   if (!has(P, "scaled") || atoi(P->params.at("scaled").c_str()) != 0)
     if ((ps = scaled_setup(P)) != QDG_OK) return ps;
+  cluster_setup(P);
   CK(cudaMallocHost(&P->h_cs, sizeof(qdg::ChebyState)));
   return QDG_OK;
 }

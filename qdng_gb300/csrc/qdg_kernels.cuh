@@ -242,6 +242,31 @@ struct StepArgs {
 };
 
 int cheby_step_max_blocks(int bulk, int S, int nd, int block, size_t smem);
+
+// The Chebyshev step of one 1-D line of N = 8 M points on a cluster of 8
+// blocks (qdg_step_cluster.cu), pre-scaled point work.
+template <typename T>
+struct ClusterStepArgs {
+  int N, M;
+  RadixPlan rp;              // plan of the M-point transforms
+  const cplx<T> *twN;        // N twiddles exp(-2 pi i m/N)
+  const T *ktab;             // [N] f kfac min(k, N - k)^2
+  const T *V;                // [N] f V
+  const cplx<double> *psi;
+  cplx<double> *psi_out;
+  double soff_hi, soff_lo;   // -f offset as value and residual
+  int rt;                    // real time: phi_n = i H' phi ...
+  const double *a;
+  int order;
+  double prec;
+  int imag, offim0, diff;
+  cplx<double> ph;
+  ChebyState *cs;
+};
+template <typename T>
+cudaError_t launch_cheby_step_cluster(const ClusterStepArgs<T> &a, cudaStream_t st);
+template <typename T>
+size_t cluster_step_smem(int M);
 template <typename T>
 cudaError_t launch_cheby_step(const StepArgs<T> &a, int grid, int block, size_t smem, cudaStream_t st);
 

@@ -98,12 +98,14 @@ def test_cfg5_eigenstates_then_krylov(eng):
     implementations (two FFT radix orders of the oracle, say) differ by
     O(1) after one step; at dt = 2 (R = 4.2) they agree to ~1e-14.
 
-    The Krylov steps use dt = 5.  At dt = 20 a Krylov space of 16 does not
-    converge for this state (all 16 vectors are used every step and the
-    error estimate stays above its tolerance): the truncation error is not
-    unitary and amplifies rounding, so two binary64 builds of the oracle
-    differ by 4e-8 after 5 steps and 4e-4 after 50.  At dt = 5 the space
-    converges with 14-15 vectors and they agree to 1e-14 over 50 steps."""
+    The Krylov steps use dt = 5 and all 16 vectors (convergence tolerances
+    1e-30).  At dt = 20 a Krylov space of 16 does not converge for this
+    state: the truncation error is not unitary and amplifies rounding, so
+    two binary64 builds of the oracle differ by 4e-8 after 5 steps and 4e-4
+    after 50.  At dt = 5 the space converges with 14-15 vectors, but the
+    step where the error estimate crosses its tolerance can differ between
+    two implementations (one more vector); with the full space every step
+    the two oracle builds agree to 1e-14 over 50 steps."""
     hp, psi, run = cases.cfg5_double_well()
     nef, steps, dt_imag = 8, 16, 2.0
     S = O.System(hp)
@@ -116,8 +118,8 @@ def test_cfg5_eigenstates_then_krylov(eng):
     np.testing.assert_allclose(raw, raw_o, rtol=1e-10)
     np.testing.assert_allclose(diag, diag_o, rtol=1e-10)
     sup = cases.superposition(hp, efs_o)
-    for name, rtol in (("SIL", 1e-12), ("Arnoldi", 1e-11)):
-        r = dict(name=name, params="order=16", dt=5.0)
+    for name, prm, rtol in (("SIL", "order=16 err=1e-30", 1e-12), ("Arnoldi", "order=16 conv=1e-30", 1e-11)):
+        r = dict(name=name, params=prm, dt=5.0)
         _assert_parity(hp, *_run_both(eng, hp, sup, r, 50), rtol=rtol, check_terms=(name == "SIL"))
 
 

@@ -284,6 +284,22 @@ def test_persistent_and_graph_steps_agree(eng, fixtures, case):
     assert np.array_equal(w2.download(), w3.download())
 
 
+@pytest.mark.parametrize("imag", [False, True])
+def test_cluster_line_matches_single_block(eng, imag):
+    """The 1-D Morse line (1024 points) on a cluster of 8 blocks gives the
+    single-block step kernel's terms and wave function to rounding, in real
+    and in imaginary time."""
+    hp, psi, run = cases.cfg1_morse()
+    plan = eng.Plan(hp, "fp64")
+    kw = dict(dt=run["dt"] if not imag else 2.0, imaginary_time=imag, backward=imag)
+    P1 = eng.Propagator(plan, run["name"], run["params"], **kw)
+    P2 = eng.Propagator(plan, run["name"], run["params"] + " cluster=0", **kw)
+    w1, w2 = plan.wavefunction(psi), plan.wavefunction(psi)
+    for s in range(20):
+        assert P1.apply(w1, s) == P2.apply(w2, s)
+    assert rel(w1.download(), w2.download()) < 1e-12
+
+
 def test_run_counts_terms(eng, fixtures):
     hp, psi, run = cases.tgp_expec(fixtures)
     plan = eng.Plan(hp, "fp64")

@@ -27,7 +27,7 @@ def _get(lib, ctx, n, prec):
 
 
 def test_greedy_defaults_and_overrides(lib):
-    lib.qdg_fft_schedule_reset(0)
+    lib.qdg_fft_schedule_reset(0)  # the table off: greedy orders
     assert _get(lib, 0, 256, 0) == ([16, 16], 0)
     assert _get(lib, 0, 1024, 0) == ([16, 16, 4], 0)
     assert _get(lib, 1, 384, 1) == ([16, 8, 3], 0)
@@ -38,8 +38,16 @@ def test_greedy_defaults_and_overrides(lib):
     assert lib.qdg_fft_schedule_set(0, 256, 0, (C.c_int32 * 2)(4, 32), 2, 0) != 0  # 32 is no radix
     assert lib.qdg_fft_schedule_set(0, 256, 0, (C.c_int32 * 2)(4, 16), 2, 0) != 0  # product 64
     assert lib.qdg_fft_schedule_set(0, 256, 0, arr, 3, 99) != 0                    # lines above 64
-    lib.qdg_fft_schedule_reset(1)
+    lib.qdg_fft_schedule_reset(0)
     assert _get(lib, 0, 256, 0) == ([16, 16], 0)
+    # with the table: the committed autotuner entry for this size, if any
+    lib.qdg_fft_schedule_reset(1)
+    want = ([16, 16], 0)
+    for line in open(os.path.join(ROOT, "qdng_gb300", "fft_schedules.txt")):
+        f = line.split("#")[0].split()
+        if f[:3] == ["plan", "256", "fp64"]:
+            want = ([int(x) for x in f[3].split(",")], int(f[4]))
+    assert _get(lib, 0, 256, 0) == want
 
 
 def test_table_file_is_read(tmp_path):
