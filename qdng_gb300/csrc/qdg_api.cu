@@ -15,6 +15,7 @@
 #include <cstring>
 #include <map>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/qdg.h"
@@ -162,7 +163,8 @@ struct qdg_prop {
   // and its rounding residual (scaled_setup)
   int scaled = 0, scaled_rt = 0;
   int scaled_ne = 0;                   // entries of the scaled potential matrix
-  int cluster = 0;                     // 1-D single line on a cluster of 8 blocks (qdg_step_cluster.cu)
+  int cluster = 0;                     // 1-D single line on a cluster: 1 qdg_step_cluster.cu, 2 qdg_step_line64.cu
+  int cluster_size = 8;                // blocks of the cluster
   qdg::RadixPlan crp;                  // its M = N/8-point transforms
   double soff_hi = 0, soff_lo = 0;
   void *sk[QDG_MAX_DIMS] = {nullptr, nullptr, nullptr, nullptr};  // [S][N_d] f kfac k^2 (step bulk type)
@@ -800,12 +802,15 @@ qdg_status step_setup(qdg_prop *P) {
 
 // Device copy of host values in the step kernel's bulk type (binary64,
 // double-float for the DF64 form, FP32 for the mixed form).
+// The scaled tables in the step kernel's bulk type: FP32 (mixed), double-
+// float (the DF64 form's multi-dimensional kernel) or binary64 (FP64, and
+// one-dimensional grids in both FP64 forms).
 qdg_status upload_bulk(const qdg_plan *p, const std::vector<long double> &v, void **out) {
   if (p->precision == QDG_PREC_MIXED) {
     std::vector<float> h(v.begin(), v.end());
     CK(cudaMalloc(out, sizeof(float) * std::max<size_t>(1, h.size())));
     CK(cudaMemcpy(*out, h.data(), sizeof(float) * h.size(), cudaMemcpyHostToDevice));
-  } else if (p->precision == QDG_PREC_DF64) {
+  } else if (p->precision == QDG_PREC_DF64 && p->nd > 1) {
     std::vector<qdg::dfl> h(v.size());
     for (size_t i = 0; i < v.size(); ++i) {
       const float hi = (float)v[i];
@@ -910,16 +915,30 @@ qdg_status scaled_setup(qdg_prop *P) {
 }
 
 // One line of a 1-D single-state grid with only a static potential goes to
-// the cluster kernel when N = 8 M with M a multiple of 8 (the exchange
-// splits the M columns evenly over the 8 blocks).
+// a cluster kernel: in binary64 with N a power of two from 512 to 2048, the
+// one-component-per-thread kernel on 16 (or 8) blocks; otherwise, when
+// N = 8 M with M a multiple of 8 (the exchange splits the M columns evenly
+// over the 8 blocks), the radix-plan kernel on 8 blocks.  The propagator
+// parameter cluster=0 keeps the line on the single-block step kernel,
+// cluster=1 selects the radix-plan kernel.
 void cluster_setup(qdg_prop *P) {
   qdg_plan *p = P->plan;
   if (!P->scaled || p->nd != 1 || p->S != 1 || P->scaled_ne != 1) return;
-  if (has(P, "cluster") && atoi(P->params.at("cluster").c_str()) == 0) return;
+  const int want = has(P, "cluster") ? atoi(P->params.at("cluster").c_str()) : 2;
+  if (want == 0) return;
   const int N = p->dim[0].n;
+  if (want == 2 && is64(p) && (N & (N - 1)) == 0) {
+    const int C = qdg::line64_cluster_size(N);
+    if (C > 0) {
+      P->cluster = 2;
+      P->cluster_size = C;
+      return;
+    }
+  }
   if (N % 64 != 0 || N < 512 || N > 8192) return;
   if (!qdg::schedule_radix(qdg::SCHED_PLAN, N / 8, p->precision, P->crp)) return;
   P->cluster = 1;
+  P->cluster_size = 8;
 }
 
 template <typename T>
@@ -949,6 +968,12 @@ qdg_status cheby_step_cluster(qdg_prop *P, cplx<double> *psi) {
   size_t slot = 0;
   qdg_status s = prof_begin<T>(p, 6, &slot);
   if (s != QDG_OK) return s;
+  if constexpr (std::is_same<T, double>::value) {
+    if (P->cluster == 2) {
+      CK(qdg::launch_cheby_line64(a, P->cluster_size, p->stream));
+      return prof_end(p, slot);
+    }
+  }
   CK(qdg::launch_cheby_step_cluster<T>(a, p->stream));
   return prof_end(p, slot);
 }

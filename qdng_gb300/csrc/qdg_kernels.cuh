@@ -267,6 +267,11 @@ template <typename T>
 cudaError_t launch_cheby_step_cluster(const ClusterStepArgs<T> &a, cudaStream_t st);
 template <typename T>
 size_t cluster_step_smem(int M);
+// One binary64 line of N points on a cluster of 16 or 8 blocks, one real
+// component per thread (qdg_step_line64.cu).  line64_cluster_size returns
+// the cluster size the device schedules for N, or 0.
+int line64_cluster_size(int N);
+cudaError_t launch_cheby_line64(const ClusterStepArgs<double> &a, int C, cudaStream_t st);
 template <typename T>
 cudaError_t launch_cheby_step(const StepArgs<T> &a, int grid, int block, size_t smem, cudaStream_t st);
 
