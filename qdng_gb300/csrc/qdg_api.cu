@@ -158,6 +158,7 @@ struct qdg_prop {
   int step_tw1 = 1;
   long long line_start[QDG_MAX_DIMS + 1] = {0, 0, 0, 0, 0};
   int lmax[QDG_MAX_DIMS] = {1, 1, 1, 1};
+  long long *d_bstart = nullptr;    // [step_grid + 1] first kinetic line of each block
   // persistent step kernel: the kinetic tables and the potential grids
   // multiplied by the series factor f once, -f offset per point as a value
   // and its rounding residual (scaled_setup)
@@ -732,6 +733,60 @@ int step_bulk(const qdg_plan *p) {
   return p->precision == QDG_PREC_MIXED ? qdg::BULK_F32 : p->precision == QDG_PREC_DF64 ? qdg::BULK_DF64 : qdg::BULK_F64;
 }
 
+// Kinetic lines of the multi-dimensional step kernel per block.  The lines
+// of one dimension and one state form a segment; a block whose lines span
+// two segments transforms two partial batches, and the blocks of a term wait
+// for the slowest one.  So every segment gets a whole number of blocks, in
+// proportion to its work (lines x N (log2 N + 4): the transforms and the
+// point work), and its lines are split evenly among them.  With fewer
+// blocks than segments the even split over all lines stays.
+qdg_status partition_lines(qdg_prop *P) {
+  qdg_plan *p = P->plan;
+  const int G = P->step_grid;
+  const int nseg = p->nd * p->S;
+  if (G < nseg || (has(P, "partition") && P->params.at("partition") == "even")) return QDG_OK;
+  std::vector<double> cost(nseg);
+  std::vector<long long> nl(nseg);
+  double total = 0;
+  for (int d = 0; d < p->nd; ++d)
+    for (int s = 0; s < p->S; ++s) {
+      const int n = p->dim[d].n;
+      nl[d * p->S + s] = p->npts / n;
+      cost[d * p->S + s] = (double)(p->npts / n) * n * (std::log2((double)n) + 4.0);
+      total += cost[d * p->S + s];
+    }
+  std::vector<int> nb(nseg);
+  int used = 0;
+  for (int k = 0; k < nseg; ++k) {
+    nb[k] = (int)std::max<long long>(1, std::min<long long>(nl[k], std::llround(G * cost[k] / total)));
+    used += nb[k];
+  }
+  // settle the count: take from or give to the segment with the most / least lines per block
+  while (used != G) {
+    int best = -1;
+    for (int k = 0; k < nseg; ++k) {
+      if (used > G && nb[k] <= 1) continue;
+      if (used < G && nb[k] >= nl[k]) continue;
+      const double lpb = (double)nl[k] / nb[k];
+      if (best < 0 || (used > G ? lpb < (double)nl[best] / nb[best] : lpb > (double)nl[best] / nb[best])) best = k;
+    }
+    if (best < 0) return QDG_OK;  // cannot settle: keep the even split
+    nb[best] += used > G ? -1 : 1;
+    used += used > G ? -1 : 1;
+  }
+  std::vector<long long> bs;
+  bs.reserve(G + 1);
+  long long base = 0;
+  for (int k = 0; k < nseg; ++k) {
+    for (int j = 0; j < nb[k]; ++j) bs.push_back(base + nl[k] * j / nb[k]);
+    base += nl[k];
+  }
+  bs.push_back(base);
+  CK(cudaMalloc(&P->d_bstart, sizeof(long long) * bs.size()));
+  CK(cudaMemcpy(P->d_bstart, bs.data(), sizeof(long long) * bs.size(), cudaMemcpyHostToDevice));
+  return QDG_OK;
+}
+
 template <typename T>
 qdg_status step_setup(qdg_prop *P) {
   qdg_plan *p = P->plan;
@@ -772,10 +827,15 @@ qdg_status step_setup(qdg_prop *P) {
   // large grids transform more lines per batch; otherwise two blocks fit
   const size_t budget =
       qdg::cheby_step_max_blocks(bulk, p->S, p->nd, 256, 16 * 1024) == 1 ? 200 * 1024 : 112 * 1024;
+  // the staging slots of the gather (binary64 and double-float bulk, one or
+  // two states) sit in front of the twiddles and line buffers
+  const size_t stage = (bulk != qdg::BULK_F32 && qdg::step_staged((int)cs, p->S))
+                           ? (size_t)qdg::step_stage_bytes_c(p->nd, p->S) : 0;
+  if (stage + 16 * 1024 > budget) return QDG_OK;
   int grid = 0;
   size_t smem = 0;
   for (int iter = 0, per_sm = 0; iter < 3; ++iter) {
-    const size_t probe = iter == 0 ? 16 * 1024 : smem;
+    const size_t probe = iter == 0 ? stage + 16 * 1024 : smem;
     per_sm = qdg::cheby_step_max_blocks(bulk, p->S, p->nd, 256, probe);
     if (per_sm <= 0) return QDG_OK;
     grid = (int)std::min<long long>((long long)per_sm * p->sm_count, std::min<long long>(total, p->max_parts));
@@ -783,12 +843,12 @@ qdg_status step_setup(qdg_prop *P) {
     smem = 0;
     for (int d = 0; d < p->nd; ++d) {
       const long long n = p->dim[d].n;
-      long long cap = (long long)((budget / cs - n) / (2 * (size_t)qdg::lstride((int)n)));
+      long long cap = (long long)(((budget - stage) / cs - n) / (2 * (size_t)qdg::lstride((int)n)));
       int lm = (int)std::max<long long>(1, std::min<long long>(std::min<long long>(chunk, cap), qdg::kMaxBatchLines));
       const int tuned = qdg::schedule_lines(qdg::SCHED_PLAN, (int)n, p->precision);
       if (tuned > 0) lm = std::min(lm, tuned);
       P->lmax[d] = lm;
-      smem = std::max(smem, ((size_t)n + 2 * qdg::line_buf_elems((int)n, lm)) * cs);
+      smem = std::max(smem, stage + ((size_t)n + 2 * qdg::line_buf_elems((int)n, lm)) * cs);
     }
     if (smem > 227 * 1024) return QDG_OK;
     if (qdg::cheby_step_max_blocks(bulk, p->S, p->nd, 256, smem) >= per_sm) break;
@@ -796,8 +856,9 @@ qdg_status step_setup(qdg_prop *P) {
   const int per_sm = qdg::cheby_step_max_blocks(bulk, p->S, p->nd, 256, smem);
   if (per_sm <= 0) return QDG_OK;
   P->step_grid = std::min(grid, per_sm * p->sm_count);
+  if (has(P, "step_blocks")) P->step_grid = std::max(1, std::min(P->step_grid, atoi(P->params.at("step_blocks").c_str())));
   P->step_smem = smem;
-  return QDG_OK;
+  return partition_lines(P);
 }
 
 // Device copy of host values in the step kernel's bulk type (binary64,
@@ -1007,6 +1068,7 @@ qdg_status cheby_step_persistent(qdg_prop *P, cplx<double> *psi, long long step)
   a.item_start[p->nd] = items;
   for (int d = 0; d <= p->nd; ++d) a.line_start[d] = P->line_start[d];
   for (int d = 0; d < p->nd; ++d) a.lmax[d] = P->lmax[d];
+  a.bstart = P->d_bstart;
   a.TW1 = P->step_tw1;
   a.psi = psi;
   a.buf[0] = reinterpret_cast<cplx<T> *>(P->k0);
@@ -2203,6 +2265,7 @@ qdg_status qdg_prop_destroy(qdg_prop *P) {
   if (P->d_coeffs) cudaFree(P->d_coeffs);
   if (P->d_a) cudaFree(P->d_a);
   if (P->d_cs) cudaFree(P->d_cs);
+  if (P->d_bstart) cudaFree(P->d_bstart);
   if (P->h_cs) cudaFreeHost(P->h_cs);
   for (auto &g : P->gtab) for (auto v : g) if (v) cudaFree(v);
   for (auto v : P->gcp_d) if (v) cudaFree(v);

@@ -118,6 +118,22 @@ template <typename T> __device__ __forceinline__ cplx<T> ldg(const cplx<T> *p) {
   V v = __ldg(reinterpret_cast<const V *>(p));
   return mk<T>(v.x, v.y);
 }
+// Asynchronous global -> shared copies (cp.async): 16-byte copies through L2
+// only (data written by other blocks of the same kernel), 8-byte copies of
+// read-only data through L1; committed as groups and awaited by count.
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void *dst, const void *src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
 // Load through L2 only: data written by other blocks earlier in the same
 // kernel (after a grid barrier) must not come from a stale L1 line.
 template <typename T> __device__ __forceinline__ cplx<T> ldcg(const cplx<T> *p) {

@@ -38,6 +38,15 @@ struct Couplings {
 };
 static const int kMaxRowEntries = 4;  // entries per row the fused step kernel unrolls
 static const int kMaxBatchLines = 64; // lines one block of the step kernel transforms at once
+// The multi-dimensional step kernel stages the gather's operands in shared
+// memory with asynchronous copies when its bulk elements are 16-byte
+// complex numbers (binary64, double-float) and it handles one or two
+// states: kStageDepth slots of one point per thread (256 threads).
+static const int kStageDepth = 3;
+__host__ __device__ constexpr bool step_staged(int cplx_bytes, int states) { return cplx_bytes == 16 && states <= 2; }
+__host__ __device__ constexpr int step_stage_bytes_c(int nd, int states) {
+  return kStageDepth * (((nd + states + 1) * 256 * 16) + kMaxRowEntries * 256 * 8 + 256 * 16);
+}
 
 // Per-step Chebyshev control block in device memory.
 struct ChebyState {
@@ -215,6 +224,7 @@ struct StepArgs {
   long long item_start[5];
   long long line_start[5];   // kinetic lines of dims < d (all states)
   int lmax[4];               // lines of dim d one block transforms at once (shared memory)
+  const long long *bstart;   // first line of each block (segment-aligned), or null: even split
   int TW1;                   // 1-D grids: lines per tile (all states in one block)
   cplx<double> *psi;
   cplx<T> *buf[3];           // rotating phi buffers (phi_{i-2}, phi_{i-1}, phi_i)

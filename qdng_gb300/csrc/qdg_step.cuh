@@ -90,6 +90,40 @@ __device__ __forceinline__ cplx<B> add_soff(cplx<B> h, cplx<B> x, B hi, B lo) {
   else return mk(fma(hi, x.re, fma(lo, x.re, h.re)), fma(hi, x.im, fma(lo, x.im, h.im)));
 }
 
+// The potential-matrix row of each state as the point work reads it: entry
+// columns, grids and field coefficients (1 for static potentials).  Filled
+// once per launch (the coefficients are those of the step) so that a batch
+// of lines starts without a chain of dependent global loads.
+template <typename B>
+struct RowCache {
+  int ne[kMaxStates];
+  int col[kMaxStates][kMaxRowEntries];
+  int gid[kMaxStates][kMaxRowEntries];
+  B coef[kMaxStates][kMaxRowEntries];
+  int unit[kMaxStates];  // only static potentials (coefficient 1) in the row
+};
+template <typename T, typename B>
+__device__ void fill_rows(const StepArgs<T> &a, RowCache<B> &rc) {
+  const bool scaled = a.scaled != 0;
+  const Couplings *__restrict__ cpx = scaled ? a.scp : a.cp;
+  for (int s = threadIdx.x; s < a.S && s < kMaxStates; s += blockDim.x) {
+    const int e0 = cpx->rs[s];
+    const int ne = min(cpx->rs[s + 1] - e0, kMaxRowEntries);
+    rc.ne[s] = ne;
+    int unit = 1;
+    for (int k = 0; k < kMaxRowEntries; ++k) {
+      rc.col[s][k] = k < ne ? cpx->col[e0 + k] : 0;
+      rc.gid[s][k] = k < ne ? cpx->gid[e0 + k] : 0;
+      // the field coefficient of the entry (scaled entries name the plan entry, -1: static)
+      const int ci = k >= ne ? -1 : scaled ? cpx->lid[e0 + k] : e0 + k;
+      const double c = ci >= 0 ? a.coef[ci] : (k < ne ? 1.0 : 0.0);
+      rc.coef[s][k] = d2b<B>(c);
+      if (k < ne && c != 1.0) unit = 0;
+    }
+    rc.unit[s] = unit;
+  }
+}
+
 // Kinetic transforms of phi_i (computed on load) for every dimension;
 // results go to Pnext.  PK_LAST only finishes phi_i and psi (row lines).
 // Loads of UNR points per thread are issued before any use or store, so the
@@ -98,7 +132,8 @@ template <typename T, typename FT, int ND, int SM>
 __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__restrict__ phim1,
                             const cplx<T> *__restrict__ phim2, cplx<T> *__restrict__ phout,
                             cplx<T> *const *Pprev, cplx<T> *const *Pnext, double coeff_i, double &acc,
-                            cplx<T> *smem, unsigned long long *tp = nullptr) {
+                            cplx<T> *smem, int &cur_dim, const RowCache<FT> &rc,
+                            unsigned long long *tp = nullptr) {
   typedef FT B;
   const bool tr = tp != nullptr && threadIdx.x == 0;
   const cplx<B> *phim1b = reinterpret_cast<const cplx<B> *>(phim1);
@@ -111,10 +146,23 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
   const long long npts = a.npts;
   const long long total = a.line_start[ND];
   const long long G = gridDim.x;
-  const long long end = total * (blockIdx.x + 1) / G;
-  long long l = total * blockIdx.x / G;
-  int cur_dim = -1;
-  cplx<FT> *tws = reinterpret_cast<cplx<FT> *>(smem);  // same size as cplx<T> for every FT but float/double
+  const long long end = a.bstart ? a.bstart[blockIdx.x + 1] : total * (blockIdx.x + 1) / G;
+  long long l = a.bstart ? a.bstart[blockIdx.x] : total * blockIdx.x / G;
+  // cur_dim: the dimension whose twiddles the shared table holds; it lives
+  // in the caller across terms (a block keeps its dimension with the
+  // segment-aligned line split, so the table is loaded once per step)
+  // asynchronous staging of the gather's operands (binary64 and double-float
+  // bulk, one or two states): kStageDepth slots of one point per thread in
+  // front of the twiddle table; per slot the kinetic parts, phi_{i-1} of
+  // every state and phi_{i-2} (16 bytes each), the potential values (8
+  // bytes) and psi (16 bytes), each as an array over the 256 threads
+  constexpr bool kStaged = step_staged(sizeof(cplx<FT>), SM);
+  constexpr int kVgOff = (ND + SM + 1) * 256 * 16;
+  constexpr int kPsOff = kVgOff + kMaxRowEntries * 256 * 8;
+  constexpr int kSlotBytes = kPsOff + 256 * 16;
+  static_assert(!kStaged || kStageDepth * kSlotBytes == step_stage_bytes_c(ND, SM), "staging layout");
+  cplx<FT> *tws = reinterpret_cast<cplx<FT> *>(reinterpret_cast<unsigned char *>(smem) +
+                                               (kStaged ? kStageDepth * kSlotBytes : 0));
   __shared__ long long lbase[kMaxBatchLines];
   const cplx<B> off = {d2b<B>(a.offset.re), d2b<B>(a.offset.im)};
   const cplx<double> facd = kind == PK_FIRST ? a.fac1 : a.fac;
@@ -126,18 +174,20 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
   // are applied per point
   const bool scaled = a.scaled != 0;
   const bool srt = a.scaled_rt != 0;
-  const Couplings *__restrict__ cpx = scaled ? a.scp : a.cp;
   const B *__restrict__ grids = scaled ? reinterpret_cast<const B *>(a.sgrids) : step_grids<T, FT>(a);
   const B soh = soff_part<B>(a.soff_hi, a.soff_lo, 0), sol = soff_part<B>(a.soff_hi, a.soff_lo, 1);
+  const B rsg = d2b<B>(a.imag ? -1.0 : 1.0);  // sign of phi_{i-2} in the recurrence
   while (l < end) {
     int d = 0;
     while (l >= a.line_start[d + 1]) ++d;
     const DimPass<T> &g = a.dp[d];
     const int N = g.N;
     const long long stride = g.ls == 1 ? (long long)g.es : 1;
-    const long long nl = npts / N;
+    // the divisions in 32 bits while the grid has fewer than 2^31 points
+    const bool i32 = npts < (1LL << 31);
+    const long long nl = i32 ? (long long)((unsigned)npts / (unsigned)N) : npts / N;
     const long long local = l - a.line_start[d];
-    const int s = (int)(local / nl);
+    const int s = i32 ? (int)((unsigned)local / (unsigned)nl) : (int)(local / nl);
     const long long l0 = local - (long long)s * nl;
     long long cnt = end - l;
     if (cnt > nl - l0) cnt = nl - l0;
@@ -155,36 +205,175 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
       for (int i = threadIdx.x; i < N; i += blockDim.x) tws[i] = twg[i];
       cur_dim = d;
     }
-    // first point of each line of the batch (one 64-bit division per line)
+    // first point of each line of the batch
     if (threadIdx.x < L) {
       const long long line = l0 + threadIdx.x;
-      lbase[threadIdx.x] = (line % stride) + (line / stride) * stride * N;
+      if (i32) {
+        const unsigned q = (unsigned)line / (unsigned)stride;
+        lbase[threadIdx.x] = (long long)((unsigned)line - q * (unsigned)stride) + (long long)q * stride * N;
+      } else {
+        lbase[threadIdx.x] = (line % stride) + (line / stride) * stride * N;
+      }
     }
     __syncthreads();
     const int istr = (int)stride;  // element stride of a line (< 2^31 points per dimension block)
     // potential-matrix entries of row s
-    const int e0 = cpx->rs[s];
-    const int ne = cpx->rs[s + 1] - e0;
+    const int ne = rc.ne[s];
     int ecol[RE], egid[RE];
     B ecoef[RE];
-    bool unit_coef = true;  // only static potentials (coefficient 1) in this row
 #pragma unroll
     for (int k = 0; k < RE; ++k) {
-      ecol[k] = k < ne ? cpx->col[e0 + k] : 0;
-      egid[k] = k < ne ? cpx->gid[e0 + k] : 0;
-      // the field coefficient of the entry (scaled entries name the plan entry, -1: static)
-      const int ci = k >= ne ? -1 : scaled ? cpx->lid[e0 + k] : e0 + k;
-      const double c = ci >= 0 ? a.coef[ci] : (k < ne ? 1.0 : 0.0);
-      ecoef[k] = d2b<B>(c);
-      if (k < ne && c != 1.0) unit_coef = false;
+      ecol[k] = rc.col[s][k];
+      egid[k] = rc.gid[s][k];
+      ecoef[k] = rc.coef[s][k];
     }
+    const bool unit_coef = rc.unit[s] != 0;
     const long long so = (long long)s * npts;
     const int tot = L * N;
     unsigned long long tg0 = tr ? gtimer() : 0;
+    // the point of item idx of the batch: its offset and its shared-memory slot
+    auto locate = [&](int idx, long long &p, int &sx) {
+      int w, i;
+      if (istr == 1) { w = idx / N; i = idx - w * N; }
+      else { i = idx / L; w = idx - i * L; }
+      sx = lidx(w, i, LS);
+      p = lbase[w] + (long long)i * istr;
+    };
+    // phi_i at point p from its loaded operands (H phi_{i-1} = h + the
+    // potential matrix, the offset, the recurrence); the row owner stores
+    // phi_i, updates psi and its norm; the FFT input goes to slot sx
+    auto finish = [&](long long p, int sx, cplx<B> h, const cplx<B> *pm, const B *vg, cplx<B> km2,
+                      cplx<double> ps) {
+      cplx<B> v = h;
+      if (kind != PK_START) {
+        cplx<B> self = pm[0];
+#pragma unroll
+        for (int j = 1; j < SM; ++j)
+          if (j == s) self = pm[j];
+#pragma unroll
+        for (int k = 0; k < RE; ++k) {
+          if (k < ne) {
+            cplx<B> x = pm[0];
+#pragma unroll
+            for (int j = 1; j < SM; ++j)
+              if (j == ecol[k]) x = pm[j];
+            const B vv = unit_coef ? vg[k] : ecoef[k] * vg[k];
+            h.re = fma_b(x.re, vv, h.re);
+            h.im = fma_b(x.im, vv, h.im);
+          }
+        }
+        cplx<B> bf;
+        if (scaled) {
+          h = add_soff(h, self, soh, sol);
+          bf = srt ? mk(-h.im, h.re) : h;
+          if (kind == PK_FIRST) bf = cmulr(bf, d2b<B>(0.5));
+        } else {
+          // (h - offset phi) * factor; a real offset and a purely imaginary
+          // factor (real-time propagation) need half the multiplications
+          cplx<B> hm;
+          if (off_real) {
+            hm.re = fma_b(-off.re, self.re, h.re);
+            hm.im = fma_b(-off.re, self.im, h.im);
+          } else {
+            hm = h - cmul(off, self);
+          }
+          bf = fac_imag ? mk(-fac.im * hm.im, fac.im * hm.re) : cmul(hm, fac);
+        }
+        const long long gidx = so + p;
+        if (kind == PK_FIRST) {
+          v = bf;
+          if (owner) {
+            acc += cabs2(ps);
+            st(phoutb + gidx, bf);
+            const cplx<double> b = {b2d(bf.re), b2d(bf.im)};
+            st(a.psi + gidx, mk(fma(b.re, a.a[1], ps.re * a.a[0]), fma(b.im, a.a[1], ps.im * a.a[0])));
+          }
+        } else {
+          // bf +- km2: one exact fused multiply-add by the sign (no select
+          // between two computed sums); double-float keeps its additions
+          cplx<B> k2;
+          if constexpr (std::is_same<B, dfl>::value) k2 = a.imag ? bf - km2 : bf + km2;
+          else k2 = cplx<B>{fma_b(rsg, km2.re, bf.re), fma_b(rsg, km2.im, bf.im)};
+          v = k2;
+          if (owner) {
+            st(phoutb + gidx, k2);
+            ps.re = fma(coeff_i, b2d(k2.re), ps.re);
+            ps.im = fma(coeff_i, b2d(k2.im), ps.im);
+            st(a.psi + gidx, ps);
+            acc = fma(ps.re, ps.re, fma(ps.im, ps.im, acc));
+          }
+        }
+      }
+      if (kind != PK_LAST) b0[sx] = v;
+    };
+    if constexpr (kStaged) {
+      // operands staged in shared memory by asynchronous copies, kStageDepth
+      // chunks of one point per thread in flight: the loads of the next
+      // chunks overlap the arithmetic of this one.  Each thread reads only
+      // what it copied itself, so no block barrier is needed between chunks.
+      unsigned char *stage = reinterpret_cast<unsigned char *>(smem);
+      const int t = threadIdx.x;
+      const int nch = (tot + 255) >> 8;
+      auto issue = [&](int ch) {
+        const int idx = (ch << 8) + t;
+        if (ch < nch && idx < tot) {
+          long long p;
+          int sx;
+          locate(idx, p, sx);
+          unsigned char *sl = stage + (size_t)(ch % kStageDepth) * kSlotBytes;
+          if (kind == PK_START) {
+            cp_async16(sl + t * 16, phim1b + so + p);
+          } else {
+#pragma unroll
+            for (int dd = 0; dd < ND; ++dd)
+              cp_async16(sl + (dd * 256 + t) * 16, reinterpret_cast<const cplx<B> *>(Pprev[dd]) + so + p);
+#pragma unroll
+            for (int j = 0; j < SM; ++j)
+              if (j < a.S) cp_async16(sl + ((ND + j) * 256 + t) * 16, phim1b + (long long)j * npts + p);
+            if (kind != PK_FIRST) cp_async16(sl + ((ND + SM) * 256 + t) * 16, phim2b + so + p);
+#pragma unroll
+            for (int k = 0; k < RE; ++k)
+              if (k < ne) cp_async8(sl + kVgOff + (k * 256 + t) * 8, grids + (long long)egid[k] * npts + p);
+            if (owner) cp_async16(sl + kPsOff + t * 16, a.psi + so + p);
+          }
+        }
+        cp_async_commit();
+      };
+#pragma unroll
+      for (int c = 0; c < kStageDepth - 1; ++c) issue(c);
+      for (int ch = 0; ch < nch; ++ch) {
+        issue(ch + kStageDepth - 1);
+        cp_async_wait<kStageDepth - 1>();
+        const int idx = (ch << 8) + t;
+        if (idx >= tot) continue;
+        long long p;
+        int sx;
+        locate(idx, p, sx);
+        const unsigned char *sl = stage + (size_t)(ch % kStageDepth) * kSlotBytes;
+        const cplx<B> *cb = reinterpret_cast<const cplx<B> *>(sl);
+        if (kind == PK_START) {
+          finish(p, sx, cb[t], nullptr, nullptr, cplx<B>{}, cplx<double>{});
+          continue;
+        }
+        cplx<B> h = cb[t];
+#pragma unroll
+        for (int dd = 1; dd < ND; ++dd) h = h + cb[dd * 256 + t];
+        cplx<B> pm[SM];
+#pragma unroll
+        for (int j = 0; j < SM; ++j) pm[j] = j < a.S ? cb[(ND + j) * 256 + t] : cplx<B>{};
+        const cplx<B> km2 = kind != PK_FIRST ? cb[(ND + SM) * 256 + t] : cplx<B>{};
+        B vg[RE];
+        const B *vb = reinterpret_cast<const B *>(sl + kVgOff);
+#pragma unroll
+        for (int k = 0; k < RE; ++k) vg[k] = k < ne ? vb[k * 256 + t] : B(0);
+        const cplx<double> ps = owner ? reinterpret_cast<const cplx<double> *>(sl + kPsOff)[t] : cplx<double>{};
+        finish(p, sx, h, pm, vg, km2, ps);
+      }
+      cp_async_wait<0>();
+    } else {
     for (int base = threadIdx.x; base < tot; base += UNR * blockDim.x) {
       long long pp[UNR];
       int sidx[UNR];
-      cplx<B> v[UNR];
       // ---- gather
       cplx<B> hP[UNR], pm[UNR][SM], km2[UNR];
       B vg[UNR][RE];
@@ -193,16 +382,12 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
       for (int u = 0; u < UNR; ++u) {
         const int idx = base + u * blockDim.x;
         const bool ok = idx < tot;
-        int w = 0, i = 0;
-        if (ok) {
-          if (istr == 1) { w = idx / N; i = idx - w * N; }
-          else { i = idx / L; w = idx - i * L; }
-        }
-        sidx[u] = ok ? lidx(w, i, LS) : -1;
-        const long long p = lbase[w] + (long long)i * istr;
-        pp[u] = p;
+        sidx[u] = -1;
+        pp[u] = 0;
         if (!ok) continue;
-        if (kind == PK_START) { v[u] = ldcg(phim1b + so + p); continue; }
+        locate(idx, pp[u], sidx[u]);
+        const long long p = pp[u];
+        if (kind == PK_START) { hP[u] = ldcg(phim1b + so + p); continue; }
         cplx<B> h = ldcg(reinterpret_cast<const cplx<B> *>(Pprev[0]) + so + p);
 #pragma unroll
         for (int dd = 1; dd < ND; ++dd) h = h + ldcg(reinterpret_cast<const cplx<B> *>(Pprev[dd]) + so + p);
@@ -219,66 +404,9 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
 #pragma unroll
       for (int u = 0; u < UNR; ++u) {
         if (sidx[u] < 0) continue;
-        if (kind != PK_START) {
-          cplx<B> h = hP[u];
-          cplx<B> self = pm[u][0];
-#pragma unroll
-          for (int j = 1; j < SM; ++j)
-            if (j == s) self = pm[u][j];
-#pragma unroll
-          for (int k = 0; k < RE; ++k) {
-            if (k < ne) {
-              cplx<B> x = pm[u][0];
-#pragma unroll
-              for (int j = 1; j < SM; ++j)
-                if (j == ecol[k]) x = pm[u][j];
-              const B vv = unit_coef ? vg[u][k] : ecoef[k] * vg[u][k];
-              h.re = fma_b(x.re, vv, h.re);
-              h.im = fma_b(x.im, vv, h.im);
-            }
-          }
-          cplx<B> bf;
-          if (scaled) {
-            h = add_soff(h, self, soh, sol);
-            bf = srt ? mk(-h.im, h.re) : h;
-            if (kind == PK_FIRST) bf = cmulr(bf, d2b<B>(0.5));
-          } else {
-            // (h - offset phi) * factor; a real offset and a purely imaginary
-            // factor (real-time propagation) need half the multiplications
-            cplx<B> hm;
-            if (off_real) {
-              hm.re = fma_b(-off.re, self.re, h.re);
-              hm.im = fma_b(-off.re, self.im, h.im);
-            } else {
-              hm = h - cmul(off, self);
-            }
-            bf = fac_imag ? mk(-fac.im * hm.im, fac.im * hm.re) : cmul(hm, fac);
-          }
-          const long long gidx = so + pp[u];
-          if (kind == PK_FIRST) {
-            v[u] = bf;
-            if (owner) {
-              const cplx<double> p0 = ps[u];
-              acc += cabs2(p0);
-              st(phoutb + gidx, bf);
-              const cplx<double> b = {b2d(bf.re), b2d(bf.im)};
-              st(a.psi + gidx, mk(fma(b.re, a.a[1], p0.re * a.a[0]), fma(b.im, a.a[1], p0.im * a.a[0])));
-            }
-          } else {
-            const cplx<B> k2 = a.imag ? bf - km2[u] : bf + km2[u];
-            v[u] = k2;
-            if (owner) {
-              st(phoutb + gidx, k2);
-              cplx<double> p0 = ps[u];
-              p0.re = fma(coeff_i, b2d(k2.re), p0.re);
-              p0.im = fma(coeff_i, b2d(k2.im), p0.im);
-              st(a.psi + gidx, p0);
-              acc = fma(p0.re, p0.re, fma(p0.im, p0.im, acc));
-            }
-          }
-        }
-        if (kind != PK_LAST) b0[sidx[u]] = v[u];
+        finish(pp[u], sidx[u], hP[u], pm[u], vg[u], km2[u], ps[u]);
       }
+    }
     }
     if (kind == PK_LAST) continue;
     __syncthreads();
@@ -498,13 +626,17 @@ __global__ void __launch_bounds__(256, OCC) cheby_step_kernel(StepArgs<T> a) {
       done = step_cut(tot_s, norm0, last, norm_last, a.imag, a.diff, a.prec, a.offim0, status);
     }
   } else {
+    int tw_dim = -1;  // dimension of the twiddles held in shared memory
+    __shared__ RowCache<FT> rows;
+    fill_rows(a, rows);
+    __syncthreads();
     // phase 1: T_d phi_0 -> P[1]
-    phase_fused<T, FT, ND, SM>(a, PK_START, a.buf[0], nullptr, nullptr, nullptr, a.Pn[1], 0.0, acc, smem);
+    phase_fused<T, FT, ND, SM>(a, PK_START, a.buf[0], nullptr, nullptr, nullptr, a.Pn[1], 0.0, acc, smem, tw_dim, rows);
     if (!grid_sync(a.bar)) return;
     // phase 2: phi_1 (+ psi = a0 psi + a1 phi_1, raw norm of psi) and T_d phi_1 -> P[0]
     acc = 0.0;
     phase_fused<T, FT, ND, SM>(a, a.order > 2 ? PK_FIRST : PK_LAST, a.buf[0], nullptr, a.buf[1], a.Pn[1], a.Pn[0],
-                               0.0, acc, smem);
+                               0.0, acc, smem, tw_dim, rows);
     t = block_sum(acc, red);
     if (threadIdx.x == 0) a.partials[blockIdx.x] = t;
     if (!grid_sync(a.bar)) return;
@@ -519,7 +651,8 @@ __global__ void __launch_bounds__(256, OCC) cheby_step_kernel(StepArgs<T> a) {
       acc = 0.0;
       const int kind = (i + 1 < a.order) ? PK_TERM : PK_LAST;
       phase_fused<T, FT, ND, SM>(a, kind, a.buf[(i - 1) % 3], a.buf[(i - 2) % 3], a.buf[i % 3], a.Pn[i & 1],
-                                 a.Pn[(i + 1) & 1], a.a[i], acc, smem, tr ? tpi : nullptr);
+                                 a.Pn[(i + 1) & 1], a.a[i], acc, smem, tw_dim, rows,
+                                 tr ? tpi : nullptr);
       const unsigned long long t1 = tr ? gtimer() : 0;
       t = block_sum(acc, red);
       if (threadIdx.x == 0) a.partials[blockIdx.x] = t;
