@@ -59,9 +59,10 @@ struct ChebyState {
   unsigned int arrive;  // blocks of the current reduction that have stored their partial sum
   int i;             // index of the next term (device-driven term loop)
   double acc_last;   // accumulated norm after the previous term (differential cut)
-  // phase timing of the persistent step kernel as seen by block 0 (ns,
-  // accumulated while tracing): own kinetic work, wait at the barrier after
-  // it, own point work, wait at the norm barrier
+  // phase timing of the persistent step kernel as seen by one block (ns,
+  // accumulated over the terms after the first while tracing): gathering
+  // and finishing phi, the FFTs, the whole term, the norm reduction and the
+  // grid barrier
   unsigned long long t_phase[4];
 };
 

@@ -648,6 +648,7 @@ __global__ void __launch_bounds__(256, OCC) cheby_step_kernel(StepArgs<T> a) {
     if (done) status = 2;
     // phase i+1: phi_i from P[i&1], phi_{i-1} = buf[(i-1)%3], phi_{i-2} = buf[(i-2)%3] -> buf[i%3]
     for (int i = 2; i < a.order && !done; ++i) {
+      const unsigned long long t0 = tr ? gtimer() : 0;
       acc = 0.0;
       const int kind = (i + 1 < a.order) ? PK_TERM : PK_LAST;
       phase_fused<T, FT, ND, SM>(a, kind, a.buf[(i - 1) % 3], a.buf[(i - 2) % 3], a.buf[i % 3], a.Pn[i & 1],
@@ -663,6 +664,7 @@ __global__ void __launch_bounds__(256, OCC) cheby_step_kernel(StepArgs<T> a) {
       __syncthreads();
       used = i + 1;
       done = step_cut(tot_s, norm0, last, norm_last, a.imag, a.diff, a.prec, a.offim0, status);
+      if (tr) tp[2] += gtimer() - t0;  // the whole term
     }
   }
 

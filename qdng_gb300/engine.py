@@ -168,11 +168,15 @@ class Propagator:
         return used.value
 
     def phase_times(self):
-        """ns spent by block 0 of the persistent step kernel while profiling: loading and
-        finishing phi (gather), the shared-memory FFTs, storing T_d phi, waiting at the barrier."""
+        """ns spent by one block (block 0, or QDG_TRACE_BLOCK) of the persistent step kernel
+        while profiling, over the terms after the first: gathering and finishing phi
+        (gather), the shared-memory FFTs (fft), the norm reduction and grid barrier
+        (barrier), and the rest of the term (other: batch setup, the sum of the block
+        partials, the series cut)."""
         ns = np.zeros(4)
         check(self.lib.qdg_prop_phase_times(self.h, _dp(ns)))
-        return dict(gather=ns[0], fft=ns[1], store=ns[2], barrier=ns[3])
+        other = max(0.0, ns[2] - ns[0] - ns[1] - ns[3]) if ns[2] > 0 else 0.0
+        return dict(gather=ns[0], fft=ns[1], barrier=ns[3], other=other)
 
     def eigen_imag(self, psi_init, nef, maxsteps, conv, diag=True):
         """ProgEigen::ImagTimeEF (+ DiagBasis): returns (efs [nef x size],
