@@ -159,6 +159,9 @@ struct qdg_prop {
   long long line_start[QDG_MAX_DIMS + 1] = {0, 0, 0, 0, 0};
   int lmax[QDG_MAX_DIMS] = {1, 1, 1, 1};
   long long *d_bstart = nullptr;    // [step_grid + 1] first kinetic line of each block
+  long long *d_bstartA = nullptr;   // the same for the lines of dimension 0 (two-phase terms)
+  long long *d_bstartB = nullptr;   // ... and for the lines of the other dimensions
+  bool two_phase = false;           // grids of 3+ dimensions: phi_i stored once per term
   // persistent step kernel: the kinetic tables and the potential grids
   // multiplied by the series factor f once, -f offset per point as a value
   // and its rounding residual (scaled_setup)
@@ -739,21 +742,24 @@ int step_bulk(const qdg_plan *p) {
 // for the slowest one.  So every segment gets a whole number of blocks, in
 // proportion to its work (lines x N (log2 N + 4): the transforms and the
 // point work), and its lines are split evenly among them.  With fewer
-// blocks than segments the even split over all lines stays.
-qdg_status partition_lines(qdg_prop *P) {
-  qdg_plan *p = P->plan;
+// blocks than segments the even split over the lines stays (no table).
+// Tables for the dimensions [d0, d1): first line of every block, G + 1
+// entries, in the kernel's global line numbering.
+static bool line_table(const qdg_prop *P, int d0, int d1, std::vector<long long> &bs) {
+  const qdg_plan *p = P->plan;
   const int G = P->step_grid;
-  const int nseg = p->nd * p->S;
-  if (G < nseg || (has(P, "partition") && P->params.at("partition") == "even")) return QDG_OK;
+  const int nseg = (d1 - d0) * p->S;
+  bs.clear();
+  if (G < nseg || (has(P, "partition") && P->params.at("partition") == "even")) return false;
   std::vector<double> cost(nseg);
   std::vector<long long> nl(nseg);
   double total = 0;
-  for (int d = 0; d < p->nd; ++d)
+  for (int d = d0; d < d1; ++d)
     for (int s = 0; s < p->S; ++s) {
-      const int n = p->dim[d].n;
-      nl[d * p->S + s] = p->npts / n;
-      cost[d * p->S + s] = (double)(p->npts / n) * n * (std::log2((double)n) + 4.0);
-      total += cost[d * p->S + s];
+      const int n = p->dim[d].n, k = (d - d0) * p->S + s;
+      nl[k] = p->npts / n;
+      cost[k] = (double)(p->npts / n) * n * (std::log2((double)n) + 4.0);
+      total += cost[k];
     }
   std::vector<int> nb(nseg);
   int used = 0;
@@ -770,20 +776,43 @@ qdg_status partition_lines(qdg_prop *P) {
       const double lpb = (double)nl[k] / nb[k];
       if (best < 0 || (used > G ? lpb < (double)nl[best] / nb[best] : lpb > (double)nl[best] / nb[best])) best = k;
     }
-    if (best < 0) return QDG_OK;  // cannot settle: keep the even split
+    if (best < 0) return false;  // cannot settle: keep the even split
     nb[best] += used > G ? -1 : 1;
     used += used > G ? -1 : 1;
   }
-  std::vector<long long> bs;
   bs.reserve(G + 1);
-  long long base = 0;
+  long long base = P->line_start[d0];
   for (int k = 0; k < nseg; ++k) {
     for (int j = 0; j < nb[k]; ++j) bs.push_back(base + nl[k] * j / nb[k]);
     base += nl[k];
   }
   bs.push_back(base);
-  CK(cudaMalloc(&P->d_bstart, sizeof(long long) * bs.size()));
-  CK(cudaMemcpy(P->d_bstart, bs.data(), sizeof(long long) * bs.size(), cudaMemcpyHostToDevice));
+  return true;
+}
+
+// Grids of three or more dimensions take two phases per term: the lines of
+// dimension 0 finish phi_i (and psi, its norm) and store it, then, after a
+// grid barrier, the lines of the other dimensions load phi_i instead of
+// recomputing it from the kinetic parts of every dimension, both phi
+// buffers and the potentials (cfg3 128^3: that recomputation was a sixth of
+// the FP64 work and most of the DRAM traffic).  Two-dimensional grids keep
+// one phase per term (their 1024 lines over 152 blocks: a second barrier
+// per term costs more than the recomputation).
+qdg_status partition_lines(qdg_prop *P) {
+  qdg_plan *p = P->plan;
+  std::vector<long long> bs;
+  if (line_table(P, 0, p->nd, bs)) {
+    CK(cudaMalloc(&P->d_bstart, sizeof(long long) * bs.size()));
+    CK(cudaMemcpy(P->d_bstart, bs.data(), sizeof(long long) * bs.size(), cudaMemcpyHostToDevice));
+  }
+  P->two_phase = p->nd >= 3 && !(has(P, "phases") && atoi(P->params.at("phases").c_str()) == 1);
+  if (!P->two_phase) return QDG_OK;
+  for (int ph = 0; ph < 2; ++ph) {
+    if (!line_table(P, ph == 0 ? 0 : 1, ph == 0 ? 1 : p->nd, bs)) continue;
+    long long *&dst = ph == 0 ? P->d_bstartA : P->d_bstartB;
+    CK(cudaMalloc(&dst, sizeof(long long) * bs.size()));
+    CK(cudaMemcpy(dst, bs.data(), sizeof(long long) * bs.size(), cudaMemcpyHostToDevice));
+  }
   return QDG_OK;
 }
 
@@ -1069,6 +1098,9 @@ qdg_status cheby_step_persistent(qdg_prop *P, cplx<double> *psi, long long step)
   for (int d = 0; d <= p->nd; ++d) a.line_start[d] = P->line_start[d];
   for (int d = 0; d < p->nd; ++d) a.lmax[d] = P->lmax[d];
   a.bstart = P->d_bstart;
+  a.bstartA = P->d_bstartA;
+  a.bstartB = P->d_bstartB;
+  a.two_phase = P->two_phase ? 1 : 0;
   a.TW1 = P->step_tw1;
   a.psi = psi;
   a.buf[0] = reinterpret_cast<cplx<T> *>(P->k0);
@@ -2227,9 +2259,19 @@ qdg_status qdg_prop_create(qdg_plan *plan, const char *name, const char *params,
   //   range/beta, and the energies it perturbs turn into a phase error that
   //   grows with the propagation time (6e-4 in the autocorrelation after
   //   2000 a.u. on the 128^2 double well).  The parameter krylov_fp32=1 keeps
-  //   the FP32 basis (about 1.2x faster there).
+  //   the FP32 basis (about 1.2x faster there);
+  // * Chebyshev on one line of 512 to 2048 points (a power of two): the
+  //   binary64 cluster kernel (one component per thread, qdg_step_line64.cu)
+  //   is latency bound and faster than the FP32 line kernels (1-D Morse,
+  //   1024 points: 1.20 against 1.85 ms per step), so the mixed form takes
+  //   the binary64 step there; cluster=0 or cluster=1 keeps the FP32 kernels.
   const bool krylov_twin = P->kind >= 3 && !(has(P, "krylov_fp32") && atoi(P->params["krylov_fp32"].c_str()) != 0);
-  if (plan->precision == QDG_PREC_MIXED && ((P->kind == 1 && P->imag) || krylov_twin)) {
+  bool line_twin = false;
+  if (P->kind == 1 && plan->precision == QDG_PREC_MIXED && plan->nd == 1 && plan->S == 1 && !has(P, "cluster")) {
+    const int N = plan->dim[0].n;
+    line_twin = (N & (N - 1)) == 0 && N >= 512 && N <= 2048 && qdg::line64_cluster_size(N) > 0;
+  }
+  if (plan->precision == QDG_PREC_MIXED && ((P->kind == 1 && P->imag) || krylov_twin || line_twin)) {
     qdg_hplan_desc d;
     memset(&d, 0, sizeof(d));
     d.grid = plan->grid;
@@ -2266,6 +2308,8 @@ qdg_status qdg_prop_destroy(qdg_prop *P) {
   if (P->d_a) cudaFree(P->d_a);
   if (P->d_cs) cudaFree(P->d_cs);
   if (P->d_bstart) cudaFree(P->d_bstart);
+  if (P->d_bstartA) cudaFree(P->d_bstartA);
+  if (P->d_bstartB) cudaFree(P->d_bstartB);
   if (P->h_cs) cudaFreeHost(P->h_cs);
   for (auto &g : P->gtab) for (auto v : g) if (v) cudaFree(v);
   for (auto v : P->gcp_d) if (v) cudaFree(v);

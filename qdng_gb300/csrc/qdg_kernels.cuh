@@ -226,6 +226,9 @@ struct StepArgs {
   long long line_start[5];   // kinetic lines of dims < d (all states)
   int lmax[4];               // lines of dim d one block transforms at once (shared memory)
   const long long *bstart;   // first line of each block (segment-aligned), or null: even split
+  const long long *bstartA;  // two-phase terms: the same for the lines of dimension 0 ...
+  const long long *bstartB;  // ... and for the lines of the other dimensions
+  int two_phase;             // grids of 3+ dimensions: phi_i stored by dimension 0, loaded by the others
   int TW1;                   // 1-D grids: lines per tile (all states in one block)
   cplx<double> *psi;
   cplx<T> *buf[3];           // rotating phi buffers (phi_{i-2}, phi_{i-1}, phi_i)

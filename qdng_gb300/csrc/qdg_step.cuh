@@ -132,8 +132,8 @@ template <typename T, typename FT, int ND, int SM>
 __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__restrict__ phim1,
                             const cplx<T> *__restrict__ phim2, cplx<T> *__restrict__ phout,
                             cplx<T> *const *Pprev, cplx<T> *const *Pnext, double coeff_i, double &acc,
-                            cplx<T> *smem, int &cur_dim, const RowCache<FT> &rc,
-                            unsigned long long *tp = nullptr) {
+                            cplx<T> *smem, int &cur_n, const RowCache<FT> &rc, const long long *bs,
+                            long long lo, long long hi, unsigned long long *tp = nullptr) {
   typedef FT B;
   const bool tr = tp != nullptr && threadIdx.x == 0;
   const cplx<B> *phim1b = reinterpret_cast<const cplx<B> *>(phim1);
@@ -144,13 +144,13 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
   constexpr int UNR = SM > 2 ? 1 : std::is_same<FT, double>::value ? 3 : 2;
   constexpr int RE = kMaxRowEntries;
   const long long npts = a.npts;
-  const long long total = a.line_start[ND];
+  // this block's lines of the phase: from the table bs, or an even split of [lo, hi)
   const long long G = gridDim.x;
-  const long long end = a.bstart ? a.bstart[blockIdx.x + 1] : total * (blockIdx.x + 1) / G;
-  long long l = a.bstart ? a.bstart[blockIdx.x] : total * blockIdx.x / G;
-  // cur_dim: the dimension whose twiddles the shared table holds; it lives
-  // in the caller across terms (a block keeps its dimension with the
-  // segment-aligned line split, so the table is loaded once per step)
+  const long long end = bs ? bs[blockIdx.x + 1] : lo + (hi - lo) * (blockIdx.x + 1) / G;
+  long long l = bs ? bs[blockIdx.x] : lo + (hi - lo) * blockIdx.x / G;
+  // cur_n: the line length whose twiddles the shared table holds (the
+  // table depends on N only); it lives in the caller across terms, so a
+  // block that keeps its line length loads it once per step
   // asynchronous staging of the gather's operands (binary64 and double-float
   // bulk, one or two states): kStageDepth slots of one point per thread in
   // front of the twiddle table; per slot the kinetic parts, phi_{i-1} of
@@ -200,10 +200,10 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
     cplx<FT> *b0 = tws + N;
     cplx<FT> *b1 = b0 + line_buf_elems(N, a.lmax[d]);
     __syncthreads();
-    if (d != cur_dim && kind != PK_LAST) {
+    if (N != cur_n && kind != PK_LAST) {
       const cplx<FT> *twg = step_twiddles<T, FT>(g);
       for (int i = threadIdx.x; i < N; i += blockDim.x) tws[i] = twg[i];
-      cur_dim = d;
+      cur_n = N;
     }
     // first point of each line of the batch
     if (threadIdx.x < L) {
@@ -626,17 +626,34 @@ __global__ void __launch_bounds__(256, OCC) cheby_step_kernel(StepArgs<T> a) {
       done = step_cut(tot_s, norm0, last, norm_last, a.imag, a.diff, a.prec, a.offim0, status);
     }
   } else {
-    int tw_dim = -1;  // dimension of the twiddles held in shared memory
-    __shared__ RowCache<FT> rows;
+    int tw_n = -1;  // line length of the twiddles held in shared memory
+    // raw storage: the double-float coefficient type has constructors
+    __shared__ __align__(16) unsigned char rows_raw[sizeof(RowCache<FT>)];
+    RowCache<FT> &rows = *reinterpret_cast<RowCache<FT> *>(rows_raw);
     fill_rows(a, rows);
     __syncthreads();
-    // phase 1: T_d phi_0 -> P[1]
-    phase_fused<T, FT, ND, SM>(a, PK_START, a.buf[0], nullptr, nullptr, nullptr, a.Pn[1], 0.0, acc, smem, tw_dim, rows);
+    const long long all = a.line_start[ND];
+    // the lines of a term: all of them in one phase, or dimension 0 (phase A)
+    // and then the others (phase B) for grids of three or more dimensions
+    const bool two = a.two_phase != 0;
+    const long long *bsA = two ? a.bstartA : a.bstart;
+    const long long hiA = two ? a.line_start[1] : all;
+    // phase B: T_d phi_i for d >= 1 from the stored phi_i
+    auto phase_b = [&](const cplx<T> *phi_i, cplx<T> *const *Pnext) -> bool {
+      double dummy = 0.0;
+      phase_fused<T, FT, ND, SM>(a, PK_START, phi_i, nullptr, nullptr, nullptr, Pnext, 0.0, dummy, smem, tw_n, rows,
+                                 a.bstartB, a.line_start[1], all);
+      return grid_sync(a.bar);
+    };
+    // phase 1: T_d phi_0 -> P[1] (all dimensions)
+    phase_fused<T, FT, ND, SM>(a, PK_START, a.buf[0], nullptr, nullptr, nullptr, a.Pn[1], 0.0, acc, smem, tw_n, rows,
+                               a.bstart, 0, all);
     if (!grid_sync(a.bar)) return;
     // phase 2: phi_1 (+ psi = a0 psi + a1 phi_1, raw norm of psi) and T_d phi_1 -> P[0]
     acc = 0.0;
-    phase_fused<T, FT, ND, SM>(a, a.order > 2 ? PK_FIRST : PK_LAST, a.buf[0], nullptr, a.buf[1], a.Pn[1], a.Pn[0],
-                               0.0, acc, smem, tw_dim, rows);
+    const int kind1 = a.order > 2 ? PK_FIRST : PK_LAST;
+    phase_fused<T, FT, ND, SM>(a, kind1, a.buf[0], nullptr, a.buf[1], a.Pn[1], a.Pn[0], 0.0, acc, smem, tw_n, rows,
+                               bsA, 0, hiA);
     t = block_sum(acc, red);
     if (threadIdx.x == 0) a.partials[blockIdx.x] = t;
     if (!grid_sync(a.bar)) return;
@@ -646,13 +663,14 @@ __global__ void __launch_bounds__(256, OCC) cheby_step_kernel(StepArgs<T> a) {
     norm0 = last = tot_s;
     done = !isfinite(norm0);
     if (done) status = 2;
+    if (two && !done && kind1 != PK_LAST && !phase_b(a.buf[1], a.Pn[0])) return;
     // phase i+1: phi_i from P[i&1], phi_{i-1} = buf[(i-1)%3], phi_{i-2} = buf[(i-2)%3] -> buf[i%3]
     for (int i = 2; i < a.order && !done; ++i) {
       const unsigned long long t0 = tr ? gtimer() : 0;
       acc = 0.0;
       const int kind = (i + 1 < a.order) ? PK_TERM : PK_LAST;
       phase_fused<T, FT, ND, SM>(a, kind, a.buf[(i - 1) % 3], a.buf[(i - 2) % 3], a.buf[i % 3], a.Pn[i & 1],
-                                 a.Pn[(i + 1) & 1], a.a[i], acc, smem, tw_dim, rows,
+                                 a.Pn[(i + 1) & 1], a.a[i], acc, smem, tw_n, rows, bsA, 0, hiA,
                                  tr ? tpi : nullptr);
       const unsigned long long t1 = tr ? gtimer() : 0;
       t = block_sum(acc, red);
@@ -664,6 +682,7 @@ __global__ void __launch_bounds__(256, OCC) cheby_step_kernel(StepArgs<T> a) {
       __syncthreads();
       used = i + 1;
       done = step_cut(tot_s, norm0, last, norm_last, a.imag, a.diff, a.prec, a.offim0, status);
+      if (two && !done && kind != PK_LAST && !phase_b(a.buf[i % 3], a.Pn[(i + 1) & 1])) return;
       if (tr) tp[2] += gtimer() - t0;  // the whole term
     }
   }
