@@ -342,18 +342,26 @@ def engine_arm(args, world, rank, local):
         ach = per_launch / avg_s / 1e9
         # DRAM bytes (read + write) of one launch of the dominant kernel, from
         # an ncu capture of the same command (dram__bytes_read.sum +
-        # dram__bytes_write.sum); the 256^2 x 2 working set stays in L2, the
-        # 128^3 step re-reads its inputs once per dimension; workloads not
-        # captured report null
+        # dram__bytes_write.sum, profiles/); the 256^2 x 2 working set stays
+        # in L2, the 128^3 step streams the kinetic parts of three dimensions;
+        # workloads not captured report null
         traffic = None
         if args.workload == "cfg2" and modes[top] == "cheby_step":
-            traffic = {"df64": 5.31e6, "mixed": 3.75e6}.get(args.precision)
+            traffic = {"fp64": 6.13e6, "mixed": 3.75e6}.get(args.precision)
         elif args.workload == "cfg3" and modes[top] == "cheby_step" and args.precision == "fp64":
-            traffic = 1.652e10
+            traffic = 9.52e9
+        elif args.workload == "cfg1" and modes[top] == "cheby_step" and args.precision == "fp64":
+            traffic = 7.35e4
         elif args.workload == "cfg2gspo" and modes[top] == "gspo_kin":
             traffic = 2.21e6
+        if args.workload == "cfg1" and modes[top] == "cheby_step":
+            kname = "cheby_line64_kernel (one line on a cluster of 16 blocks, whole step)"
+        # what binds these kernels instead: binary64 arithmetic on GB300's FP64
+        # pipe (the mixed and double-float forms: latency of the term chain)
+        limiter = ("FP64 pipe (binary64 FFTs; cfg2: 60% busy in ncu, working set L2-resident)"
+                   if args.precision == "fp64" and modes[top] == "cheby_step" else None)
         roof = {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(ach / peak, 4), "traffic": traffic, "kernel": kname,
+                "frac": round(ach / peak, 4), "traffic": traffic, "kernel": kname, "limiter": limiter,
                 "algorithmic_bytes_per_launch": int(per_launch), "bytes_note": what,
                 "avg_launch_us": round(avg_s * 1e6, 2), "peak_source": peak_src + " (MEASURED_PEAKS.json hbm_gbs)"}
     per_mode = {modes[i]: {"ms": round(float(prof_ms[i]), 3), "launches": int(prof_n[i])}

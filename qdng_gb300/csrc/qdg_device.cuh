@@ -18,8 +18,9 @@ namespace qdg {
 template <typename T> struct cplx { T re, im; };
 
 // ---- double-float: an unevaluated sum hi + lo of two FP32 numbers ---------
-// GB300 executes FP64 at 1/64 of the FP32 rate.  The FFTs of the FP64 path
-// run in this type: about 48 significant bits (error-free transformations:
+// GB300 executes FP64 at 1/64 of the FP32 rate.  The DF64 precision form
+// (QDG_PREC_DF64) runs the bulk and the FFTs of its multi-dimensional step
+// kernel in this type; the FP64 form is binary64 throughout.  About 48 significant bits (error-free transformations:
 // Knuth's TwoSum, Dekker/FMA products; the addition is the "sloppy" form,
 // whose error is bounded by ~2^-47 of the operands' magnitude, which is what
 // a normwise FFT error bound needs).  The round-to-nearest intrinsics keep
@@ -85,18 +86,6 @@ __device__ __forceinline__ cplx<dfl> ldcg(const cplx<dfl> *p) {
 }
 __device__ __forceinline__ void st(cplx<dfl> *p, cplx<dfl> c) {
   *reinterpret_cast<float4 *>(p) = make_float4(c.re.hi, c.re.lo, c.im.hi, c.im.lo);
-}
-
-// Arithmetic type of the FFTs: double-float for the FP64 path, float for FP32.
-template <typename T> struct FftType { typedef T type; };
-template <> struct FftType<double> { typedef dfl type; };
-template <typename F, typename T> __device__ __forceinline__ cplx<F> to_fft(cplx<T> v) {
-  if constexpr (std::is_same<F, T>::value) return v;
-  else return cplx<F>{df_from_double(v.re), df_from_double(v.im)};
-}
-template <typename T, typename F> __device__ __forceinline__ cplx<T> from_fft(cplx<F> v) {
-  if constexpr (std::is_same<F, T>::value) return v;
-  else return cplx<T>{df_to_double(v.re), df_to_double(v.im)};
 }
 
 template <typename T> struct vec2;

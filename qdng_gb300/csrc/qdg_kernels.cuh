@@ -137,7 +137,7 @@ struct DimPass {
   const double *kfac;   // [S] dk^2/(2m)/N
   cplx<T> *P;           // T_d phi output (state stride npts)
   const T *ktab;        // [S][N] kinetic multipliers kfac[s] * min(i, N-i)^2 (precomputed)
-  const cplx<dfl> *twdf;  // FP64 path: twiddles and multipliers in double-float (the FFT type)
+  const cplx<dfl> *twdf;  // DF64 form: twiddles and multipliers in double-float (the FFT type)
   const dfl *ktdf;
 };
 
@@ -236,7 +236,7 @@ struct StepArgs {
   const Couplings *cp;
   const double *coef;
   const T *grids;
-  const dfl *gdf;            // FP64 path: the grids in double-float (the phases' bulk type)
+  const dfl *gdf;            // DF64 form: the grids in double-float (the phases' bulk type)
   cplx<double> offset, fac1, fac, ph;  // offset, exp/scaling, 2 exp/scaling, exp(c0 offset)
   const double *a;           // real series coefficients a_i (J_0, 2 J_i / I_0, 2 I_i)
   int order;
