@@ -53,8 +53,13 @@ typedef enum qdg_term_kind {
   QDG_TERM_KINETIC = 1,    /* OGridNablaSq: -1/(2m) Laplacian via FFT (src/qdlib/OGridNablaSq.cpp:28-111) */
   QDG_TERM_POTENTIAL = 2,  /* OGridPotential: V(x) psi (src/qdlib/OGridPotential.cpp:134-142) */
   QDG_TERM_DIPOLE = 3,     /* OGridDipole: -mu(x) E(t) psi (src/qdlib/OGridDipole.cpp:46-60) */
-  QDG_TERM_NAC = 4         /* OGridNAC: sign/(2 mass) sum_d [f_d d/dx_d psi + d/dx_d (f_d psi)]
+  QDG_TERM_NAC = 4,        /* OGridNAC: sign/(2 mass) sum_d [f_d d/dx_d psi + d/dx_d (f_d psi)]
                               (src/qdlib/OGridNAC.cpp:131-148), derivatives by FFT (OGridNabla.cpp:76-95) */
+  QDG_TERM_GOBBLER = 5     /* OGobbler (src/qdlib/OGobbler.cpp:30-84,176-204): a diagonal grid term W(x)
+                              = gain x (product of Butterworth filters); laser = 1 makes it a negative
+                              imaginary potential, H psi += -i W psi (nip="true"), else H psi += W psi;
+                              mass[0] = gain (Emax = gain, Emin = -i gain with nip, else 0).
+                              Not a member type of GSPO (OGSPO.cpp:71-85 needs ODSpace operators). */
 } qdg_term_kind;
 
 /* Arithmetic of a plan.  FP64 is the drop-in form: every value (psi, phi_n,
@@ -176,6 +181,26 @@ qdg_status qdg_h_apply(qdg_plan *plan, const qdg_wf *in, qdg_wf *out, int64_t st
 /* Reporter::Analyze values of psi at clock step `step` (psi0 may be NULL). */
 qdg_status qdg_observables_compute(qdg_plan *plan, const qdg_wf *psi, const qdg_wf *psi0,
                                    int64_t step, qdg_observables *out);
+
+/* ---- expectation filters: FiltersList expec / expeconly
+ * (src/FiltersList.cpp:289-308), renormalised by <psi|psi> as ProgPropa
+ * sets them (ProgPropa.cpp:260,276). Values are Re <psi|O|psi> / <psi|psi>. */
+
+/* OGridPosition (OGridPosition.cpp:41-80): x of dimension dim (dim < 0: the
+ * sum over all dimensions), times scale. */
+qdg_status qdg_expec_position(qdg_plan *plan, const qdg_wf *psi, int32_t dim, double scale, double *out);
+/* GridMomentum = OGridNabla(momentum) (OGridNabla.cpp:76-95, Kspace.cpp:60-96):
+ * k of dimension dim (dim < 0: the sum over all dimensions), times factor. */
+qdg_status qdg_expec_momentum(qdg_plan *plan, const qdg_wf *psi, int32_t dim, double factor, double *out);
+/* The kinetic terms of the plan (OGridNablaSq): sum of their expectation values. */
+qdg_status qdg_expec_kinetic(qdg_plan *plan, const qdg_wf *psi, double *out);
+/* A real diagonal grid of the plan (grid index into grid_data) on every
+ * state: OGridPotential / OGobbler (no nip) as a filter operator. */
+qdg_status qdg_expec_grid(qdg_plan *plan, const qdg_wf *psi, int32_t grid, double *out);
+/* OProjection (OProjection.cpp:133-149): sum_k |<phi_k|psi>|^2 over nfun
+ * functions given as host arrays of the wave function's size (complex128). */
+qdg_status qdg_expec_projection(qdg_plan *plan, const qdg_wf *psi, const double *const *funcs, int32_t nfun,
+                                double *out);
 
 /* ---- propagators: replace OCheby / OGSPO / OSIL / OArnoldi ------------- */
 

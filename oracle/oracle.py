@@ -59,6 +59,13 @@ def lib():
         L.orc_erange.argtypes = [vp, dp, dp]
         L.orc_h_apply.argtypes = [vp, dp, dp, C.c_long]
         L.orc_observables.argtypes = [vp, dp, dp, C.c_long, dp]
+        for f, args in (("orc_expec_position", [vp, dp, C.c_int, C.c_double]),
+                        ("orc_expec_momentum", [vp, dp, C.c_int, C.c_double]),
+                        ("orc_expec_kinetic", [vp, dp]),
+                        ("orc_expec_grid", [vp, dp, C.c_int]),
+                        ("orc_expec_projection", [vp, dp, dp, C.c_int])):
+            getattr(L, f).argtypes = args
+            getattr(L, f).restype = C.c_double
         L.orc_prop_create.restype = vp
         L.orc_prop_create.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_double, C.c_int, C.c_int]
         L.orc_prop_destroy.argtypes = [vp]
@@ -132,6 +139,26 @@ class System:
         lib().orc_observables(self.h, _dp(x), _dp(p0) if p0 is not None else None, step, _dp(out))
         return dict(norm2=out[0], pops=out[1:1 + self.S], energy=out[1 + self.S],
                     autocorr=complex(out[2 + self.S], out[3 + self.S]))
+
+    # expectation filters, Re <psi|O|psi> / <psi|psi> (FiltersList.cpp:289-308, ProgPropa.cpp:260,276)
+    def _x(self, psi):
+        return np.ascontiguousarray(psi, dtype=np.complex128).reshape(-1)
+
+    def expec_position(self, psi, dim=-1, scale=1.0):
+        return lib().orc_expec_position(self.h, _dp(self._x(psi)), dim, scale)
+
+    def expec_momentum(self, psi, dim=-1, factor=1.0):
+        return lib().orc_expec_momentum(self.h, _dp(self._x(psi)), dim, factor)
+
+    def expec_kinetic(self, psi):
+        return lib().orc_expec_kinetic(self.h, _dp(self._x(psi)))
+
+    def expec_grid(self, psi, grid):
+        return lib().orc_expec_grid(self.h, _dp(self._x(psi)), grid)
+
+    def expec_projection(self, psi, funcs):
+        f = np.ascontiguousarray(np.stack([self._x(v) for v in funcs]))
+        return lib().orc_expec_projection(self.h, _dp(self._x(psi)), _dp(f), len(funcs))
 
 
 class Propagator:

@@ -362,6 +362,7 @@ static cd term_emax(const System &s, const qdg_hterm &t) {
     return T;
   }
   if (t.kind == QDG_TERM_POTENTIAL) return vec_max(s.grids[t.grid]);
+  if (t.kind == QDG_TERM_GOBBLER) return t.mass[0];  /* OGobbler::Emax = gain (OGobbler.cpp:161-164) */
   if (t.kind == QDG_TERM_NAC) {  /* OGridNAC::Emax (OGridNAC.cpp:105-115): dx of dim 0 */
     double m = 0;
     for (int d = 0; d < s.g.ndims; ++d) m += vec_max(s.grids[t.grid + d]);
@@ -373,6 +374,8 @@ static cd term_emax(const System &s, const qdg_hterm &t) {
  * returns 0; that is kept. */
 static cd term_emin(const System &s, const qdg_hterm &t) {
   if (t.kind == QDG_TERM_POTENTIAL) return vec_min(s.grids[t.grid]);
+  /* OGobbler::Emin (OGobbler.cpp:166-170): -i gain as negative imaginary potential */
+  if (t.kind == QDG_TERM_GOBBLER) return t.laser == 1 ? cd(0, -t.mass[0]) : cd(0);
   return 0.0;
 }
 
@@ -474,6 +477,12 @@ static void h_apply(const System &s, const cd *in, cd *out, long step) {
             const double *v = s.grids[t.grid].data();
             #pragma omp parallel for schedule(static) if (N >= 8192)
             for (long p = 0; p < N; ++p) o[p] += x[p] * v[p];
+          } else if (t.kind == QDG_TERM_GOBBLER) {
+            /* OGobbler::Apply (OGobbler.cpp:187-206): psi * W, or psi * (-i W) as NIP */
+            const double *v = s.grids[t.grid].data();
+            const cd f = t.laser == 1 ? cd(0, -1) : cd(1, 0);
+            #pragma omp parallel for schedule(static) if (N >= 8192)
+            for (long p = 0; p < N; ++p) o[p] += x[p] * (f * v[p]);
           } else {
             const double *v = s.grids[t.grid].data();
             double e = (-1) * laser_at(s, t.laser, step);
@@ -939,6 +948,122 @@ int orc_erange(void *sp, double *emax, double *emin) {
 int orc_h_apply(void *sp, const double *in, double *out, long step) {
   h_apply(*static_cast<System *>(sp), reinterpret_cast<const cd *>(in), reinterpret_cast<cd *>(out), step);
   return 0;
+}
+
+/* ---- expectation filters (FiltersList.cpp:289-308), renormalised by
+ * <psi|psi> as ProgPropa sets them (ProgPropa.cpp:260,276), computed as the
+ * reference applies the operators: N-dimensional FFT, multiplier / N,
+ * inverse FFT, scalar product. */
+static double raw_dot_re(long n, const cd *a, const cd *b) {
+  CSum r;
+  for (long j = 0; j < n; ++j) r.add((std::conj(a[j]) * b[j]).real());
+  return r.get();
+}
+
+/* <psi| O |psi> / <psi|psi> for O = IFFT tab_s FFT / N on state s (tabs: one
+ * table for all states, or one per state) */
+static double expec_kspace(const System &s, const cd *psi, const std::vector<std::vector<double>> &tabs) {
+  long N = s.npts;
+  std::vector<cd> b(N);
+  double num = 0, den = 0;
+  for (int st = 0; st < s.S; ++st) {
+    const cd *x = psi + st * N;
+    const std::vector<double> &tab = tabs.size() == 1 ? tabs[0] : tabs[st];
+    for (long p = 0; p < N; ++p) b[p] = x[p];
+    s.fft.exec(b.data(), -1);
+    for (long p = 0; p < N; ++p) b[p] *= tab[p] / double(N);
+    s.fft.exec(b.data(), +1);
+    num += raw_dot_re(N, x, b.data());
+    den += raw_dot_re(N, x, x);
+  }
+  return num / den;
+}
+
+/* OGridPosition::_InitDim (OGridPosition.cpp:41-53): (xmin + dx n) scale, summed over dims for dim < 0 */
+double orc_expec_position(void *sp, const double *psi_, int dim, double scale) {
+  const System &s = *static_cast<System *>(sp);
+  const cd *psi = reinterpret_cast<const cd *>(psi_);
+  CSum num, den;
+  for (int st = 0; st < s.S; ++st)
+    for (long p = 0; p < s.npts; ++p) {
+      double x = 0;
+      long stride = 1;
+      for (int d = 0; d < s.g.ndims; ++d) {
+        if (dim < 0 || d == dim) x += (s.g.xmin[d] + s.dx[d] * double((p / stride) % s.g.n[d])) * scale;
+        stride *= s.g.n[d];
+      }
+      const double m = std::norm(psi[st * s.npts + p]);
+      num.add(x * m);
+      den.add(m);
+    }
+  return num.get() / den.get();
+}
+
+/* GridMomentum: OGridNabla(momentum) with Kspace::Init1Dddx (Kspace.cpp:60-96) summed over dims for dim < 0 */
+double orc_expec_momentum(void *sp, const double *psi_, int dim, double factor) {
+  const System &s = *static_cast<System *>(sp);
+  std::vector<double> tab(s.npts, 0.0);
+  long stride = 1;
+  for (int d = 0; d < s.g.ndims; ++d) {
+    const int Nx = s.g.n[d];
+    const double dp = 2 * M_PI / (s.g.xmax[d] - s.g.xmin[d] + s.dx[d]);
+    std::vector<double> k1(Nx);
+    if (Nx % 2 == 0) {
+      for (int i = 0; i < Nx / 2; ++i) { k1[i] = double(i) * dp; k1[Nx - i - 1] = -1 * double(i + 1) * dp; }
+    } else {
+      k1[0] = 0;
+      for (int i = 1; i < (Nx + 1) / 2; ++i) { k1[i] = double(i) * dp; k1[Nx - i] = -1 * double(i) * dp; }
+    }
+    if (dim < 0 || d == dim)
+      for (long p = 0; p < s.npts; ++p) tab[p] += factor * k1[(p / stride) % Nx];
+    stride *= Nx;
+  }
+  return expec_kspace(s, reinterpret_cast<const cd *>(psi_), {tab});
+}
+
+/* the kinetic terms (OGridNablaSq) of the system, each on its own state */
+double orc_expec_kinetic(void *sp, const double *psi_) {
+  const System &s = *static_cast<System *>(sp);
+  std::vector<std::vector<double>> tabs(s.S, std::vector<double>(s.npts, 0.0));
+  size_t kt = 0;
+  for (auto &t : s.terms)
+    if (t.kind == QDG_TERM_KINETIC) {
+      for (long p = 0; p < s.npts; ++p) tabs[t.row][p] += s.ktab[kt][p];
+      ++kt;
+    }
+  return expec_kspace(s, reinterpret_cast<const cd *>(psi_), tabs);
+}
+
+/* a real diagonal grid on every state (OGridPotential, OGobbler without nip) */
+double orc_expec_grid(void *sp, const double *psi_, int grid) {
+  const System &s = *static_cast<System *>(sp);
+  const cd *psi = reinterpret_cast<const cd *>(psi_);
+  const double *v = s.grids[grid].data();
+  CSum num, den;
+  for (int st = 0; st < s.S; ++st)
+    for (long p = 0; p < s.npts; ++p) {
+      const double m = std::norm(psi[st * s.npts + p]);
+      num.add(v[p] * m);
+      den.add(m);
+    }
+  return num.get() / den.get();
+}
+
+/* OProjection::MatrixElement (OProjection.cpp:133-149): sum_k |<phi_k|psi>|^2, scalar products with the volume element */
+double orc_expec_projection(void *sp, const double *psi_, const double *funcs, int nfun) {
+  const System &s = *static_cast<System *>(sp);
+  const cd *psi = reinterpret_cast<const cd *>(psi_);
+  const long n = s.npts * s.S;
+  double dv = 1;
+  for (int d = 0; d < s.g.ndims; ++d) dv *= s.dx[d];
+  double acc = 0;
+  for (int k = 0; k < nfun; ++k) {
+    const cd *f = reinterpret_cast<const cd *>(funcs) + k * n;
+    CSum re, im;
+    for (long j = 0; j < n; ++j) { const cd c = std::conj(f[j]) * psi[j]; re.add(c.real()); im.add(c.imag()); }
+    acc += std::norm(cd(re.get(), im.get()) * dv);
+  }
+  return acc / (raw_dot_re(n, psi, psi) * dv);
 }
 
 /* Reporter::Analyze (Reporter.cpp:99-141): norm^2, pops, <H>, <psi|psi0>. */

@@ -26,6 +26,7 @@ TERM_KINETIC = 1
 TERM_POTENTIAL = 2
 TERM_DIPOLE = 3
 TERM_NAC = 4
+TERM_GOBBLER = 5
 
 PREC_FP64 = 0
 PREC_MIXED = 1
@@ -122,6 +123,11 @@ SIGNATURES = [
     ("qdg_wf_copy", _i32, [_vp, _vp]),
     ("qdg_h_apply", _i32, [_vp, _vp, _vp, _i64]),
     ("qdg_observables_compute", _i32, [_vp, _vp, _vp, _i64, C.POINTER(Observables)]),
+    ("qdg_expec_position", _i32, [_vp, _vp, _i32, C.c_double, C.POINTER(C.c_double)]),
+    ("qdg_expec_momentum", _i32, [_vp, _vp, _i32, C.c_double, C.POINTER(C.c_double)]),
+    ("qdg_expec_kinetic", _i32, [_vp, _vp, C.POINTER(C.c_double)]),
+    ("qdg_expec_grid", _i32, [_vp, _vp, _i32, C.POINTER(C.c_double)]),
+    ("qdg_expec_projection", _i32, [_vp, _vp, C.POINTER(C.POINTER(C.c_double)), _i32, C.POINTER(C.c_double)]),
     ("qdg_prop_create", _i32, [_vp, C.c_char_p, C.c_char_p, C.c_double, _i32, _i32, C.POINTER(_vp)]),
     ("qdg_prop_destroy", _i32, [_vp]),
     ("qdg_prop_init", _i32, [_vp]),

@@ -22,7 +22,9 @@ SOURCES = ["qdg_kernels.cu", "qdg_persistent.cu", "qdg_api.cu", "qdg_noalloc.cu"
            "qdg_step_f64_1.cu", "qdg_step_f64_2.cu", "qdg_step_f64_34.cu", "qdg_step_df_2.cu",
            "qdg_step_df_34.cu", "qdg_step_f32_1.cu", "qdg_step_f32_2.cu", "qdg_step_f32_34.cu",
            # one 1-D line on a thread-block cluster
-           "qdg_step_cluster.cu", "qdg_step_line64.cu"]
+           "qdg_step_cluster.cu", "qdg_step_line64.cu",
+           # expectation values of filter operators
+           "qdg_filters.cu"]
 
 
 def nvcc():

@@ -242,6 +242,7 @@ cd term_emax(const qdg_plan *p, const qdg_hterm &t) {
     for (int d = 0; d < p->nd; ++d) m += *std::max_element(g + d * n, g + (d + 1) * n);
     return m * M_PI / t.mass[0] / p->dx[0];
   }
+  if (t.kind == QDG_TERM_GOBBLER) return t.mass[0];  // OGobbler::Emax = gain (OGobbler.cpp:161-164)
   double gm = *std::max_element(g, g + n);
   if (t.kind == QDG_TERM_POTENTIAL) return gm;
   const double *l = p->lasers_h.data() + (long long)t.laser * p->laser_nt;
@@ -250,6 +251,8 @@ cd term_emax(const qdg_plan *p, const qdg_hterm &t) {
 // OGridNAC::Emin (OGridNAC.cpp:118-128) computes minima but never adds them:
 // it returns 0, and so does this.
 cd term_emin(const qdg_plan *p, const qdg_hterm &t) {
+  // OGobbler::Emin (OGobbler.cpp:166-170): -i gain as a negative imaginary potential, else 0
+  if (t.kind == QDG_TERM_GOBBLER) return t.laser == 1 ? cd(0.0, -t.mass[0]) : cd(0.0);
   if (t.kind != QDG_TERM_POTENTIAL) return 0.0;
   const double *g = p->grids_h.data() + (long long)t.grid * p->npts;
   return *std::min_element(g, g + p->npts);
@@ -647,13 +650,14 @@ void release_child(qdg_plan *p) {
 // Couplings of the terms selected by `pick` (kinetic terms excluded).
 template <typename F>
 qdg_status build_couplings(const qdg_plan *p, F pick, qdg::Couplings &cp) {
-  struct E { int row, col, gid, lid; };
+  struct E { int row, col, gid, lid, nim; };
   std::vector<E> es;
   for (auto &t : p->terms) {
     if (t.kind == QDG_TERM_KINETIC || t.kind == QDG_TERM_NAC || !pick(t)) continue;
     const int nrep = (p->hermitian && t.row != t.col) ? 2 : 1;
+    const int nim = t.kind == QDG_TERM_GOBBLER && t.laser == 1 ? 1 : 0;  // -i W (negative imaginary potential)
     for (int r = 0; r < nrep; ++r)
-      es.push_back({r ? t.col : t.row, r ? t.row : t.col, t.grid, t.kind == QDG_TERM_DIPOLE ? t.laser : -1});
+      es.push_back({r ? t.col : t.row, r ? t.row : t.col, t.grid, t.kind == QDG_TERM_DIPOLE ? t.laser : -1, nim});
   }
   if ((int)es.size() > qdg::kMaxCouplings) return fail(QDG_EUNSUPPORTED, "too many potential/dipole matrix entries");
   std::stable_sort(es.begin(), es.end(), [](const E &a, const E &b) { return a.row < b.row; });
@@ -661,6 +665,8 @@ qdg_status build_couplings(const qdg_plan *p, F pick, qdg::Couplings &cp) {
   cp.ne = (int)es.size();
   for (int e = 0; e < cp.ne; ++e) {
     cp.row[e] = es[e].row; cp.col[e] = es[e].col; cp.gid[e] = es[e].gid; cp.lid[e] = es[e].lid;
+    cp.nim[e] = es[e].nim;
+    if (es[e].nim) cp.any_nim = 1;
   }
   for (int s = 0, e = 0; s <= qdg::kMaxStates; ++s) {
     while (e < cp.ne && cp.row[e] < s) ++e;
@@ -931,6 +937,7 @@ qdg_status upload_bulk(const qdg_plan *p, const std::vector<long double> &v, voi
 qdg_status scaled_setup(qdg_prop *P) {
   qdg_plan *p = P->plan;
   if (P->step_grid <= 0) return QDG_OK;
+  if (p->cp_h.any_nim) return QDG_OK;  // negative imaginary potentials: the unscaled point work
   const cd fac = 2.0 * (P->c0 / P->dt) / P->scaling;
   if (P->offset.imag() != 0 || (fac.real() != 0 && fac.imag() != 0)) return QDG_OK;
   const bool rt = fac.real() == 0;
@@ -1406,7 +1413,8 @@ qdg_status gspo_init(qdg_prop *P) {
   if (ng < 1) return fail(QDG_EINVAL, "GSPO is empty!");
   if (ng > QDG_MAX_GROUPS) return fail(QDG_EINVAL, "too many GSPO members");
   for (auto &t : p->terms)  // OGSPO::Init takes ODSpace members only (OGSPO.cpp:71-85); OGridNAC is none
-    if (t.kind == QDG_TERM_NAC) return fail(QDG_EUNSUPPORTED, "GridNAC has no diagonal representation for GSPO");
+    if (t.kind == QDG_TERM_NAC || t.kind == QDG_TERM_GOBBLER)
+      return fail(QDG_EUNSUPPORTED, "GSPO members must be ODSpace operators (no GridNAC, no Gobbler)");
   if (!p->hermitian) return fail(QDG_EUNSUPPORTED, "GSPO members must be hermitian matrices");
   P->ngroups = ng;
   P->group_kinetic.assign(ng, 0);
@@ -2038,8 +2046,9 @@ qdg_status qdg_plan_create(const qdg_hplan_desc *desc, int32_t precision, qdg_pl
     } else if (t.kind == QDG_TERM_NAC) {
       if (t.grid < 0 || t.grid + p->nd > p->ngrids || !desc->grid_data) { free_plan(p); return fail(QDG_EINVAL, "NACME grid index out of range"); }
       if (!(t.mass[0] > 0)) { free_plan(p); return fail(QDG_EINVAL, "Zero mass defined"); }
-    } else if (t.kind == QDG_TERM_POTENTIAL || t.kind == QDG_TERM_DIPOLE) {
+    } else if (t.kind == QDG_TERM_POTENTIAL || t.kind == QDG_TERM_DIPOLE || t.kind == QDG_TERM_GOBBLER) {
       if (t.grid < 0 || t.grid >= p->ngrids || !desc->grid_data) { free_plan(p); return fail(QDG_EINVAL, "potential grid index out of range"); }
+      if (t.kind == QDG_TERM_GOBBLER && t.row != t.col) { free_plan(p); return fail(QDG_EUNSUPPORTED, "Gobbler off the diagonal"); }
       if (t.kind == QDG_TERM_DIPOLE && (t.laser < 0 || t.laser >= p->nlasers || p->laser_nt < 1 || !desc->laser_data)) {
         free_plan(p); return fail(QDG_EINVAL, "dipole operator without a laser field");
       }
@@ -2187,6 +2196,191 @@ qdg_status qdg_h_apply(qdg_plan *plan, const qdg_wf *in, qdg_wf *out, int64_t st
   }
   if (s != QDG_OK) return s;
   CK(cudaStreamSynchronize(plan->stream));
+  return QDG_OK;
+}
+
+// ---- expectation filters (FiltersList expec / expeconly) -----------------
+namespace {
+struct DevBuf {
+  void *p = nullptr;
+  ~DevBuf() { if (p) cudaFree(p); }
+};
+
+int expec_grid(const qdg_plan *p) {
+  const long long items = (p->npts * p->S + 255) / 256;
+  return (int)std::max<long long>(1, std::min<long long>(items, 4LL * p->sm_count));
+}
+
+// sum w |psi|^2 and sum |psi|^2 (weights: a binary64 device grid, or the coordinate)
+qdg_status expec_point(qdg_plan *p, const qdg_wf *psi, const double *grid, int dim, double scale, double &ws,
+                       double &ns) {
+  const int G = expec_grid(p);
+  DevBuf part;
+  CK(cudaMalloc(&part.p, sizeof(double) * 2 * G));
+  qdg::PointExpecArgs a;
+  memset(&a, 0, sizeof(a));
+  a.psi = psi->d;
+  a.npts = p->npts;
+  a.S = p->S;
+  a.grid = grid;
+  a.nd = p->nd;
+  a.dim = dim;
+  a.scale = scale;
+  for (int d = 0; d < p->nd; ++d) {
+    a.stride[d] = p->dim[d].stride;
+    a.n[d] = p->dim[d].n;
+    a.xmin[d] = p->grid.xmin[d];
+    a.dx[d] = p->dx[d];
+  }
+  a.partials = static_cast<double *>(part.p);
+  CK(qdg::launch_point_expec(a, G, p->stream));
+  std::vector<double> h(2 * G);
+  CK(cudaMemcpyAsync(h.data(), part.p, sizeof(double) * 2 * G, cudaMemcpyDeviceToHost, p->stream));
+  CK(cudaStreamSynchronize(p->stream));
+  ws = 0;
+  ns = 0;
+  for (int b = 0; b < G; ++b) { ws += h[2 * b]; ns += h[2 * b + 1]; }
+  return QDG_OK;
+}
+
+// sum over the lines of dimension d of sum_k w[s][k] |FFT_d psi (k)|^2
+qdg_status expec_spectral(qdg_plan *p, const qdg_wf *psi, int d, const std::vector<double> &w, double &out) {
+  const int N = p->dim[d].n;
+  if (qdg::spectral_expec_smem(N) > 227 * 1024) return fail(QDG_EUNSUPPORTED, "line too long for the filter transform");
+  std::vector<cplx<double>> tw(N);
+  const long double pi = 3.141592653589793238462643383279502884L;
+  for (int m = 0; m < N; ++m) {
+    const long double ang = -2.0L * pi * (long double)m / (long double)N;
+    tw[m] = cplx<double>{(double)cosl(ang), (double)sinl(ang)};
+  }
+  const long long lines = (p->npts / N) * p->S;
+  const int G = (int)std::max<long long>(1, std::min<long long>(lines, 4LL * p->sm_count));
+  DevBuf dtw, dw, part;
+  CK(cudaMalloc(&dtw.p, sizeof(cplx<double>) * N));
+  CK(cudaMalloc(&dw.p, sizeof(double) * w.size()));
+  CK(cudaMalloc(&part.p, sizeof(double) * G));
+  CK(cudaMemcpyAsync(dtw.p, tw.data(), sizeof(cplx<double>) * N, cudaMemcpyHostToDevice, p->stream));
+  CK(cudaMemcpyAsync(dw.p, w.data(), sizeof(double) * w.size(), cudaMemcpyHostToDevice, p->stream));
+  qdg::SpecExpecArgs a;
+  memset(&a, 0, sizeof(a));
+  a.psi = psi->d;
+  a.npts = p->npts;
+  a.S = p->S;
+  a.N = N;
+  a.es = p->dim[d].stride;
+  a.rp = p->dim[d].rp;
+  a.tw = static_cast<const cplx<double> *>(dtw.p);
+  a.w = static_cast<const double *>(dw.p);
+  a.partials = static_cast<double *>(part.p);
+  CK(qdg::launch_spectral_expec(a, G, p->stream));
+  std::vector<double> h(G);
+  CK(cudaMemcpyAsync(h.data(), part.p, sizeof(double) * G, cudaMemcpyDeviceToHost, p->stream));
+  CK(cudaStreamSynchronize(p->stream));
+  out = 0;
+  for (int b = 0; b < G; ++b) out += h[b];
+  return QDG_OK;
+}
+
+qdg_status expec_check(const qdg_plan *plan, const qdg_wf *psi, const double *out) {
+  if (!plan || !psi || !out || psi->plan != plan) return fail(QDG_EINVAL, "bad arguments");
+  return QDG_OK;
+}
+}  // namespace
+
+qdg_status qdg_expec_position(qdg_plan *plan, const qdg_wf *psi, int32_t dim, double scale, double *out) {
+  qdg_status s = expec_check(plan, psi, out);
+  if (s != QDG_OK) return s;
+  if (dim >= plan->nd) return fail(QDG_EINVAL, "Dimension for position operator exceeds dimensions of Wavefunction");
+  double ws, ns;
+  if ((s = expec_point(plan, psi, nullptr, dim, scale, ws, ns)) != QDG_OK) return s;
+  *out = ws / ns;
+  return QDG_OK;
+}
+
+qdg_status qdg_expec_momentum(qdg_plan *plan, const qdg_wf *psi, int32_t dim, double factor, double *out) {
+  qdg_status s = expec_check(plan, psi, out);
+  if (s != QDG_OK) return s;
+  if (dim >= plan->nd) return fail(QDG_EINVAL, "Dimension for momentum operator exceeds dimensions of Wavefunction");
+  double ws, ns, num = 0;
+  if ((s = expec_point(plan, psi, nullptr, 0, 1.0, ws, ns)) != QDG_OK) return s;
+  for (int d = 0; d < plan->nd; ++d) {
+    if (dim >= 0 && d != dim) continue;
+    // Kspace::Init1Dddx (Kspace.cpp:60-96): k_j = j dk below the middle,
+    // (j - N) dk above it, both parities; OGridNabla divides by N
+    const int N = plan->dim[d].n;
+    std::vector<double> w((size_t)plan->S * N);
+    for (int st = 0; st < plan->S; ++st)
+      for (int j = 0; j < N; ++j) {
+        const double k = (j < (N + 1) / 2 ? (double)j : (double)(j - N)) * plan->dk[d];
+        w[(size_t)st * N + j] = factor * k / (double)N;
+      }
+    double v;
+    if ((s = expec_spectral(plan, psi, d, w, v)) != QDG_OK) return s;
+    num += v;
+  }
+  *out = num / ns;
+  return QDG_OK;
+}
+
+qdg_status qdg_expec_kinetic(qdg_plan *plan, const qdg_wf *psi, double *out) {
+  qdg_status s = expec_check(plan, psi, out);
+  if (s != QDG_OK) return s;
+  double ws, ns, num = 0;
+  if ((s = expec_point(plan, psi, nullptr, 0, 1.0, ws, ns)) != QDG_OK) return s;
+  for (int d = 0; d < plan->nd; ++d) {
+    // OGridNablaSq: k^2 / (2 m_d) of every kinetic term on the state, 1/N of the transform pair
+    const int N = plan->dim[d].n;
+    std::vector<double> kf(plan->S, 0.0);
+    bool any = false;
+    for (auto &t : plan->terms)
+      if (t.kind == QDG_TERM_KINETIC) { kf[t.row] += plan->dk[d] * plan->dk[d] / (2.0 * t.mass[d]) / N; any = true; }
+    if (!any) continue;
+    std::vector<double> w((size_t)plan->S * N);
+    for (int st = 0; st < plan->S; ++st)
+      for (int j = 0; j < N; ++j) {
+        const double kq = std::min(j, N - j);
+        w[(size_t)st * N + j] = kf[st] * kq * kq;
+      }
+    double v;
+    if ((s = expec_spectral(plan, psi, d, w, v)) != QDG_OK) return s;
+    num += v;
+  }
+  *out = num / ns;
+  return QDG_OK;
+}
+
+qdg_status qdg_expec_grid(qdg_plan *plan, const qdg_wf *psi, int32_t grid, double *out) {
+  qdg_status s = expec_check(plan, psi, out);
+  if (s != QDG_OK) return s;
+  if (grid < 0 || grid >= plan->ngrids) return fail(QDG_EINVAL, "grid index out of range");
+  DevBuf g;
+  CK(cudaMalloc(&g.p, sizeof(double) * plan->npts));
+  CK(cudaMemcpyAsync(g.p, plan->grids_h.data() + (size_t)grid * plan->npts, sizeof(double) * plan->npts,
+                     cudaMemcpyHostToDevice, plan->stream));
+  double ws, ns;
+  if ((s = expec_point(plan, psi, static_cast<const double *>(g.p), 0, 1.0, ws, ns)) != QDG_OK) return s;
+  *out = ws / ns;
+  return QDG_OK;
+}
+
+qdg_status qdg_expec_projection(qdg_plan *plan, const qdg_wf *psi, const double *const *funcs, int32_t nfun,
+                                double *out) {
+  qdg_status s = expec_check(plan, psi, out);
+  if (s != QDG_OK) return s;
+  if (nfun < 0 || (nfun > 0 && !funcs)) return fail(QDG_EINVAL, "bad projection functions");
+  const size_t n = (size_t)plan->npts * plan->S;
+  DevBuf f;
+  CK(cudaMalloc(&f.p, sizeof(cplx<double>) * n));
+  std::vector<cd> d;
+  double acc = 0;
+  for (int k = 0; k < nfun; ++k) {
+    if (!funcs[k]) return fail(QDG_EINVAL, "null projection function");
+    CK(cudaMemcpyAsync(f.p, funcs[k], sizeof(cplx<double>) * n, cudaMemcpyHostToDevice, plan->stream));
+    if ((s = dots<double, double>(plan, static_cast<const cplx<double> *>(f.p), psi->d, d)) != QDG_OK) return s;
+    acc += std::norm(total(d));
+  }
+  if ((s = dots<double, double>(plan, psi->d, psi->d, d)) != QDG_OK) return s;
+  *out = acc / total(d).real();
   return QDG_OK;
 }
 

@@ -100,6 +100,11 @@ template <typename T> __device__ __forceinline__ cplx<T> cmul(cplx<T> a, cplx<T>
 }
 template <typename T> __device__ __forceinline__ cplx<T> cmulr(cplx<T> a, T r) { return mk(a.re * r, a.im * r); }
 template <typename T> __device__ __forceinline__ T cabs2(cplx<T> a) { return a.re * a.re + a.im * a.im; }
+// The operand of a potential-matrix entry: x, or -i x for an entry that acts
+// as a negative imaginary potential (selects and a sign flip, no arithmetic).
+template <typename T> __device__ __forceinline__ cplx<T> nim_operand(cplx<T> x, int nim) {
+  return nim ? mk(x.im, -x.re) : x;
+}
 template <typename T, typename U> __device__ __forceinline__ cplx<T> ccast(cplx<U> a) { return mk((T)a.re, (T)a.im); }
 
 template <typename T> __device__ __forceinline__ cplx<T> ldg(const cplx<T> *p) {

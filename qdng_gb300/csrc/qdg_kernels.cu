@@ -183,12 +183,13 @@ __global__ void __launch_bounds__(256) linepass_kernel(PassArgs<T> a) {
         for (int e = 0; e < ne; ++e) {
           const int r = a.cp->row[e], c = a.cp->col[e];
           const T v = (T)(a.coef[e]) * a.grids[(long long)a.cp->gid[e] * npts + p];
+          const int nim = a.cp->nim[e];
 #pragma unroll
           for (int s = 0; s < ((SS > 0) ? SS : kMaxStates); ++s)
             if (s == r) {
 #pragma unroll
               for (int q = 0; q < ((SS > 0) ? SS : kMaxStates); ++q)
-                if (q == c) h[s] = h[s] + cmulr(ph[q], v);
+                if (q == c) h[s] = h[s] + cmulr(nim_operand(ph[q], nim), v);
             }
         }
 #pragma unroll
@@ -398,12 +399,13 @@ __global__ void __launch_bounds__(256) combine_kernel(CombArgs<T> a) {
     for (int e = 0; e < ne; ++e) {
       const int r = a.cp->row[e], c = a.cp->col[e];
       const T v = (T)(a.coef[e]) * a.grids[(long long)a.cp->gid[e] * npts + p];
+      const int nim = a.cp->nim[e];
 #pragma unroll
       for (int s = 0; s < SM; ++s)
         if (s == r) {
 #pragma unroll
           for (int q = 0; q < SM; ++q)
-            if (q == c) h[s] = h[s] + cmulr(ph[q], v);
+            if (q == c) h[s] = h[s] + cmulr(nim_operand(ph[q], nim), v);
         }
     }
 #pragma unroll

@@ -33,6 +33,8 @@ struct Couplings {
   int col[kMaxCouplings];
   int gid[kMaxCouplings];
   int lid[kMaxCouplings];  // -1: static potential
+  int nim[kMaxCouplings];  // 1: the entry acts as -i coef grid (OGobbler as a negative imaginary potential)
+  int any_nim;
   // entries sorted by row: entries of row s are [rs[s], rs[s+1]) (the list above is in this order)
   int rs[kMaxStates + 1];
 };
@@ -281,6 +283,33 @@ template <typename T>
 cudaError_t launch_cheby_step_cluster(const ClusterStepArgs<T> &a, cudaStream_t st);
 template <typename T>
 size_t cluster_step_smem(int M);
+// Expectation values of filter operators (qdg_filters.cu).
+struct PointExpecArgs {
+  const cplx<double> *psi;
+  long long npts;
+  int S;
+  const double *grid;  // [npts] weights, or null: the coordinate
+  int nd, dim;         // coordinate of dimension dim (dim < 0: the sum over all)
+  long long stride[4];
+  int n[4];
+  double xmin[4], dx[4], scale;
+  double *partials;  // [2 gridDim]: weighted sum, plain sum
+};
+struct SpecExpecArgs {
+  const cplx<double> *psi;
+  long long npts;
+  int S;
+  int N;
+  long long es;  // element stride of the dimension's lines
+  RadixPlan rp;
+  const cplx<double> *tw;  // [N] exp(-2 pi i m / N)
+  const double *w;         // [S][N] multiplier per k index (with the 1/N)
+  double *partials;        // [gridDim]
+};
+cudaError_t launch_point_expec(const PointExpecArgs &a, int grid, cudaStream_t st);
+cudaError_t launch_spectral_expec(const SpecExpecArgs &a, int grid, cudaStream_t st);
+size_t spectral_expec_smem(int N);
+
 // One binary64 line of N points on a cluster of 16 or 8 blocks, one real
 // component per thread (qdg_step_line64.cu).  line64_cluster_size returns
 // the cluster size the device schedules for N, or 0.

@@ -100,6 +100,7 @@ struct RowCache {
   int col[kMaxStates][kMaxRowEntries];
   int gid[kMaxStates][kMaxRowEntries];
   B coef[kMaxStates][kMaxRowEntries];
+  int nim[kMaxStates][kMaxRowEntries];  // entry acts as -i coef grid (negative imaginary potential)
   int unit[kMaxStates];  // only static potentials (coefficient 1) in the row
 };
 template <typename T, typename B>
@@ -114,6 +115,7 @@ __device__ void fill_rows(const StepArgs<T> &a, RowCache<B> &rc) {
     for (int k = 0; k < kMaxRowEntries; ++k) {
       rc.col[s][k] = k < ne ? cpx->col[e0 + k] : 0;
       rc.gid[s][k] = k < ne ? cpx->gid[e0 + k] : 0;
+      rc.nim[s][k] = (k < ne && !scaled) ? cpx->nim[e0 + k] : 0;
       // the field coefficient of the entry (scaled entries name the plan entry, -1: static)
       const int ci = k >= ne ? -1 : scaled ? cpx->lid[e0 + k] : e0 + k;
       const double c = ci >= 0 ? a.coef[ci] : (k < ne ? 1.0 : 0.0);
@@ -219,13 +221,14 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
     const int istr = (int)stride;  // element stride of a line (< 2^31 points per dimension block)
     // potential-matrix entries of row s
     const int ne = rc.ne[s];
-    int ecol[RE], egid[RE];
+    int ecol[RE], egid[RE], enim[RE];
     B ecoef[RE];
 #pragma unroll
     for (int k = 0; k < RE; ++k) {
       ecol[k] = rc.col[s][k];
       egid[k] = rc.gid[s][k];
       ecoef[k] = rc.coef[s][k];
+      enim[k] = rc.nim[s][k];
     }
     const bool unit_coef = rc.unit[s] != 0;
     const long long so = (long long)s * npts;
@@ -257,6 +260,7 @@ __device__ void phase_fused(const StepArgs<T> &a, int kind, const cplx<T> *__res
 #pragma unroll
             for (int j = 1; j < SM; ++j)
               if (j == ecol[k]) x = pm[j];
+            x = nim_operand(x, enim[k]);
             const B vv = unit_coef ? vg[k] : ecoef[k] * vg[k];
             h.re = fma_b(x.re, vv, h.re);
             h.im = fma_b(x.im, vv, h.im);
@@ -446,12 +450,13 @@ __device__ __forceinline__ void point_term(const StepArgs<T> &a, long long p, co
     const int ci = scaled ? cpx->lid[e] : e;
     const T gv = grids[(long long)cpx->gid[e] * a.npts + p];
     const T v = ci >= 0 ? (T)(a.coef[ci]) * gv : gv;
+    const int nim = scaled ? 0 : cpx->nim[e];
 #pragma unroll
     for (int s = 0; s < SM; ++s)
       if (s == r) {
 #pragma unroll
         for (int q = 0; q < SM; ++q)
-          if (q == c) h[s] = h[s] + cmulr(ph[q], v);
+          if (q == c) h[s] = h[s] + cmulr(nim_operand(ph[q], nim), v);
       }
   }
   const cplx<T> off = ccast<T>(a.offset);

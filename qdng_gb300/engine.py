@@ -83,6 +83,34 @@ class Plan:
         return dict(norm2=o.norm2, pops=np.array(o.pops[:self.S]), energy=o.energy,
                     autocorr=complex(o.autocorr_re, o.autocorr_im))
 
+    # expectation filters (FiltersList expec/expeconly), each Re <psi|O|psi> / <psi|psi>
+    def expec_position(self, psi, dim=-1, scale=1.0):
+        v = C.c_double()
+        check(self.lib.qdg_expec_position(self.h, psi.h, dim, scale, C.byref(v)))
+        return v.value
+
+    def expec_momentum(self, psi, dim=-1, factor=1.0):
+        v = C.c_double()
+        check(self.lib.qdg_expec_momentum(self.h, psi.h, dim, factor, C.byref(v)))
+        return v.value
+
+    def expec_kinetic(self, psi):
+        v = C.c_double()
+        check(self.lib.qdg_expec_kinetic(self.h, psi.h, C.byref(v)))
+        return v.value
+
+    def expec_grid(self, psi, grid):
+        v = C.c_double()
+        check(self.lib.qdg_expec_grid(self.h, psi.h, grid, C.byref(v)))
+        return v.value
+
+    def expec_projection(self, psi, funcs):
+        fs = [np.ascontiguousarray(f, dtype=np.complex128).reshape(-1) for f in funcs]
+        ptrs = (C.POINTER(C.c_double) * max(1, len(fs)))(*[_dp(f) for f in fs])
+        v = C.c_double()
+        check(self.lib.qdg_expec_projection(self.h, psi.h, ptrs, len(fs), C.byref(v)))
+        return v.value
+
 
 class WaveFunction:
     def __init__(self, plan):

@@ -161,6 +161,78 @@ class GridDipole(Operator):
         return [t]
 
 
+def _bw_lowpass(n, center, order):
+    """FunctionGenerator::BwLowpass (src/math/math_functions.h:60-70): 1 / (1 + (i / center)^(2 order))."""
+    i = np.arange(n, dtype=np.float64)
+    with np.errstate(divide="ignore", over="ignore"):
+        return 1.0 / (1.0 + np.power(i / center, 2.0 * order))
+
+
+def _bw_highpass(n, center, order):
+    """FunctionGenerator::BwHighpass (src/math/math_functions.h:40-50): 1 / (1 + (center / i)^(2 order))."""
+    i = np.arange(n, dtype=np.float64)
+    with np.errstate(divide="ignore", over="ignore"):
+        return 1.0 / (1.0 + np.power(center / i, 2.0 * order))
+
+
+class Gobbler(Operator):
+    """OGobbler (src/qdlib/OGobbler.cpp): Butterworth filter functions along
+    the dimensions.  ``lp`` / ``rp`` map a dimension to the cut-off x of a
+    left pass (keeps smaller x) / right pass (keeps larger x); ``order`` the
+    filter order (default 20); ``gain`` a factor.  With ``nip`` the filter is
+    a negative imaginary potential, H psi += -i W psi, else H psi += W psi.
+    Emax = gain, Emin = -i gain (nip) or 0 (OGobbler.cpp:161-170)."""
+
+    def __init__(self, dims=None, lp=None, rp=None, order=20, gain=1.0, nip=False):
+        if order < 1:
+            raise EParamProblem("Filter order to small")
+        self.dims = dims
+        self.lp = dict(lp or {})
+        self.rp = dict(rp or {})
+        self.order = int(order)
+        self.gain = float(gain)
+        self.nip = bool(nip)
+        self.W = None
+
+    def filter(self, grid):
+        """OGobbler::_Init (OGobbler.cpp:30-84) on the grid (dim 0 fastest)."""
+        if self.dims is not None and self.dims != grid.ndims:
+            raise EIncompatible("OGobbler: Number of dims doesn't match WF")
+        shape = tuple(reversed(grid.n))
+        f = np.zeros(shape) if self.nip else np.ones(shape)
+        dx = grid.dx
+        for d in range(grid.ndims):
+            bshape = [1] * grid.ndims
+            bshape[grid.ndims - 1 - d] = grid.n[d]
+            for side, table in (("lp", self.lp), ("rp", self.rp)):
+                if d not in table:
+                    continue
+                x = (table[d] - grid.xmin[d]) / dx[d]
+                if int(x) > grid.n[d] or int(x) < 0:
+                    raise EParamProblem("Center of filter edge out of the grid")
+                if side == "lp":
+                    f = f * _bw_lowpass(grid.n[d], x, self.order).reshape(bshape)
+                elif self.nip:
+                    f = f + _bw_highpass(grid.n[d], x, self.order).reshape(bshape)
+                else:
+                    f = f * _bw_highpass(grid.n[d], x, self.order).reshape(bshape)
+        if self.gain != 1:
+            f = f * self.gain
+        return np.ascontiguousarray(f).reshape(-1)
+
+    def terms(self, row, col, group, ctx):
+        if row != col:
+            raise EIncompatible("Gobbler off the diagonal")
+        if self.W is None or self.W.size != ctx.grid.npts:
+            self.W = self.filter(ctx.grid)
+        t = abi.HTerm()
+        t.kind, t.row, t.col, t.group = abi.TERM_GOBBLER, row, col, group
+        t.grid = ctx.add_grid(self.W)
+        t.laser = 1 if self.nip else 0
+        t.mass[0] = self.gain
+        return [t]
+
+
 class GridNAC(Operator):
     """Non-adiabatic first-derivative coupling (OGridNAC::Apply,
     src/qdlib/OGridNAC.cpp:131-148):
@@ -298,6 +370,7 @@ class HPlan:
             self.laser_data = np.zeros(1)
             self.laser_nt = 0
         self.ngrids = len(ctx.grids)
+        self._grids = list(ctx.grids)
         self.nlasers = len(ctx.lasers)
         self._terms_c = (abi.HTerm * max(1, len(terms)))(*terms)
         d = abi.HPlanDesc()
@@ -320,3 +393,12 @@ class HPlan:
     def size(self):
         """Complex values of one wave function (all states)."""
         return self.npts * self.nstates
+
+    def grid_of(self, op):
+        """Index in grid_data of a GridPotential's values or a Gobbler's filter
+        (the operator a filter's ref= names in QDng)."""
+        v = op.W if isinstance(op, Gobbler) else getattr(op, "values", None)
+        for i, g in enumerate(self._grids):
+            if g is v:
+                return i
+        raise EParamProblem("operator not part of this Hamiltonian")

@@ -26,6 +26,17 @@ def tgp_expec(fx):
     return hp, psi, dict(name="Cheby", params="prec=1e-12", dt=20.0, steps=1000)
 
 
+def tgp_nip(fx):
+    """tests/TGP-NIP-Cheby.qdi.in: Cheby, Sum(T, Gobbler nip rp0=5.5 order 5 gain 0.02,
+    Gobbler lp0=2 order 20 gain 0.3 (key V)), ef_0, dt=10, 1000 steps."""
+    g = mgh_grid(fx)
+    V = op.Gobbler(dims=1, lp={0: 2.0}, order=20, gain=0.3, nip=False)
+    hp = op.HPlan(g, op.Sum([op.GridNablaSq([1763.2]),
+                             op.Gobbler(dims=1, rp={0: 5.5}, order=5, gain=0.02, nip=True), V]))
+    psi = _normalize(hp, fx["GridPot0_ef_0"].astype(np.complex128))
+    return hp, psi, dict(name="Cheby", params="", dt=10.0, steps=1000, V=V)
+
+
 def tgpms(fx, gspo=False):
     """tests/TGPMS-Cheby.qdi.in / TGPMS-GSPO.qdi.in: two uncoupled states."""
     g = mgh_grid(fx)

@@ -107,6 +107,56 @@ def test_tgp_expec(fixtures, golden):
     _check(golden["propagation"]["TGP-Expec"], obs, 1)
 
 
+def _expec_row(S, hp, x, V, fixtures=None):
+    """The filterpost columns of the golden expec lines: GridMomentum,
+    GridPosition, [Projection on ef_0..3], T, V."""
+    row = [S.expec_momentum(x), S.expec_position(x)]
+    if fixtures is not None:
+        row.append(S.expec_projection(x, [fixtures[f"GridPot0_ef_{k}"] for k in range(4)]))
+    row += [S.expec_kinetic(x), S.expec_grid(x, hp.grid_of(V))]
+    return row
+
+
+def _check_expec(golden_line, row):
+    """Each value to the digits printed before the golden's [0-9]* wildcard."""
+    for got, (txt, want) in zip(row, zip(golden_line["text"].split()[1:], golden_line["values"][1:])):
+        mant = txt.split("[")[0].split("e")[0]
+        digits = len(mant.split(".")[1]) if "." in mant else 0
+        exp = int(txt.split("e")[1]) if "e" in txt else 0
+        tol = 10.0 ** (exp - digits)
+        assert abs(got - want) <= tol, (got, want, tol)
+
+
+def test_tgp_expec_filters(fixtures, golden):
+    """TGP-Expec's filterpost line after 1000 steps: <p>, <x>, the projection
+    on the four eigenfunctions, <T>, <V>, each renormalised by <psi|psi>."""
+    hp, psi, run = cases.tgp_expec(fixtures)
+    S = O.System(hp)
+    P = O.Propagator(S, run["name"], run["params"], dt=run["dt"])
+    x = psi.copy()
+    P.propagate(x, psi.copy(), run["steps"])
+    V = hp  # the potential is the Sum's GridPotential
+    row = [S.expec_momentum(x), S.expec_position(x),
+           S.expec_projection(x, [fixtures[f"GridPot0_ef_{k}"] for k in range(4)]),
+           S.expec_kinetic(x), S.expec_grid(x, 0)]
+    _check_expec(golden["expec"]["TGP-Expec"], row)
+
+
+def test_tgp_nip_cheby(fixtures, golden):
+    """TGP-NIP-Cheby: a negative imaginary potential (Gobbler nip) absorbs the
+    wave packet (norm 0.0959 after 999 steps); Reporter line and filterpost
+    line (<p>, <x>, <T>, <V> of the nip-free Gobbler) against QDng."""
+    hp, psi, run = cases.tgp_nip(fixtures)
+    S = O.System(hp)
+    emax, emin = S.erange()
+    assert emin.imag == -0.02 and emax.real > 0
+    P = O.Propagator(S, run["name"], run["params"], dt=run["dt"])
+    x = psi.copy()
+    obs, terms = P.propagate(x, psi.copy(), run["steps"])
+    _check(golden["propagation"]["TGP-NIP-Cheby"], obs[-1], 1)
+    _check_expec(golden["expec"]["TGP-NIP-Cheby"], _expec_row(S, hp, x, run["V"]))
+
+
 def test_tgpms_cheby(fixtures, golden):
     hp, psi, run = cases.tgpms(fixtures)
     obs, _ = _last_line(hp, psi, run)
