@@ -258,6 +258,22 @@ qdg_status qdg_eigen_imag(qdg_prop *prop, const double *psi_init, int32_t nef, i
                           double convergence, int32_t diag, double *efs, double *e_raw, double *e_diag,
                           int32_t *steps);
 
+/* ProgEigen::AutoCorrEF (src/ProgEigen.cpp:414-600) with a real-time
+ * propagator: psi_init (host, as given; the reference normalises it on
+ * input) is propagated for nsteps - 1 steps and every step is kept in device
+ * memory; a_s = <psi_s|psi_init> (a_0 = 1), Hann window when win != 0,
+ * forward FFT, peaks of |spectrum| by QDng's PeakFinder (mean + tol sigma
+ * over the spectrum, or over windows of +-width around local maxima when
+ * width > 0); for each peak at E = index dw (index - nsteps above the middle,
+ * dw = 2 pi / (dt nsteps)) the eigenfunction psi_0 + sum_s exp(i E s dt)
+ * psi_s, normalised, and its energy Re <psi|H|psi>.  nef_out = the number of
+ * peaks; the first max_nef are returned in energies, efs (max_nef x
+ * nstates*npoints complex128, may be NULL) and the spectrum (nsteps
+ * complex128, may be NULL). */
+qdg_status qdg_eigen_autocorr(qdg_prop *prop, const double *psi_init, int32_t nsteps, double tol, int32_t width,
+                              int32_t win, int32_t max_nef, double *energies, int32_t *nef_out, double *efs,
+                              double *spectrum);
+
 /* ---- batched ensemble of independent wavepackets ------------------------ */
 
 /* One member: a single-state Hamiltonian Sum(GridNablaSq, GridPotential,

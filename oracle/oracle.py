@@ -59,6 +59,8 @@ def lib():
         L.orc_erange.argtypes = [vp, dp, dp]
         L.orc_h_apply.argtypes = [vp, dp, dp, C.c_long]
         L.orc_observables.argtypes = [vp, dp, dp, C.c_long, dp]
+        L.orc_eigen_ac.argtypes = [vp, dp, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, dp,
+                                   C.POINTER(C.c_int), dp, dp]
         for f, args in (("orc_expec_position", [vp, dp, C.c_int, C.c_double]),
                         ("orc_expec_momentum", [vp, dp, C.c_int, C.c_double]),
                         ("orc_expec_kinetic", [vp, dp]),
@@ -203,6 +205,21 @@ class Propagator:
         if rc < 0:
             raise ValueError(lib().orc_last_error().decode())
         return obs, terms
+
+    def eigen_autocorr(self, psi_init, nsteps, tol=1.0, width=-1, win=True, max_nef=64):
+        """ProgEigen::AutoCorrEF: (energies, efs [k x size], spectrum, peaks found)."""
+        n = self.system.S * self.system.npts
+        x = np.ascontiguousarray(psi_init, dtype=np.complex128).reshape(-1)
+        e = np.zeros(max(max_nef, 1))
+        efs = np.zeros((max(max_nef, 1), n), dtype=np.complex128)
+        spec = np.zeros(nsteps, dtype=np.complex128)
+        nef = C.c_int(0)
+        rc = lib().orc_eigen_ac(self.h, _dp(x), nsteps, tol, width, int(win), max_nef, _dp(e), C.byref(nef),
+                                _dp(efs), _dp(spec))
+        if rc < 0:
+            raise ValueError(lib().orc_last_error().decode())
+        k = min(nef.value, max_nef)
+        return e[:k], efs[:k], spec, nef.value
 
     def eigen_imag(self, psi_init, nef, maxsteps, conv, diag=True):
         n = self.system.npts * self.system.S

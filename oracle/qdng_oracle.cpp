@@ -1162,6 +1162,100 @@ int orc_propagate(void *pp, double *psi, const double *psi0, long start, int nst
  * with imag=1, backward=1 (ProgEigen.cpp:692-693). efs receives nef
  * eigenfunctions, e_raw/e_diag the raw and diagonalised energies,
  * steps the relaxation steps per function. */
+/* ProgEigen::AutoCorrEF (ProgEigen.cpp:414-600) with its PeakFinder
+ * (src/tools/PeakFinder.cpp) and FunctionGenerator::Hann: propagation kept
+ * in memory, autocorrelation <psi_s|psi_0> (a_0 = 1), Hann window, forward
+ * FFT, peaks of |spectrum|, time integration at the peak energies,
+ * normalisation, <psi|H|psi>. */
+static void pf_mean_sigma(const std::vector<double> &d, size_t b, size_t e, double &mean, double &sigma) {
+  mean = 0;
+  for (size_t i = b; i < e; ++i) mean += d[i];
+  mean /= double(e - b);
+  sigma = 0;
+  for (size_t i = b; i < e; ++i) sigma += (d[i] - mean) * (d[i] - mean);
+  sigma = std::sqrt(1. / double(e - b) * sigma);
+}
+static std::vector<int> pf_find(const std::vector<double> &d, double tol, int width) {
+  std::vector<int> pk;
+  const size_t n = d.size();
+  if (width <= 0) {  /* PeakFinder::Find / _FindData */
+    double mean, sigma;
+    pf_mean_sigma(d, 0, n, mean, sigma);
+    bool start = false;
+    double dmax = 0;
+    int indmax = -1;
+    for (size_t i = 0; i < n; ++i) {
+      if (!start && d[i] > mean + tol * sigma) { start = true; dmax = 0; indmax = -1; }
+      if (start && d[i] < mean + tol * sigma) { start = false; pk.push_back(indmax); }
+      if (start && d[i] > dmax) { dmax = d[i]; indmax = int(i); }
+    }
+    if (start && indmax != -1 && d[n - 1] < dmax) pk.push_back(indmax);
+    return pk;
+  }
+  /* PeakFinder::Find(data, winsize) over PeakFinder::Maximas */
+  double delta = 0;
+  std::vector<size_t> maxima;
+  for (size_t i = 1; i < n; ++i) {
+    if (d[i] < d[i - 1] && delta > 0) maxima.push_back(i - 1);
+    delta = d[i] - d[i - 1];
+  }
+  for (size_t m : maxima) {
+    size_t lo = m < size_t(width) ? 0 : m - width;
+    size_t hi = m + width > n - 1 ? n - 1 : m + width;
+    double mean, sigma;
+    pf_mean_sigma(d, lo, hi, mean, sigma);
+    if (d[m] > mean + tol * sigma) pk.push_back(int(m));
+  }
+  return pk;
+}
+
+int orc_eigen_ac(void *pp, const double *psi_init, int nsteps, double tol, int width, int win, int max_nef,
+                 double *energies, int *nef_out, double *efs, double *spectrum) {
+  Prop &p = *static_cast<Prop *>(pp);
+  System &s = *p.sys;
+  const long n = s.npts * s.S;
+  const int M = nsteps;
+  std::vector<std::vector<cd>> buf(M, std::vector<cd>(n));
+  const cd *init = reinterpret_cast<const cd *>(psi_init);
+  std::copy(init, init + n, buf[0].begin());
+  std::vector<cd> psi(buf[0]);
+  std::vector<cd> ac(M);
+  ac[0] = 1;
+  for (int i = 1; i < M; ++i) {
+    if (orc_prop_apply(pp, reinterpret_cast<double *>(psi.data()), i - 1) < 0) return -1;
+    buf[i] = psi;
+    ac[i] = dot(s, psi.data(), buf[0].data());
+    if (std::isnan(ac[i].real())) { g_err = "Correlation is not a number"; return -QDG_ENONFINITE; }
+  }
+  if (win)
+    for (int i = 0; i < M; ++i) ac[i] *= 0.5 * (1. - std::cos(2 * M_PI * double(i) / double(M - 1)));
+  FFT1 f; f.init(M);
+  std::vector<cd> work(M), spec(ac);
+  f.exec(spec.data(), work.data(), -1);
+  std::vector<double> power(M);
+  for (int i = 0; i < M; ++i) power[i] = std::abs(spec[i]);
+  const std::vector<int> pk = pf_find(power, tol, width);
+  *nef_out = int(pk.size());
+  if (spectrum) std::copy(spec.begin(), spec.end(), reinterpret_cast<cd *>(spectrum));
+  const double dw = 2 * M_PI / (p.dt * double(M));
+  std::vector<cd> ef(n), hef(n);
+  for (int k = 0; k < std::min(int(pk.size()), max_nef); ++k) {
+    const int index = pk[k];
+    const double energy = index < M / 2 ? double(index) * dw : double(index - M) * dw;
+    ef = buf[0];
+    for (int st = 1; st < M; ++st) {
+      const cd c(std::cos(energy * double(st) * p.dt), std::sin(energy * double(st) * p.dt));
+      for (long j = 0; j < n; ++j) ef[j] += buf[st][j] * c;
+    }
+    const double nn = norm(s, ef.data());
+    for (auto &v : ef) v *= 1 / nn;
+    h_apply(s, ef.data(), hef.data(), 0);
+    energies[k] = dot(s, ef.data(), hef.data()).real();
+    if (efs) std::copy(ef.begin(), ef.end(), reinterpret_cast<cd *>(efs) + (long)k * n);
+  }
+  return 0;
+}
+
 int orc_eigen_imag(void *pp, const double *psi_init, int nef, int maxsteps, double convergence,
                    int diag, double *efs, double *e_raw, double *e_diag, int *steps) {
   Prop &p = *static_cast<Prop *>(pp);

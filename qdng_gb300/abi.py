@@ -123,6 +123,9 @@ SIGNATURES = [
     ("qdg_wf_copy", _i32, [_vp, _vp]),
     ("qdg_h_apply", _i32, [_vp, _vp, _vp, _i64]),
     ("qdg_observables_compute", _i32, [_vp, _vp, _vp, _i64, C.POINTER(Observables)]),
+    ("qdg_eigen_autocorr", _i32, [_vp, C.POINTER(C.c_double), _i32, C.c_double, _i32, _i32, _i32,
+                                  C.POINTER(C.c_double), C.POINTER(_i32), C.POINTER(C.c_double),
+                                  C.POINTER(C.c_double)]),
     ("qdg_expec_position", _i32, [_vp, _vp, _i32, C.c_double, C.POINTER(C.c_double)]),
     ("qdg_expec_momentum", _i32, [_vp, _vp, _i32, C.c_double, C.POINTER(C.c_double)]),
     ("qdg_expec_kinetic", _i32, [_vp, _vp, C.POINTER(C.c_double)]),

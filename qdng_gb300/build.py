@@ -24,7 +24,9 @@ SOURCES = ["qdg_kernels.cu", "qdg_persistent.cu", "qdg_api.cu", "qdg_noalloc.cu"
            # one 1-D line on a thread-block cluster
            "qdg_step_cluster.cu", "qdg_step_line64.cu",
            # expectation values of filter operators
-           "qdg_filters.cu"]
+           "qdg_filters.cu",
+           # the autocorrelation eigen driver
+           "qdg_eigen_ac.cu"]
 
 
 def nvcc():

@@ -2629,6 +2629,106 @@ qdg_status qdg_eigen_imag(qdg_prop *P, const double *psi_init, int32_t nef, int3
   return eigen_imag(P, psi_init, nef, maxsteps, convergence, diag, efs, e_raw, e_diag, steps);
 }
 
+qdg_status qdg_eigen_autocorr(qdg_prop *P, const double *psi_init, int32_t nsteps, double tol, int32_t width,
+                              int32_t win, int32_t max_nef, double *energies, int32_t *nef_out, double *efs,
+                              double *spectrum) {
+  if (!P || !psi_init || nsteps < 2 || max_nef < 0 || !nef_out || (max_nef > 0 && !energies))
+    return fail(QDG_EINVAL, "bad arguments");
+  if (!(tol >= 0)) return fail(QDG_EINVAL, "Tolerance factor for peak finder is non-sense. Must >= 0");
+  if (!P->inited) return fail(QDG_EINVAL, "propagator not initialised");
+  if (P->imag) return fail(QDG_EINVAL, "AutoCorrEF needs a real-time propagator");
+  sync_twin(P);
+  qdg_plan *p = P->plan;
+  const long long n = wf_elems(p);
+  const int M = nsteps;
+  const size_t wbytes = sizeof(cplx<double>) * (size_t)n;
+  std::vector<void *> bufs;
+  auto cleanup = [&](qdg_status st) {
+    cudaStreamSynchronize(p->stream);
+    for (void *b : bufs) cudaFree(b);
+    return st;
+  };
+  auto alloc = [&](size_t bytes) -> void * {
+    void *b = nullptr;
+    if (cudaMalloc(&b, std::max<size_t>(bytes, 16)) != cudaSuccess) return nullptr;
+    bufs.push_back(b);
+    return b;
+  };
+  // the propagation psi_0 .. psi_{M-1} (the reference's WFBuffer)
+  cplx<double> *T = static_cast<cplx<double> *>(alloc(wbytes * (size_t)M));
+  cplx<double> *psi = static_cast<cplx<double> *>(alloc(wbytes));
+  cplx<double> *d_a = static_cast<cplx<double> *>(alloc(sizeof(cplx<double>) * (size_t)M));
+  if (!T || !psi || !d_a) return cleanup(fail(QDG_ENOMEM, "device allocation for the stored propagation failed"));
+  qdg_status s;
+  std::vector<cd> d;
+#define ECHK(expr) do { if ((s = (expr)) != QDG_OK) return cleanup(s); } while (0)
+#define ECUDA(expr) do { if ((expr) != cudaSuccess) return cleanup(fail(QDG_ECUDA, #expr)); } while (0)
+  ECUDA(cudaMemcpyAsync(T, psi_init, wbytes, cudaMemcpyHostToDevice, p->stream));
+  ECUDA(cudaMemcpyAsync(psi, T, wbytes, cudaMemcpyDeviceToDevice, p->stream));
+  for (int st = 1; st < M; ++st) {
+    int used = 0;
+    ECHK(prop_step(P, psi, st - 1, &used, P->kind >= 3));
+    ECUDA(cudaMemcpyAsync(T + (size_t)st * n, psi, wbytes, cudaMemcpyDeviceToDevice, p->stream));
+  }
+  // autocorrelation <psi_s|psi_0> with the volume element (a_0 = 1, ProgEigen.cpp:445)
+  ECUDA(qdg::launch_step_overlaps(T, n, M, d_a, p->sm_count, p->stream));
+  std::vector<cplx<double>> ha(M);
+  ECUDA(cudaMemcpyAsync(ha.data(), d_a, sizeof(cplx<double>) * M, cudaMemcpyDeviceToHost, p->stream));
+  ECUDA(cudaStreamSynchronize(p->stream));
+  double dv = 1.0;
+  for (int k = 0; k < p->nd; ++k) dv *= p->dx[k];
+  std::vector<cd> a(M);
+  a[0] = 1.0;
+  for (int st = 1; st < M; ++st) {
+    a[st] = cd(ha[st].re, ha[st].im) * dv;
+    if (!std::isfinite(a[st].real())) return cleanup(fail(QDG_ENONFINITE, "Correlation is not a number"));
+  }
+  // Hann window (FunctionGenerator::Hann), FFT, power spectrum, peaks
+  if (win)
+    for (int st = 0; st < M; ++st) a[st] *= 0.5 * (1. - cos(2 * M_PI * double(st) / double(M - 1)));
+  const std::vector<cd> spec = qdg::host::dft(a, -1);
+  std::vector<double> power(M);
+  for (int st = 0; st < M; ++st) power[st] = std::abs(spec[st]);
+  const std::vector<int> peaks = qdg::host::find_peaks(power, tol, width);
+  *nef_out = (int32_t)peaks.size();
+  if (spectrum) memcpy(spectrum, spec.data(), sizeof(cd) * M);
+  const int K = std::min<int>((int)peaks.size(), max_nef);
+  if (K > 0) {
+    // eigenfunctions by time integration at the peak energies (ProgEigen.cpp:560-580)
+    const double dw = 2 * M_PI / (P->dt * double(M));
+    std::vector<cplx<double>> C((size_t)K * M);
+    std::vector<double> E(K);
+    for (int k = 0; k < K; ++k) {
+      const int idx = peaks[k];
+      E[k] = idx < M / 2 ? double(idx) * dw : double(idx - M) * dw;
+      for (int st = 0; st < M; ++st) {
+        const double ang = E[k] * double(st) * P->dt;
+        C[(size_t)k * M + st] = cplx<double>{cos(ang), sin(ang)};
+      }
+    }
+    cplx<double> *dC = static_cast<cplx<double> *>(alloc(sizeof(cplx<double>) * C.size()));
+    cplx<double> *ef = static_cast<cplx<double> *>(alloc(wbytes * (size_t)K));
+    if (!dC || !ef) return cleanup(fail(QDG_ENOMEM, "device allocation failed"));
+    ECUDA(cudaMemcpyAsync(dC, C.data(), sizeof(cplx<double>) * C.size(), cudaMemcpyHostToDevice, p->stream));
+    ECUDA(qdg::launch_integrate_steps(T, n, M, dC, K, ef, p->sm_count, p->stream));
+    for (int k = 0; k < K; ++k) {
+      cplx<double> *f = ef + (size_t)k * n;
+      ECHK((dots<double, double>(p, f, f, d)));
+      const double nr = std::sqrt(total(d).real());
+      if (!std::isfinite(nr) || !(nr > 0)) return cleanup(fail(QDG_ENONFINITE, "Norm is not a number"));
+      ECUDA(qdg::launch_lincomb<double>(f, (const cplx<double> *)nullptr, cplx<double>{1.0 / nr, 0}, cplx<double>{0, 0},
+                                        n, p->stream));
+      cd e;
+      ECHK(h_expec(p, f, f, &e));
+      energies[k] = e.real();
+      if (efs) ECUDA(cudaMemcpyAsync(efs + 2 * (size_t)k * n, f, wbytes, cudaMemcpyDeviceToHost, p->stream));
+    }
+  }
+#undef ECHK
+#undef ECUDA
+  return cleanup(QDG_OK);
+}
+
 qdg_status qdg_prop_run(qdg_prop *P, qdg_wf *psi, int64_t step0, int32_t nsteps, int64_t *terms_total) {
   if (!P || !psi || psi->plan != P->user || nsteps < 0) return fail(QDG_EINVAL, "bad arguments");
   sync_twin(P);

@@ -210,5 +210,77 @@ std::string cheby_series(cd Emax, cd Emin, double dt, cd c0, bool imag,
   return std::string();
 }
 
+// Recursive decimation in time: n = p m with p the smallest prime factor;
+// the p sub-sequences x[j p + r] are transformed (length m) and combined
+// with twiddles from long double sin/cos.
+static void dft_rec(const cd *x, long stride, long n, int sign, cd *out) {
+  if (n == 1) { out[0] = x[0]; return; }
+  long p = 2;
+  while (n % p) ++p;
+  const long m = n / p;
+  std::vector<cd> sub((size_t)n);
+  for (long r = 0; r < p; ++r) dft_rec(x + r * stride, stride * p, m, sign, sub.data() + r * m);
+  const long double pi = 3.141592653589793238462643383279502884L;
+  for (long k = 0; k < n; ++k) {
+    std::complex<long double> acc = 0;
+    for (long r = 0; r < p; ++r) {
+      const long double ang = sign * 2.0L * pi * (long double)((r * k) % n) / (long double)n;
+      const cd v = sub[(size_t)(r * m + k % m)];
+      acc += std::complex<long double>(v.real(), v.imag()) * std::complex<long double>(cosl(ang), sinl(ang));
+    }
+    out[k] = cd((double)acc.real(), (double)acc.imag());
+  }
+}
+
+std::vector<cd> dft(const std::vector<cd> &x, int sign) {
+  std::vector<cd> out(x.size());
+  if (!x.empty()) dft_rec(x.data(), 1, (long)x.size(), sign < 0 ? -1 : 1, out.data());
+  return out;
+}
+
+static void mean_sigma(const std::vector<double> &d, size_t b, size_t e, double &mean, double &sigma) {
+  mean = 0;
+  for (size_t i = b; i < e; ++i) mean += d[i];
+  mean /= double(e - b);
+  sigma = 0;
+  for (size_t i = b; i < e; ++i) sigma += (d[i] - mean) * (d[i] - mean);
+  sigma = std::sqrt(sigma / double(e - b));
+}
+
+std::vector<int> find_peaks(const std::vector<double> &data, double tol, int width) {
+  std::vector<int> peaks;
+  const size_t n = data.size();
+  if (n < 2) return peaks;
+  if (width <= 0) {
+    double mean, sigma;
+    mean_sigma(data, 0, n, mean, sigma);
+    const double thr = mean + tol * sigma;
+    bool open = false;
+    double dmax = 0;
+    int imax = -1;
+    for (size_t i = 0; i < n; ++i) {
+      if (!open && data[i] > thr) { open = true; dmax = 0; imax = -1; }
+      if (open && data[i] < thr) { open = false; peaks.push_back(imax); }
+      if (open && data[i] > dmax) { dmax = data[i]; imax = (int)i; }
+    }
+    // a region still open at the end counts if the last value is below its maximum
+    if (open && imax != -1 && data[n - 1] < dmax) peaks.push_back(imax);
+    return peaks;
+  }
+  double delta = 0;
+  for (size_t i = 1; i < n; ++i) {  // local maxima: a rise followed by a fall
+    if (data[i] < data[i - 1] && delta > 0) {
+      const size_t c = i - 1;
+      const size_t lo = c < (size_t)width ? 0 : c - width;
+      const size_t hi = c + width > n - 1 ? n - 1 : c + width;
+      double mean, sigma;
+      mean_sigma(data, lo, hi, mean, sigma);
+      if (data[c] > mean + tol * sigma) peaks.push_back((int)c);
+    }
+    delta = data[i] - data[i - 1];
+  }
+  return peaks;
+}
+
 }  // namespace host
 }  // namespace qdg

@@ -45,5 +45,15 @@ struct ChebySeries {
 std::string cheby_series(cd emax, cd emin, double dt, cd c0, bool imag,
                          const std::map<std::string, std::string> &params, ChebySeries &out);
 
+// Unnormalised DFT of any length (sign -1 forward, as FFTW_FORWARD): mixed
+// radix by decimation in time over the prime factors of n.
+std::vector<cd> dft(const std::vector<cd> &x, int sign);
+
+// QDng's PeakFinder (src/tools/PeakFinder.cpp) on a power spectrum: with
+// width <= 0 the regions above mean + tol sigma of the whole spectrum and
+// the maximum of each; otherwise every local maximum that stands above
+// mean + tol sigma of the window [i - width, i + width).  Ascending indices.
+std::vector<int> find_peaks(const std::vector<double> &data, double tol, int width);
+
 }  // namespace host
 }  // namespace qdg

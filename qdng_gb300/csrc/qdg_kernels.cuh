@@ -283,6 +283,13 @@ template <typename T>
 cudaError_t launch_cheby_step_cluster(const ClusterStepArgs<T> &a, cudaStream_t st);
 template <typename T>
 size_t cluster_step_smem(int M);
+// ProgEigen::AutoCorrEF on the device (qdg_eigen_ac.cu): overlaps of M stored
+// steps with step 0, and the integration of the steps at K energies.
+cudaError_t launch_step_overlaps(const cplx<double> *T, long long n, int M, cplx<double> *out, int sm_count,
+                                 cudaStream_t st);
+cudaError_t launch_integrate_steps(const cplx<double> *T, long long n, int M, const cplx<double> *C, int K,
+                                   cplx<double> *out, int sm_count, cudaStream_t st);
+
 // Expectation values of filter operators (qdg_filters.cu).
 struct PointExpecArgs {
   const cplx<double> *psi;

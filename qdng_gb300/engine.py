@@ -218,6 +218,20 @@ class Propagator:
                                       _dp(e_diag), steps.ctypes.data_as(C.c_void_p)))
         return efs, e_raw, e_diag, steps
 
+    def eigen_autocorr(self, psi_init, nsteps, tol=1.0, width=-1, win=True, max_nef=64, want_efs=True):
+        """ProgEigen::AutoCorrEF: (energies, efs [k x size] or None, spectrum [nsteps],
+        number of peaks found)."""
+        n = self.plan.S * self.plan.npts
+        x = np.ascontiguousarray(psi_init, dtype=np.complex128).reshape(-1)
+        e = np.zeros(max(max_nef, 1))
+        efs = np.zeros((max(max_nef, 1), n), dtype=np.complex128) if want_efs else None
+        spec = np.zeros(nsteps, dtype=np.complex128)
+        nef = C.c_int32(0)
+        check(self.lib.qdg_eigen_autocorr(self.h, _dp(x), nsteps, tol, width, int(win), max_nef, _dp(e), C.byref(nef),
+                                          _dp(efs) if efs is not None else None, _dp(spec)))
+        k = min(nef.value, max_nef)
+        return e[:k], (efs[:k] if efs is not None else None), spec, nef.value
+
     def run(self, wf, step0, nsteps):
         tot = C.c_int64(0)
         check(self.lib.qdg_prop_run(self.h, wf.h, step0, nsteps, C.byref(tot)))

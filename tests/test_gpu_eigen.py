@@ -80,3 +80,44 @@ def test_double_well_eigen_on_mixed_plan(eng):
         out[prec] = P.eigen_imag(psi, nef, maxsteps, conv, diag=True)
     assert list(out["mixed"][3]) == list(out["fp64"][3])
     np.testing.assert_allclose(out["mixed"][2], out["fp64"][2], rtol=1e-13)
+
+
+@pytest.mark.parametrize("method", ["Cheby", "SIL"])
+def test_tge_autocorr_matches_oracle_and_golden(eng, fixtures, golden, method):
+    """ProgEigen::AutoCorrEF on the GPU (2048 stored steps, autocorrelation,
+    Hann window, FFT, peaks, time integration) against the oracle: the same
+    peaks, spectrum to 1e-10, energies to 1e-10, eigenfunctions to 1e-9;
+    and QDng's TGE-ac golden energies."""
+    hp, psi, run = cases.tge(fixtures, method)
+    S = O.System(hp)
+    Qi = O.Propagator(S, run["name"], run["params"], dt=run["dt"], imaginary_time=True, backward=True)
+    efs, _, _, _ = Qi.eigen_imag(psi, run["nef"], run["steps"], run["conv"], diag=True)
+    lc = cases._normalize(hp, efs[:6].sum(axis=0))
+    Q = O.Propagator(S, run["name"], run["params"], dt=run["dt"])
+    e_o, ef_o, spec_o, npk_o = Q.eigen_autocorr(lc, 2048)
+    plan = eng.Plan(hp, "fp64")
+    P = eng.Propagator(plan, run["name"], run["params"], dt=run["dt"])
+    e, ef, spec, npk = P.eigen_autocorr(lc, 2048)
+    assert npk == npk_o >= 6
+    assert np.abs(spec - spec_o).max() <= 1e-10 * np.abs(spec_o).max()
+    np.testing.assert_allclose(e, e_o, rtol=1e-10)
+    dx = np.prod(hp.grid.dx)
+    for i in range(len(e)):
+        assert np.abs(ef[i] - ef_o[i]).max() <= 1e-9 * np.abs(ef_o[i]).max(), i
+    for i, txt in golden["tge_ac"]:
+        dec = len(txt.split(".")[1])
+        assert abs(e[i] - float(txt)) < 1.5 * 10 ** (-dec), (method, i, e[i], txt)
+
+
+def test_autocorr_2d_double_well(eng):
+    """A 2-D superposition (48^2 double well), 512 steps, windowed peaks with
+    width 8: engine and oracle find the same peaks and energies."""
+    hp, psi, run = cases.cfg5_double_well(n=48)
+    S = O.System(hp)
+    Q = O.Propagator(S, "Cheby", "", dt=20.0)
+    plan = eng.Plan(hp, "fp64")
+    P = eng.Propagator(plan, "Cheby", "", dt=20.0)
+    e_o, _, _, npk_o = Q.eigen_autocorr(psi, 512, tol=2.0, width=8, max_nef=12)
+    e, _, _, npk = P.eigen_autocorr(psi, 512, tol=2.0, width=8, max_nef=12)
+    assert npk == npk_o and npk > 0
+    np.testing.assert_allclose(e, e_o, rtol=1e-9)

@@ -212,3 +212,22 @@ def test_tge_imag(fixtures, golden, method):
         dec = len(txt.split(".")[1])
         got = f"{e_diag[i]:.{dec + 3}f}"
         assert got.startswith(txt) or abs(e_diag[i] - float(txt)) < 1.5 * 10 ** (-dec), (method, i, e_diag[i], txt)
+
+
+@pytest.mark.parametrize("method", ["Cheby", "SIL", "Arnoldi"])
+def test_tge_autocorr(fixtures, golden, method):
+    """TGE-<method>-ac: the normalised sum of the first six imaginary-time
+    eigenfunctions propagated for 2048 steps of dt = 5; AutoCorrEF (Hann
+    window, PeakFinder tol 1) must find the golden energies (energy.dat of
+    the reference, 6 digits, raw energies: diag is off for ac)."""
+    hp, psi, run = cases.tge(fixtures, method)
+    S = O.System(hp)
+    Pi = O.Propagator(S, run["name"], run["params"], dt=run["dt"], imaginary_time=True, backward=True)
+    efs, _, _, _ = Pi.eigen_imag(psi, run["nef"], run["steps"], run["conv"], diag=True)
+    lc = cases._normalize(hp, efs[:6].sum(axis=0))
+    P = O.Propagator(S, run["name"], run["params"], dt=run["dt"])
+    e, ef, spec, npk = P.eigen_autocorr(lc, 2048)
+    assert npk >= 6
+    for i, txt in golden["tge_ac"]:
+        dec = len(txt.split(".")[1])
+        assert abs(e[i] - float(txt)) < 1.5 * 10 ** (-dec), (method, i, e[i], txt)
