@@ -1469,9 +1469,8 @@ qdg_status gspo_init(qdg_prop *P) {
     } else {
       qdg_status s = build_couplings(p, [g](const qdg_hterm &t) { return t.group == g; }, P->gcp_h[g]);
       if (s != QDG_OK) return s;
-      bool offd = false;
-      for (int e = 0; e < P->gcp_h[g].ne; ++e) offd |= P->gcp_h[g].row[e] != P->gcp_h[g].col[e];
-      if (offd && p->S > 2) return fail(QDG_EUNSUPPORTED, "GSPO coupled potential member supports 2 states");
+      // coupled members of any number of states: per-point S x S exponentials
+      // (closed form for S = 2, Jacobi rotations above)
       CK(cudaMalloc(&P->gcp_d[g], sizeof(qdg::Couplings)));
       CK(cudaMemcpy(P->gcp_d[g], &P->gcp_h[g], sizeof(qdg::Couplings), cudaMemcpyHostToDevice));
       CK(cudaMalloc(&P->gcoef_d[g], sizeof(double) * qdg::kMaxCouplings));
@@ -1499,7 +1498,7 @@ qdg_status gspo_member(qdg_prop *P, int g, cplx<T> *x, long long step) {
   } else if (!P->gdyn[g]) {
     // static member (OGSPO::InitExp computes its exponential once, OGSPO.cpp:30-52)
     if (!P->gU[g]) {
-      const int kU = p->S == 2 ? 3 : p->S;
+      const int kU = p->S == 2 ? 3 : p->S * p->S;  // S > 2: the full per-point matrix
       CK(cudaMalloc(&P->gU[g], sizeof(cplx<double>) * kU * (size_t)p->npts));
       CK(qdg::launch_set_coefs(P->gcoef_d[g], P->gcp_d[g], p->d_lasers, p->laser_nt, step, p->stream));
       double *g64 = nullptr;  // the grids in binary64 (a mixed plan keeps FP32 copies)

@@ -964,6 +964,66 @@ __device__ __forceinline__ cplx<double> cexpd(cplx<double> z) {
 // 2x2: exp(cM) = e^{c m} [cosh(c r) I + sinh(c r)/r (M - m I)], m = (a+d)/2,
 // r = sqrt(((a-d)/2)^2 + b^2) -- the spectral form of the per-point
 // eigenbasis transform of TransformMSD (TransformMSD.cpp:47-62,84-98).
+// exp(c M) of a real symmetric S x S matrix m (row-major, destroyed): cyclic
+// Jacobi rotations give M = Z diag(w) Z^T, then E = Z diag(exp(c w)) Z^T --
+// the per-point diagonalisation and transformation of ODMultistate and
+// TransformMSD (ODMultistate.cpp:133-152, TransformMSD.cpp:31-100).  At most
+// 50 sweeps; the rotations stop when the off-diagonal part is below 1e-32 of
+// the matrix's square norm.
+__device__ __forceinline__ bool offdiag_nonzero(const double *m, int S) {
+  for (int a = 0; a < S; ++a)
+    for (int b = 0; b < S; ++b)
+      if (a != b && m[a * S + b] != 0.0) return true;
+  return false;
+}
+__device__ void expm_sym(double *m, int S, cplx<double> c, cplx<double> *E) {
+  double z[kMaxStates * kMaxStates];
+  for (int i = 0; i < S * S; ++i) z[i] = 0.0;
+  for (int i = 0; i < S; ++i) z[i * S + i] = 1.0;
+  double tot = 0.0;
+  for (int i = 0; i < S * S; ++i) tot += m[i] * m[i];
+  for (int sweep = 0; sweep < 50; ++sweep) {
+    double off = 0.0;
+    for (int p = 0; p < S; ++p)
+      for (int q = p + 1; q < S; ++q) off += m[p * S + q] * m[p * S + q];
+    if (!(off > 1e-32 * tot)) break;
+    for (int p = 0; p < S; ++p)
+      for (int q = p + 1; q < S; ++q) {
+        const double apq = m[p * S + q];
+        if (fabs(apq) < 1e-300) continue;
+        const double theta = (m[q * S + q] - m[p * S + p]) / (2.0 * apq);
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+        const double cs = 1.0 / sqrt(t * t + 1.0), sn = t * cs;
+        for (int k = 0; k < S; ++k) {
+          const double akp = m[k * S + p], akq = m[k * S + q];
+          m[k * S + p] = cs * akp - sn * akq;
+          m[k * S + q] = sn * akp + cs * akq;
+        }
+        for (int k = 0; k < S; ++k) {
+          const double apk = m[p * S + k], aqk = m[q * S + k];
+          m[p * S + k] = cs * apk - sn * aqk;
+          m[q * S + k] = sn * apk + cs * aqk;
+        }
+        for (int k = 0; k < S; ++k) {
+          const double zkp = z[k * S + p], zkq = z[k * S + q];
+          z[k * S + p] = cs * zkp - sn * zkq;
+          z[k * S + q] = sn * zkp + cs * zkq;
+        }
+      }
+  }
+  cplx<double> ew[kMaxStates];
+  for (int k = 0; k < S; ++k) ew[k] = cexpd(mk(c.re * m[k * S + k], c.im * m[k * S + k]));
+  for (int a = 0; a < S; ++a)
+    for (int b = 0; b < S; ++b) {
+      cplx<double> acc = mk(0.0, 0.0);
+      for (int k = 0; k < S; ++k) {
+        const double zz = z[a * S + k] * z[b * S + k];
+        acc = acc + mk(zz * ew[k].re, zz * ew[k].im);
+      }
+      E[a * S + b] = acc;
+    }
+}
+
 template <typename T>
 __global__ void gspo_potential_kernel(cplx<T> *psi, int S, long long npts, const Couplings *cp, const double *coef,
                                       const T *grids, cplx<double> c) {
@@ -993,6 +1053,15 @@ __global__ void gspo_potential_kernel(cplx<T> *psi, int S, long long npts, const
       const cplx<double> y1 = dmul(ch, x1) + dmul(shr, mk(b * x0.re - h * x1.re, b * x0.im - h * x1.im));
       st(psi + p, ccast<T>(dmul(em, y0)));
       st(psi + npts + p, ccast<T>(dmul(em, y1)));
+    } else if (S > 2 && offdiag_nonzero(m, S)) {
+      cplx<double> E[kMaxStates * kMaxStates], x[kMaxStates];
+      expm_sym(m, S, c, E);
+      for (int s = 0; s < S; ++s) x[s] = ccast<double>(ld(psi + s * npts + p));
+      for (int a = 0; a < S; ++a) {
+        cplx<double> y = mk(0.0, 0.0);
+        for (int b = 0; b < S; ++b) y = y + dmul(E[a * S + b], x[b]);
+        st(psi + a * npts + p, ccast<T>(y));
+      }
     } else {
       for (int s = 0; s < S; ++s) {
         const double v = m[s * S + s];
@@ -1006,7 +1075,7 @@ __global__ void gspo_potential_kernel(cplx<T> *psi, int S, long long npts, const
 // The same exponent as gspo_potential_kernel, stored instead of applied.
 __global__ void gspo_umat_kernel(cplx<double> *U, int S, long long npts, const Couplings *cp, const double *coef,
                                  const double *grids, cplx<double> c) {
-  const int kU = S == 2 ? 3 : S;
+  const int kU = S == 2 ? 3 : S * S;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npts; p += (long long)gridDim.x * blockDim.x) {
     double m[kMaxStates * kMaxStates];
     for (int i = 0; i < S * S; ++i) m[i] = 0;
@@ -1035,8 +1104,10 @@ __global__ void gspo_umat_kernel(cplx<double> *U, int S, long long npts, const C
       u[0] = cexpd(mk(c.re * m[0], c.im * m[0]));
       u[1] = mk(0.0, 0.0);
       u[2] = cexpd(mk(c.re * m[3], c.im * m[3]));
+    } else if (S == 1) {
+      u[0] = cexpd(mk(c.re * m[0], c.im * m[0]));
     } else {
-      for (int s = 0; s < S; ++s) u[s] = cexpd(mk(c.re * m[s * S + s], c.im * m[s * S + s]));
+      expm_sym(m, S, c, u);  // S > 2: the full per-point matrix
     }
   }
 }
@@ -1049,10 +1120,18 @@ cudaError_t launch_gspo_umat(cplx<double> *U, int S, long long npts, const Coupl
 
 template <typename T>
 __global__ void gspo_apply_kernel(cplx<T> *psi, int S, long long npts, const cplx<double> *U) {
-  const int kU = S == 2 ? 3 : S;
+  const int kU = S == 2 ? 3 : S * S;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npts; p += (long long)gridDim.x * blockDim.x) {
     const cplx<double> *u = U + (long long)kU * p;
-    if (S == 2) {
+    if (S > 2) {
+      cplx<double> x[kMaxStates];
+      for (int s = 0; s < S; ++s) x[s] = ccast<double>(ld(psi + s * npts + p));
+      for (int a = 0; a < S; ++a) {
+        cplx<double> y = mk(0.0, 0.0);
+        for (int b = 0; b < S; ++b) y = y + dmul(u[a * S + b], x[b]);
+        st(psi + a * npts + p, ccast<T>(y));
+      }
+    } else if (S == 2) {
       const cplx<double> x0 = ccast<double>(ld(psi + p)), x1 = ccast<double>(ld(psi + npts + p));
       st(psi + p, ccast<T>(dmul(u[0], x0) + dmul(u[1], x1)));
       st(psi + npts + p, ccast<T>(dmul(u[1], x0) + dmul(u[2], x1)));

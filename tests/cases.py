@@ -265,12 +265,7 @@ def member_hplan(mem):
 
 
 def lpt_partition(costs, nparts):
-    """Largest-processing-time-first assignment of independent members to ranks."""
-    order = sorted(range(len(costs)), key=lambda i: -costs[i])
-    loads = [0.0] * nparts
-    parts = [[] for _ in range(nparts)]
-    for i in order:
-        r = min(range(nparts), key=lambda k: loads[k])
-        parts[r].append(i)
-        loads[r] += costs[i]
-    return [sorted(p) for p in parts], loads
+    """Largest-processing-time-first assignment of independent members to ranks
+    (the package's, qdng_gb300.sharding)."""
+    from qdng_gb300.sharding import lpt_partition as lpt
+    return lpt(costs, nparts)

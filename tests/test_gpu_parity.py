@@ -342,3 +342,35 @@ def test_run_counts_terms(eng, fixtures):
     x = psi.copy()
     expect = sum(Q.apply(x, s) for s in range(10))
     assert P.run(w, 0, 10) == expect
+
+
+def _three_state_gspo(dynamic):
+    """Three coupled diabatic states as GSPO members: kinetic DMultistate and
+    a potential DMultistate with couplings (0,1), (1,2), (0,2); dynamic adds a
+    laser-driven dipole coupling to the potential member."""
+    g = op.GridSystem([64, 48], [-4.0, -4.0], [4.0, 4.0])
+    X, Y = g.mesh()
+    m = [1500.0, 2500.0]
+    kin = op.DMultistate({(s, s): op.GridNablaSq(m) for s in range(3)})
+    el = {(0, 0): op.GridPotential(0.01 * (X ** 2 + Y ** 2)),
+          (1, 1): op.GridPotential(0.01 * ((X - 1) ** 2 + Y ** 2) + 0.02),
+          (2, 2): op.GridPotential(0.012 * (X ** 2 + (Y - 0.5) ** 2) + 0.04),
+          (0, 1): op.GridPotential(0.005 * np.exp(-X ** 2 - Y ** 2)),
+          (1, 2): op.GridPotential(0.004 * np.exp(-(X - 0.5) ** 2)),
+          (0, 2): op.GridPotential(0.002 * np.exp(-Y ** 2))}
+    if dynamic:
+        el[(1, 2)] = op.Sum([el[(1, 2)], op.GridDipole(0.2 * X * np.exp(-0.1 * Y ** 2),
+                                                        0.03 * np.sin(0.05 * np.arange(64)))])
+    hp = op.HPlan(g, members=[kin, op.DMultistate(el)])
+    psi0 = np.exp(-(X - 0.5) ** 2 - Y ** 2).reshape(-1).astype(np.complex128)
+    psi = np.concatenate([psi0, 0.5 * psi0, 0.2j * psi0])
+    return hp, psi / np.sqrt((np.abs(psi) ** 2).sum() * np.prod(g.dx))
+
+
+@pytest.mark.parametrize("dynamic", [False, True], ids=["static", "laser"])
+def test_gspo_three_coupled_states(eng, dynamic):
+    """GSPO with a coupled three-state potential member: the per-point 3x3
+    exponential by Jacobi rotations (ODMultistate / TransformMSD for S > 2),
+    stored once for a static member, per half step with a laser."""
+    hp, psi = _three_state_gspo(dynamic)
+    _assert_parity(hp, *_run_both(eng, hp, psi, dict(name="GSPO", params="", dt=2.0), 30), check_terms=False)
