@@ -274,6 +274,16 @@ qdg_status qdg_eigen_autocorr(qdg_prop *prop, const double *psi_init, int32_t ns
                               int32_t win, int32_t max_nef, double *energies, int32_t *nef_out, double *efs,
                               double *spectrum);
 
+/* ProgEigen::LanczosEF (src/ProgEigen.cpp:604-648) + DiagBasis with an
+ * Arnoldi propagator: the Krylov basis of psi_init (OArnoldi::BuildLZB, the
+ * propagator's order and convergence), the Ritz values and functions of its
+ * Hessenberg matrix, then H diagonalised in that basis.  nef_out = the basis
+ * size; the first max_nef values ascending in e_raw (Ritz values) and e_diag,
+ * and the diagonalised functions in efs (max_nef x nstates*npoints
+ * complex128, may be NULL). */
+qdg_status qdg_eigen_lanczos(qdg_prop *prop, const double *psi_init, int32_t max_nef, double *e_raw,
+                             double *e_diag, int32_t *nef_out, double *efs);
+
 /* ---- batched ensemble of independent wavepackets ------------------------ */
 
 /* One member: a single-state Hamiltonian Sum(GridNablaSq, GridPotential,

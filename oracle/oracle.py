@@ -59,6 +59,7 @@ def lib():
         L.orc_erange.argtypes = [vp, dp, dp]
         L.orc_h_apply.argtypes = [vp, dp, dp, C.c_long]
         L.orc_observables.argtypes = [vp, dp, dp, C.c_long, dp]
+        L.orc_eigen_lanczos.argtypes = [vp, dp, C.c_int, dp, dp, C.POINTER(C.c_int), dp]
         L.orc_eigen_ac.argtypes = [vp, dp, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, dp,
                                    C.POINTER(C.c_int), dp, dp]
         for f, args in (("orc_expec_position", [vp, dp, C.c_int, C.c_double]),
@@ -220,6 +221,17 @@ class Propagator:
             raise ValueError(lib().orc_last_error().decode())
         k = min(nef.value, max_nef)
         return e[:k], efs[:k], spec, nef.value
+
+    def eigen_lanczos(self, psi_init, max_nef=64):
+        """ProgEigen::LanczosEF + DiagBasis: (e_raw, e_diag, efs, basis size)."""
+        n = self.system.S * self.system.npts
+        x = np.ascontiguousarray(psi_init, dtype=np.complex128).reshape(-1)
+        er, ed = np.zeros(max(max_nef, 1)), np.zeros(max(max_nef, 1))
+        efs = np.zeros((max(max_nef, 1), n), dtype=np.complex128)
+        nef = C.c_int(0)
+        lib().orc_eigen_lanczos(self.h, _dp(x), max_nef, _dp(er), _dp(ed), C.byref(nef), _dp(efs))
+        k = min(nef.value, max_nef)
+        return er[:k], ed[:k], efs[:k], nef.value
 
     def eigen_imag(self, psi_init, nef, maxsteps, conv, diag=True):
         n = self.system.npts * self.system.S

@@ -832,7 +832,9 @@ static int sil_step(Prop &p, cd *psi, long step) {
 }
 
 /* OArnoldi::BuildLZB / DiagLZB / Propagate (OArnoldi.cpp:86-199). */
-static int arnoldi_step(Prop &p, cd *psi, long step) {
+/* OArnoldi::BuildLZB (OArnoldi.cpp:86-152): the basis in p.lzb, the
+ * Hessenberg matrix HA (order x order) */
+static int arnoldi_build(Prop &p, const cd *psi, long step, std::vector<cd> &HA) {
   System &s = *p.sys;
   long n = s.npts * s.S;
   int maxorder = p.kord;
@@ -862,8 +864,16 @@ static int arnoldi_step(Prop &p, cd *psi, long step) {
   int order = p.aorder;
   h_apply(s, p.lzb[order - 1].data(), buf0.data(), step);
   for (int j = 0; j < order; ++j) tHA[j * maxorder + order - 1] = dot(s, p.lzb[j].data(), buf0.data());
-  std::vector<cd> HA(order * order);
+  HA.assign(order * order, 0);
   for (int i = 0; i < order; ++i) for (int j = 0; j < order; ++j) HA[i * order + j] = tHA[i * maxorder + j];
+  return order;
+}
+
+static int arnoldi_step(Prop &p, cd *psi, long step) {
+  System &s = *p.sys;
+  long n = s.npts * s.S;
+  std::vector<cd> HA;
+  const int order = arnoldi_build(p, psi, step, HA);
   std::vector<cd> vect = expm_e0(order, HA, p.c0);
   for (long q = 0; q < n; ++q) psi[q] *= vect[0];
   for (int i = 1; i < order; ++i) for (long q = 0; q < n; ++q) psi[q] += p.lzb[i][q] * vect[i];
@@ -1252,6 +1262,55 @@ int orc_eigen_ac(void *pp, const double *psi_init, int nsteps, double tol, int w
     h_apply(s, ef.data(), hef.data(), 0);
     energies[k] = dot(s, ef.data(), hef.data()).real();
     if (efs) std::copy(ef.begin(), ef.end(), reinterpret_cast<cd *>(efs) + (long)k * n);
+  }
+  return 0;
+}
+
+/* ProgEigen::LanczosEF (ProgEigen.cpp:604-648) + DiagBasis (ProgEigen.cpp:94-138):
+ * OArnoldi::BuildLZB, the Ritz pairs of the Hessenberg matrix (its symmetric
+ * part by Jacobi rotations, standing in for zhseqr/zhsein; eigenvectors
+ * scaled to a largest component of modulus 1 as zhsein scales them), the
+ * Ritz functions, H in that basis (diagonal: the Ritz values) diagonalised. */
+int orc_eigen_lanczos(void *pp, const double *psi_init, int max_nef, double *e_raw, double *e_diag, int *nef_out,
+                      double *efs) {
+  Prop &p = *static_cast<Prop *>(pp);
+  System &s = *p.sys;
+  const long n = s.npts * s.S;
+  std::vector<cd> HA;
+  const int order = arnoldi_build(p, reinterpret_cast<const cd *>(psi_init), 0, HA);
+  *nef_out = order;
+  std::vector<long double> A(order * order), w, z;
+  for (int i = 0; i < order; ++i)
+    for (int j = 0; j < order; ++j) A[i * order + j] = 0.5L * ((long double)HA[i * order + j].real() + HA[j * order + i].real());
+  jacobi_eig(order, A, w, z);
+  std::vector<std::vector<cd>> rf(order, std::vector<cd>(n, 0.0));
+  for (int i = 0; i < order; ++i) {
+    long double zmax = 0;
+    for (int j = 0; j < order; ++j) zmax = std::max(zmax, fabsl(z[j * order + i]));
+    for (int j = 0; j < order; ++j) {
+      const double c = (double)(z[j * order + i] / zmax);
+      for (long q = 0; q < n; ++q) rf[i][q] += p.lzb[j][q] * c;
+    }
+  }
+  std::vector<long double> Sm(order * order, 0), wd, zd;
+  std::vector<cd> hb(n);
+  for (int i = 0; i < order; ++i) {
+    for (int j = 0; j < i; ++j) {
+      h_apply(s, rf[j].data(), hb.data(), 0);
+      Sm[j * order + i] = Sm[i * order + j] = dot(s, rf[i].data(), hb.data()).real();
+    }
+    Sm[i * order + i] = w[i];
+  }
+  jacobi_eig(order, Sm, wd, zd);
+  for (int k = 0; k < std::min(order, max_nef); ++k) {
+    e_raw[k] = (double)w[k];
+    e_diag[k] = (double)wd[k];
+    if (efs) {
+      cd *out = reinterpret_cast<cd *>(efs) + (long)k * n;
+      for (long q = 0; q < n; ++q) out[q] = 0;
+      for (int j = 0; j < order; ++j)
+        for (long q = 0; q < n; ++q) out[q] += rf[j][q] * (double)zd[j * order + k];
+    }
   }
   return 0;
 }

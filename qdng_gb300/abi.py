@@ -126,6 +126,8 @@ SIGNATURES = [
     ("qdg_eigen_autocorr", _i32, [_vp, C.POINTER(C.c_double), _i32, C.c_double, _i32, _i32, _i32,
                                   C.POINTER(C.c_double), C.POINTER(_i32), C.POINTER(C.c_double),
                                   C.POINTER(C.c_double)]),
+    ("qdg_eigen_lanczos", _i32, [_vp, C.POINTER(C.c_double), _i32, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                 C.POINTER(_i32), C.POINTER(C.c_double)]),
     ("qdg_expec_position", _i32, [_vp, _vp, _i32, C.c_double, C.POINTER(C.c_double)]),
     ("qdg_expec_momentum", _i32, [_vp, _vp, _i32, C.c_double, C.POINTER(C.c_double)]),
     ("qdg_expec_kinetic", _i32, [_vp, _vp, C.POINTER(C.c_double)]),

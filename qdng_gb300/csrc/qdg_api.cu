@@ -2728,6 +2728,118 @@ qdg_status qdg_eigen_autocorr(qdg_prop *P, const double *psi_init, int32_t nstep
   return cleanup(QDG_OK);
 }
 
+// ProgEigen::LanczosEF (src/ProgEigen.cpp:604-648) with DiagBasis
+// (ProgEigen.cpp:94-138): the Arnoldi basis of psi_init (OArnoldi::BuildLZB,
+// the propagator's own basis build), the Ritz pairs of its Hessenberg
+// matrix, the Ritz functions sum_j z_ji v_j, then the Hamiltonian in that
+// basis diagonalised.  For a hermitian H the Hessenberg matrix is real
+// symmetric tridiagonal up to rounding, so its symmetric part is
+// diagonalised by Jacobi rotations in place of LAPACK's zhseqr/zhsein; each
+// eigenvector is scaled as zhsein scales it (largest component of modulus
+// 1), which DiagBasis sees through its off-diagonal matrix elements.
+extern "C++" {
+template <typename T>
+qdg_status eigen_lanczos(qdg_prop *P, const double *psi_init, int max_nef, double *e_raw, double *e_diag,
+                         int32_t *nef_out, double *efs) {
+  qdg_plan *p = P->plan;
+  const long long n = wf_elems(p);
+  const size_t wbytes = sizeof(cplx<double>) * (size_t)n;
+  const int m = P->kord;
+  if (m > qdg::kMaxKrylov) return fail(QDG_EUNSUPPORTED, "Krylov order above 64");
+  std::vector<cplx<double> *> bufs;
+  auto cleanup = [&](qdg_status st) {
+    cudaStreamSynchronize(p->stream);
+    for (auto *b : bufs) cudaFree(b);
+    return st;
+  };
+  auto alloc = [&]() -> cplx<double> * {
+    cplx<double> *b = nullptr;
+    if (cudaMalloc(&b, wbytes) != cudaSuccess) return nullptr;
+    bufs.push_back(b);
+    return b;
+  };
+  cplx<double> *psi = alloc();
+  if (!psi) return cleanup(fail(QDG_ENOMEM, "device allocation failed"));
+  qdg_status s;
+  std::vector<cd> d;
+#define ECHK(expr) do { if ((s = (expr)) != QDG_OK) return cleanup(s); } while (0)
+#define ECUDA(expr) do { if ((expr) != cudaSuccess) return cleanup(fail(QDG_ECUDA, #expr)); } while (0)
+  ECUDA(cudaMemcpyAsync(psi, psi_init, wbytes, cudaMemcpyHostToDevice, p->stream));
+  ECUDA(qdg::launch_set_coefs(p->d_coef, p->d_cp, p->d_lasers, p->laser_nt, 0, p->stream));
+  // the basis of the propagator's step (OArnoldi::BuildLZB: lzb[0] = psi);
+  // psi itself is left as it is
+  ECHK(arnoldi_body<T>(P, psi));
+  ECUDA(cudaStreamSynchronize(p->stream));
+  const int order = *P->h_kdone;
+  const double *H = P->h_ks;
+  if (!std::isfinite(H[2 * m * m])) return cleanup(fail(QDG_ENONFINITE, "Norm is not a number"));
+  std::vector<double> A((size_t)order * order), w, z;
+  for (int i = 0; i < order; ++i)
+    for (int j = 0; j < order; ++j)
+      A[(size_t)i * order + j] = 0.5 * (H[2 * (i * m + j)] + H[2 * (j * m + i)]);
+  qdg::host::sym_eig(order, A, w, z);
+  const int K = std::min(order, max_nef);
+  *nef_out = order;
+  // Ritz functions
+  std::vector<cplx<double> *> rf(order, nullptr);
+  for (int i = 0; i < order; ++i) {
+    if (!(rf[i] = alloc())) return cleanup(fail(QDG_ENOMEM, "device allocation failed"));
+    double zmax = 0;
+    for (int j = 0; j < order; ++j) zmax = std::max(zmax, std::fabs(z[(size_t)j * order + i]));
+    qdg::KCombine<T> kc;
+    memset(&kc, 0, sizeof(kc));
+    kc.m = order;
+    for (int j = 0; j < order; ++j) {
+      kc.c[j] = cplx<double>{z[(size_t)j * order + i] / zmax, 0.0};
+      kc.q[j] = reinterpret_cast<const cplx<T> *>(P->lzb[j]);
+    }
+    // kcombine forms rf c_0 + sum_{j >= 1} c_j q_j: rf starts as v_0 = psi
+    ECUDA(cudaMemcpyAsync(rf[i], psi, wbytes, cudaMemcpyDeviceToDevice, p->stream));
+    ECUDA(qdg::launch_kcombine<T>(rf[i], kc, n, p->stream));
+  }
+  // DiagBasis: S(j, i) = Re <f_i|H|f_j> for j < i, S(i, i) = the Ritz value
+  std::vector<double> Sm((size_t)order * order, 0.0), wd, zd;
+  for (int i = 0; i < order; ++i) {
+    for (int j = 0; j < i; ++j) {
+      cd e;
+      ECHK(h_expec(p, rf[i], rf[j], &e));
+      Sm[(size_t)j * order + i] = Sm[(size_t)i * order + j] = e.real();
+    }
+    Sm[(size_t)i * order + i] = w[i];
+  }
+  qdg::host::sym_eig(order, Sm, wd, zd);
+  for (int k = 0; k < K; ++k) {
+    e_raw[k] = w[k];
+    e_diag[k] = wd[k];
+  }
+  if (efs) {
+    cplx<double> *out = alloc();
+    if (!out) return cleanup(fail(QDG_ENOMEM, "device allocation failed"));
+    for (int k = 0; k < K; ++k) {
+      ECUDA(cudaMemsetAsync(out, 0, wbytes, p->stream));
+      for (int j = 0; j < order; ++j)
+        ECUDA(qdg::launch_lincomb<double>(out, rf[j], cplx<double>{1, 0}, cplx<double>{zd[(size_t)j * order + k], 0},
+                                          n, p->stream));
+      ECUDA(cudaMemcpyAsync(efs + 2 * (size_t)k * n, out, wbytes, cudaMemcpyDeviceToHost, p->stream));
+    }
+  }
+#undef ECHK
+#undef ECUDA
+  return cleanup(QDG_OK);
+}
+}  // extern "C++"
+
+qdg_status qdg_eigen_lanczos(qdg_prop *P, const double *psi_init, int32_t max_nef, double *e_raw, double *e_diag,
+                             int32_t *nef_out, double *efs) {
+  if (!P || !psi_init || max_nef < 0 || !nef_out || (max_nef > 0 && (!e_raw || !e_diag)))
+    return fail(QDG_EINVAL, "bad arguments");
+  if (!P->inited) return fail(QDG_EINVAL, "propagator not initialised");
+  if (P->kind != 4) return fail(QDG_EINVAL, "Arnoldi Propagator is needed to find Lanczos Eigenvalues");
+  sync_twin(P);
+  if (is64(P->plan)) return eigen_lanczos<double>(P, psi_init, max_nef, e_raw, e_diag, nef_out, efs);
+  return eigen_lanczos<float>(P, psi_init, max_nef, e_raw, e_diag, nef_out, efs);
+}
+
 qdg_status qdg_prop_run(qdg_prop *P, qdg_wf *psi, int64_t step0, int32_t nsteps, int64_t *terms_total) {
   if (!P || !psi || psi->plan != P->user || nsteps < 0) return fail(QDG_EINVAL, "bad arguments");
   sync_twin(P);

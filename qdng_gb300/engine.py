@@ -232,6 +232,18 @@ class Propagator:
         k = min(nef.value, max_nef)
         return e[:k], (efs[:k] if efs is not None else None), spec, nef.value
 
+    def eigen_lanczos(self, psi_init, max_nef=64, want_efs=True):
+        """ProgEigen::LanczosEF + DiagBasis: (e_raw, e_diag, efs or None, basis size)."""
+        n = self.plan.S * self.plan.npts
+        x = np.ascontiguousarray(psi_init, dtype=np.complex128).reshape(-1)
+        er, ed = np.zeros(max(max_nef, 1)), np.zeros(max(max_nef, 1))
+        efs = np.zeros((max(max_nef, 1), n), dtype=np.complex128) if want_efs else None
+        nef = C.c_int32(0)
+        check(self.lib.qdg_eigen_lanczos(self.h, _dp(x), max_nef, _dp(er), _dp(ed), C.byref(nef),
+                                         _dp(efs) if efs is not None else None))
+        k = min(nef.value, max_nef)
+        return er[:k], ed[:k], (efs[:k] if efs is not None else None), nef.value
+
     def run(self, wf, step0, nsteps):
         tot = C.c_int64(0)
         check(self.lib.qdg_prop_run(self.h, wf.h, step0, nsteps, C.byref(tot)))

@@ -121,3 +121,31 @@ def test_autocorr_2d_double_well(eng):
     e, _, _, npk = P.eigen_autocorr(psi, 512, tol=2.0, width=8, max_nef=12)
     assert npk == npk_o and npk > 0
     np.testing.assert_allclose(e, e_o, rtol=1e-9)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_lanczos_matches_oracle(eng, fixtures, precision):
+    """ProgEigen::LanczosEF on the GPU (the Arnoldi propagator's basis build,
+    Ritz pairs, DiagBasis) against the oracle (a mixed plan builds the Krylov
+    basis on its binary64 copy).  Fifteen modified Gram-Schmidt vectors lose
+    orthogonality, and the Ritz values of two binary64 implementations part
+    at 1e-7 relative for the upper ones (the low ones to 1e-9): the basis
+    size, the six lowest Ritz values to 1e-8, all to 1e-6, DiagBasis equal to
+    the Ritz values, and the three lowest functions to 1e-6 up to sign."""
+    hp, psi, run = cases.tge(fixtures, "Arnoldi")
+    S = O.System(hp)
+    Qi = O.Propagator(S, "Cheby", "", dt=5.0, imaginary_time=True, backward=True)
+    efs, _, _, _ = Qi.eigen_imag(psi, run["nef"], run["steps"], run["conv"], diag=True)
+    lc = cases._normalize(hp, efs[:6].sum(axis=0))
+    Q = O.Propagator(S, "Arnoldi", run["params"], dt=run["dt"])
+    er_o, ed_o, ef_o, nb_o = Q.eigen_lanczos(lc)
+    plan = eng.Plan(hp, precision)
+    P = eng.Propagator(plan, "Arnoldi", run["params"], dt=run["dt"])
+    er, ed, ef, nb = P.eigen_lanczos(lc)
+    assert nb == nb_o
+    np.testing.assert_allclose(er[:6], er_o[:6], rtol=1e-8)
+    np.testing.assert_allclose(er, er_o, rtol=1e-6)
+    np.testing.assert_allclose(ed, er, rtol=1e-12, atol=1e-15)
+    for i in range(3):
+        s = np.sign(np.vdot(ef_o[i], ef[i]).real)
+        assert np.abs(s * ef[i] - ef_o[i]).max() <= 1e-6 * np.abs(ef_o[i]).max(), i

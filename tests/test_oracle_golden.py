@@ -231,3 +231,23 @@ def test_tge_autocorr(fixtures, golden, method):
     for i, txt in golden["tge_ac"]:
         dec = len(txt.split(".")[1])
         assert abs(e[i] - float(txt)) < 1.5 * 10 ** (-dec), (method, i, e[i], txt)
+
+
+def test_lanczos_eigen_driver(fixtures, golden):
+    """ProgEigen::LanczosEF with the TGE Arnoldi propagator (order 15) on the
+    normalised sum of six imaginary-time eigenfunctions: the Ritz values
+    approach the golden eigenenergies (the ground state to the golden's
+    digits, the others to the accuracy of the relaxed functions), and
+    DiagBasis leaves them (the Ritz functions are H-orthogonal)."""
+    hp, psi, run = cases.tge(fixtures, "Arnoldi")
+    S = O.System(hp)
+    Pi = O.Propagator(S, "Cheby", "", dt=5.0, imaginary_time=True, backward=True)
+    efs, _, _, _ = Pi.eigen_imag(psi, run["nef"], run["steps"], run["conv"], diag=True)
+    lc = cases._normalize(hp, efs[:6].sum(axis=0))
+    P = O.Propagator(S, "Arnoldi", run["params"], dt=run["dt"])
+    er, ed, ef, nb = P.eigen_lanczos(lc)
+    assert nb == 15
+    np.testing.assert_allclose(ed, er, rtol=1e-12, atol=1e-15)
+    gold = [float(t) for _, t in golden["tge_imag"][:6]]
+    assert abs(er[0] - gold[0]) < 1.5e-7
+    np.testing.assert_allclose(er[:6], gold, rtol=2e-3)
