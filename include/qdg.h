@@ -50,16 +50,25 @@ typedef enum qdg_status {
 
 /* Hamiltonian term kinds (one per QDng operator class on the path). */
 typedef enum qdg_term_kind {
-  QDG_TERM_KINETIC = 1,    /* OGridNablaSq: -1/(2m) Laplacian via FFT (src/qdlib/OGridNablaSq.cpp:28-111) */
+  QDG_TERM_KINETIC = 1,    /* OGridNablaSq: -1/(2m) Laplacian via FFT, or by finite differences with
+                              fd_order (src/qdlib/OGridNablaSq.cpp:28-111) */
   QDG_TERM_POTENTIAL = 2,  /* OGridPotential: V(x) psi (src/qdlib/OGridPotential.cpp:134-142) */
   QDG_TERM_DIPOLE = 3,     /* OGridDipole: -mu(x) E(t) psi (src/qdlib/OGridDipole.cpp:46-60) */
   QDG_TERM_NAC = 4,        /* OGridNAC: sign/(2 mass) sum_d [f_d d/dx_d psi + d/dx_d (f_d psi)]
                               (src/qdlib/OGridNAC.cpp:131-148), derivatives by FFT (OGridNabla.cpp:76-95) */
-  QDG_TERM_GOBBLER = 5     /* OGobbler (src/qdlib/OGobbler.cpp:30-84,176-204): a diagonal grid term W(x)
+  QDG_TERM_GOBBLER = 5,    /* OGobbler (src/qdlib/OGobbler.cpp:30-84,176-204): a diagonal grid term W(x)
                               = gain x (product of Butterworth filters); laser = 1 makes it a negative
                               imaginary potential, H psi += -i W psi (nip="true"), else H psi += W psi;
                               mass[0] = gain (Emax = gain, Emin = -i gain with nip, else 0).
                               Not a member type of GSPO (OGSPO.cpp:71-85 needs ODSpace operators). */
+  QDG_TERM_GMAT = 6        /* OGridGMat (src/qdlib/OGridGMat.cpp:307-386): -1/2 sum_ij d/dx_j G_ij(x) d/dx_i,
+                              first derivatives by FFT (Diff.cpp:223-272); diagonal only.  grid = index of
+                              the first of ndims (ndims + 1) / 2 grid arrays G_ij, lower triangle row by
+                              row ((0,0), (1,0), (1,1), (2,0), ...); flags holds two bits per element k =
+                              i (i + 1) / 2 + j: 0 = no element ("x" in Gdef, or coup="false" off the
+                              diagonal), 1 = a grid, 2 = a constant (its grid array holds the constant;
+                              Emax and Emin then follow OGridGMat.cpp:250-305 for constants).
+                              Not a member type of GSPO (not an ODSpace operator). */
 } qdg_term_kind;
 
 /* Arithmetic of a plan.  FP64 is the drop-in form: every value (psi, phi_n,
@@ -104,6 +113,11 @@ typedef struct qdg_hterm {
   double mass[QDG_MAX_DIMS];     /* KINETIC: masses per dimension, all > 0;
                                     NAC: mass[0] = the reduced mass (1 for N-D, OGridNAC.cpp:83-85) */
   double sign;                   /* NAC: sign of the element (+1 or -1; 0 means the default +1) */
+  int32_t fd_order;              /* KINETIC: 0 = FFT (OGridNablaSq method="FFT"); an even order 2..50 =
+                                    central finite differences (method="HOFD", Diff.cpp:203-218 ->
+                                    HOFD::Diff over all dimensions, src/qdlib/HOFD.h:124-176) */
+  int32_t flags;                 /* KINETIC with fd_order: 1 = periodic boundaries (pbc="true"; grids
+                                    of one dimension only); GMAT: the element sources (see above) */
 } qdg_hterm;
 
 typedef struct qdg_hplan_desc {

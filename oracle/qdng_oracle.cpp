@@ -353,6 +353,9 @@ static bool term_at(const System &s, const qdg_hterm &t, int i, int j) {
   return (t.row == i && t.col == j) || (s.hermitian && t.row != t.col && t.row == j && t.col == i);
 }
 
+static double gmat_emax(const System &s, const qdg_hterm &t);
+static double gmat_emin(const System &s, const qdg_hterm &t);
+
 /* Emax/Emin of one operator: OGridNablaSq.cpp:89-106, OGridPotential.cpp:124-132, OGridDipole.cpp:36-44. */
 static cd term_emax(const System &s, const qdg_hterm &t) {
   if (t.kind == QDG_TERM_KINETIC) {
@@ -362,6 +365,7 @@ static cd term_emax(const System &s, const qdg_hterm &t) {
     return T;
   }
   if (t.kind == QDG_TERM_POTENTIAL) return vec_max(s.grids[t.grid]);
+  if (t.kind == QDG_TERM_GMAT) return gmat_emax(s, t);
   if (t.kind == QDG_TERM_GOBBLER) return t.mass[0];  /* OGobbler::Emax = gain (OGobbler.cpp:161-164) */
   if (t.kind == QDG_TERM_NAC) {  /* OGridNAC::Emax (OGridNAC.cpp:105-115): dx of dim 0 */
     double m = 0;
@@ -374,6 +378,7 @@ static cd term_emax(const System &s, const qdg_hterm &t) {
  * returns 0; that is kept. */
 static cd term_emin(const System &s, const qdg_hterm &t) {
   if (t.kind == QDG_TERM_POTENTIAL) return vec_min(s.grids[t.grid]);
+  if (t.kind == QDG_TERM_GMAT) return gmat_emin(s, t);
   /* OGobbler::Emin (OGobbler.cpp:166-170): -i gain as negative imaginary potential */
   if (t.kind == QDG_TERM_GOBBLER) return t.laser == 1 ? cd(0, -t.mass[0]) : cd(0);
   return 0.0;
@@ -440,6 +445,183 @@ static void nac_apply(const System &s, const qdg_hterm &t, const cd *x, cd *o) {
   for (long p = 0; p < N; ++p) o[p] += acc[p];
 }
 
+/* Central finite-difference weights in the layout of QDng's HOFD table
+ * (HOFD.h:31-36, filled from cfd_table_1.h / cfd_table_2.h at HOFD.h:99-103):
+ * cf[o2] weighs the point itself and cf[o2 - k] the neighbours at distance k
+ * (for the first derivative cf is the lower neighbour's weight and the upper
+ * one gets -cf).  The oracle does not read that table: it evaluates the
+ * closed form of the central-difference weights on 2 o2 + 1 points
+ * (B. Fornberg, Math. Comp. 51 (1988) 699-706), with r_k = (o2!)^2 /
+ * ((o2 - k)! (o2 + k)!):
+ *   second derivative  w_k = 2 (-1)^(k+1) r_k / k^2,  w_0 = -2 sum_k 1/k^2
+ *   first derivative   w_+k = (-1)^(k+1) r_k / k,     w_0 = 0. */
+static void fd_weights(int deriv, int order, std::vector<double> &cf) {
+  const int o2 = order / 2;
+  cf.assign(o2 + 1, 0.0);
+  long double r = 1, c0 = 0;
+  for (int k = 1; k <= o2; ++k) {
+    r *= (long double)(o2 - k + 1) / (long double)(o2 + k);
+    const long double sg = (k % 2) ? 1.0L : -1.0L;
+    if (deriv == 2) {
+      cf[o2 - k] = (double)(2.0L * sg * r / ((long double)k * k));
+      c0 += 1.0L / ((long double)k * k);
+    } else {
+      cf[o2 - k] = (double)(-sg * r / (long double)k);
+    }
+  }
+  cf[o2] = deriv == 2 ? (double)(-2.0L * c0) : 0.0;
+}
+
+/* OGridNablaSq with method="HOFD": Diff::DnDxn (Diff.cpp:203-218) sets the
+ * scalar factor to 1 and calls HOFD::Diff over all dimensions
+ * (HOFD.h:124-176) with the per-dimension factors -1/(2 m_d)
+ * (OGridNablaSq.cpp:47-52), h_d = 1/dx_d^2 * 1 * (-1/(2 m_d)).  The neighbour
+ * rules are the reference's, for every point i (flat index, dim 0 fastest),
+ * dimension d with stride lo and size N, and lrep = i / N:
+ *   above: i + k lo while (i + k lo) / N == lrep;
+ *   below: (N + i - k lo) mod N while (N + k lo) / N == lrep + 1;
+ *   pbc:   (i + k lo) mod N and (N + i - k lo) mod N for every k.
+ * On a one-dimensional grid that is: neighbours above the grid are dropped,
+ * those below it wrap around to its top end (or periodic with pbc).  With
+ * more dimensions the rule is not a per-dimension Laplacian, and it is
+ * reproduced as it stands: every index it forms is inside the grid (pbc is
+ * one-dimensional only: the reference's pbc index can leave the grid there). */
+static void fd_apply(const System &s, const qdg_hterm &t, const cd *x, cd *o) {
+  std::vector<double> cf;
+  fd_weights(2, t.fd_order, cf);
+  const int o2 = t.fd_order / 2;
+  const bool pbc = (t.flags & 1) != 0;
+  const double df = 1;  /* even derivative (HOFD.h:130-131) */
+  const int nd = s.g.ndims;
+  double h[QDG_MAX_DIMS];
+  int lo[QDG_MAX_DIMS];
+  int stride = 1;
+  for (int d = 0; d < nd; ++d) {
+    h[d] = 1. / (s.dx[d] * s.dx[d]) * 1.0 * (-1. / 2. / t.mass[d]);
+    lo[d] = stride;
+    stride *= s.g.n[d];
+  }
+  const int np = (int)s.npts;
+  #pragma omp parallel for schedule(static) if (np >= 8192)
+  for (int i = 0; i < np; ++i) {
+    cd D = 0;
+    for (int d = 0; d < nd; ++d) {
+      const int N = s.g.n[d], l = lo[d];
+      const int lrep = i / N;
+      cd v = cf[o2] * x[i];
+      if (pbc) {
+        int step = l;
+        for (int j = o2 - 1; j >= 0; --j) {
+          v += df * cf[j] * x[(i + step) % N];
+          v += cf[j] * x[(N + i - step) % N];
+          step += l;
+        }
+      } else {
+        int step = i + l;
+        for (int j = o2 - 1; j >= 0 && step / N == lrep; --j) {
+          v += df * cf[j] * x[step];
+          step += l;
+        }
+        step = i - l;
+        for (int j = o2 - 1; j >= 0 && (N + i - step) / N == lrep + 1; --j) {
+          v += cf[j] * x[(N + step) % N];
+          step -= l;
+        }
+      }
+      D += h[d] * v;
+    }
+    o[i] += D;
+  }
+}
+
+/* Source of G-matrix element (i, j), i >= j: 0 none, 1 grid, 2 constant. */
+static int gmat_src(const qdg_hterm &t, int i, int j) {
+  if (i < j) std::swap(i, j);
+  return (t.flags >> (2 * (i * (i + 1) / 2 + j))) & 3;
+}
+static const std::vector<double> &gmat_grid(const System &s, const qdg_hterm &t, int i, int j) {
+  if (i < j) std::swap(i, j);
+  return s.grids[t.grid + i * (i + 1) / 2 + j];
+}
+
+/* OGridGMat::Emax (OGridGMat.cpp:250-284): pi^2/2 sum over the lower
+ * triangle; a constant off-diagonal element enters without 1/(dx_i dx_j). */
+static double gmat_emax(const System &s, const qdg_hterm &t) {
+  double T = 0;
+  for (int i = 0; i < s.g.ndims; ++i)
+    for (int j = 0; j <= i; ++j) {
+      const int src = gmat_src(t, i, j);
+      if (i != j) {
+        double mx = 0, mn = 0;
+        if (src == 1) {
+          mx = vec_max(gmat_grid(s, t, i, j)) / (s.dx[i] * s.dx[j]);
+          mn = vec_min(gmat_grid(s, t, i, j)) / (s.dx[i] * s.dx[j]);
+        } else if (src == 2) {
+          mx = mn = gmat_grid(s, t, i, j)[0];
+        }
+        if (mn < 0 && std::fabs(mn) > std::fabs(mx)) T += 2 * std::fabs(mn);
+        else T += 2 * mx;
+      } else if (src == 1) {
+        T += vec_max(gmat_grid(s, t, i, j)) / (s.dx[i] * s.dx[j]);
+      } else if (src == 2) {
+        T += gmat_grid(s, t, i, j)[0] / (s.dx[i] * s.dx[j]);
+      }
+    }
+  return T * (M_PI * M_PI / 2);
+}
+/* OGridGMat::Emin (OGridGMat.cpp:286-305): negative off-diagonal minima only. */
+static double gmat_emin(const System &s, const qdg_hterm &t) {
+  double T = 0;
+  for (int i = 0; i < s.g.ndims; ++i)
+    for (int j = 0; j < i; ++j) {
+      const int src = gmat_src(t, i, j);
+      double mn = 0;
+      if (src == 1) mn = vec_min(gmat_grid(s, t, i, j)) / (s.dx[i] * s.dx[j]);
+      else if (src == 2) mn = gmat_grid(s, t, i, j)[0];
+      if (mn < 0) T += mn;
+    }
+  return T;
+}
+
+/* one FFT derivative along d times fac: Diff::DnDxn / DnDxnAdd with method
+ * FFT (Diff.cpp:223-272), as the full transform with k_d (the oracle's
+ * transform is N-dimensional; k_d depends on the index along d only) */
+static void fft_ddx(const System &s, int d, double fac, std::vector<cd> &b) {
+  std::vector<double> k;
+  kspace_ddx(s, d, 1.0, k);
+  const double f = fac / double(s.npts);
+  s.fft.exec(b.data(), -1);
+  for (long p = 0; p < s.npts; ++p) b[p] = b[p] * (k[p] * cd(0, 1)) * f;
+  s.fft.exec(b.data(), +1);
+}
+
+/* OGridGMat::ApplyAdd (OGridGMat.cpp:313-386) without chain rule and PML:
+ * for every i, w_i = d/dx_i psi; for every j with an element, a grid element
+ * adds d/dx_j (G_ij w_i) times -1/2, a constant one d/dx_j w_i times
+ * -G_ij / 2. */
+static void gmat_apply(const System &s, const qdg_hterm &t, const cd *x, cd *o) {
+  const long N = s.npts;
+  std::vector<cd> w(N), b(N), acc(N, 0.0);
+  for (int i = 0; i < s.g.ndims; ++i) {
+    for (long p = 0; p < N; ++p) w[p] = x[p];
+    fft_ddx(s, i, 1.0, w);
+    for (int j = 0; j < s.g.ndims; ++j) {
+      const int src = gmat_src(t, i, j);
+      if (src == 0) continue;
+      const std::vector<double> &g = gmat_grid(s, t, i, j);
+      if (src == 1) {
+        for (long p = 0; p < N; ++p) b[p] = w[p] * g[p];
+        fft_ddx(s, j, -0.5, b);
+      } else {
+        for (long p = 0; p < N; ++p) b[p] = w[p];
+        fft_ddx(s, j, -0.5 * g[0], b);
+      }
+      for (long p = 0; p < N; ++p) acc[p] += b[p];
+    }
+  }
+  for (long p = 0; p < N; ++p) o[p] += acc[p];
+}
+
 /* H psi: OMultistate::Apply (OMultistate.cpp:206-231) over OSum::Apply/ApplyAdd
  * (OSum.cpp:53-60); kinetic via Diff::DnDxn (Diff.cpp:203-218); potential
  * MultElementsAdd (OGridPotential.cpp:139-142); dipole with -E(step)
@@ -461,6 +643,10 @@ static void h_apply(const System &s, const cd *in, cd *out, long step) {
           /* elementwise codelets are OpenMP loops in the reference (src/math/codelets) */
           if (t.kind == QDG_TERM_NAC) {
             nac_apply(s, t, x, o);
+          } else if (t.kind == QDG_TERM_GMAT) {
+            gmat_apply(s, t, x, o);
+          } else if (kin && t.fd_order > 0) {
+            fd_apply(s, t, x, o);
           } else if (kin) {
             cd *b = buf.data();
             #pragma omp parallel for schedule(static) if (N >= 8192)
@@ -683,6 +869,10 @@ static int gspo_init(Prop &p) {
     bool any = false, kin = false, pot = false;
     for (auto &t : s.terms) if (t.group == g) { any = true; if (t.kind == QDG_TERM_KINETIC) kin = true; else pot = true; }
     if (!any) return fail(QDG_EINVAL, "GSPO misses an operator. Sequence must be A, B, C, ...");
+    /* OGridGMat is no ODSpace; OGridNablaSq with method HOFD has no k-space table (Diff.cpp:52-54) */
+    for (auto &t : s.terms)
+      if (t.group == g && (t.kind == QDG_TERM_GMAT || (t.kind == QDG_TERM_KINETIC && t.fd_order > 0)))
+        return fail(QDG_EUNSUPPORTED, "GSPO members need a diagonal representation (no HOFD, no GridGMat)");
     if (kin && pot) return fail(QDG_EUNSUPPORTED, "GSPO: Operator has no diagonal representation");
     if (kin) for (int st = 0; st < s.S; ++st) {
       int c = 0; for (auto &t : s.terms) if (t.group == g && t.kind == QDG_TERM_KINETIC && t.row == st) ++c;
@@ -1034,6 +1224,30 @@ double orc_expec_momentum(void *sp, const double *psi_, int dim, double factor) 
 /* the kinetic terms (OGridNablaSq) of the system, each on its own state */
 double orc_expec_kinetic(void *sp, const double *psi_) {
   const System &s = *static_cast<System *>(sp);
+  bool direct = false;
+  for (auto &t : s.terms)
+    if (t.kind == QDG_TERM_GMAT || (t.kind == QDG_TERM_KINETIC && t.fd_order > 0)) direct = true;
+  if (direct) {
+    /* finite differences and the G-matrix have no k-space table:
+     * <psi|T psi> / <psi|psi> from the operator applied on each state */
+    const cd *psi = reinterpret_cast<const cd *>(psi_);
+    std::vector<cd> tp(s.npts);
+    CSum num, den;
+    for (int st = 0; st < s.S; ++st) {
+      const cd *x = psi + st * s.npts;
+      std::fill(tp.begin(), tp.end(), cd(0));
+      for (auto &t : s.terms) {
+        if (t.row != st || t.col != st) continue;
+        if (t.kind == QDG_TERM_GMAT) gmat_apply(s, t, x, tp.data());
+        else if (t.kind == QDG_TERM_KINETIC) fd_apply(s, t, x, tp.data());
+      }
+      for (long p = 0; p < s.npts; ++p) {
+        num.add((std::conj(x[p]) * tp[p]).real());
+        den.add(std::norm(x[p]));
+      }
+    }
+    return num.get() / den.get();
+  }
   std::vector<std::vector<double>> tabs(s.S, std::vector<double>(s.npts, 0.0));
   size_t kt = 0;
   for (auto &t : s.terms)

@@ -27,6 +27,7 @@ TERM_POTENTIAL = 2
 TERM_DIPOLE = 3
 TERM_NAC = 4
 TERM_GOBBLER = 5
+TERM_GMAT = 6
 
 PREC_FP64 = 0
 PREC_MIXED = 1
@@ -52,6 +53,8 @@ class HTerm(C.Structure):
         ("group", C.c_int32),
         ("mass", C.c_double * QDG_MAX_DIMS),
         ("sign", C.c_double),
+        ("fd_order", C.c_int32),
+        ("flags", C.c_int32),
     ]
 
 

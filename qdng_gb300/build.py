@@ -26,7 +26,7 @@ SOURCES = ["qdg_kernels.cu", "qdg_persistent.cu", "qdg_api.cu", "qdg_noalloc.cu"
            # expectation values of filter operators
            "qdg_filters.cu",
            # the autocorrelation eigen driver
-           "qdg_eigen_ac.cu"]
+           "qdg_eigen_ac.cu", "qdg_fdkin.cu"]
 
 
 def nvcc():

@@ -48,6 +48,8 @@ namespace {
 
 cplx<double> C(cd z) { cplx<double> c; c.re = z.real(); c.im = z.imag(); return c; }
 
+enum { KIN_FFT = 0, KIN_FD = 1, KIN_GMAT = 2 };
+
 // Per-dimension line geometry and FFT tables.
 struct DimInfo {
   int n;
@@ -83,6 +85,15 @@ struct qdg_plan {
   size_t nac_smem = 0;
   int nac_per_sm = 1;
   int nac_tw[QDG_MAX_DIMS] = {1, 1, 1, 1};
+  // Kinetic operators without a k-space table: OGridNablaSq with method
+  // HOFD (finite differences) or OGridGMat.  Either replaces the FFT kinetic
+  // pass of the graph path; the fused step kernels do not take them.
+  int kin_form = 0;                               // KIN_FFT, KIN_FD or KIN_GMAT
+  int fd_order = 0, fd_pbc = 0;
+  double fd_h[qdg::kMaxStates][4] = {};           // -1/(2 m_d) / dx_d^2 per state, summed over terms
+  long long gm_base[qdg::kMaxStates];             // first G grid of each state, -1 = none
+  unsigned gm_mask[qdg::kMaxStates] = {};
+  int gm_grid = 1;
   // device
   void *d_grids = nullptr;      // bulk type
   void *d_grids_df = nullptr;   // DF64 plans: the grids in double-float
@@ -226,10 +237,58 @@ void parse_params(const char *s, std::map<std::string, std::string> &out) {
 }
 
 // ------------------------------------------------------ energy range
-// Emax/Emin of one operator (OGridNablaSq.cpp:89-106, OGridPotential.cpp:124-132,
-// OGridDipole.cpp:36-44).
+// G-matrix element (i, j) of a GMAT term: its source code (0 none, 1 grid,
+// 2 constant) and its grid values (lower triangle, row by row).
+int gmat_code(const qdg_hterm &t, int i, int j) {
+  if (i < j) std::swap(i, j);
+  return (t.flags >> (2 * (i * (i + 1) / 2 + j))) & 3;
+}
+const double *gmat_values(const qdg_plan *p, const qdg_hterm &t, int i, int j) {
+  if (i < j) std::swap(i, j);
+  return p->grids_h.data() + (long long)(t.grid + i * (i + 1) / 2 + j) * p->npts;
+}
+
+// OGridGMat::Emax (OGridGMat.cpp:250-284): pi^2/2 times the diagonal maxima
+// over dx_i^2 plus twice the larger of the off-diagonal maximum and |minimum|
+// over dx_i dx_j; a constant off-diagonal element enters as it is.
+double gmat_emax(const qdg_plan *p, const qdg_hterm &t) {
+  const long long n = p->npts;
+  double T = 0;
+  for (int i = 0; i < p->nd; ++i)
+    for (int j = 0; j <= i; ++j) {
+      const int c = gmat_code(t, i, j);
+      if (c == 0) continue;
+      const double *g = gmat_values(p, t, i, j);
+      const double hx = p->dx[i] * p->dx[j];
+      if (i != j) {
+        const double mx = c == 1 ? *std::max_element(g, g + n) / hx : g[0];
+        const double mn = c == 1 ? *std::min_element(g, g + n) / hx : g[0];
+        T += (mn < 0 && std::fabs(mn) > std::fabs(mx)) ? 2 * std::fabs(mn) : 2 * mx;
+      } else {
+        T += (c == 1 ? *std::max_element(g, g + n) : g[0]) / hx;
+      }
+    }
+  return T * (M_PI * M_PI / 2);
+}
+// OGridGMat::Emin (OGridGMat.cpp:286-305): the negative off-diagonal minima.
+double gmat_emin(const qdg_plan *p, const qdg_hterm &t) {
+  double T = 0;
+  for (int i = 0; i < p->nd; ++i)
+    for (int j = 0; j < i; ++j) {
+      const int c = gmat_code(t, i, j);
+      if (c == 0) continue;
+      const double *g = gmat_values(p, t, i, j);
+      const double mn = c == 1 ? *std::min_element(g, g + p->npts) / (p->dx[i] * p->dx[j]) : g[0];
+      if (mn < 0) T += mn;
+    }
+  return T;
+}
+
+// Emax/Emin of one operator (OGridNablaSq.cpp:89-106 for either method,
+// OGridPotential.cpp:124-132, OGridDipole.cpp:36-44).
 cd term_emax(const qdg_plan *p, const qdg_hterm &t) {
   const long long n = p->npts;
+  if (t.kind == QDG_TERM_GMAT) return gmat_emax(p, t);
   if (t.kind == QDG_TERM_KINETIC) {
     double T = 0;
     for (int d = 0; d < p->nd; ++d)
@@ -253,6 +312,7 @@ cd term_emax(const qdg_plan *p, const qdg_hterm &t) {
 cd term_emin(const qdg_plan *p, const qdg_hterm &t) {
   // OGobbler::Emin (OGobbler.cpp:166-170): -i gain as a negative imaginary potential, else 0
   if (t.kind == QDG_TERM_GOBBLER) return t.laser == 1 ? cd(0.0, -t.mass[0]) : cd(0.0);
+  if (t.kind == QDG_TERM_GMAT) return gmat_emin(p, t);
   if (t.kind != QDG_TERM_POTENTIAL) return 0.0;
   const double *g = p->grids_h.data() + (long long)t.grid * p->npts;
   return *std::min_element(g, g + p->npts);
@@ -436,8 +496,117 @@ qdg_status run_nac(qdg_plan *p, const cplx<T> *phi, const Epi &e) {
   return QDG_OK;
 }
 
+// The point-wise pass of an H application on grids with more than one
+// dimension (or extra line passes): H phi = sum of the nP kinetic partial
+// results + the potential matrix, then the series epilogue.
+template <typename T>
+qdg_status run_combine(qdg_plan *p, int final_mode, const cplx<T> *phi, const Epi &e, int nP) {
+  qdg::CombArgs<T> c;
+  memset(&c, 0, sizeof(c));
+  c.S = p->S;
+  c.nd = nP;
+  c.npts = p->npts;
+  c.phi = phi;
+  for (int d = 0; d < nP; ++d) c.P[d] = reinterpret_cast<const cplx<T> *>(p->d_Pd[d]);
+  c.out = reinterpret_cast<cplx<T> *>(e.out);
+  c.psi = e.psi;
+  c.k0 = reinterpret_cast<cplx<T> *>(e.k0);
+  c.cp = p->d_cp;
+  c.coef = p->d_coef;
+  c.grids = reinterpret_cast<const T *>(p->d_grids);
+  c.offset = C(e.offset); c.fac = C(e.fac); c.fac_lo = C(e.fac_lo); c.c0p = C(e.c0p); c.c1p = C(e.c1p); c.coeff = C(e.coeff);
+  c.imag = e.imag;
+  c.partials = p->d_partials;
+  c.cut = e.cut;
+  c.bufs[0] = reinterpret_cast<const cplx<T> *>(e.bufs[0]);
+  c.bufs[1] = reinterpret_cast<const cplx<T> *>(e.bufs[1]);
+  size_t slot = 0;
+  qdg_status s = prof_begin<T>(p, final_mode, &slot);
+  if (s != QDG_OK) return s;
+  CK(qdg::launch_combine<T>(final_mode, c, p->comb_grid, 256, p->stream));
+  return prof_end(p, slot);
+}
+
+// The kinetic pass of a plan whose kinetic operator has no k-space table:
+// finite differences into P[0] (one launch), or the G-matrix line passes
+// (D_i = d/dx_i phi, then P_j).  tw: each dimension's twiddles in type T;
+// with tw_lines > 0 the line tiles hold at most that many lines (the
+// binary64 expectation value on a mixed plan, whose tiles were sized for FP32).
+template <typename T>
+qdg_status run_kin_tablefree(qdg_plan *p, const cplx<T> *phi, const int *done, const qdg::ChebyState *cs, int dyn,
+                             const void *const *bufs, const cplx<T> *const *tw, const T *grids, cplx<T> *const *D,
+                             cplx<T> *const *P, int tw_lines) {
+  if (p->kin_form == KIN_FD) {
+    qdg::FdArgs<T> a;
+    memset(&a, 0, sizeof(a));
+    a.nd = p->nd; a.S = p->S; a.o2 = p->fd_order / 2; a.pbc = p->fd_pbc; a.npts = p->npts;
+    for (int d = 0; d < p->nd; ++d) { a.n[d] = p->dim[d].n; a.lo[d] = p->dim[d].stride; }
+    qdg::host::fd_weights2(p->fd_order, a.cf);
+    memcpy(a.h, p->fd_h, sizeof(a.h));
+    a.phi = phi; a.out = P[0]; a.done = done; a.cs = cs; a.dyn = dyn;
+    a.bufs[0] = static_cast<const cplx<T> *>(bufs[0]);
+    a.bufs[1] = static_cast<const cplx<T> *>(bufs[1]);
+    const long long blocks = (p->npts * p->S + 255) / 256;
+    CK(qdg::launch_fd_kinetic<T>(a, (int)std::max<long long>(1, std::min<long long>(blocks, 8LL * p->sm_count)), p->stream));
+    return QDG_OK;
+  }
+  qdg::GmatArgs<T> a;
+  memset(&a, 0, sizeof(a));
+  a.nd = p->nd; a.S = p->S; a.npts = p->npts;
+  long long items = 0;
+  size_t smem = 0;
+  for (int d = 0; d < p->nd; ++d) {
+    const DimInfo &di = p->dim[d];
+    int TW = di.TW_k;
+    if (tw_lines > 0) TW = std::min(TW, tw_lines);
+    qdg::DimPass<T> &g = a.dp[d];
+    g.N = di.n; g.TW = TW; g.rp = di.rp; g.tw = tw[d];
+    if (d == 0) { g.es = 1; g.ls = di.n; g.tiles_per_hi = 1; g.hi_stride = (long long)TW * di.n; }
+    else { g.es = (int)di.stride; g.ls = 1; g.tiles_per_hi = (int)(di.stride / TW); g.hi_stride = di.stride * di.n; }
+    g.ntiles = p->npts / ((long long)di.n * TW);
+    a.item_start[d] = items;
+    items += g.ntiles * p->S;
+    a.kmul[d] = p->dk[d] / (double)di.n;  // Diff::DnDxn factor 1 (Diff.cpp:229-232)
+    smem = std::max(smem, ((size_t)di.n + 2 * qdg::line_buf_elems(di.n, TW)) * sizeof(cplx<T>));
+    a.D[d] = D[d];
+    a.P[d] = P[d];
+  }
+  a.item_start[p->nd] = items;
+  if (smem > 227 * 1024) return fail(QDG_EUNSUPPORTED, "grid line too long for the shared-memory FFT");
+  for (int st = 0; st < qdg::kMaxStates; ++st) { a.gbase[st] = p->gm_base[st]; a.gmask[st] = p->gm_mask[st]; }
+  a.grids = grids;
+  a.phi = phi; a.done = done; a.cs = cs; a.dyn = dyn;
+  a.bufs[0] = static_cast<const cplx<T> *>(bufs[0]);
+  a.bufs[1] = static_cast<const cplx<T> *>(bufs[1]);
+  const int grid = (int)std::max<long long>(1, std::min<long long>(items, (long long)qdg::gmat_max_blocks<T>(256, smem) * p->sm_count));
+  a.pass = 0;
+  CK(qdg::launch_gmat_pass<T>(a, grid, 256, smem, p->stream));
+  a.pass = 1;
+  for (int d = 0; d < p->nd; ++d) a.kmul[d] = -0.5 * p->dk[d] / (double)p->dim[d].n;  // DnDxnAdd factor -1/2
+  CK(qdg::launch_gmat_pass<T>(a, grid, 256, smem, p->stream));
+  return QDG_OK;
+}
+
 template <typename T>
 qdg_status run_h(qdg_plan *p, int final_mode, const cplx<T> *phi, const Epi &e) {
+  if (p->kin_form != KIN_FFT) {
+    size_t slot = 0;
+    qdg_status s = prof_begin<T>(p, qdg::PM_KIN_FIRST, &slot);
+    if (s != QDG_OK) return s;
+    const cplx<T> *tw[QDG_MAX_DIMS] = {};
+    cplx<T> *D[QDG_MAX_DIMS] = {}, *P[QDG_MAX_DIMS] = {};
+    for (int d = 0; d < p->nd; ++d) {
+      tw[d] = reinterpret_cast<const cplx<T> *>(p->dim[d].tw);
+      D[d] = reinterpret_cast<cplx<T> *>(p->d_Pd2[d]);
+      P[d] = reinterpret_cast<cplx<T> *>(p->d_Pd[d]);
+    }
+    if ((s = run_kin_tablefree<T>(p, phi, e.done, e.cut.cs, e.cut.dyn, e.bufs, tw,
+                                  reinterpret_cast<const T *>(p->d_grids), D, P, 0)) != QDG_OK)
+      return s;
+    if ((s = prof_end(p, slot)) != QDG_OK) return s;
+    if (!p->nac.empty() && (s = run_nac<T>(p, phi, e)) != QDG_OK) return s;
+    return run_combine<T>(p, final_mode, phi, e, p->kin_form == KIN_FD ? 1 : p->nd);
+  }
   if (p->nd == 1 && p->nac.empty()) {
     qdg::PassArgs<T> a;
     memset(&a, 0, sizeof(a));
@@ -490,28 +659,7 @@ qdg_status run_h(qdg_plan *p, int final_mode, const cplx<T> *phi, const Epi &e) 
   if ((s = prof_end(p, slot)) != QDG_OK) return s;
   if (!p->nac.empty() && (s = run_nac<T>(p, phi, e)) != QDG_OK) return s;
 
-  qdg::CombArgs<T> c;
-  memset(&c, 0, sizeof(c));
-  c.S = p->S;
-  c.nd = p->nd;
-  c.npts = p->npts;
-  c.phi = phi;
-  for (int d = 0; d < p->nd; ++d) c.P[d] = reinterpret_cast<const cplx<T> *>(p->d_Pd[d]);
-  c.out = reinterpret_cast<cplx<T> *>(e.out);
-  c.psi = e.psi;
-  c.k0 = reinterpret_cast<cplx<T> *>(e.k0);
-  c.cp = p->d_cp;
-  c.coef = p->d_coef;
-  c.grids = reinterpret_cast<const T *>(p->d_grids);
-  c.offset = C(e.offset); c.fac = C(e.fac); c.fac_lo = C(e.fac_lo); c.c0p = C(e.c0p); c.c1p = C(e.c1p); c.coeff = C(e.coeff);
-  c.imag = e.imag;
-  c.partials = p->d_partials;
-  c.cut = e.cut;
-  c.bufs[0] = reinterpret_cast<const cplx<T> *>(e.bufs[0]);
-  c.bufs[1] = reinterpret_cast<const cplx<T> *>(e.bufs[1]);
-  if ((s = prof_begin<T>(p, final_mode, &slot)) != QDG_OK) return s;
-  CK(qdg::launch_combine<T>(final_mode, c, p->comb_grid, 256, p->stream));
-  return prof_end(p, slot);
+  return run_combine<T>(p, final_mode, phi, e, p->nd);
 }
 
 template <typename T>
@@ -532,7 +680,7 @@ qdg_status upload_tables(qdg_plan *p) {
     // kinetic multipliers per state: sum over the state's GridNablaSq terms
     std::vector<double> kf(S, 0.0);
     for (auto &t : p->terms)
-      if (t.kind == QDG_TERM_KINETIC) kf[t.row] += (p->dk[d] * p->dk[d]) / (2.0 * t.mass[d]) / (double)n;
+      if (t.kind == QDG_TERM_KINETIC && t.fd_order == 0) kf[t.row] += (p->dk[d] * p->dk[d]) / (2.0 * t.mass[d]) / (double)n;
     CK(cudaMalloc(&di.kfac, sizeof(double) * S));
     CK(cudaMemcpy(di.kfac, kf.data(), sizeof(double) * S, cudaMemcpyHostToDevice));
     std::vector<T> kt((size_t)S * n);
@@ -572,7 +720,7 @@ qdg_status upload_tables(qdg_plan *p) {
     if (!gd.empty()) CK(cudaMemcpy(p->d_grids_df, gd.data(), sizeof(qdg::dfl) * gd.size(), cudaMemcpyHostToDevice));
   }
   CK(cudaMalloc(&p->d_P, sizeof(cplx<T>) * wf_elems(p)));
-  if (p->nd > 1 || !p->nac.empty()) {
+  if (p->nd > 1 || !p->nac.empty() || p->kin_form != KIN_FFT) {
     size_t smem = 0;
     long long items = 0;
     for (int d = 0; d < p->nd; ++d) {
@@ -653,7 +801,7 @@ qdg_status build_couplings(const qdg_plan *p, F pick, qdg::Couplings &cp) {
   struct E { int row, col, gid, lid, nim; };
   std::vector<E> es;
   for (auto &t : p->terms) {
-    if (t.kind == QDG_TERM_KINETIC || t.kind == QDG_TERM_NAC || !pick(t)) continue;
+    if (t.kind == QDG_TERM_KINETIC || t.kind == QDG_TERM_NAC || t.kind == QDG_TERM_GMAT || !pick(t)) continue;
     const int nrep = (p->hermitian && t.row != t.col) ? 2 : 1;
     const int nim = t.kind == QDG_TERM_GOBBLER && t.laser == 1 ? 1 : 0;  // -i W (negative imaginary potential)
     for (int r = 0; r < nrep; ++r)
@@ -829,6 +977,7 @@ qdg_status step_setup(qdg_prop *P) {
   // graph form of the step (a cross-check of the persistent kernel)
   if (has(P, "path") && P->params.at("path") == "graph") return QDG_OK;
   if (!p->nac.empty()) return QDG_OK;  // NAC elements run as extra line passes (graph path)
+  if (p->kin_form != KIN_FFT) return QDG_OK;  // HOFD / GridGMat kinetic passes (graph path)
   // The DF64 form's multi-dimensional step kernel computes its bulk in
   // double-float (~48 bits, FP32 exponent range).  Imaginary-time series
   // reach the low states through cancellations of terms ~1/sqrt(2 pi R) down
@@ -1415,6 +1564,10 @@ qdg_status gspo_init(qdg_prop *P) {
   for (auto &t : p->terms)  // OGSPO::Init takes ODSpace members only (OGSPO.cpp:71-85); OGridNAC is none
     if (t.kind == QDG_TERM_NAC || t.kind == QDG_TERM_GOBBLER)
       return fail(QDG_EUNSUPPORTED, "GSPO members must be ODSpace operators (no GridNAC, no Gobbler)");
+  // OGridGMat is no ODSpace; OGridNablaSq with method HOFD has no k-space
+  // table to exponentiate (Diff::_InitKspace returns early, Diff.cpp:52-54)
+  if (p->kin_form != KIN_FFT)
+    return fail(QDG_EUNSUPPORTED, "GSPO members need a diagonal representation (no HOFD, no GridGMat)");
   if (!p->hermitian) return fail(QDG_EUNSUPPORTED, "GSPO members must be hermitian matrices");
   P->ngroups = ng;
   P->group_kinetic.assign(ng, 0);
@@ -2042,6 +2195,19 @@ qdg_status qdg_plan_create(const qdg_hplan_desc *desc, int32_t precision, qdg_pl
       if (t.row != t.col) { free_plan(p); return fail(QDG_EUNSUPPORTED, "kinetic operator off the diagonal"); }
       for (int d = 0; d < p->nd; ++d)
         if (!(t.mass[d] > 0)) { free_plan(p); return fail(QDG_EINVAL, "Zero mass defined"); }
+      // HOFD::_CheckSetup (HOFD.h:82-89)
+      if (t.fd_order != 0 && (t.fd_order < 2 || t.fd_order > 2 * qdg::kMaxFdHalf || t.fd_order % 2 != 0)) {
+        free_plan(p); return fail(QDG_EINVAL, "Invalid order of FD derivative");
+      }
+      if (t.fd_order != 0 && (t.flags & 1) && (p->nd != 1 || p->dim[0].n <= t.fd_order / 2)) {
+        free_plan(p); return fail(QDG_EUNSUPPORTED, "HOFD with pbc needs a one-dimensional grid longer than order/2");
+      }
+    } else if (t.kind == QDG_TERM_GMAT) {
+      if (t.row != t.col) { free_plan(p); return fail(QDG_EUNSUPPORTED, "GridGMat off the diagonal"); }
+      const int ne = p->nd * (p->nd + 1) / 2;
+      if (t.grid < 0 || t.grid + ne > p->ngrids || !desc->grid_data) { free_plan(p); return fail(QDG_EINVAL, "G-matrix grid index out of range"); }
+      for (int k = 0; k < ne; ++k)
+        if (((t.flags >> (2 * k)) & 3) == 3) { free_plan(p); return fail(QDG_EINVAL, "bad G-matrix element source"); }
     } else if (t.kind == QDG_TERM_NAC) {
       if (t.grid < 0 || t.grid + p->nd > p->ngrids || !desc->grid_data) { free_plan(p); return fail(QDG_EINVAL, "NACME grid index out of range"); }
       if (!(t.mass[0] > 0)) { free_plan(p); return fail(QDG_EINVAL, "Zero mass defined"); }
@@ -2062,6 +2228,37 @@ qdg_status qdg_plan_create(const qdg_hplan_desc *desc, int32_t precision, qdg_pl
   for (auto &a : p->terms)
     for (auto &b : p->terms)
       if (a.row != a.col && a.row == b.col && a.col == b.row) p->hermitian = false;
+  // one kinetic form per plan: FFT, finite differences (one order and
+  // boundary rule) or the G-matrix (one per state)
+  {
+    bool fft = false, fd = false, gm = false;
+    for (int st = 0; st < qdg::kMaxStates; ++st) p->gm_base[st] = -1;
+    for (auto &t : p->terms) {
+      if (t.kind == QDG_TERM_KINETIC && t.fd_order == 0) fft = true;
+      if (t.kind == QDG_TERM_KINETIC && t.fd_order != 0) {
+        if (fd && (t.fd_order != p->fd_order || (t.flags & 1) != p->fd_pbc)) {
+          free_plan(p); return fail(QDG_EUNSUPPORTED, "finite-difference kinetic terms of different order or boundaries");
+        }
+        fd = true;
+        p->fd_order = t.fd_order;
+        p->fd_pbc = t.flags & 1;
+        for (int d = 0; d < p->nd; ++d)  // HOFD.h:136-138: 1/dx^2 * 1 * (-1/(2 m_d))
+          p->fd_h[t.row][d] += 1. / (p->dx[d] * p->dx[d]) * 1.0 * (-1. / 2. / t.mass[d]);
+      }
+      if (t.kind == QDG_TERM_GMAT) {
+        if (p->gm_base[t.row] >= 0) { free_plan(p); return fail(QDG_EUNSUPPORTED, "two GridGMat operators on one state"); }
+        gm = true;
+        p->gm_base[t.row] = t.grid;
+        const int ne = p->nd * (p->nd + 1) / 2;
+        for (int k = 0; k < ne; ++k)
+          if ((t.flags >> (2 * k)) & 3) p->gm_mask[t.row] |= 1u << k;
+      }
+    }
+    if ((int)fft + (int)fd + (int)gm > 1) {
+      free_plan(p); return fail(QDG_EUNSUPPORTED, "one kinetic form per plan: FFT, HOFD or GridGMat");
+    }
+    p->kin_form = fd ? KIN_FD : gm ? KIN_GMAT : KIN_FFT;
+  }
   for (auto &t : p->terms) {
     if (t.kind != QDG_TERM_NAC) continue;
     const double c = 0.5 * (t.sign == 0 ? 1.0 : t.sign) / t.mass[0];  // PreFactor(0.5 sign / mass)
@@ -2284,6 +2481,60 @@ qdg_status expec_check(const qdg_plan *plan, const qdg_wf *psi, const double *ou
   if (!plan || !psi || !out || psi->plan != plan) return fail(QDG_EINVAL, "bad arguments");
   return QDG_OK;
 }
+
+// Kinetic operators without a k-space table (HOFD, GridGMat): Re <psi|T psi>
+// / <psi|psi> with T psi from the binary64 kinetic kernels on the binary64
+// psi (twiddles and G grids uploaded in binary64 for the call on a mixed plan).
+qdg_status expec_kinetic_direct(qdg_plan *p, const qdg_wf *psi, double *out) {
+  const int nd = p->nd;
+  const size_t n = (size_t)p->npts * p->S;
+  DevBuf Pb[QDG_MAX_DIMS], Db[QDG_MAX_DIMS], twb[QDG_MAX_DIMS], gb;
+  const cplx<double> *tw[QDG_MAX_DIMS] = {};
+  cplx<double> *D[QDG_MAX_DIMS] = {}, *P[QDG_MAX_DIMS] = {};
+  const int nP = p->kin_form == KIN_FD ? 1 : nd;
+  for (int d = 0; d < nP; ++d) {
+    CK(cudaMalloc(&Pb[d].p, sizeof(cplx<double>) * n));
+    P[d] = static_cast<cplx<double> *>(Pb[d].p);
+  }
+  const double *grids = is64(p) ? static_cast<const double *>(p->d_grids) : nullptr;
+  if (p->kin_form == KIN_GMAT) {
+    const long double pi = 3.141592653589793238462643383279502884L;
+    for (int d = 0; d < nd; ++d) {
+      CK(cudaMalloc(&Db[d].p, sizeof(cplx<double>) * n));
+      D[d] = static_cast<cplx<double> *>(Db[d].p);
+      if (is64(p)) {
+        tw[d] = static_cast<const cplx<double> *>(p->dim[d].tw);
+      } else {
+        const int N = p->dim[d].n;
+        std::vector<cplx<double>> h(N);
+        for (int m = 0; m < N; ++m) {
+          const long double ang = -2.0L * pi * (long double)m / (long double)N;
+          h[m] = cplx<double>{(double)cosl(ang), (double)sinl(ang)};
+        }
+        CK(cudaMalloc(&twb[d].p, sizeof(cplx<double>) * N));
+        CK(cudaMemcpyAsync(twb[d].p, h.data(), sizeof(cplx<double>) * N, cudaMemcpyHostToDevice, p->stream));
+        tw[d] = static_cast<const cplx<double> *>(twb[d].p);
+      }
+    }
+    if (!is64(p)) {
+      CK(cudaMalloc(&gb.p, sizeof(double) * p->grids_h.size()));
+      CK(cudaMemcpyAsync(gb.p, p->grids_h.data(), sizeof(double) * p->grids_h.size(), cudaMemcpyHostToDevice, p->stream));
+      grids = static_cast<const double *>(gb.p);
+    }
+  }
+  const void *bufs[2] = {nullptr, nullptr};
+  qdg_status s = run_kin_tablefree<double>(p, psi->d, nullptr, nullptr, 0, bufs, tw, grids, D, P, is64(p) ? 0 : 1);
+  if (s != QDG_OK) return s;
+  std::vector<cd> dd;
+  double num = 0;
+  for (int d = 0; d < nP; ++d) {
+    if ((s = dots<double, double>(p, psi->d, P[d], dd)) != QDG_OK) return s;
+    num += total(dd).real();
+  }
+  if ((s = dots<double, double>(p, psi->d, psi->d, dd)) != QDG_OK) return s;
+  *out = num / total(dd).real();
+  return QDG_OK;
+}
 }  // namespace
 
 qdg_status qdg_expec_position(qdg_plan *plan, const qdg_wf *psi, int32_t dim, double scale, double *out) {
@@ -2324,6 +2575,7 @@ qdg_status qdg_expec_momentum(qdg_plan *plan, const qdg_wf *psi, int32_t dim, do
 qdg_status qdg_expec_kinetic(qdg_plan *plan, const qdg_wf *psi, double *out) {
   qdg_status s = expec_check(plan, psi, out);
   if (s != QDG_OK) return s;
+  if (plan->kin_form != KIN_FFT) return expec_kinetic_direct(plan, psi, out);
   double ws, ns, num = 0;
   if ((s = expec_point(plan, psi, nullptr, 0, 1.0, ws, ns)) != QDG_OK) return s;
   for (int d = 0; d < plan->nd; ++d) {

@@ -247,6 +247,18 @@ static void mean_sigma(const std::vector<double> &d, size_t b, size_t e, double 
   sigma = std::sqrt(sigma / double(e - b));
 }
 
+void fd_weights2(int order, double *cf) {
+  const int o2 = order / 2;
+  long double ratio = 1, center = 0;  // ratio = (o2!)^2 / ((o2 - k)! (o2 + k)!)
+  for (int k = 1; k <= o2; ++k) {
+    ratio = ratio * (long double)(o2 + 1 - k) / (long double)(o2 + k);
+    const long double kk = (long double)k * (long double)k;
+    cf[o2 - k] = (double)((k & 1 ? 2.0L : -2.0L) * ratio / kk);
+    center += 1.0L / kk;
+  }
+  cf[o2] = (double)(-2.0L * center);
+}
+
 std::vector<int> find_peaks(const std::vector<double> &data, double tol, int width) {
   std::vector<int> peaks;
   const size_t n = data.size();

@@ -55,5 +55,13 @@ std::vector<cd> dft(const std::vector<cd> &x, int sign);
 // mean + tol sigma of the window [i - width, i + width).  Ascending indices.
 std::vector<int> find_peaks(const std::vector<double> &data, double tol, int width);
 
+// Central finite-difference weights of the second derivative on 2 o2 + 1
+// points in the layout of QDng's HOFD table (src/qdlib/HOFD.h:31-36):
+// cf[o2] weighs the point, cf[o2 - k] both neighbours at distance k.  From
+// the closed form w_k = 2 (-1)^(k+1) (o2!)^2 / (k^2 (o2 - k)! (o2 + k)!),
+// w_0 = -2 sum_k 1/k^2 (Fornberg, Math. Comp. 51 (1988) 699-706), evaluated
+// in long double and rounded once.
+void fd_weights2(int order, double *cf);
+
 }  // namespace host
 }  // namespace qdg

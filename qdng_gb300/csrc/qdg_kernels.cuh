@@ -200,6 +200,48 @@ struct CombArgs {
   const cplx<T> *bufs[2];  // device-driven term loop: phi = bufs[(i+1)&1], k0 = bufs[i&1]
 };
 
+// OGridNablaSq with method="HOFD" (src/qdlib/HOFD.h:124-176): the kinetic
+// energy of every state by central finite differences over all dimensions,
+// with QDng's neighbour rule (qdg_fdkin.cu), written to out (state stride npts).
+static const int kMaxFdHalf = 25;  // order 50 (HOFD_MAXORDER, HOFD.h:17)
+template <typename T>
+struct FdArgs {
+  int nd, S, o2, pbc;
+  long long npts;
+  int n[4];
+  long long lo[4];                 // stride of each dimension
+  double cf[kMaxFdHalf + 1];       // cf[o2] the point, cf[o2 - k] the neighbours at distance k
+  double h[kMaxStates][4];         // per state and dimension: -1/(2 m_d) / dx_d^2, 0 = no term
+  const cplx<T> *phi;
+  cplx<T> *out;
+  const int *done;
+  const ChebyState *cs;            // device-driven term loop: phi = bufs[(cs->i + 1) & 1]
+  const cplx<T> *bufs[2];
+  int dyn;
+};
+
+// OGridGMat (src/qdlib/OGridGMat.cpp:313-386) in two launches of line
+// passes over all dimensions (qdg_fdkin.cu): pass 0 stores D_i = d/dx_i phi,
+// pass 1 stores P_j = -1/2 d/dx_j sum_i G_ij D_i, which the combine pass sums.
+template <typename T>
+struct GmatArgs {
+  int nd, S, pass;
+  long long npts;
+  DimPass<T> dp[4];                // geometry and twiddles of each dimension (kfac, P unused)
+  long long item_start[5];
+  double kmul[4];                  // dk_d / N_d (pass 0) or -dk_d / (2 N_d) (pass 1)
+  long long gbase[kMaxStates];     // per state: first of its nd (nd + 1) / 2 G grids, -1 = none
+  unsigned gmask[kMaxStates];      // per state: bit k set = lower-triangle element k present
+  const T *grids;
+  const cplx<T> *phi;
+  cplx<T> *D[4];
+  cplx<T> *P[4];
+  const int *done;
+  const ChebyState *cs;
+  const cplx<T> *bufs[2];
+  int dyn;
+};
+
 // Grid-wide barrier state of the persistent step kernel (device memory,
 // zeroed once; the last block of each barrier resets `count`).
 struct GridBarrier {
@@ -335,6 +377,12 @@ template <typename T>
 int nac_max_blocks(int block, size_t smem);
 template <typename T>
 cudaError_t launch_combine(int mode, const CombArgs<T> &a, int grid, int block, cudaStream_t st);
+template <typename T>
+cudaError_t launch_fd_kinetic(const FdArgs<T> &a, int grid, cudaStream_t st);
+template <typename T>
+cudaError_t launch_gmat_pass(const GmatArgs<T> &a, int grid, int block, size_t smem, cudaStream_t st);
+template <typename T>
+int gmat_max_blocks(int block, size_t smem);
 
 // coef[e] for clock step `step` (Laser::Get, src/qdlib/Laser.cpp:125-128).
 cudaError_t launch_set_coefs(double *coef, const Couplings *cp, const double *lasers, int laser_nt, long long step,

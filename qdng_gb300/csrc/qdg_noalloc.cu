@@ -157,6 +157,7 @@ qdg_status qdg_h_apply_noalloc(const qdg_hplan_desc *desc, const double *psi_in,
     if (h.row < 0 || h.col < 0 || h.row >= S || h.col >= S) return na_fail(QDG_EINVAL, "matrix element outside the states");
     if (h.kind == QDG_TERM_KINETIC) {
       if (h.row != h.col) return na_fail(QDG_EUNSUPPORTED, "kinetic operator off the diagonal");
+      if (h.fd_order != 0) return na_fail(QDG_EUNSUPPORTED, "finite-difference kinetic (method HOFD) needs a plan");
       for (int d = 0; d < g.ndims; ++d) {
         if (!(h.mass[d] > 0)) return na_fail(QDG_EINVAL, "Zero mass defined");
         t.kfac[d][h.row] += (dk[d] * dk[d]) / (2.0 * h.mass[d]) / (double)g.n[d];

@@ -3,7 +3,8 @@
 The classes keep the reference's names and the meaning of their XML
 attributes, and flatten the tree into the qdg_hplan_desc the C ABI takes:
 
-* ``GridNablaSq(mass=[...])``   -- src/qdlib/OGridNablaSq.cpp:28-58
+* ``GridNablaSq(mass=[...], method, order, pbc)`` -- src/qdlib/OGridNablaSq.cpp:28-58, Diff.cpp:149-200
+* ``GridGMat(dims, gmat, G, Gdef, coup)`` -- src/qdlib/OGridGMat.cpp:142-386 (G-matrix kinetic energy)
 * ``GridPotential(values)``     -- src/qdlib/OGridPotential.cpp:26-109 (setzero/offset/scale)
 * ``GridDipole(mu, laser)``     -- src/qdlib/OGridDipole.cpp:18-60, Laser.cpp:125-128
 * ``GridNAC([f_0, ...], mass, sign)`` -- src/qdlib/OGridNAC.cpp:26-148 (first-derivative coupling)
@@ -97,9 +98,12 @@ class Operator:
 
 
 class GridNablaSq(Operator):
-    """Kinetic energy -1/(2m) d^2/dx^2 per dimension via FFT."""
+    """Kinetic energy -1/(2m) d^2/dx^2 per dimension, by FFT (``method="FFT"``)
+    or by central finite differences of even ``order`` 2..50 (``method="HOFD"``,
+    Diff.cpp:149-200, default order 8 = DIFF_DEF_ORDER, Diff.h:20) with
+    ``pbc`` periodic boundaries (one-dimensional grids)."""
 
-    def __init__(self, mass):
+    def __init__(self, mass, method="FFT", order=8, pbc=False):
         mass = [float(m) for m in np.atleast_1d(mass)]
         if len(mass) < 1:
             raise EParamProblem("Nabla operator needs at least one dimension")
@@ -109,16 +113,99 @@ class GridNablaSq(Operator):
             if m < 0:
                 raise EIncompatible("negative masses (excluded dimensions) are not supported")
         self.mass = mass
+        if method not in ("FFT", "HOFD"):
+            raise EParamProblem("Unknown differenciation method", method)
+        self.method = method
+        self.order = int(order) if method == "HOFD" else 0
+        self.pbc = bool(pbc) and method == "HOFD"
+        if method == "HOFD" and (self.order > 50 or self.order % 2 != 0 or self.order < 2):
+            # HOFD::_CheckSetup (HOFD.h:82-89)
+            raise EParamProblem("Invalid order of FD derivative", self.order)
 
     def terms(self, row, col, group, ctx):
         if row != col:
             raise EIncompatible("GridNablaSq must sit on the diagonal")
         if len(self.mass) != ctx.grid.ndims:
             raise EIncompatible("OGridNablaSq: Number of dims doesn't match WF")
+        if self.pbc and ctx.grid.ndims != 1:
+            raise EIncompatible("HOFD with pbc on grids of more than one dimension")
         t = abi.HTerm()
         t.kind, t.row, t.col, t.grid, t.laser, t.group = abi.TERM_KINETIC, row, col, -1, -1, group
         for i, m in enumerate(self.mass):
             t.mass[i] = m
+        t.fd_order = self.order
+        t.flags = 1 if self.pbc else 0
+        return [t]
+
+
+class GridGMat(Operator):
+    """OGridGMat (src/qdlib/OGridGMat.cpp:142-248, 307-386): the G-matrix
+    kinetic energy -1/2 sum_ij d/dx_j G_ij(x) d/dx_i with FFT derivatives.
+
+    ``gmat`` maps (i, j), i >= j, to the grid array of G_ij (the files
+    ``<gmat>_ij`` of the reference); ``G`` lists constant elements and
+    ``Gdef`` the source of each element ('g' grid, 'c' constant, 'x' none),
+    both in lower-triangle order (0,0), (1,0), (1,1), (2,0), ...
+    (ReorderLowerTriangular, tools/helpers.h:95-112).  Without ``Gdef`` every
+    element is a constant when ``G`` is given, else a grid.  ``coup=False``
+    drops the off-diagonal elements.  The chain-rule form, PML and finite
+    difference derivatives are not provided."""
+
+    def __init__(self, dims, gmat=None, G=None, Gdef=None, coup=True, chainrule=False, pml=False,
+                 method="FFT"):
+        n = int(dims)
+        if n < 1:
+            raise EParamProblem("G-matrix operator needs at least one dimension")
+        if chainrule or pml or method != "FFT":
+            raise EIncompatible("GridGMat: only the FFT form without chain rule and PML is provided")
+        self.n = n
+        self.coup = bool(coup)
+        nl = n * (n + 1) // 2
+        src = ["c" if G is not None else "g"] * nl
+        if Gdef is not None:
+            for k, c in enumerate(list(Gdef)[:nl]):
+                src[k] = c
+        const = [0.0] * nl
+        if G is not None:
+            for k, v in enumerate(list(np.atleast_1d(G))[:nl]):
+                const[k] = float(v)
+        gmat = dict(gmat or {})
+        self.elements = []  # per lower-triangle element: (source code, array or constant)
+        for i in range(n):
+            for j in range(i + 1):
+                k = i * (i + 1) // 2 + j
+                if i != j and not self.coup:
+                    self.elements.append((0, None))
+                elif src[k] == "g":
+                    if (i, j) not in gmat:
+                        raise EParamProblem("No G-matrix elements given")
+                    self.elements.append((1, np.array(gmat[(i, j)], dtype=np.float64).reshape(-1)))
+                elif src[k] == "c":
+                    self.elements.append((2, const[k]))
+                else:
+                    self.elements.append((0, None))
+
+    def terms(self, row, col, group, ctx):
+        if row != col:
+            raise EIncompatible("GridGMat must sit on the diagonal")
+        if self.n != ctx.grid.ndims:
+            raise EIncompatible("Gmatrix element is incompatible with wave function")
+        t = abi.HTerm()
+        t.kind, t.row, t.col, t.laser, t.group = abi.TERM_GMAT, row, col, -1, group
+        flags = 0
+        arrs = []
+        for k, (code, val) in enumerate(self.elements):
+            if code == 1:
+                if val.size != ctx.grid.npts:
+                    raise EIncompatible("Gmatrix element is incompatible with wave function")
+                arrs.append(val)
+            elif code == 2:
+                arrs.append(np.full(ctx.grid.npts, val))
+            else:
+                arrs.append(np.zeros(ctx.grid.npts))
+            flags |= code << (2 * k)
+        t.grid = ctx.add_grids(arrs)
+        t.flags = flags
         return [t]
 
 

@@ -26,6 +26,26 @@ def tgp_expec(fx):
     return hp, psi, dict(name="Cheby", params="prec=1e-12", dt=20.0, steps=1000)
 
 
+def tgp_expec_lc(fx, kinetic="FFT"):
+    """tests/TGP-Expec-SP.qdi.in (kinetic="FFT"), TGP-Expec-HOFD.qdi.in ("HOFD":
+    GridNablaSq method=HOFD order=8, prec 1e-10) and TGP-Gmat.qdi.in ("GMAT":
+    GridGMat dims=1 with the GridGM_00 grid): Cheby, dt=20, 1000 steps, from the
+    normalised linear combination of GridPot0_ef_0..3 (ChainLoader.cpp:257-284
+    adds each function twice; the normalisation removes the factor)."""
+    g = mgh_grid(fx)
+    if kinetic == "GMAT":
+        T = op.GridGMat(1, gmat={(0, 0): fx["GridGM_00"]})
+    elif kinetic == "HOFD":
+        T = op.GridNablaSq([1763.2], method="HOFD", order=8)
+    else:
+        T = op.GridNablaSq([1763.2])
+    V = op.GridPotential(fx["GridPot0"])
+    hp = op.HPlan(g, op.Sum([T, V]))
+    psi = sum(2.0 * fx[f"GridPot0_ef_{k}"].astype(np.complex128) for k in range(4))
+    prec = "1e-10" if kinetic == "HOFD" else "1e-12"
+    return hp, _normalize(hp, psi), dict(name="Cheby", params=f"prec={prec}", dt=20.0, steps=1000, V=V)
+
+
 def tgp_nip(fx):
     """tests/TGP-NIP-Cheby.qdi.in: Cheby, Sum(T, Gobbler nip rp0=5.5 order 5 gain 0.02,
     Gobbler lp0=2 order 20 gain 0.3 (key V)), ef_0, dt=10, 1000 steps."""

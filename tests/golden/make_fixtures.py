@@ -32,7 +32,7 @@ def read_meta(path):
 def main(ref):
     tdir = os.path.join(ref, "tests")
     out = {}
-    for name in ["GridPot0", "GridPot1", "GridDip0", "GridDip01"]:
+    for name in ["GridPot0", "GridPot1", "GridDip0", "GridDip01", "GridGM_00"]:
         meta = read_meta(os.path.join(tdir, name + ".meta"))
         n = int(meta["N0"])
         out[name] = np.fromfile(os.path.join(tdir, name + ".op"), dtype="<f8")[:n]

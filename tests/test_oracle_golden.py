@@ -11,6 +11,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
+from qdng_gb300 import operators as op
 from tests import cases
 
 
@@ -140,6 +141,49 @@ def test_tgp_expec_filters(fixtures, golden):
            S.expec_projection(x, [fixtures[f"GridPot0_ef_{k}"] for k in range(4)]),
            S.expec_kinetic(x), S.expec_grid(x, 0)]
     _check_expec(golden["expec"]["TGP-Expec"], row)
+
+
+@pytest.mark.parametrize("kinetic,name", [("FFT", "TGP-Expec-SP"), ("HOFD", "TGP-Expec-HOFD"),
+                                          ("GMAT", "TGP-Gmat")])
+def test_tgp_expec_kinetic_forms(fixtures, golden, kinetic, name):
+    """One packet under three kinetic operators: GridNablaSq by FFT, by 8th
+    order finite differences (OGridNablaSq method=HOFD) and the G-matrix
+    (OGridGMat with G = 1/m): the Reporter line after 999 steps and the
+    filterpost line (<p>, <x>, projection, <T>, <V>) against QDng."""
+    hp, psi, run = cases.tgp_expec_lc(fixtures, kinetic)
+    S = O.System(hp)
+    P = O.Propagator(S, run["name"], run["params"], dt=run["dt"])
+    x = psi.copy()
+    obs, terms = P.propagate(x, psi.copy(), run["steps"])
+    _check(golden["propagation"][name], obs[-1], 1)
+    _check_expec(golden["expec"][name], _expec_row(S, hp, x, run["V"], fixtures))
+
+
+def test_fd_weights_and_stencil():
+    """The finite-difference weights (closed form) reproduce QDng's table
+    values (HOFD.h cfd tables: order 2 {1, -2}, order 4 {-1/12, 4/3, -5/2}),
+    and the 1-D HOFD stencil follows QDng's boundary rule: neighbours above
+    the grid are dropped, those below it wrap to the top end."""
+    n = 16
+    g = op.GridSystem([n], [0.0], [float(n - 1)])
+    for order, w in [(2, [1.0, -2.0]), (4, [-1 / 12, 4 / 3, -2.5])]:
+        hp = op.HPlan(g, op.GridNablaSq([0.5], method="HOFD", order=order))
+        S = O.System(hp)
+        o2 = order // 2
+        for i in [0, 1, n // 2, n - 1]:
+            e = np.zeros(n, complex)
+            e[i] = 1.0
+            col = S.h_apply(e)  # column i of -1/(2m) D2 with m = 1/2, dx = 1: -D2
+            want = np.zeros(n)
+            want[i] += -w[o2]
+            for k in range(1, o2 + 1):
+                # point i feeds the point below it (i - k, if on the grid) through
+                # that point's upper neighbour, and the point above (i + k) through
+                # its lower neighbour, which wraps around
+                if i - k >= 0:
+                    want[i - k] += -w[o2 - k]
+                want[(i + k) % n] += -w[o2 - k]
+            assert np.allclose(col.real, want, rtol=0, atol=1e-13), (order, i, col.real, want)
 
 
 def test_tgp_nip_cheby(fixtures, golden):

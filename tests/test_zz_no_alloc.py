@@ -120,3 +120,21 @@ def test_noalloc_rejects_oversized_problem():
                                  C.cast(C.c_void_p(y.data_ptr()), C.POINTER(C.c_double)), 0, None)
     assert rc == abi.QDG_EINVAL
     assert "scratch" in lib.qdg_last_error().decode()
+
+
+@pytest.mark.parametrize("kinetic", ["HOFD", "GMAT"])
+def test_noalloc_rejects_table_free_kinetic(kinetic):
+    """Finite-difference (method HOFD) and G-matrix kinetic operators need a
+    plan's buffers: the no-alloc entry refuses them instead of applying an
+    FFT kinetic in their place."""
+    torch = pytest.importorskip("torch")
+    from qdng_gb300._lib import load
+    lib = load()
+    g = op.GridSystem([64], [-1.0], [1.0])
+    T = op.GridNablaSq([1.0], method="HOFD") if kinetic == "HOFD" else op.GridGMat(1, G=[1.0])
+    hp = op.HPlan(g, op.Sum([T, op.GridPotential(np.zeros(64))]))
+    x = torch.zeros(hp.size * 2, dtype=torch.float64, device="cuda")
+    y = torch.zeros_like(x)
+    rc = lib.qdg_h_apply_noalloc(C.byref(hp.desc), C.cast(C.c_void_p(x.data_ptr()), C.POINTER(C.c_double)),
+                                 C.cast(C.c_void_p(y.data_ptr()), C.POINTER(C.c_double)), 0, None)
+    assert rc == abi.QDG_EUNSUPPORTED
