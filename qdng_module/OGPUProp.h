@@ -27,7 +27,9 @@
 #include "modules/Module.h"
 #include "qdg.h"
 #include "qdlib/ODSpace.h"
+#include "qdlib/OGobbler.h"
 #include "qdlib/OGridDipole.h"
+#include "qdlib/OGridGMat.h"
 #include "qdlib/OGridNAC.h"
 #include "qdlib/OGridNablaSq.h"
 #include "qdlib/OGridPotential.h"
@@ -115,10 +117,89 @@ class OGPUProp : public OPropagator {
         if (d == 0) t.grid = g;
       }
     } else if (OGridNablaSq *T = dynamic_cast<OGridNablaSq *>(O)) {
+      ParamContainer &tp = T->Params();
       vector<double> m;
-      T->Params().GetArray("mass", m);
+      tp.GetArray("mass", m);
       t.kind = QDG_TERM_KINETIC;
       for (size_t d = 0; d < m.size() && d < QDG_MAX_DIMS; d++) t.mass[d] = m[d];
+      // method, order and pbc as Diff::InitParams reads them (Diff.cpp:149-200)
+      string method = "FFT";
+      if (tp.isPresent("method")) tp.GetValue("method", method);
+      if (method == "HOFD") {
+        int order = 8;  // DIFF_DEF_ORDER (Diff.h:20)
+        if (tp.isPresent("order")) tp.GetValue("order", order);
+        bool pbc;
+        tp.GetValue("pbc", pbc, false);
+        t.fd_order = order;
+        t.flags = pbc ? 1 : 0;
+      } else if (method != "FFT") {
+        throw EParamProblem("Unknown differenciation method", method);
+      }
+    } else if (OGobbler *Gb = dynamic_cast<OGobbler *>(O)) {
+      // the filter grid W, gain included, is built by OGobbler::Init(WaveFunction*)
+      // (OGobbler.cpp:118-185); nip and gain as OGobbler::Init(ParamContainer&) reads them
+      Gb->Init(_proto);
+      ParamContainer &bp = Gb->Params();
+      bool nip;
+      bp.GetValue("nip", nip, false);
+      double gain = 1;
+      if (bp.isPresent("gain")) bp.GetValue("gain", gain);
+      t.kind = QDG_TERM_GOBBLER;
+      t.grid = add_grid(static_cast<dVec &>(*Gb));
+      t.laser = nip ? 1 : 0;
+      t.mass[0] = gain;
+    } else if (OGridGMat *Gm = dynamic_cast<OGridGMat *>(O)) {
+      // OGridGMat keeps its elements private: read them the way its
+      // Init(ParamContainer&) does (OGridGMat.cpp:142-248), lower triangle row by row
+      ParamContainer &gp = Gm->Params();
+      int n = 0;
+      gp.GetValue("dims", n);
+      bool coup, chain, pml;
+      gp.GetValue("coup", coup, true);
+      gp.GetValue("chainrule", chain, false);
+      gp.GetValue("pml", pml, false);
+      string method = "FFT";
+      if (gp.isPresent("method")) gp.GetValue("method", method);
+      if (chain || pml || method != "FFT")
+        throw EIncompatible("GPU propagator: GridGMat with chain rule, PML or finite differences", O->Name());
+      const int ne = n * (n + 1) / 2;
+      vector<char> src(ne, gp.isPresent("G") ? 'c' : 'g');
+      if (gp.isPresent("Gdef")) {
+        vector<char> v;
+        gp.GetArray("Gdef", v);
+        for (size_t k = 0; k < v.size() && (int)k < ne; k++) src[k] = v[k];
+      }
+      vector<double> gc(ne, 0.0);
+      if (gp.isPresent("G")) {
+        vector<double> v;
+        gp.GetArray("G", v);
+        for (size_t k = 0; k < v.size() && (int)k < ne; k++) gc[k] = v[k];
+      }
+      string name;
+      gp.GetValue("gmat", name);
+      t.kind = QDG_TERM_GMAT;
+      for (int i = 0, k = 0; i < n; i++)
+        for (int j = 0; j <= i; j++, k++) {
+          int code = (i != j && !coup) ? 0 : src[k] == 'g' ? 1 : src[k] == 'c' ? 2 : 0;
+          dVec vals(_proto->size());
+          vals = code == 2 ? gc[k] : 0.0;
+          int g;
+          if (code == 1) {
+            if (name.length() < 2) throw EParamProblem("No G-matrix elements given");
+            std::ostringstream fn;
+            fn << name << "_" << i << j;
+            ParamContainer pf;
+            pf.SetValue("file", fn.str());
+            OGridPotential f;
+            f.Init(pf);
+            f.Init(_proto);
+            g = add_grid(static_cast<dVec &>(f));
+          } else {
+            g = add_grid(vals);
+          }
+          if (k == 0) t.grid = g;
+          t.flags |= code << (2 * k);
+        }
     } else if (OGridDipole *D = dynamic_cast<OGridDipole *>(O)) {  // before OGridPotential (its base)
       t.kind = QDG_TERM_DIPOLE;
       t.grid = add_grid(static_cast<dVec &>(*D));
