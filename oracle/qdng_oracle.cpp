@@ -79,7 +79,9 @@ struct FFT1 {
     if (n == 1) return;
     cd *in = x, *out = work;
     long Ns = 1;
-    cd v[64], y[64];
+    int rmax = 1;
+    for (int R : radix) rmax = std::max(rmax, R);
+    std::vector<cd> v(rmax), y(rmax);  /* any prime factor: a direct R-point DFT */
     for (int R : radix) {
       long M = n / R;
       long step = n / (Ns * R);

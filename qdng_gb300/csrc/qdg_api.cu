@@ -89,6 +89,8 @@ struct qdg_plan {
   // HOFD (finite differences) or OGridGMat.  Either replaces the FFT kinetic
   // pass of the graph path; the fused step kernels do not take them.
   int kin_form = 0;                               // KIN_FFT, KIN_FD or KIN_GMAT
+  // a line length with a prime factor above 5: direct-DFT stages, graph path only
+  bool generic_fft = false;
   int fd_order = 0, fd_pbc = 0;
   double fd_h[qdg::kMaxStates][4] = {};           // -1/(2 m_d) / dx_d^2 per state, summed over terms
   long long gm_base[qdg::kMaxStates];             // first G grid of each state, -1 = none
@@ -978,6 +980,7 @@ qdg_status step_setup(qdg_prop *P) {
   if (has(P, "path") && P->params.at("path") == "graph") return QDG_OK;
   if (!p->nac.empty()) return QDG_OK;  // NAC elements run as extra line passes (graph path)
   if (p->kin_form != KIN_FFT) return QDG_OK;  // HOFD / GridGMat kinetic passes (graph path)
+  if (p->generic_fft) return QDG_OK;          // prime radices above 5 (graph path)
   // The DF64 form's multi-dimensional step kernel computes its bulk in
   // double-float (~48 bits, FP32 exponent range).  Imaginary-time series
   // reach the low states through cancellations of terms ~1/sqrt(2 pi R) down
@@ -2177,10 +2180,15 @@ qdg_status qdg_plan_create(const qdg_hplan_desc *desc, int32_t precision, qdg_pl
     p->dim[d].n = g.n[d];
     p->dim[d].stride = stride;
     // the autotuner's schedule for this line length, else the greedy order
-    // (largest radices first: 256 = 16 x 16, 1024 = 16 x 16 x 4, 384 = 16 x 8 x 3)
+    // (largest radices first: 256 = 16 x 16, 1024 = 16 x 16 x 4, 384 = 16 x 8 x 3);
+    // other prime factors become direct-DFT stages of the graph path's
+    // transforms (FFTW takes any N, src/fft/fft.cpp:98-122)
     if (!qdg::schedule_radix(qdg::SCHED_PLAN, g.n[d], precision, p->dim[d].rp)) {
-      free_plan(p);
-      return fail(QDG_EUNSUPPORTED, "grid size must be 2^a 3^b 5^c");
+      if (!qdg::any_radix(g.n[d], p->dim[d].rp)) {
+        free_plan(p);
+        return fail(QDG_EUNSUPPORTED, "grid size has more than 16 prime factors");
+      }
+      p->generic_fft = true;
     }
     stride *= g.n[d];
   }

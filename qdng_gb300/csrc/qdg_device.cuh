@@ -321,6 +321,46 @@ __device__ __forceinline__ void stockham_stage(const cplx<T> *__restrict__ in, c
   }
 }
 
+// A stage of a prime radix R outside {2, 3, 5} (a line length with other
+// prime factors, which FFTW takes too): the same Stockham indexing with R a
+// runtime value; each output is a direct R-point sum over the twiddled
+// inputs, read from shared memory again for every output (O(R^2) work per
+// item, no register array of R values).
+template <typename T>
+__device__ __noinline__ void stockham_stage_gen(const cplx<T> *__restrict__ in, cplx<T> *__restrict__ out, int N,
+                                                int R, int nlines, int Ns, const cplx<T> *__restrict__ tw,
+                                                int sign) {
+  const int M = N / R;
+  const int step = N / (Ns * R);
+  const int items = nlines * M;
+  const int LS = lstride(N);
+  for (int it = threadIdx.x; it < items; it += blockDim.x) {
+    const int line = it / M, j = it - line * M;
+    const int q = j / Ns, k = j - q * Ns;
+    const cplx<T> *src = in + line * LS;
+    cplx<T> *dst = out + line * LS;
+    const int o = q * Ns * R + k;
+    for (int qq = 0; qq < R; ++qq) {
+      cplx<T> acc = src[lpos(j)];
+      int e = 0;  // (r qq) mod R
+      for (int r = 1; r < R; ++r) {
+        e += qq;
+        if (e >= R) e -= R;
+        cplx<T> v = src[lpos(j + r * M)];
+        if (k) {
+          cplx<T> w = tw[r * k * step];  // r k step < R Ns step = N
+          if (sign > 0) w.im = -w.im;
+          v = cmul(v, w);
+        }
+        cplx<T> w = tw[e * M];
+        if (sign > 0) w.im = -w.im;
+        acc = acc + cmul(v, w);
+      }
+      dst[lpos(o + qq * Ns)] = acc;
+    }
+  }
+}
+
 // The same stage with the element reads and writes as functors, load(idx)
 // and store(idx, value) with idx = line * N + position, so that a caller can
 // fuse a multiply into the loads of a stage or its point update into the
@@ -385,7 +425,8 @@ __device__ int fft_lines(cplx<T> *buf0, cplx<T> *buf1, const RadixPlan &rp, int 
     else if (R == 4) stockham_stage<T, 4>(b[cur], b[cur ^ 1], rp.n, nlines, Ns, tw, sign);
     else if (R == 2) stockham_stage<T, 2>(b[cur], b[cur ^ 1], rp.n, nlines, Ns, tw, sign);
     else if (R == 3) stockham_stage<T, 3>(b[cur], b[cur ^ 1], rp.n, nlines, Ns, tw, sign);
-    else stockham_stage<T, 5>(b[cur], b[cur ^ 1], rp.n, nlines, Ns, tw, sign);
+    else if (R == 5) stockham_stage<T, 5>(b[cur], b[cur ^ 1], rp.n, nlines, Ns, tw, sign);
+    else stockham_stage_gen<T>(b[cur], b[cur ^ 1], rp.n, R, nlines, Ns, tw, sign);
     __syncthreads();
     cur ^= 1;
     Ns *= R;
@@ -533,7 +574,39 @@ __device__ __forceinline__ void stage_s(const cplx<T> *__restrict__ in, Store st
   }
 }
 
+// stage_s with a runtime prime radix R (the direct sum of stockham_stage_gen).
 template <typename T, int SIGN, typename Store, typename TwF>
+__device__ void stage_s_gen(int R, const cplx<T> *__restrict__ in, Store store, int N, int nlines, int Ns,
+                            bool lfast, TwF twf) {
+  const int M = N / R;
+  const int step = N / (Ns * R);
+  const int items = nlines * M;
+  const int LS = lstride(N);
+  for (int it = threadIdx.x; it < items; it += blockDim.x) {
+    int line, j;
+    if (lfast) { j = it / nlines; line = it - j * nlines; }
+    else { line = it / M; j = it - line * M; }
+    const int q = j / Ns, k = j - q * Ns;
+    const cplx<T> *src = in + line * LS;
+    const int o = q * Ns * R + k;
+    for (int qq = 0; qq < R; ++qq) {
+      cplx<T> acc = src[lpos(j)];
+      int e = 0;
+      for (int r = 1; r < R; ++r) {
+        e += qq;
+        if (e >= R) e -= R;
+        cplx<T> v = src[lpos(j + r * M)];
+        if (k) v = twmul<SIGN>(v, twf(r * k * step));
+        acc = acc + twmul<SIGN>(v, twf(e * M));
+      }
+      store(line, o + qq * Ns, acc);
+    }
+  }
+}
+
+// GEN: also take prime radices outside {2, 3, 5} (callers whose plans may
+// hold them; the step kernels' plans never do).
+template <typename T, int SIGN, bool GEN = false, typename Store, typename TwF>
 __device__ __forceinline__ void stage_s_any(int R, const cplx<T> *__restrict__ in, Store store, int N, int nlines,
                                             int Ns, bool lfast, TwF twf) {
   if (R == 16) stage_s<T, 16, SIGN>(in, store, N, nlines, Ns, lfast, twf);
@@ -541,7 +614,8 @@ __device__ __forceinline__ void stage_s_any(int R, const cplx<T> *__restrict__ i
   else if (R == 4) stage_s<T, 4, SIGN>(in, store, N, nlines, Ns, lfast, twf);
   else if (R == 2) stage_s<T, 2, SIGN>(in, store, N, nlines, Ns, lfast, twf);
   else if (R == 3) stage_s<T, 3, SIGN>(in, store, N, nlines, Ns, lfast, twf);
-  else stage_s<T, 5, SIGN>(in, store, N, nlines, Ns, lfast, twf);
+  else if (!GEN || R == 5) stage_s<T, 5, SIGN>(in, store, N, nlines, Ns, lfast, twf);
+  else stage_s_gen<T, SIGN>(R, in, store, N, nlines, Ns, lfast, twf);
 }
 
 // T_d of a batch of lines held in shared memory: forward FFT, the kinetic

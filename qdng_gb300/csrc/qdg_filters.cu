@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(256) spectral_expec_kernel(SpecExpecArgs a) {
     int cur = 0, Ns = 1;
     for (int st = 0; st < a.rp.nstages; ++st) {
       cplx<double> *dst = bb[cur ^ 1];
-      stage_s_any<double, -1>(a.rp.radix[st], bb[cur], [dst](int, int i, cplx<double> v) { dst[lpos(i)] = v; }, N, 1,
+      stage_s_any<double, -1, true>(a.rp.radix[st], bb[cur], [dst](int, int i, cplx<double> v) { dst[lpos(i)] = v; }, N, 1,
                               Ns, false, twf);
       __syncthreads();
       cur ^= 1;

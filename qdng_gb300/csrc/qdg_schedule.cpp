@@ -124,6 +124,27 @@ bool greedy_radix(int n, RadixPlan &rp) {
   return m == 1;
 }
 
+bool any_radix(int n, RadixPlan &rp) {
+  if (n < 1) return false;
+  greedy_radix(n, rp);
+  int m = n;
+  for (int i = 0; i < rp.nstages; ++i) m /= rp.radix[i];
+  // the other prime factors, ascending, one direct-DFT stage each
+  for (int p = 7; m > 1 && rp.nstages < 16; p += 2) {
+    if ((long long)p * p > m) p = m;  // what is left is prime
+    while (m % p == 0 && rp.nstages < 16) { rp.radix[rp.nstages++] = p; m /= p; }
+  }
+  return m == 1;
+}
+
+bool generic_radix(const RadixPlan &rp) {
+  for (int i = 0; i < rp.nstages; ++i) {
+    const int r = rp.radix[i];
+    if (r != 2 && r != 3 && r != 4 && r != 5 && r != 8 && r != 16) return true;
+  }
+  return false;
+}
+
 bool schedule_radix(int context, int n, int precision, RadixPlan &rp) {
   Entry e;
   if (lookup(context, n, precision, e)) {

@@ -44,11 +44,13 @@ def _check(golden_line, obs_row, nstates):
 
 def test_fft_matches_numpy():
     rng = np.random.default_rng(1)
-    for n in [1, 2, 3, 5, 8, 9, 12, 64, 96, 128, 384, 1024, 1536, 3072, 4096]:
+    # 2^a 3^b 5^c and lengths with other prime factors (FFTW takes any N):
+    # 7, 11 x 13, the primes 97 and 257 (above the radix buffers of 64)
+    for n in [1, 2, 3, 5, 8, 9, 12, 64, 96, 128, 384, 1024, 1536, 3072, 4096, 7, 28, 143, 97, 257, 2 * 3 * 7 * 11]:
         x = rng.normal(size=n) + 1j * rng.normal(size=n)
         ref = np.fft.fft(x)
         sc = np.abs(ref).max()
-        assert np.abs(O.fft1(x, -1) - ref).max() <= 1e-14 * sc
+        assert np.abs(O.fft1(x, -1) - ref).max() <= 1e-14 * sc, n
         assert np.abs(O.fft1(x, +1) - np.fft.ifft(x) * n).max() <= 1e-14 * sc
 
 
