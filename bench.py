@@ -490,6 +490,9 @@ def ensemble_arm(args, world, rank, local):
             nrms.append(float(abs(n - n_ref) / n_ref))
         err = {"max_rel_psi_error_vs_fp64": max(errs), "median": float(np.median(errs)),
                "max_rel_autocorrelation_error": max(acs), "max_rel_norm_error": max(nrms), "steps": args.steps}
+    plain = None
+    if args.plain_baseline and rank == 0:
+        plain = plain_fp64_members(ens, E, psi0, args.steps, dt_max / args.steps)
     bytes_io = int(sum(p.size for p in psi0) * 16)
     line = {
         "metric": "wavepackets/s (512 laser-driven members, 5000 steps each)",
@@ -511,10 +514,48 @@ def ensemble_arm(args, world, rank, local):
                 "h2d_bytes_per_step": bytes_io // args.steps, "d2h_bytes_per_step": bytes_io // args.steps},
         "gpu_launches": int(launches),
         "error_vs_fp64": err,
+        "plain_fp64_path": plain,
         "clocks": clocks,
     }
     if rank == 0:
         print(json.dumps(line))
+
+
+def plain_fp64_members(ens, E, psi0, steps, batched_s_per_step):
+    """The batched form against the plain binary64 GPU path: the same members
+    one at a time, each through its own plan and Chebyshev propagator (the
+    qdg_prop_run call), device time of the steps only (plan set-up excluded),
+    and the largest difference between the two results per member."""
+    import numpy as np
+    import torch
+
+    from qdng_gb300 import engine
+    from tests import cases
+
+    total = 0.0
+    outs = []
+    for m in ens:
+        plan = engine.Plan(cases.member_hplan(m), "fp64")
+        P = engine.Propagator(plan, "Cheby", "", dt=10.0)
+        w = plan.wavefunction(m["psi"])
+        plan.synchronize()
+        t0 = time.perf_counter()
+        P.run(w, 0, steps)
+        plan.synchronize()
+        total += time.perf_counter() - t0
+        outs.append(w.download())
+        P.close()
+        w.close()
+        plan.close()
+    torch.cuda.synchronize()
+    R = engine.Ensemble(ens, dt=10.0, precision="fp64")
+    R.upload(psi0)
+    R.run(0, steps)
+    diff = max(float(np.abs(a - b).max() / np.abs(b).max()) for a, b in zip(R.download(), outs))
+    plain_s = total / steps
+    return {"ms_per_step": round(plain_s * 1e3, 3), "batched_speedup": round(plain_s / batched_s_per_step, 2),
+            "max_rel_diff_batched_fp64_vs_plain": diff, "steps": steps,
+            "what": "every member one at a time: its own plan, Cheby propagator and qdg_prop_run (binary64)"}
 
 
 def reference_arm(args, world, rank):
@@ -572,6 +613,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="cfg2", choices=list(WORKLOADS) + ["ensemble"])
     ap.add_argument("--members", type=int, default=512)
+    ap.add_argument("--plain-baseline", action="store_true",
+                    help="ensemble: also run the members one at a time through the plain binary64 plan API")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
