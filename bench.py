@@ -360,8 +360,15 @@ def engine_arm(args, world, rank, local):
         # pipe (the mixed and double-float forms: latency of the term chain)
         limiter = ("FP64 pipe (binary64 FFTs; cfg2: 60% busy in ncu, working set L2-resident)"
                    if args.precision == "fp64" and modes[top] == "cheby_step" else None)
+        # the bound that does apply to the binary64 step kernels: how busy the
+        # FP64 pipe is, from the ncu capture of the same kernel
+        # (sm__inst_executed_pipe_fp64.avg.pct_of_peak_sustained_active, profiles/)
+        fp64_busy = None
+        if args.precision == "fp64" and modes[top] == "cheby_step":
+            fp64_busy = {"cfg2": 59.5, "cfg1": 36.1}.get(args.workload)
         roof = {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(ach / peak, 4), "traffic": traffic, "kernel": kname, "limiter": limiter,
+                "fp64_pipe_busy_pct_ncu": fp64_busy,
                 "algorithmic_bytes_per_launch": int(per_launch), "bytes_note": what,
                 "avg_launch_us": round(avg_s * 1e6, 2), "peak_source": peak_src + " (MEASURED_PEAKS.json hbm_gbs)"}
     per_mode = {modes[i]: {"ms": round(float(prof_ms[i]), 3), "launches": int(prof_n[i])}

@@ -144,3 +144,35 @@ def test_cfg4_member_size_classes(eng):
         err_psi = rel(out[i], x)
         err_ac = abs(np.vdot(p0, out[i]) - np.vdot(p0, x)) / abs(np.vdot(p0, x))
         assert err_psi < 1e-12 and err_ac < 1e-12, (m["grid"].n, err_psi, err_ac)
+
+
+def _horizon(eng, hp, psi, run, params):
+    plan = eng.Plan(hp, "fp64")
+    fwd = eng.Propagator(plan, run["name"], params, dt=run["dt"])
+    bwd = eng.Propagator(plan, run["name"], params, dt=run["dt"], backward=True)
+    w = plan.wavefunction(psi)
+    o0 = plan.observables(w)
+    fwd.run(w, 0, run["steps"])
+    o1 = plan.observables(w)
+    bwd.run(w, 0, run["steps"])
+    dn = abs(o1["norm2"] - o0["norm2"]) / o0["norm2"]
+    de = abs(o1["energy"] - o0["energy"]) / abs(o0["energy"])
+    return dn, de, rel(w.download(), psi)
+
+
+def test_cfg2_full_horizon_time_reversal(eng):
+    """The whole cfg2 horizon (4000 steps of dt = 5 on 256 x 256 x 2 states)
+    in binary64, checked by properties that hold at any length: the norm and
+    <H> of the time-independent Hamiltonian stay put, and 4000 steps backward
+    return psi_0.  (The oracle comparison at this size covers 100 steps.)
+    With the reference's default series precision (1e-10, OCheby.h:11) every
+    step is truncated at that level, so the drift over 4000 steps is bounded
+    by 4000 x 1e-10; with prec = 1e-14 what is left is rounding."""
+    hp, psi, run = cases.cfg2_two_state()
+    dn, de, dr = _horizon(eng, hp, psi, run, run["params"])
+    print(f"cfg2 4000 steps, prec 1e-10: norm drift {dn:.3g}, <H> drift {de:.3g}, forward-backward {dr:.3g}")
+    assert dn <= run["steps"] * 1e-10 and de <= run["steps"] * 1e-10
+    dn, de, dr = _horizon(eng, hp, psi, run, "prec=1e-14")
+    print(f"cfg2 4000 steps, prec 1e-14: norm drift {dn:.3g}, <H> drift {de:.3g}, forward-backward {dr:.3g}")
+    # measured on a GB300: 8.1e-12, 1.1e-12, 4.1e-11
+    assert dn <= 1e-10 and de <= 1e-10 and dr <= 1e-9
