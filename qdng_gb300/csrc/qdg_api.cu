@@ -1708,8 +1708,9 @@ qdg_status krylov_alloc(qdg_prop *P) {
   // Krylov scalars: Lanczos alpha, beta, |psi|, order (2 m + 2); Arnoldi H (2 m^2) and |psi|
   const size_t nks = std::max<size_t>(2 * (size_t)P->kord + 2, 2 * (size_t)P->kord * P->kord + 1);
   CK(cudaMalloc(&P->d_ks, sizeof(double) * nks));
-  CK(cudaMalloc(&P->d_kdone, 3 * sizeof(int)));  // stop flags [0], [1]; Arnoldi order [2]
-  const int o0[3] = {0, 0, P->kord};             // the reference starts at the full order
+  // stop flags [0], [1]; Arnoldi order [2]; [3] the ticket of the fused launches
+  CK(cudaMalloc(&P->d_kdone, 4 * sizeof(int)));
+  const int o0[4] = {0, 0, P->kord, 0};          // the reference starts at the full order
   CK(cudaMemcpy(P->d_kdone, o0, sizeof(o0), cudaMemcpyHostToDevice));
   CK(cudaMallocHost(&P->h_ks, sizeof(double) * nks));
   CK(cudaMallocHost(&P->h_kdone, sizeof(int)));
@@ -1746,12 +1747,6 @@ qdg_status sil_body(qdg_prop *P, cplx<double> *psi) {
   const int grid = dots_grid(p);
   double w = 1.0;
   for (int d = 0; d < p->nd; ++d) w *= p->dx[d];
-  auto finish = [&](int mode, int slot, int it) {
-    qdg::KsFinish f;
-    f.grid = grid; f.S = p->S; f.mode = mode; f.slot = slot; f.order = order; f.w = w;
-    f.it = it; f.dt = P->dt; f.tol = P->err;
-    return qdg::launch_ks_finish(p->d_partials, f, ks, done, p->stream);
-  };
   Epi e;
   e.done = done;
   auto hq_if = [&](const cplx<T> *q, cplx<T> *out) {
@@ -1759,34 +1754,41 @@ qdg_status sil_body(qdg_prop *P, cplx<double> *psi) {
     return run_h<T>(p, qdg::PM_HAPPLY, q, e);
   };
   qdg_status s;
+  // each dot product's block partials are finished by the last block of its
+  // own launch (the fused kernels), so an iteration is H q, <q|H q> -> alpha,
+  // the two updates with |w|^2 -> beta, and the normalisation with the commit
+  unsigned int *ticket = reinterpret_cast<unsigned int *>(done + 3);
+  auto fin = [&](int mode, int slot, int it) {
+    qdg::KsFinish f;
+    f.grid = grid; f.S = p->S; f.mode = mode; f.slot = slot; f.order = order; f.w = w;
+    f.it = it; f.dt = P->dt; f.tol = P->err;
+    return f;
+  };
   CK(cudaMemsetAsync(ks, 0, sizeof(double) * (2 * order + 2), p->stream));
   CK(cudaMemsetAsync(done, 0, 2 * sizeof(int), p->stream));
-  CK(qdg::launch_dots_if<double, double>(psi, psi, p->S, p->npts, p->d_partials, grid, done, p->stream));
-  CK(finish(qdg::KS_PSN, 2 * order, 0));
+  CK(qdg::launch_dots_ks<double, double>(psi, psi, p->S, p->npts, p->d_partials, fin(qdg::KS_PSN, 2 * order, 0), ks,
+                                         done, ticket, p->stream));
   CK(qdg::launch_convert<T>(L[0], psi, n, p->stream));
-  if ((s = hq_if(L[0], buf0)) != QDG_OK) return s;
-  CK(qdg::launch_dots_if<T, T>(L[0], buf0, p->S, p->npts, p->d_partials, grid, done, p->stream));
-  CK(finish(qdg::KS_ALPHA, 0, 0));
-  CK(cudaMemcpyAsync(L[1], buf0, sizeof(cplx<T>) * n, cudaMemcpyDeviceToDevice, p->stream));
+  if ((s = hq_if(L[0], L[1])) != QDG_OK) return s;
+  CK(qdg::launch_dots_ks<T, T>(L[0], L[1], p->S, p->npts, p->d_partials, fin(qdg::KS_ALPHA, 0, 0), ks, done, ticket,
+                               p->stream));
   CK(qdg::launch_ks_lincomb<T>(L[1], L[0], ks, 0, n, done, p->stream));
-  CK(qdg::launch_dots_if<T, T>(L[1], L[1], p->S, p->npts, p->d_partials, grid, done, p->stream));
-  CK(finish(qdg::KS_BETA, order + 0, 0));
-  CK(qdg::launch_ks_lincomb<T>(L[1], (const cplx<T> *)nullptr, ks, order + 0, n, done, p->stream));
+  CK(qdg::launch_dots_ks<T, T>(L[1], L[1], p->S, p->npts, p->d_partials, fin(qdg::KS_BETA, order + 0, 0), ks, done,
+                               ticket, p->stream));
+  CK(qdg::launch_ks_scale_commit<T>(L[1], ks, order + 0, n, done, ticket, p->stream));
   for (int it = 2; it < order; ++it) {
     if ((s = hq_if(L[it - 1], L[it])) != QDG_OK) return s;
-    CK(qdg::launch_dots_if<T, T>(L[it - 1], L[it], p->S, p->npts, p->d_partials, grid, done, p->stream));
-    CK(finish(qdg::KS_ALPHA, it - 1, it));
-    CK(qdg::launch_ks_lincomb<T>(L[it], L[it - 1], ks, it - 1, n, done, p->stream));
-    CK(qdg::launch_ks_lincomb<T>(L[it], L[it - 2], ks, order + it - 2, n, done, p->stream));
-    CK(qdg::launch_dots_if<T, T>(L[it], L[it], p->S, p->npts, p->d_partials, grid, done, p->stream));
-    CK(finish(qdg::KS_BETA, order + it - 1, it));
-    CK(qdg::launch_ks_lincomb<T>(L[it], (const cplx<T> *)nullptr, ks, order + it - 1, n, done, p->stream));
-    CK(qdg::launch_ks_commit(done, p->stream));
+    CK(qdg::launch_dots_ks<T, T>(L[it - 1], L[it], p->S, p->npts, p->d_partials, fin(qdg::KS_ALPHA, it - 1, it), ks,
+                                 done, ticket, p->stream));
+    CK(qdg::launch_ks_lincomb2_dot<T>(L[it], L[it - 1], it - 1, L[it - 2], order + it - 2, p->S, p->npts,
+                                      p->d_partials, fin(qdg::KS_BETA, order + it - 1, it), ks, done, ticket,
+                                      p->stream));
+    CK(qdg::launch_ks_scale_commit<T>(L[it], ks, order + it - 1, n, done, ticket, p->stream));
   }
   // alpha of the last vector when the recursion ran to the full order
   if ((s = hq_if(L[order - 1], buf0)) != QDG_OK) return s;
-  CK(qdg::launch_dots_if<T, T>(L[order - 1], buf0, p->S, p->npts, p->d_partials, grid, done, p->stream));
-  CK(finish(qdg::KS_ALPHA, order - 1, order));
+  CK(qdg::launch_dots_ks<T, T>(L[order - 1], buf0, p->S, p->npts, p->d_partials,
+                               fin(qdg::KS_ALPHA, order - 1, order), ks, done, ticket, p->stream));
   CK(cudaMemcpyAsync(P->h_ks, ks, sizeof(double) * (2 * order + 2), cudaMemcpyDeviceToHost, p->stream));
   CK(cudaMemcpyAsync(P->h_kdone, done, sizeof(int), cudaMemcpyDeviceToHost, p->stream));
   return QDG_OK;
@@ -1894,22 +1896,27 @@ qdg_status arnoldi_body(qdg_prop *P, cplx<double> *psi) {
     return run_h<T>(p, qdg::PM_HAPPLY, q, e);
   };
   qdg_status s;
+  // fused launches (each dot product finished by the last block of its own
+  // launch): H q, <q_0|H q>, then per Gram-Schmidt step the update together
+  // with the next dot product (the last one with |w|^2), and the
+  // normalisation together with the commit
+  unsigned int *ticket = reinterpret_cast<unsigned int *>(done + 3);
   CK(cudaMemsetAsync(ks, 0, sizeof(double) * (2 * (size_t)m * m + 1), p->stream));
   CK(cudaMemsetAsync(done, 0, 2 * sizeof(int), p->stream));
-  CK(qdg::launch_dots_if<double, double>(psi, psi, p->S, p->npts, p->d_partials, grid, done, p->stream));
-  CK(qdg::launch_ka_finish(p->d_partials, ka, qdg::KA_PSN, 0, 0, ks, ia, done, p->stream));
+  CK(qdg::launch_dots_ka<double, double>(psi, psi, p->S, p->npts, p->d_partials, ka, qdg::KA_PSN, 0, 0, ks, ia, done,
+                                         ticket, p->stream));
   CK(qdg::launch_convert<T>(L[0], psi, n, p->stream));
   for (int it = 1; it < m; ++it) {
     if ((s = hq_if(L[it - 1], buf0)) != QDG_OK) return s;
+    CK(qdg::launch_dots_ka<T, T>(L[0], buf0, p->S, p->npts, p->d_partials, ka, qdg::KA_H, 0, it - 1, ks, ia, done,
+                                 ticket, p->stream));
     for (int j = 0; j <= it - 1; ++j) {  // modified Gram-Schmidt
-      CK(qdg::launch_dots_if<T, T>(L[j], buf0, p->S, p->npts, p->d_partials, grid, done, p->stream));
-      CK(qdg::launch_ka_finish(p->d_partials, ka, qdg::KA_H, j, it - 1, ks, ia, done, p->stream));
-      CK(qdg::launch_ka_lincomb<T>(buf0, L[j], ks, m, j, it - 1, n, done, p->stream));
+      const bool next = j + 1 <= it - 1;
+      CK(qdg::launch_ka_lincomb_dot<T>(buf0, L[j], next ? L[j + 1] : nullptr, j, p->S, p->npts, p->d_partials, ka,
+                                       next ? qdg::KA_H : qdg::KA_NORM, next ? j + 1 : it, it - 1, ks, ia, done,
+                                       ticket, p->stream));
     }
-    CK(qdg::launch_dots_if<T, T>(buf0, buf0, p->S, p->npts, p->d_partials, grid, done, p->stream));
-    CK(qdg::launch_ka_finish(p->d_partials, ka, qdg::KA_NORM, it, it - 1, ks, ia, done, p->stream));
-    CK(qdg::launch_ks_lincomb<T>(buf0, (const cplx<T> *)nullptr, ks, 2 * (it * m + it - 1), n, done, p->stream));
-    CK(qdg::launch_ka_commit<T>(L[it], buf0, n, it, ia, done, p->stream));
+    CK(qdg::launch_ka_scale_commit<T>(L[it], buf0, ks, 2 * (it * m + it - 1), n, it, ia, done, ticket, p->stream));
   }
   // last column H[j][order-1] from H q_{order-1}
   qdg::KaBasis<T> kb;
@@ -1918,10 +1925,9 @@ qdg_status arnoldi_body(qdg_prop *P, cplx<double> *psi) {
   CK(qdg::launch_ka_select<T>(last, kb, ia, n, p->stream));
   e.done = nullptr;
   if ((s = hq_if(last, buf0)) != QDG_OK) return s;
-  for (int j = 0; j < m; ++j) {
-    CK(qdg::launch_dots_lt<T>(L[j], buf0, p->S, p->npts, p->d_partials, grid, ia, j, p->stream));
-    CK(qdg::launch_ka_finish(p->d_partials, ka, qdg::KA_LAST, j, 0, ks, ia, done, p->stream));
-  }
+  for (int j = 0; j < m; ++j)
+    CK(qdg::launch_dots_ka<T, T>(L[j], buf0, p->S, p->npts, p->d_partials, ka, qdg::KA_LAST, j, 0, ks, ia, done,
+                                 ticket, p->stream));
   CK(cudaMemcpyAsync(P->h_ks, ks, sizeof(double) * (2 * (size_t)m * m + 1), cudaMemcpyDeviceToHost, p->stream));
   CK(cudaMemcpyAsync(P->h_kdone, ia, sizeof(int), cudaMemcpyDeviceToHost, p->stream));
   return QDG_OK;

@@ -681,17 +681,6 @@ cudaError_t launch_dots(const cplx<T> *a, const cplx<U> *b, int S, long long npt
   COUNT_LAUNCH();
   return cudaGetLastError();
 }
-template <typename T, typename U>
-cudaError_t launch_dots_if(const cplx<T> *a, const cplx<U> *b, int S, long long npts, double *partials, int grid,
-                           const int *done, cudaStream_t st) {
-  dots_kernel<T, U><<<grid, 256, 0, st>>>(a, b, S, npts, partials, done);
-  COUNT_LAUNCH();
-  return cudaGetLastError();
-}
-template cudaError_t launch_dots_if<double, double>(const cplx<double> *, const cplx<double> *, int, long long,
-                                                    double *, int, const int *, cudaStream_t);
-template cudaError_t launch_dots_if<float, float>(const cplx<float> *, const cplx<float> *, int, long long, double *,
-                                                  int, const int *, cudaStream_t);
 
 // Per-state sums of the dots kernels' block partials (layout
 // [block][state][re, im]) in the order of the host's dot products: blocks
@@ -729,8 +718,7 @@ __device__ __forceinline__ void sum_partials(const double *partials, int grid, i
 
 // Partial sums -> scalar, summed in the order of the host's dot products
 // (blocks outer, states inner; states weighted, then added in order).
-__global__ void ks_finish_kernel(const double *partials, KsFinish f, double *ks, int *done) {
-  if (*done) return;  // same value for every thread: nothing in the kernel writes done[0]
+__device__ void ks_finish_body(const double *partials, const KsFinish &f, double *ks, int *done) {
   double re[kMaxStates], im[kMaxStates];
   sum_partials(partials, f.grid, f.S, re, im);
   if (threadIdx.x != 0) return;
@@ -754,15 +742,8 @@ __global__ void ks_finish_kernel(const double *partials, KsFinish f, double *ks,
   }
 }
 
-__global__ void ks_commit_kernel(int *done) {
-  if (threadIdx.x == 0 && done[1]) done[0] = 1;
-}
-__global__ void ka_finish_kernel(const double *partials, KaArgs a, int op, int j, int col, double *ks, int *ia,
-                                 int *done) {
-  // both exits are the same for every thread: done[0] and ia[0] are written
-  // below by thread 0 only after every thread has read them
-  if (op != KA_LAST && *done) return;
-  if (op == KA_LAST && j >= ia[0]) return;
+__device__ void ka_finish_body(const double *partials, const KaArgs &a, int op, int j, int col, double *ks, int *ia,
+                               int *done) {
   double re[kMaxStates], im[kMaxStates];
   sum_partials(partials, a.grid, a.S, re, im);
   if (threadIdx.x != 0) return;
@@ -797,62 +778,210 @@ __global__ void ka_finish_kernel(const double *partials, KaArgs a, int op, int j
   }
   if (hypot(er, ei) < a.conv) done[1] = 1;  // after this iteration's vector is stored
 }
-cudaError_t launch_ka_finish(const double *partials, const KaArgs &a, int op, int j, int col, double *ks, int *ia,
-                             int *done, cudaStream_t st) {
-  ka_finish_kernel<<<1, 32, 0, st>>>(partials, a, op, j, col, ks, ia, done);
-  COUNT_LAUNCH();
-  return cudaGetLastError();
+
+// ---- fused Krylov launches: a pass over the vectors, its dot product's
+// block partials, and the finishing scalar work in the block that arrives
+// last (an atomic ticket: no block waits for another).  The sums are those
+// of the dots + finish launches they replace (same partial layout, same
+// order), and the vector arithmetic is that of the lincomb kernels.
+
+// True in the one block whose ticket is the last of the grid; its threads
+// then see every block's partials (each block fenced before its ticket).
+__device__ __forceinline__ bool arrive_last(unsigned int *ticket) {
+  __shared__ unsigned int last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(ticket, 1u) == gridDim.x - 1 ? 1u : 0u;
+  }
+  __syncthreads();
+  return last != 0;
 }
 
-template <typename T>
-__global__ void ka_lincomb_kernel(cplx<T> *y, const cplx<T> *x, const double *ks, int m, int j, int col, long long n,
-                                  const int *done) {
-  if (*done) return;
-  const cplx<double> a = cplx<double>{1.0, 0.0};
-  const cplx<double> b = cplx<double>{-ks[2 * (j * m + col)], -ks[2 * (j * m + col) + 1]};
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    cplx<double> r = dmul(ccast<double>(ld(y + i)), a);
-    r = r + dmul(ccast<double>(ld(x + i)), b);
-    st(y + i, ccast<T>(r));
+// Partials of a per-state dot product whose terms t(s, i) = conj(a) b are
+// produced by a functor (which may also update the vectors).
+template <typename Term>
+__device__ __forceinline__ void dots_terms(int S, long long npts, double *partials, Term term) {
+  __shared__ double red[32];
+  for (int s = 0; s < S; ++s) {
+    double re = 0, im = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npts;
+         i += (long long)gridDim.x * blockDim.x) {
+      cplx<double> x, y;
+      term((long long)s * npts + i, x, y);
+      re += x.re * y.re + x.im * y.im;
+      im += x.re * y.im - x.im * y.re;
+    }
+    const double tr = block_sum(re, red);
+    const double ti = block_sum(im, red);
+    if (threadIdx.x == 0) {
+      partials[((long long)blockIdx.x * S + s) * 2 + 0] = tr;
+      partials[((long long)blockIdx.x * S + s) * 2 + 1] = ti;
+    }
   }
 }
-template <typename T>
-cudaError_t launch_ka_lincomb(cplx<T> *y, const cplx<T> *x, const double *ks, int m, int j, int col, long long n,
-                              const int *done, cudaStream_t st) {
-  ka_lincomb_kernel<T><<<ew_grid(n), 256, 0, st>>>(y, x, ks, m, j, col, n, done);
-  COUNT_LAUNCH();
-  return cudaGetLastError();
-}
-template cudaError_t launch_ka_lincomb<double>(cplx<double> *, const cplx<double> *, const double *, int, int, int,
-                                               long long, const int *, cudaStream_t);
-template cudaError_t launch_ka_lincomb<float>(cplx<float> *, const cplx<float> *, const double *, int, int, int,
-                                              long long, const int *, cudaStream_t);
 
-// The commit reads done[0] as set before this iteration; its own error test
-// (done[1]) takes effect for the kernels after it.
+// <a|b> finished into the Lanczos scalars (dots_if + ks_finish)
+template <typename T, typename U>
+__global__ void dots_ks_kernel(const cplx<T> *a, const cplx<U> *b, int S, long long npts, double *partials,
+                               KsFinish f, double *ks, int *done, unsigned int *ticket) {
+  if (*done) return;
+  dots_body<T, U>(a, b, S, npts, partials);
+  if (!arrive_last(ticket)) return;
+  ks_finish_body(partials, f, ks, done);
+  if (threadIdx.x == 0) *ticket = 0;
+}
+// y -= alpha x1 (rounded to T), y -= beta x2, then |y|^2 finished as beta
+// (two ks_lincomb launches + dots_if + ks_finish)
 template <typename T>
-__global__ void ka_commit_kernel(cplx<T> *q, const cplx<T> *buf, long long n, int it, int *ia, int *done) {
-  if (*(volatile int *)done) return;
+__global__ void ks_lincomb2_dot_kernel(cplx<T> *y, const cplx<T> *x1, int i1, const cplx<T> *x2, int i2, int S,
+                                       long long npts, double *partials, KsFinish f, double *ks, int *done,
+                                       unsigned int *ticket) {
+  if (*done) return;
+  const cplx<double> one = cplx<double>{1.0, 0.0};
+  const cplx<double> b1 = cplx<double>{-ks[i1], 0.0}, b2 = cplx<double>{-ks[i2], 0.0};
+  dots_terms(S, npts, partials, [&](long long g, cplx<double> &xa, cplx<double> &xb) {
+    const cplx<T> r1 = ccast<T>(dmul(ccast<double>(ld(y + g)), one) + dmul(ccast<double>(ld(x1 + g)), b1));
+    const cplx<T> r2 = ccast<T>(dmul(ccast<double>(r1), one) + dmul(ccast<double>(ld(x2 + g)), b2));
+    st(y + g, r2);
+    xa = xb = ccast<double>(r2);
+  });
+  if (!arrive_last(ticket)) return;
+  ks_finish_body(partials, f, ks, done);
+  if (threadIdx.x == 0) *ticket = 0;
+}
+// y /= ks[idx] (ks_lincomb without x), then done[0] |= done[1] in the last
+// block (ks_commit) once every block has read done[0]
+template <typename T>
+__global__ void ks_scale_commit_kernel(cplx<T> *y, const double *ks, int idx, long long n, int *done,
+                                       unsigned int *ticket) {
+  if (*done) return;
+  const cplx<double> a = cplx<double>{1.0 / ks[idx], 0.0};
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    q[i] = buf[i];
+    st(y + i, ccast<T>(dmul(ccast<double>(ld(y + i)), a)));
+  if (!arrive_last(ticket)) return;
+  if (threadIdx.x == 0) {
+    if (done[1]) done[0] = 1;
+    *ticket = 0;
+  }
 }
-__global__ void ka_order_kernel(int it, int *ia, int *done) {
-  if (threadIdx.x != 0 || done[0]) return;
-  ia[0] = it + 1;
-  if (done[1]) done[0] = 1;
+// <a|b> finished into the Arnoldi scalars (dots_if / dots_lt + ka_finish)
+template <typename T, typename U>
+__global__ void dots_ka_kernel(const cplx<T> *a, const cplx<U> *b, int S, long long npts, double *partials,
+                               KaArgs ka, int op, int j, int col, double *ks, int *ia, int *done,
+                               unsigned int *ticket) {
+  if (op != KA_LAST && *done) return;
+  if (op == KA_LAST && j >= ia[0]) return;
+  dots_body<T, U>(a, b, S, npts, partials);
+  if (!arrive_last(ticket)) return;
+  ka_finish_body(partials, ka, op, j, col, ks, ia, done);
+  if (threadIdx.x == 0) *ticket = 0;
 }
+// one modified Gram-Schmidt step y -= H[jc][col] x, then the next dot
+// product <a|y> (a = nullptr: <y|y>) finished as op (ka_lincomb + dots_if +
+// ka_finish)
 template <typename T>
-cudaError_t launch_ka_commit(cplx<T> *q, const cplx<T> *buf, long long n, int it, int *ia, int *done, cudaStream_t st) {
-  ka_commit_kernel<T><<<ew_grid(n), 256, 0, st>>>(q, buf, n, it, ia, done);
-  ka_order_kernel<<<1, 32, 0, st>>>(it, ia, done);
-  COUNT_LAUNCH();
+__global__ void ka_lincomb_dot_kernel(cplx<T> *y, const cplx<T> *x, const cplx<T> *a, int jc, int S,
+                                      long long npts, double *partials, KaArgs ka, int op, int j, int col, double *ks,
+                                      int *ia, int *done, unsigned int *ticket) {
+  if (*done) return;
+  const int m = ka.m;
+  const cplx<double> one = cplx<double>{1.0, 0.0};
+  const cplx<double> b = cplx<double>{-ks[2 * (jc * m + col)], -ks[2 * (jc * m + col) + 1]};
+  dots_terms(S, npts, partials, [&](long long g, cplx<double> &xa, cplx<double> &xb) {
+    const cplx<T> r = ccast<T>(dmul(ccast<double>(ld(y + g)), one) + dmul(ccast<double>(ld(x + g)), b));
+    st(y + g, r);
+    xb = ccast<double>(r);
+    xa = a ? ccast<double>(ld(a + g)) : xb;
+  });
+  if (!arrive_last(ticket)) return;
+  ka_finish_body(partials, ka, op, j, col, ks, ia, done);
+  if (threadIdx.x == 0) *ticket = 0;
+}
+// q = buf / H[it][it-1] (ks_lincomb without x, then ka_commit's copy), and
+// in the last block ia[0] = it + 1, done[0] |= done[1] (ka_order)
+template <typename T>
+__global__ void ka_scale_commit_kernel(cplx<T> *q, const cplx<T> *buf, const double *ks, int idx, long long n, int it,
+                                       int *ia, int *done, unsigned int *ticket) {
+  if (*done) return;
+  const cplx<double> a = cplx<double>{1.0 / ks[idx], 0.0};
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    st(q + i, ccast<T>(dmul(ccast<double>(ld(buf + i)), a)));
+  if (!arrive_last(ticket)) return;
+  if (threadIdx.x == 0) {
+    ia[0] = it + 1;
+    if (done[1]) done[0] = 1;
+    *ticket = 0;
+  }
+}
+
+template <typename T, typename U>
+cudaError_t launch_dots_ks(const cplx<T> *a, const cplx<U> *b, int S, long long npts, double *partials,
+                           const KsFinish &f, double *ks, int *done, unsigned int *ticket, cudaStream_t st) {
+  dots_ks_kernel<T, U><<<f.grid, 256, 0, st>>>(a, b, S, npts, partials, f, ks, done, ticket);
   COUNT_LAUNCH();
   return cudaGetLastError();
 }
-template cudaError_t launch_ka_commit<double>(cplx<double> *, const cplx<double> *, long long, int, int *, int *,
-                                              cudaStream_t);
-template cudaError_t launch_ka_commit<float>(cplx<float> *, const cplx<float> *, long long, int, int *, int *,
-                                             cudaStream_t);
+template <typename T>
+cudaError_t launch_ks_lincomb2_dot(cplx<T> *y, const cplx<T> *x1, int i1, const cplx<T> *x2, int i2, int S,
+                                   long long npts, double *partials, const KsFinish &f, double *ks, int *done,
+                                   unsigned int *ticket, cudaStream_t st) {
+  ks_lincomb2_dot_kernel<T><<<f.grid, 256, 0, st>>>(y, x1, i1, x2, i2, S, npts, partials, f, ks, done, ticket);
+  COUNT_LAUNCH();
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch_ks_scale_commit(cplx<T> *y, const double *ks, int idx, long long n, int *done, unsigned int *ticket,
+                                   cudaStream_t st) {
+  ks_scale_commit_kernel<T><<<ew_grid(n), 256, 0, st>>>(y, ks, idx, n, done, ticket);
+  COUNT_LAUNCH();
+  return cudaGetLastError();
+}
+template <typename T, typename U>
+cudaError_t launch_dots_ka(const cplx<T> *a, const cplx<U> *b, int S, long long npts, double *partials,
+                           const KaArgs &ka, int op, int j, int col, double *ks, int *ia, int *done,
+                           unsigned int *ticket, cudaStream_t st) {
+  dots_ka_kernel<T, U><<<ka.grid, 256, 0, st>>>(a, b, S, npts, partials, ka, op, j, col, ks, ia, done, ticket);
+  COUNT_LAUNCH();
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch_ka_lincomb_dot(cplx<T> *y, const cplx<T> *x, const cplx<T> *a, int jc, int S, long long npts,
+                                  double *partials, const KaArgs &ka, int op, int j, int col, double *ks, int *ia,
+                                  int *done, unsigned int *ticket, cudaStream_t st) {
+  ka_lincomb_dot_kernel<T><<<ka.grid, 256, 0, st>>>(y, x, a, jc, S, npts, partials, ka, op, j, col, ks, ia, done,
+                                                    ticket);
+  COUNT_LAUNCH();
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch_ka_scale_commit(cplx<T> *q, const cplx<T> *buf, const double *ks, int idx, long long n, int it,
+                                   int *ia, int *done, unsigned int *ticket, cudaStream_t st) {
+  ka_scale_commit_kernel<T><<<ew_grid(n), 256, 0, st>>>(q, buf, ks, idx, n, it, ia, done, ticket);
+  COUNT_LAUNCH();
+  return cudaGetLastError();
+}
+#define QDG_KRYLOV_FUSED(T)                                                                                         \
+  template cudaError_t launch_ks_lincomb2_dot<T>(cplx<T> *, const cplx<T> *, int, const cplx<T> *, int, int,          \
+                                                 long long, double *, const KsFinish &, double *, int *,             \
+                                                 unsigned int *, cudaStream_t);                                      \
+  template cudaError_t launch_ks_scale_commit<T>(cplx<T> *, const double *, int, long long, int *, unsigned int *,   \
+                                                 cudaStream_t);                                                      \
+  template cudaError_t launch_ka_lincomb_dot<T>(cplx<T> *, const cplx<T> *, const cplx<T> *, int, int, long long,     \
+                                                double *, const KaArgs &, int, int, int, double *, int *, int *,      \
+                                                unsigned int *, cudaStream_t);                                       \
+  template cudaError_t launch_ka_scale_commit<T>(cplx<T> *, const cplx<T> *, const double *, int, long long, int,    \
+                                                 int *, int *, unsigned int *, cudaStream_t);                        \
+  template cudaError_t launch_dots_ks<T, T>(const cplx<T> *, const cplx<T> *, int, long long, double *,              \
+                                            const KsFinish &, double *, int *, unsigned int *, cudaStream_t);        \
+  template cudaError_t launch_dots_ka<T, T>(const cplx<T> *, const cplx<T> *, int, long long, double *,              \
+                                            const KaArgs &, int, int, int, double *, int *, int *, unsigned int *,   \
+                                            cudaStream_t);
+QDG_KRYLOV_FUSED(double)
+QDG_KRYLOV_FUSED(float)
+#undef QDG_KRYLOV_FUSED
+
+
 
 template <typename T>
 __global__ void ka_select_kernel(cplx<T> *dst, KaBasis<T> b, const int *ia, long long n) {
@@ -871,23 +1000,6 @@ template cudaError_t launch_ka_select<double>(cplx<double> *, const KaBasis<doub
 template cudaError_t launch_ka_select<float>(cplx<float> *, const KaBasis<float> &, const int *, long long,
                                              cudaStream_t);
 
-template <typename T>
-__global__ void dots_lt_kernel(const cplx<T> *a, const cplx<T> *b, int S, long long npts, double *partials,
-                               const int *ia, int j) {
-  if (j >= ia[0]) return;
-  dots_body<T, T>(a, b, S, npts, partials);
-}
-template <typename T>
-cudaError_t launch_dots_lt(const cplx<T> *a, const cplx<T> *b, int S, long long npts, double *partials, int grid,
-                           const int *ia, int j, cudaStream_t st) {
-  dots_lt_kernel<T><<<grid, 256, 0, st>>>(a, b, S, npts, partials, ia, j);
-  COUNT_LAUNCH();
-  return cudaGetLastError();
-}
-template cudaError_t launch_dots_lt<double>(const cplx<double> *, const cplx<double> *, int, long long, double *, int,
-                                            const int *, int, cudaStream_t);
-template cudaError_t launch_dots_lt<float>(const cplx<float> *, const cplx<float> *, int, long long, double *, int,
-                                           const int *, int, cudaStream_t);
 
 template <typename T>
 __global__ void kcombine_kernel(cplx<double> *psi, KCombine<T> k, long long n) {
@@ -907,16 +1019,6 @@ cudaError_t launch_kcombine(cplx<double> *psi, const KCombine<T> &k, long long n
 template cudaError_t launch_kcombine<double>(cplx<double> *, const KCombine<double> &, long long, cudaStream_t);
 template cudaError_t launch_kcombine<float>(cplx<double> *, const KCombine<float> &, long long, cudaStream_t);
 
-cudaError_t launch_ks_commit(int *done, cudaStream_t st) {
-  ks_commit_kernel<<<1, 32, 0, st>>>(done);
-  COUNT_LAUNCH();
-  return cudaGetLastError();
-}
-cudaError_t launch_ks_finish(const double *partials, const KsFinish &f, double *ks, int *done, cudaStream_t st) {
-  ks_finish_kernel<<<1, 32, 0, st>>>(partials, f, ks, done);
-  COUNT_LAUNCH();
-  return cudaGetLastError();
-}
 
 template <typename T>
 __global__ void ks_lincomb_kernel(cplx<T> *y, const cplx<T> *x, const double *ks, int idx, long long n,

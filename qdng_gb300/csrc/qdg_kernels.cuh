@@ -447,12 +447,6 @@ struct KsFinish {
   int it;          // KS_BETA: Lanczos iteration (convergence test for it >= 2)
   double dt, tol;  // error estimate dt^(it-2) beta_0 prod beta_i / i < tol * |psi|
 };
-template <typename T, typename U>
-cudaError_t launch_dots_if(const cplx<T> *a, const cplx<U> *b, int S, long long npts, double *partials, int grid,
-                           const int *done, cudaStream_t st);
-cudaError_t launch_ks_finish(const double *partials, const KsFinish &f, double *ks, int *done, cudaStream_t st);
-// done[0] = done[1]: the error estimate of an iteration stops the kernels after it
-cudaError_t launch_ks_commit(int *done, cudaStream_t st);
 // ---- Arnoldi with its scalars on the device.  ks holds the Hessenberg
 // matrix H (m x m complex, row-major, re/im interleaved), then |psi|;
 // ia[0] is the order reached (kept across steps, like the reference's
@@ -462,27 +456,43 @@ struct KaArgs {
   double w, dt, conv;
 };
 enum KaOp { KA_H = 0, KA_NORM = 1, KA_PSN = 2, KA_LAST = 3 };
-// finish a dot product into H[j][col] (KA_H), the subdiagonal with the
-// underrun and error tests (KA_NORM, it = col + 1), |psi| (KA_PSN), or the
-// last column H[j][order-1] (KA_LAST, skipped for j >= order)
-cudaError_t launch_ka_finish(const double *partials, const KaArgs &a, int op, int j, int col, double *ks, int *ia,
-                             int *done, cudaStream_t st);
-// y -= H[j][col] x (complex coefficient), skipped once *done
+// A finished dot product goes into H[j][col] (KA_H), the subdiagonal with
+// the underrun and error tests (KA_NORM, it = col + 1), |psi| (KA_PSN), or
+// the last column H[j][order-1] (KA_LAST, skipped for j >= order).
+// Krylov launches: a pass over the vectors together with a dot product,
+// whose block partials the block taking the last ticket finishes into the
+// scalars (then resetting the ticket): <a|b> into the Lanczos / Arnoldi
+// scalars; Lanczos y -= alpha x1, y -= beta x2 with |y|^2 -> beta (it >= 2:
+// the error estimate, done[1]); y /= beta with done[0] |= done[1]; a
+// Gram-Schmidt step y -= H[jc][col] x with the next dot product; the Arnoldi
+// normalisation q_it = y / H[it][it-1] with order = it + 1 and
+// done[0] |= done[1].  Each is skipped once done[0] is set.
+template <typename T, typename U>
+cudaError_t launch_dots_ks(const cplx<T> *a, const cplx<U> *b, int S, long long npts, double *partials,
+                           const KsFinish &f, double *ks, int *done, unsigned int *ticket, cudaStream_t st);
 template <typename T>
-cudaError_t launch_ka_lincomb(cplx<T> *y, const cplx<T> *x, const double *ks, int m, int j, int col, long long n,
-                              const int *done, cudaStream_t st);
-// after the normalisation of iteration it: q_it = buf, order = it + 1, done[0] |= done[1]
+cudaError_t launch_ks_lincomb2_dot(cplx<T> *y, const cplx<T> *x1, int i1, const cplx<T> *x2, int i2, int S,
+                                   long long npts, double *partials, const KsFinish &f, double *ks, int *done,
+                                   unsigned int *ticket, cudaStream_t st);
 template <typename T>
-cudaError_t launch_ka_commit(cplx<T> *q, const cplx<T> *buf, long long n, int it, int *ia, int *done, cudaStream_t st);
+cudaError_t launch_ks_scale_commit(cplx<T> *y, const double *ks, int idx, long long n, int *done, unsigned int *ticket,
+                                   cudaStream_t st);
+template <typename T, typename U>
+cudaError_t launch_dots_ka(const cplx<T> *a, const cplx<U> *b, int S, long long npts, double *partials,
+                           const KaArgs &ka, int op, int j, int col, double *ks, int *ia, int *done,
+                           unsigned int *ticket, cudaStream_t st);
+template <typename T>
+cudaError_t launch_ka_lincomb_dot(cplx<T> *y, const cplx<T> *x, const cplx<T> *a, int jc, int S, long long npts,
+                                  double *partials, const KaArgs &ka, int op, int j, int col, double *ks, int *ia,
+                                  int *done, unsigned int *ticket, cudaStream_t st);
+template <typename T>
+cudaError_t launch_ka_scale_commit(cplx<T> *q, const cplx<T> *buf, const double *ks, int idx, long long n, int it,
+                                   int *ia, int *done, unsigned int *ticket, cudaStream_t st);
 // dst = q_{order-1} (the basis vector the last column is built from)
 template <typename T>
 struct KaBasis { const cplx<T> *q[64]; };
 template <typename T>
 cudaError_t launch_ka_select(cplx<T> *dst, const KaBasis<T> &b, const int *ia, long long n, cudaStream_t st);
-// dot products guarded by j < order (the last column)
-template <typename T>
-cudaError_t launch_dots_lt(const cplx<T> *a, const cplx<T> *b, int S, long long npts, double *partials, int grid,
-                           const int *ia, int j, cudaStream_t st);
 
 // psi = c[0] psi + sum_{i=1}^{m-1} c[i] q_i in FP64, term by term in that order
 constexpr int kMaxKrylov = 64;
