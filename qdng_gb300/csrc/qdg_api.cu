@@ -1727,8 +1727,9 @@ qdg_status hq(qdg_prop *P, const cplx<T> *q, cplx<T> *out, long long step) {
 
 // OSIL::BuildLZB / DiagLZB (src/qdlib/OSIL.cpp:83-185), FP64 scalars.
 // The Lanczos recursion runs with its scalars on the device: every dot
-// product is finished by a one-thread kernel into P->d_ks (in the order the
-// host used to sum it), the basis updates read their coefficient from there,
+// product is finished into P->d_ks by the last block of the launch that
+// computes it (fixed summation order), the basis updates read their
+// coefficient from there,
 // and the reference's error estimate sets a flag that turns the remaining
 // kernels of the step into no-ops.  The host reads alpha, beta and the order
 // once per step for the tridiagonal eigenproblem.
@@ -1827,8 +1828,9 @@ qdg_status sil_enqueue(qdg_prop *P, cplx<double> *psi) {
 
 // OSIL::BuildLZB / DiagLZB (src/qdlib/OSIL.cpp:83-185), FP64 scalars.
 // The Lanczos recursion runs with its scalars on the device: every dot
-// product is finished by a one-thread kernel into P->d_ks (in the order the
-// host used to sum it), the basis updates read their coefficient from there,
+// product is finished into P->d_ks by the last block of the launch that
+// computes it (fixed summation order), the basis updates read their
+// coefficient from there,
 // and the reference's error estimate sets a flag that turns the remaining
 // kernels of the step into no-ops.  The host reads alpha, beta and the order
 // once per step for the tridiagonal eigenproblem.

@@ -646,11 +646,35 @@ template cudaError_t launch_lincomb<double>(cplx<double> *, const cplx<double> *
 template cudaError_t launch_lincomb<float>(cplx<float> *, const cplx<float> *, cplx<double>, cplx<double>,
                                            long long, cudaStream_t);
 
+// Block sums of two values (the real and imaginary part of a dot product)
+// in a fixed order: a shuffle tree within each warp, then the warp sums by
+// another shuffle tree, the real parts in warp 0 and the imaginary parts in
+// warp 1 (two sub-partitions: a binary64 add occupies one for ~70-80
+// cycles, so dependent chains are kept short).  Valid on thread 0.
+__device__ __forceinline__ void block_sum2(double &re, double &im, double *red) {
+  for (int o = 16; o > 0; o >>= 1) {
+    re += __shfl_down_sync(0xffffffffu, re, o);
+    im += __shfl_down_sync(0xffffffffu, im, o);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  __syncthreads();
+  if (lane == 0) { red[warp] = re; red[32 + warp] = im; }
+  __syncthreads();
+  if (warp < 2) {
+    double v = lane < nw ? red[32 * warp + lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) red[64 + warp] = v;
+  }
+  __syncthreads();
+  re = red[64];
+  im = red[65];
+}
+
 // Per-state sum conj(a) b, FP64 accumulation, fixed reduction order.
 template <typename T, typename U>
 __device__ __forceinline__ void dots_body(const cplx<T> *a, const cplx<U> *b, int S, long long npts,
                                           double *partials) {
-  __shared__ double red[32];
+  __shared__ double red[66];
   for (int s = 0; s < S; ++s) {
     double re = 0, im = 0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npts;
@@ -660,12 +684,12 @@ __device__ __forceinline__ void dots_body(const cplx<T> *a, const cplx<U> *b, in
       re += x.re * y.re + x.im * y.im;
       im += x.re * y.im - x.im * y.re;
     }
-    const double tr = block_sum(re, red);
-    const double ti = block_sum(im, red);
+    block_sum2(re, im, red);
     if (threadIdx.x == 0) {
-      partials[((long long)blockIdx.x * S + s) * 2 + 0] = tr;
-      partials[((long long)blockIdx.x * S + s) * 2 + 1] = ti;
+      partials[((long long)blockIdx.x * S + s) * 2 + 0] = re;
+      partials[((long long)blockIdx.x * S + s) * 2 + 1] = im;
     }
+    __syncthreads();  // red[] is reused by the next state
   }
 }
 template <typename T, typename U>
@@ -682,42 +706,34 @@ cudaError_t launch_dots(const cplx<T> *a, const cplx<U> *b, int S, long long npt
   return cudaGetLastError();
 }
 
-// Per-state sums of the dots kernels' block partials (layout
-// [block][state][re, im]) in the order of the host's dot products: blocks
-// outer, states inner, each state's sum accumulated block by block.  The
-// block's threads stage the partials in shared memory (independent loads in
-// flight together); thread 0 then adds them in that order, so re/im (valid in
-// thread 0) are bit-identical to the host's sums.  Every thread of the block
-// calls this.
+// Per-state sums of the block partials (layout [block][state][re, im]):
+// one warp per state and component, lane l adding blocks l, l + 32, ... in
+// that order, then a shuffle tree; the warps run on different
+// sub-partitions side by side (a serial sum in one thread would take one
+// dependent binary64 add, ~80 cycles of the FP64 pipe, per partial).  A
+// fixed order, the same in every launch; the sums are valid in thread 0.
+// Every thread of the block calls this.
 __device__ __forceinline__ void sum_partials(const double *partials, int grid, int S, double *re, double *im) {
-  constexpr int kChunk = 1024;  // even: an (re, im) pair never straddles two chunks
-  __shared__ double buf[kChunk];
-  for (int s = 0; s < S; ++s) re[s] = im[s] = 0.0;
-  const int n = 2 * grid * S;
-  for (int c = 0; c < n; c += kChunk) {
-    const int m = min(kChunk, n - c);
-    for (int i = threadIdx.x; i < m; i += blockDim.x) buf[i] = __ldcg(partials + c + i);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      if (S == 1) {
-        double r = re[0], q = im[0];
-        for (int i = 0; i < m; i += 2) { r += buf[i]; q += buf[i + 1]; }
-        re[0] = r;
-        im[0] = q;
-      } else {
-        for (int i = 0; i < m; i += 2) {
-          const int s = ((c + i) >> 1) % S;
-          re[s] += buf[i];
-          im[s] += buf[i + 1];
-        }
-      }
-    }
-    __syncthreads();
+  __shared__ double out[2 * kMaxStates];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int k = warp; k < 2 * S; k += nw) {
+    const int st = k >> 1, c = k & 1;
+    double v = 0.0;
+    for (int b = lane; b < grid; b += 32) v += __ldcg(partials + ((long long)b * S + st) * 2 + c);
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) out[k] = v;
   }
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int st = 0; st < S; ++st) {
+      re[st] = out[2 * st];
+      im[st] = out[2 * st + 1];
+    }
+  __syncthreads();
 }
 
-// Partial sums -> scalar, summed in the order of the host's dot products
-// (blocks outer, states inner; states weighted, then added in order).
+// Partial sums -> scalar (sum_partials' fixed order; states weighted, then
+// added in order).
 __device__ void ks_finish_body(const double *partials, const KsFinish &f, double *ks, int *done) {
   double re[kMaxStates], im[kMaxStates];
   sum_partials(partials, f.grid, f.S, re, im);
@@ -802,7 +818,7 @@ __device__ __forceinline__ bool arrive_last(unsigned int *ticket) {
 // produced by a functor (which may also update the vectors).
 template <typename Term>
 __device__ __forceinline__ void dots_terms(int S, long long npts, double *partials, Term term) {
-  __shared__ double red[32];
+  __shared__ double red[66];
   for (int s = 0; s < S; ++s) {
     double re = 0, im = 0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npts;
@@ -812,12 +828,12 @@ __device__ __forceinline__ void dots_terms(int S, long long npts, double *partia
       re += x.re * y.re + x.im * y.im;
       im += x.re * y.im - x.im * y.re;
     }
-    const double tr = block_sum(re, red);
-    const double ti = block_sum(im, red);
+    block_sum2(re, im, red);
     if (threadIdx.x == 0) {
-      partials[((long long)blockIdx.x * S + s) * 2 + 0] = tr;
-      partials[((long long)blockIdx.x * S + s) * 2 + 1] = ti;
+      partials[((long long)blockIdx.x * S + s) * 2 + 0] = re;
+      partials[((long long)blockIdx.x * S + s) * 2 + 1] = im;
     }
+    __syncthreads();
   }
 }
 
