@@ -669,6 +669,9 @@ __device__ __forceinline__ void tile_coord(int idx, int TW, int N, int es, int &
 }
 
 // Deterministic block sum of one double per thread (fixed shuffle tree).
+// Fixed-order block sum: a shuffle tree within each warp, then the warp sums
+// by a second shuffle tree in warp 0 (a serial sum in one thread would be a
+// chain of binary64 adds, ~80 cycles of the FP64 pipe each).
 __device__ __forceinline__ double block_sum(double v, double *red) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -676,9 +679,10 @@ __device__ __forceinline__ double block_sum(double v, double *red) {
   if (lane == 0) red[warp] = v;
   __syncthreads();
   double t = 0;
-  if (threadIdx.x == 0) {
+  if (warp == 0) {
     const int nw = (blockDim.x + 31) >> 5;
-    for (int w = 0; w < nw; ++w) t += red[w];
+    t = lane < nw ? red[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
   }
   return t;  // valid on thread 0
 }

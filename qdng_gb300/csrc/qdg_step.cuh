@@ -582,6 +582,7 @@ __global__ void __launch_bounds__(256, OCC) cheby_step_kernel(StepArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double red[32];
   __shared__ double tot_s;
+  __shared__ bool done_s;  // the series cut of the term, decided by thread 0
   constexpr int SM = (SS > 0) ? SS : kMaxStates;
   cplx<T> *smem = reinterpret_cast<cplx<T> *>(smem_raw);
   const long long n = a.npts * a.S;
@@ -625,10 +626,15 @@ __global__ void __launch_bounds__(256, OCC) cheby_step_kernel(StepArgs<T> a) {
       if (threadIdx.x == 0) a.partials[blockIdx.x] = t;
       if (!grid_sync(a.bar)) return;
       t = sum_partials(a.partials, red);
-      if (threadIdx.x == 0) tot_s = t;
+      // the cut in one thread (its binary64 division costs every warp that
+      // runs it a chain of FP64 pipe slots), the decision broadcast
+      if (threadIdx.x == 0) {
+        tot_s = t;
+        done_s = step_cut(t, norm0, last, norm_last, a.imag, a.diff, a.prec, a.offim0, status);
+      }
       __syncthreads();
       used = i + 1;
-      done = step_cut(tot_s, norm0, last, norm_last, a.imag, a.diff, a.prec, a.offim0, status);
+      done = done_s;
     }
   } else {
     int tw_n = -1;  // line length of the twiddles held in shared memory
@@ -683,10 +689,13 @@ __global__ void __launch_bounds__(256, OCC) cheby_step_kernel(StepArgs<T> a) {
       if (!grid_sync(a.bar)) return;
       if (tr) tp[3] += gtimer() - t1;
       t = sum_partials(a.partials, red);
-      if (threadIdx.x == 0) tot_s = t;
+      if (threadIdx.x == 0) {
+        tot_s = t;
+        done_s = step_cut(t, norm0, last, norm_last, a.imag, a.diff, a.prec, a.offim0, status);
+      }
       __syncthreads();
       used = i + 1;
-      done = step_cut(tot_s, norm0, last, norm_last, a.imag, a.diff, a.prec, a.offim0, status);
+      done = done_s;
       if (two && !done && kind != PK_LAST && !phase_b(a.buf[i % 3], a.Pn[(i + 1) & 1])) return;
       if (tr) tp[2] += gtimer() - t0;  // the whole term
     }
