@@ -589,6 +589,57 @@ qdg_status run_kin_tablefree(qdg_plan *p, const cplx<T> *phi, const int *done, c
   return QDG_OK;
 }
 
+// Binary64 plans of at most 2^17 points (all states) whose lines are powers
+// of two up to 1024 take the latency-oriented radix-2 kinetic pass (the
+// Krylov, observable and eigen H applications on such grids are a chain of
+// small launches, each bound by the length of its FP64 instruction chains).
+template <typename T>
+bool kin_r2_ok(const qdg_plan *p) {
+  if (sizeof(T) != sizeof(double) || p->npts * p->S > (1LL << 17)) return false;
+  for (int d = 0; d < p->nd; ++d) {
+    const int N = p->dim[d].n;
+    if (N < 2 || N > 1024 || (N & (N - 1))) return false;
+  }
+  return true;
+}
+cudaError_t launch_kin_r2_plan(qdg_plan *p, const cplx<double> *phi, const Epi &e) {
+  qdg::KinR2Args r;
+  memset(&r, 0, sizeof(r));
+  r.nd = p->nd;
+  r.S = p->S;
+  r.npts = p->npts;
+  // N/2 threads per line; short lines share a block up to 64 threads
+  int maxN = 2;
+  for (int d = 0; d < p->nd; ++d) maxN = std::max(maxN, p->dim[d].n);
+  r.threads = std::max(64, maxN / 2);
+  long long items = 0;
+  for (int d = 0; d < p->nd; ++d) {
+    const int N = p->dim[d].n;
+    int lg = 0;
+    while ((1 << lg) < N) ++lg;
+    const long long lines = p->npts / N;
+    const int L = (int)std::min<long long>(std::max(1, r.threads / (N / 2)), lines);
+    r.N[d] = N;
+    r.lgN[d] = lg;
+    r.L[d] = L;
+    r.stride[d] = p->dim[d].stride;
+    r.groups[d] = lines / L;
+    r.item_start[d] = items;
+    items += r.groups[d] * p->S;
+    r.kfac[d] = p->dim[d].kfac;
+    r.tw[d] = reinterpret_cast<const cplx<double> *>(p->dim[d].tw);
+    r.P[d] = reinterpret_cast<cplx<double> *>(p->d_Pd[d]);
+  }
+  r.item_start[p->nd] = items;
+  r.phi = phi;
+  r.done = e.done;
+  r.cs = e.cut.cs;
+  r.dyn = e.cut.dyn;
+  r.bufs[0] = reinterpret_cast<const cplx<double> *>(e.bufs[0]);
+  r.bufs[1] = reinterpret_cast<const cplx<double> *>(e.bufs[1]);
+  return qdg::launch_kin_r2(r, p->stream);
+}
+
 template <typename T>
 qdg_status run_h(qdg_plan *p, int final_mode, const cplx<T> *phi, const Epi &e) {
   if (p->kin_form != KIN_FFT) {
@@ -657,7 +708,11 @@ qdg_status run_h(qdg_plan *p, int final_mode, const cplx<T> *phi, const Epi &e) 
   size_t slot = 0;
   qdg_status s = prof_begin<T>(p, qdg::PM_KIN_FIRST, &slot);
   if (s != QDG_OK) return s;
-  CK(qdg::launch_kin_all<T>(k, (int)std::min<long long>(items, p->kin_grid), 256, p->kin_smem, p->stream));
+  if (kin_r2_ok<T>(p)) {
+    CK(launch_kin_r2_plan(p, reinterpret_cast<const cplx<double> *>(phi), e));
+  } else {
+    CK(qdg::launch_kin_all<T>(k, (int)std::min<long long>(items, p->kin_grid), 256, p->kin_smem, p->stream));
+  }
   if ((s = prof_end(p, slot)) != QDG_OK) return s;
   if (!p->nac.empty() && (s = run_nac<T>(p, phi, e)) != QDG_OK) return s;
 

@@ -284,6 +284,96 @@ __global__ void __launch_bounds__(256) kin_all_kernel(KinArgs<T> a) {
   }
 }
 
+// ------------------------------------ short binary64 lines, radix 2
+// A block takes L lines of one dimension and state, N/2 threads per line.
+// Stockham radix-2 stage with Ns: for j < N/2, k = j mod Ns, a = x[j],
+// b = x[j + N/2], w = exp(-+2 pi i k / (2 Ns)): outputs (j / Ns) 2 Ns + k
+// = a + w b and that + Ns = a - w b.  Thread (l, j) computes butterfly j of
+// line l (w b once, eight binary64 instructions); a binary64 warp
+// instruction holds its sub-partition's FP64 unit for ~70-80 cycles, so
+// the lines are kept short per block (L = 1 from 128 points on) and a
+// transform costs log2 N such stages instead of a radix-8/16 item's chain.
+__global__ void __launch_bounds__(512) kin_r2_kernel(KinR2Args a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  if (a.done != nullptr && *a.done) return;
+  const cplx<double> *phi = a.dyn ? a.bufs[(a.cs->i + 1) & 1] : a.phi;
+  int d = 0;
+  while ((long long)blockIdx.x >= a.item_start[d + 1]) ++d;
+  const int N = a.N[d], L = a.L[d], lg = a.lgN[d], half = N >> 1;
+  const long long local = (long long)blockIdx.x - a.item_start[d];
+  const int s = (int)(local / a.groups[d]);
+  const long long g = local - (long long)s * a.groups[d];
+  const long long str = a.stride[d];
+  const long long so = (long long)s * a.npts;
+  const cplx<double> *tw = a.tw[d];
+  cplx<double> *b0 = reinterpret_cast<cplx<double> *>(smem_raw);
+  cplx<double> *b1 = b0 + L * N;
+  // line g L + l: dimension 0 lines are contiguous; others are (lo, hi) with
+  // lo = line mod stride fastest, so consecutive lines are adjacent in memory
+  auto addr = [&](int l, int i) -> long long {
+    const long long line = g * L + l;
+    if (d == 0) return so + line * N + i;
+    const long long hi = line / str, lo = line - hi * str;
+    return so + hi * str * N + lo + (long long)i * str;
+  };
+  const int T = L * N;
+  for (int idx = threadIdx.x; idx < T; idx += blockDim.x) {
+    int l, i;
+    if (d == 0) { l = idx / N; i = idx - l * N; } else { i = idx / L; l = idx - i * L; }
+    b0[l * N + i] = ld(phi + addr(l, i));
+  }
+  __syncthreads();
+  const int t = threadIdx.x;
+  const bool act = t < L * half;
+  const int l = t >> (lg - 1), j = t & (half - 1);
+  cplx<double> *in = b0, *out = b1;
+  for (int dir = 0; dir < 2; ++dir) {  // forward, then backward (conjugate twiddles)
+    for (int Ns = 1, ls = 0; Ns < N; Ns <<= 1, ++ls) {
+      if (act) {
+        const int k = j & (Ns - 1);
+        const cplx<double> x = in[l * N + j], y = in[l * N + j + half];
+        const cplx<double> w0 = tw[k << (lg - 1 - ls)];
+        const double wr = w0.re, wi = dir == 0 ? w0.im : -w0.im;
+        const double pr = fma(wr, y.re, -wi * y.im), pi = fma(wr, y.im, wi * y.re);
+        const int dst = l * N + ((j - k) << 1) + k;
+        out[dst] = cplx<double>{x.re + pr, x.im + pi};
+        out[dst + Ns] = cplx<double>{x.re - pr, x.im - pi};
+      }
+      __syncthreads();
+      cplx<double> *tmp = in;
+      in = out;
+      out = tmp;
+    }
+    if (dir == 0) {
+      // k^2 / (2 m) / N at k-index q = min(i, N - i), the kinetic pass's multiplier
+      for (int idx = threadIdx.x; idx < T; idx += blockDim.x) {
+        const int ll = idx / N, o = idx - ll * N;
+        const int q = o < N - o ? o : N - o;
+        const double m = a.kfac[d][s] * (double)q * (double)q;
+        in[idx] = cplx<double>{in[idx].re * m, in[idx].im * m};
+      }
+      __syncthreads();
+    }
+  }
+  for (int idx = threadIdx.x; idx < T; idx += blockDim.x) {
+    int ll, i;
+    if (d == 0) { ll = idx / N; i = idx - ll * N; } else { i = idx / L; ll = idx - i * L; }
+    st(a.P[d] + addr(ll, i), in[ll * N + i]);
+  }
+}
+
+cudaError_t launch_kin_r2(const KinR2Args &a, cudaStream_t st) {
+  size_t smem = 0;
+  for (int d = 0; d < a.nd; ++d) smem = std::max(smem, 2 * (size_t)a.L[d] * a.N[d] * sizeof(cplx<double>));
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kin_r2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  kin_r2_kernel<<<(unsigned)a.item_start[a.nd], a.threads, smem, st>>>(a);
+  COUNT_LAUNCH();
+  return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------- NAC pass
 // A tile of TW lines along d: phi lines and f phi lines are transformed
 // together (2 TW lines), multiplied by i k c / N, transformed back, and the

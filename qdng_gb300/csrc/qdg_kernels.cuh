@@ -159,6 +159,27 @@ struct KinArgs {
   int dyn;
 };
 
+// T_d phi of every dimension for binary64 lines of N = 2^p <= 1024 points,
+// latency-oriented (kin_r2_kernel): a block holds L lines, N/2 threads per
+// line, one radix-2 Stockham butterfly per thread and stage.
+struct KinR2Args {
+  int nd, S, threads;
+  long long npts;
+  int N[4], L[4], lgN[4];
+  long long stride[4];
+  long long groups[4];          // line groups of L lines per state
+  long long item_start[5];      // first block of each dimension
+  const double *kfac[4];        // [S] dk^2 / (2 m) / N of each dimension
+  const cplx<double> *tw[4];    // exp(-2 pi i m / N)
+  const cplx<double> *phi;
+  cplx<double> *P[4];
+  const int *done;
+  const ChebyState *cs;
+  const cplx<double> *bufs[2];
+  int dyn;
+};
+cudaError_t launch_kin_r2(const KinR2Args &a, cudaStream_t st);
+
 // One OGridNAC element along one dimension d (src/qdlib/OGridNAC.cpp:131-148):
 // out += c [f_d d/dx_d phi + d/dx_d (f_d phi)], c = sign/(2 mass), added to
 // the kinetic result T_0 phi of the row state, which the combine pass reads.
