@@ -825,6 +825,18 @@ __device__ __forceinline__ void sum_partials(const double *partials, int grid, i
 // Partial sums -> scalar (sum_partials' fixed order; states weighted, then
 // added in order).
 __device__ void ks_finish_body(const double *partials, const KsFinish &f, double *ks, int *done) {
+  // the error estimate's factors beta_i / i and dt^(it-2) do not depend on
+  // this dot product: warps 1 and 2 compute them while the partials are
+  // summed (one FP64 division or pow is a long chain of pipe slots)
+  __shared__ double q[kMaxKrylov];
+  __shared__ double pw;
+  const bool est = f.mode == KS_BETA && f.it >= 2;
+  if (est) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (warp == 1)
+      for (int i = 1 + lane; i < f.it - 2; i += 32) q[i] = ks[f.order + i] / double(i);
+    if (warp == 2 && lane == 0) pw = pow(f.dt, (double)(f.it - 2));
+  }
   double re[kMaxStates], im[kMaxStates];
   sum_partials(partials, f.grid, f.S, re, im);
   if (threadIdx.x != 0) return;
@@ -839,8 +851,8 @@ __device__ void ks_finish_body(const double *partials, const KsFinish &f, double
   if (f.mode != KS_BETA || f.it < 2) return;
   // OSIL::BuildLZB error estimate (src/qdlib/OSIL.cpp:106-112), tested after the iteration
   const double *beta = ks + f.order;
-  double err = pow(f.dt, (double)(f.it - 2)) * beta[0];
-  for (int i = 1; i < f.it - 2; ++i) err *= beta[i] / double(i);
+  double err = pw * beta[0];
+  for (int i = 1; i < f.it - 2; ++i) err *= q[i];
   err = fabs(err);
   if (err < f.tol * ks[2 * f.order]) {  // ks[2 order] = |psi|
     done[1] = 1;                          // stop after this iteration's normalisation
@@ -850,6 +862,20 @@ __device__ void ks_finish_body(const double *partials, const KsFinish &f, double
 
 __device__ void ka_finish_body(const double *partials, const KaArgs &a, int op, int j, int col, double *ks, int *ia,
                                int *done) {
+  // KA_NORM: the error estimate's divisions H[i+1][i] / i and dt^(it-2) in
+  // warps 1 and 2 while the partials are summed (they use earlier entries)
+  __shared__ double qr[kMaxKrylov], qi[kMaxKrylov];
+  __shared__ double pw;
+  if (op == KA_NORM) {
+    const int it = col + 1, m = a.m;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (warp == 1)
+      for (int i = 1 + lane; i < it - 2; i += 32) {
+        qr[i] = ks[2 * ((i + 1) * m + i)] / double(i);
+        qi[i] = ks[2 * ((i + 1) * m + i) + 1] / double(i);
+      }
+    if (warp == 2 && lane == 0) pw = pow(a.dt, (double)(it - 2));
+  }
   double re[kMaxStates], im[kMaxStates];
   sum_partials(partials, a.grid, a.S, re, im);
   if (threadIdx.x != 0) return;
@@ -874,10 +900,10 @@ __device__ void ka_finish_body(const double *partials, const KaArgs &a, int op, 
   H[2 * (it * m + it - 1)] = nrm;
   H[2 * (it * m + it - 1) + 1] = 0.0;
   // err = dt^(it-2) H[1][0] |psi| prod H[i+1][i] / i, complex
-  double er = pow(a.dt, (double)(it - 2)) * H[2 * m] * ks[2 * m * m];
-  double ei = pow(a.dt, (double)(it - 2)) * H[2 * m + 1] * ks[2 * m * m];
+  double er = pw * H[2 * m] * ks[2 * m * m];
+  double ei = pw * H[2 * m + 1] * ks[2 * m * m];
   for (int i = 1; i < it - 2; ++i) {
-    const double hr = H[2 * ((i + 1) * m + i)] / double(i), hi = H[2 * ((i + 1) * m + i) + 1] / double(i);
+    const double hr = qr[i], hi = qi[i];
     const double nr = er * hr - ei * hi, ni = er * hi + ei * hr;
     er = nr;
     ei = ni;
@@ -887,9 +913,10 @@ __device__ void ka_finish_body(const double *partials, const KaArgs &a, int op, 
 
 // ---- fused Krylov launches: a pass over the vectors, its dot product's
 // block partials, and the finishing scalar work in the block that arrives
-// last (an atomic ticket: no block waits for another).  The sums are those
-// of the dots + finish launches they replace (same partial layout, same
-// order), and the vector arithmetic is that of the lincomb kernels.
+// last (an atomic ticket: no block waits for another).  The updates are
+// FMAs (y - s x per component); multiplications by 1 and 0 that a complex
+// product would spend are left out (each binary64 instruction holds a
+// sub-partition's FP64 unit for ~70-80 cycles).
 
 // True in the one block whose ticket is the last of the grid; its threads
 // then see every block's partials (each block fenced before its ticket).
@@ -944,11 +971,12 @@ __global__ void ks_lincomb2_dot_kernel(cplx<T> *y, const cplx<T> *x1, int i1, co
                                        long long npts, double *partials, KsFinish f, double *ks, int *done,
                                        unsigned int *ticket) {
   if (*done) return;
-  const cplx<double> one = cplx<double>{1.0, 0.0};
-  const cplx<double> b1 = cplx<double>{-ks[i1], 0.0}, b2 = cplx<double>{-ks[i2], 0.0};
+  const double b1 = -ks[i1], b2 = -ks[i2];
   dots_terms(S, npts, partials, [&](long long g, cplx<double> &xa, cplx<double> &xb) {
-    const cplx<T> r1 = ccast<T>(dmul(ccast<double>(ld(y + g)), one) + dmul(ccast<double>(ld(x1 + g)), b1));
-    const cplx<T> r2 = ccast<T>(dmul(ccast<double>(r1), one) + dmul(ccast<double>(ld(x2 + g)), b2));
+    const cplx<double> u = ccast<double>(ld(y + g)), v1 = ccast<double>(ld(x1 + g));
+    const cplx<T> r1 = ccast<T>(cplx<double>{fma(b1, v1.re, u.re), fma(b1, v1.im, u.im)});
+    const cplx<double> w = ccast<double>(r1), v2 = ccast<double>(ld(x2 + g));
+    const cplx<T> r2 = ccast<T>(cplx<double>{fma(b2, v2.re, w.re), fma(b2, v2.im, w.im)});
     st(y + g, r2);
     xa = xb = ccast<double>(r2);
   });
@@ -962,9 +990,11 @@ template <typename T>
 __global__ void ks_scale_commit_kernel(cplx<T> *y, const double *ks, int idx, long long n, int *done,
                                        unsigned int *ticket) {
   if (*done) return;
-  const cplx<double> a = cplx<double>{1.0 / ks[idx], 0.0};
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    st(y + i, ccast<T>(dmul(ccast<double>(ld(y + i)), a)));
+  const double a = 1.0 / ks[idx];
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const cplx<double> u = ccast<double>(ld(y + i));
+    st(y + i, ccast<T>(cplx<double>{u.re * a, u.im * a}));
+  }
   if (!arrive_last(ticket)) return;
   if (threadIdx.x == 0) {
     if (done[1]) done[0] = 1;
@@ -992,10 +1022,10 @@ __global__ void ka_lincomb_dot_kernel(cplx<T> *y, const cplx<T> *x, const cplx<T
                                       int *ia, int *done, unsigned int *ticket) {
   if (*done) return;
   const int m = ka.m;
-  const cplx<double> one = cplx<double>{1.0, 0.0};
-  const cplx<double> b = cplx<double>{-ks[2 * (jc * m + col)], -ks[2 * (jc * m + col) + 1]};
+  const double br = -ks[2 * (jc * m + col)], bi = -ks[2 * (jc * m + col) + 1];
   dots_terms(S, npts, partials, [&](long long g, cplx<double> &xa, cplx<double> &xb) {
-    const cplx<T> r = ccast<T>(dmul(ccast<double>(ld(y + g)), one) + dmul(ccast<double>(ld(x + g)), b));
+    const cplx<double> u = ccast<double>(ld(y + g)), v = ccast<double>(ld(x + g));
+    const cplx<T> r = ccast<T>(cplx<double>{fma(v.re, br, fma(-v.im, bi, u.re)), fma(v.re, bi, fma(v.im, br, u.im))});
     st(y + g, r);
     xb = ccast<double>(r);
     xa = a ? ccast<double>(ld(a + g)) : xb;
@@ -1010,9 +1040,11 @@ template <typename T>
 __global__ void ka_scale_commit_kernel(cplx<T> *q, const cplx<T> *buf, const double *ks, int idx, long long n, int it,
                                        int *ia, int *done, unsigned int *ticket) {
   if (*done) return;
-  const cplx<double> a = cplx<double>{1.0 / ks[idx], 0.0};
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    st(q + i, ccast<T>(dmul(ccast<double>(ld(buf + i)), a)));
+  const double a = 1.0 / ks[idx];
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const cplx<double> u = ccast<double>(ld(buf + i));
+    st(q + i, ccast<T>(cplx<double>{u.re * a, u.im * a}));
+  }
   if (!arrive_last(ticket)) return;
   if (threadIdx.x == 0) {
     ia[0] = it + 1;
@@ -1110,9 +1142,8 @@ template cudaError_t launch_ka_select<float>(cplx<float> *, const KaBasis<float>
 template <typename T>
 __global__ void kcombine_kernel(cplx<double> *psi, KCombine<T> k, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    // the arithmetic of the sequence of lincomb launches it replaces
     cplx<double> r = dmul(ld(psi + i), k.c[0]);
-    for (int j = 1; j < k.m; ++j) r = dmul(r, cplx<double>{1.0, 0.0}) + dmul(ccast<double>(ld(k.q[j] + i)), k.c[j]);
+    for (int j = 1; j < k.m; ++j) r = r + dmul(ccast<double>(ld(k.q[j] + i)), k.c[j]);
     st(psi + i, r);
   }
 }
