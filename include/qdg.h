@@ -61,7 +61,7 @@ typedef enum qdg_term_kind {
                               imaginary potential, H psi += -i W psi (nip="true"), else H psi += W psi;
                               mass[0] = gain (Emax = gain, Emin = -i gain with nip, else 0).
                               Not a member type of GSPO (OGSPO.cpp:71-85 needs ODSpace operators). */
-  QDG_TERM_GMAT = 6        /* OGridGMat (src/qdlib/OGridGMat.cpp:307-386): -1/2 sum_ij d/dx_j G_ij(x) d/dx_i,
+  QDG_TERM_GMAT = 6,       /* OGridGMat (src/qdlib/OGridGMat.cpp:307-386): -1/2 sum_ij d/dx_j G_ij(x) d/dx_i,
                               first derivatives by FFT (Diff.cpp:223-272); diagonal only.  grid = index of
                               the first of ndims (ndims + 1) / 2 grid arrays G_ij, lower triangle row by
                               row ((0,0), (1,0), (1,1), (2,0), ...); flags holds two bits per element k =
@@ -69,6 +69,13 @@ typedef enum qdg_term_kind {
                               diagonal), 1 = a grid, 2 = a constant (its grid array holds the constant;
                               Emax and Emin then follow OGridGMat.cpp:250-305 for constants).
                               Not a member type of GSPO (not an ODSpace operator). */
+  QDG_TERM_HOFD = 7        /* OGridHOFD (src/qdlib/OGridHOFD.cpp:32-128, HOFD.h:188-211,372-433): central
+                              finite differences of order fd_order along each dimension with zero (or,
+                              flags bit 0, periodic) boundaries; flags bit 1: first derivative (deriv=1),
+                              else second; laser = the dimension it acts on (dim), -1 = all; with flags
+                              bit 2 the "mass" parameter is given in mass[] and the factor is
+                              -1/(2 mass[ndims-1]) for every dimension (OGridHOFD.cpp:74-91), else 1.
+                              Diagonal only; not a member type of GSPO. */
 } qdg_term_kind;
 
 /* Arithmetic of a plan.  FP64 is the drop-in form: every value (psi, phi_n,

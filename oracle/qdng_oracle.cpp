@@ -368,6 +368,15 @@ static cd term_emax(const System &s, const qdg_hterm &t) {
   }
   if (t.kind == QDG_TERM_POTENTIAL) return vec_max(s.grids[t.grid]);
   if (t.kind == QDG_TERM_GMAT) return gmat_emax(s, t);
+  if (t.kind == QDG_TERM_HOFD) {  /* OGridHOFD::Emax (OGridHOFD.cpp:97-111) */
+    if (t.flags & 2) return cd(0, M_PI / s.dx[0]);
+    double T = 0;
+    for (int d = 0; d < s.g.ndims; ++d) {
+      const double m = (t.flags & 4) ? t.mass[d] : 1.0;
+      if (m > 0) T += 1 / (m * s.dx[d] * s.dx[d]);
+    }
+    return T * (M_PI * M_PI / 2);
+  }
   if (t.kind == QDG_TERM_GOBBLER) return t.mass[0];  /* OGobbler::Emax = gain (OGobbler.cpp:161-164) */
   if (t.kind == QDG_TERM_NAC) {  /* OGridNAC::Emax (OGridNAC.cpp:105-115): dx of dim 0 */
     double m = 0;
@@ -381,6 +390,7 @@ static cd term_emax(const System &s, const qdg_hterm &t) {
 static cd term_emin(const System &s, const qdg_hterm &t) {
   if (t.kind == QDG_TERM_POTENTIAL) return vec_min(s.grids[t.grid]);
   if (t.kind == QDG_TERM_GMAT) return gmat_emin(s, t);
+  if (t.kind == QDG_TERM_HOFD) return (t.flags & 2) ? cd(0, -M_PI / s.dx[0]) : cd(0);  /* OGridHOFD.cpp:113-118 */
   /* OGobbler::Emin (OGobbler.cpp:166-170): -i gain as negative imaginary potential */
   if (t.kind == QDG_TERM_GOBBLER) return t.laser == 1 ? cd(0, -t.mass[0]) : cd(0);
   return 0.0;
@@ -536,6 +546,46 @@ static void fd_apply(const System &s, const qdg_hterm &t, const cd *x, cd *o) {
   }
 }
 
+/* OGridHOFD::Apply (OGridHOFD.cpp:120-128) with HOFD::Diff along one
+ * dimension (HOFD.h:188-211) and _DiffSingleDim (HOFD.h:372-433): along the
+ * dimension d (all, or the one of `laser`), point c of a line gets
+ * h (cf[o2] x_c + sum_k cf[o2-k] (x_{c-k} + df x_{c+k})), df = -1 for the
+ * first derivative and 1 for the second, h = factor / dx_d^deriv; points
+ * beyond the line's ends are zero, or wrap around with pbc.  factor =
+ * -1/(2 m) of the last dimension's mass when "mass" is given (the loop of
+ * OGridHOFD.cpp:80-86 assigns the whole vector each time), else 1. */
+static void hofd_apply(const System &s, const qdg_hterm &t, const cd *x, cd *o) {
+  const int deriv = (t.flags & 2) ? 1 : 2;
+  std::vector<double> cf;
+  fd_weights(deriv, t.fd_order, cf);
+  const int o2 = t.fd_order / 2;
+  const bool pbc = (t.flags & 1) != 0;
+  const double df = deriv % 2 ? -1.0 : 1.0;
+  const int nd = s.g.ndims;
+  const double factor = (t.flags & 4) ? -1. / (2 * t.mass[nd - 1]) : 1.0;
+  long lo = 1;
+  for (int d = 0; d < nd; ++d) {
+    const long N = s.g.n[d];
+    if (t.laser < 0 || t.laser == d) {
+      const double h = 1. / std::pow(s.dx[d], deriv) * 1.0 * factor;
+      for (long i = 0; i < s.npts; ++i) {
+        const long c = (i / lo) % N;
+        cd v = cf[o2] * x[i];
+        for (int k = 1; k <= o2; ++k) {
+          cd lw = 0, up = 0;
+          if (c - k >= 0) lw = x[i - k * lo];
+          else if (pbc) lw = x[i + (N - k) * lo];
+          if (c + k < N) up = x[i + k * lo];
+          else if (pbc) up = x[i + (k - N) * lo];
+          v += cf[o2 - k] * (lw + df * up);
+        }
+        o[i] += h * v;
+      }
+    }
+    lo *= N;
+  }
+}
+
 /* Source of G-matrix element (i, j), i >= j: 0 none, 1 grid, 2 constant. */
 static int gmat_src(const qdg_hterm &t, int i, int j) {
   if (i < j) std::swap(i, j);
@@ -647,6 +697,8 @@ static void h_apply(const System &s, const cd *in, cd *out, long step) {
             nac_apply(s, t, x, o);
           } else if (t.kind == QDG_TERM_GMAT) {
             gmat_apply(s, t, x, o);
+          } else if (t.kind == QDG_TERM_HOFD) {
+            hofd_apply(s, t, x, o);
           } else if (kin && t.fd_order > 0) {
             fd_apply(s, t, x, o);
           } else if (kin) {
@@ -873,7 +925,8 @@ static int gspo_init(Prop &p) {
     if (!any) return fail(QDG_EINVAL, "GSPO misses an operator. Sequence must be A, B, C, ...");
     /* OGridGMat is no ODSpace; OGridNablaSq with method HOFD has no k-space table (Diff.cpp:52-54) */
     for (auto &t : s.terms)
-      if (t.group == g && (t.kind == QDG_TERM_GMAT || (t.kind == QDG_TERM_KINETIC && t.fd_order > 0)))
+      if (t.group == g && (t.kind == QDG_TERM_GMAT || t.kind == QDG_TERM_HOFD ||
+                           (t.kind == QDG_TERM_KINETIC && t.fd_order > 0)))
         return fail(QDG_EUNSUPPORTED, "GSPO members need a diagonal representation (no HOFD, no GridGMat)");
     if (kin && pot) return fail(QDG_EUNSUPPORTED, "GSPO: Operator has no diagonal representation");
     if (kin) for (int st = 0; st < s.S; ++st) {
@@ -1228,7 +1281,8 @@ double orc_expec_kinetic(void *sp, const double *psi_) {
   const System &s = *static_cast<System *>(sp);
   bool direct = false;
   for (auto &t : s.terms)
-    if (t.kind == QDG_TERM_GMAT || (t.kind == QDG_TERM_KINETIC && t.fd_order > 0)) direct = true;
+    if (t.kind == QDG_TERM_GMAT || t.kind == QDG_TERM_HOFD || (t.kind == QDG_TERM_KINETIC && t.fd_order > 0))
+      direct = true;
   if (direct) {
     /* finite differences and the G-matrix have no k-space table:
      * <psi|T psi> / <psi|psi> from the operator applied on each state */
@@ -1241,6 +1295,7 @@ double orc_expec_kinetic(void *sp, const double *psi_) {
       for (auto &t : s.terms) {
         if (t.row != st || t.col != st) continue;
         if (t.kind == QDG_TERM_GMAT) gmat_apply(s, t, x, tp.data());
+        else if (t.kind == QDG_TERM_HOFD) hofd_apply(s, t, x, tp.data());
         else if (t.kind == QDG_TERM_KINETIC) fd_apply(s, t, x, tp.data());
       }
       for (long p = 0; p < s.npts; ++p) {

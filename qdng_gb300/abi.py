@@ -28,6 +28,7 @@ TERM_DIPOLE = 3
 TERM_NAC = 4
 TERM_GOBBLER = 5
 TERM_GMAT = 6
+TERM_HOFD = 7
 
 PREC_FP64 = 0
 PREC_MIXED = 1

@@ -92,6 +92,7 @@ struct qdg_plan {
   // a line length with a prime factor above 5: direct-DFT stages, graph path only
   bool generic_fft = false;
   int fd_order = 0, fd_pbc = 0;
+  int fd_mode = 0, fd_deriv = 2;                  // mode 1: OGridHOFD (per-dimension lines), deriv 1 or 2
   double fd_h[qdg::kMaxStates][4] = {};           // -1/(2 m_d) / dx_d^2 per state, summed over terms
   long long gm_base[qdg::kMaxStates];             // first G grid of each state, -1 = none
   unsigned gm_mask[qdg::kMaxStates] = {};
@@ -291,6 +292,15 @@ double gmat_emin(const qdg_plan *p, const qdg_hterm &t) {
 cd term_emax(const qdg_plan *p, const qdg_hterm &t) {
   const long long n = p->npts;
   if (t.kind == QDG_TERM_GMAT) return gmat_emax(p, t);
+  if (t.kind == QDG_TERM_HOFD) {  // OGridHOFD::Emax (OGridHOFD.cpp:97-111)
+    if (t.flags & 2) return cd(0.0, M_PI / p->dx[0]);
+    double T = 0;
+    for (int d = 0; d < p->nd; ++d) {
+      const double m = (t.flags & 4) ? t.mass[d] : 1.0;
+      if (m > 0) T += 1 / (m * p->dx[d] * p->dx[d]);
+    }
+    return T * (M_PI * M_PI / 2);
+  }
   if (t.kind == QDG_TERM_KINETIC) {
     double T = 0;
     for (int d = 0; d < p->nd; ++d)
@@ -315,6 +325,7 @@ cd term_emin(const qdg_plan *p, const qdg_hterm &t) {
   // OGobbler::Emin (OGobbler.cpp:166-170): -i gain as a negative imaginary potential, else 0
   if (t.kind == QDG_TERM_GOBBLER) return t.laser == 1 ? cd(0.0, -t.mass[0]) : cd(0.0);
   if (t.kind == QDG_TERM_GMAT) return gmat_emin(p, t);
+  if (t.kind == QDG_TERM_HOFD) return (t.flags & 2) ? cd(0.0, -M_PI / p->dx[0]) : cd(0.0);  // OGridHOFD.cpp:113-118
   if (t.kind != QDG_TERM_POTENTIAL) return 0.0;
   const double *g = p->grids_h.data() + (long long)t.grid * p->npts;
   return *std::min_element(g, g + p->npts);
@@ -542,8 +553,11 @@ qdg_status run_kin_tablefree(qdg_plan *p, const cplx<T> *phi, const int *done, c
     qdg::FdArgs<T> a;
     memset(&a, 0, sizeof(a));
     a.nd = p->nd; a.S = p->S; a.o2 = p->fd_order / 2; a.pbc = p->fd_pbc; a.npts = p->npts;
+    a.mode = p->fd_mode;
+    a.df = p->fd_deriv == 1 ? -1.0 : 1.0;
     for (int d = 0; d < p->nd; ++d) { a.n[d] = p->dim[d].n; a.lo[d] = p->dim[d].stride; }
-    qdg::host::fd_weights2(p->fd_order, a.cf);
+    if (p->fd_deriv == 1) qdg::host::fd_weights1(p->fd_order, a.cf);
+    else qdg::host::fd_weights2(p->fd_order, a.cf);
     memcpy(a.h, p->fd_h, sizeof(a.h));
     a.phi = phi; a.out = P[0]; a.done = done; a.cs = cs; a.dyn = dyn;
     a.bufs[0] = static_cast<const cplx<T> *>(bufs[0]);
@@ -858,7 +872,9 @@ qdg_status build_couplings(const qdg_plan *p, F pick, qdg::Couplings &cp) {
   struct E { int row, col, gid, lid, nim; };
   std::vector<E> es;
   for (auto &t : p->terms) {
-    if (t.kind == QDG_TERM_KINETIC || t.kind == QDG_TERM_NAC || t.kind == QDG_TERM_GMAT || !pick(t)) continue;
+    if (t.kind == QDG_TERM_KINETIC || t.kind == QDG_TERM_NAC || t.kind == QDG_TERM_GMAT || t.kind == QDG_TERM_HOFD ||
+        !pick(t))
+      continue;
     const int nrep = (p->hermitian && t.row != t.col) ? 2 : 1;
     const int nim = t.kind == QDG_TERM_GOBBLER && t.laser == 1 ? 1 : 0;  // -i W (negative imaginary potential)
     for (int r = 0; r < nrep; ++r)
@@ -2273,6 +2289,18 @@ qdg_status qdg_plan_create(const qdg_hplan_desc *desc, int32_t precision, qdg_pl
       if (t.fd_order != 0 && (t.flags & 1) && (p->nd != 1 || p->dim[0].n <= t.fd_order / 2)) {
         free_plan(p); return fail(QDG_EUNSUPPORTED, "HOFD with pbc needs a one-dimensional grid longer than order/2");
       }
+    } else if (t.kind == QDG_TERM_HOFD) {
+      if (t.row != t.col) { free_plan(p); return fail(QDG_EUNSUPPORTED, "GridHOFD off the diagonal"); }
+      if (t.fd_order < 2 || t.fd_order > 2 * qdg::kMaxFdHalf || t.fd_order % 2 != 0) {
+        free_plan(p); return fail(QDG_EINVAL, "Invalid order of FD derivative");
+      }
+      if (t.laser < -1 || t.laser >= p->nd) { free_plan(p); return fail(QDG_EINVAL, "Invalid number of active dimension"); }
+      for (int d = 0; d < p->nd; ++d) {
+        if ((t.laser < 0 || t.laser == d) && p->dim[d].n < t.fd_order) {
+          free_plan(p); return fail(QDG_EUNSUPPORTED, "GridHOFD needs lines of at least order points");
+        }
+        if ((t.flags & 4) && t.mass[d] == 0) { free_plan(p); return fail(QDG_EINVAL, "Zero mass defined"); }
+      }
     } else if (t.kind == QDG_TERM_GMAT) {
       if (t.row != t.col) { free_plan(p); return fail(QDG_EUNSUPPORTED, "GridGMat off the diagonal"); }
       const int ne = p->nd * (p->nd + 1) / 2;
@@ -2306,15 +2334,29 @@ qdg_status qdg_plan_create(const qdg_hplan_desc *desc, int32_t precision, qdg_pl
     for (int st = 0; st < qdg::kMaxStates; ++st) p->gm_base[st] = -1;
     for (auto &t : p->terms) {
       if (t.kind == QDG_TERM_KINETIC && t.fd_order == 0) fft = true;
-      if (t.kind == QDG_TERM_KINETIC && t.fd_order != 0) {
-        if (fd && (t.fd_order != p->fd_order || (t.flags & 1) != p->fd_pbc)) {
-          free_plan(p); return fail(QDG_EUNSUPPORTED, "finite-difference kinetic terms of different order or boundaries");
+      if ((t.kind == QDG_TERM_KINETIC && t.fd_order != 0) || t.kind == QDG_TERM_HOFD) {
+        const int mode = t.kind == QDG_TERM_HOFD ? 1 : 0;
+        const int deriv = (t.kind == QDG_TERM_HOFD && (t.flags & 2)) ? 1 : 2;
+        if (fd && (t.fd_order != p->fd_order || (t.flags & 1) != p->fd_pbc || mode != p->fd_mode ||
+                   deriv != p->fd_deriv)) {
+          free_plan(p);
+          return fail(QDG_EUNSUPPORTED, "finite-difference terms of different form, order, derivative or boundaries");
         }
         fd = true;
         p->fd_order = t.fd_order;
         p->fd_pbc = t.flags & 1;
-        for (int d = 0; d < p->nd; ++d)  // HOFD.h:136-138: 1/dx^2 * 1 * (-1/(2 m_d))
-          p->fd_h[t.row][d] += 1. / (p->dx[d] * p->dx[d]) * 1.0 * (-1. / 2. / t.mass[d]);
+        p->fd_mode = mode;
+        p->fd_deriv = deriv;
+        if (mode == 0) {
+          for (int d = 0; d < p->nd; ++d)  // HOFD.h:136-138: 1/dx^2 * 1 * (-1/(2 m_d))
+            p->fd_h[t.row][d] += 1. / (p->dx[d] * p->dx[d]) * 1.0 * (-1. / 2. / t.mass[d]);
+        } else {
+          // OGridHOFD.cpp:74-91 and HOFD.h:190: 1/dx^deriv * 1 * factor, factor
+          // -1/(2 m) of the last dimension's mass for every dimension, else 1
+          const double factor = (t.flags & 4) ? -1. / (2 * t.mass[p->nd - 1]) : 1.0;
+          for (int d = 0; d < p->nd; ++d)
+            if (t.laser < 0 || t.laser == d) p->fd_h[t.row][d] += 1. / std::pow(p->dx[d], deriv) * 1.0 * factor;
+        }
       }
       if (t.kind == QDG_TERM_GMAT) {
         if (p->gm_base[t.row] >= 0) { free_plan(p); return fail(QDG_EUNSUPPORTED, "two GridGMat operators on one state"); }

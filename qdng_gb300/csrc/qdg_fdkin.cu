@@ -1,10 +1,10 @@
 // qdg_fdkin.cu -- the kinetic operators that are not diagonal in k:
 //
 // * OGridNablaSq with method="HOFD" (Diff.cpp:203-218 -> HOFD::Diff over all
-//   dimensions, src/qdlib/HOFD.h:124-176): a central finite-difference
+//   dimensions, src/qdlib/HOFD.h:124-176), and OGridHOFD (HOFD::Diff along
+//   each dimension, HOFD.h:188-211, 372-433): a central finite-difference
 //   stencil, one thread per point and state, neighbours read through L1/L2
-//   (a few hundred bytes per point at order 8; the pass is bound by HBM or
-//   L2 traffic, never by the FP64 pipe);
+//   (a few hundred bytes per point at order 8);
 // * OGridGMat (src/qdlib/OGridGMat.cpp:313-386): -1/2 sum_ij d/dx_j G_ij d/dx_i
 //   with FFT first derivatives, as two launches of shared-memory line passes
 //   (the kinetic pass's tiles and transforms).  The reference adds one
@@ -49,8 +49,22 @@ __global__ void __launch_bounds__(256) fd_kinetic_kernel(FdArgs<T> a) {
       const double hd = h[s][d];
       if (hd == 0.0) continue;
       const long long N = a.n[d], lo = a.lo[d];
-      const long long lrep = i / N;
       cplx<T> v = cmulr(ld(x + i), (T)cf[o2]);
+      if (a.mode == 1) {
+        // the point's coordinate along d; neighbours past the ends are zero or wrap
+        const long long c = (i / lo) % N;
+        for (int k = 1; k <= o2; ++k) {
+          cplx<T> lw = mk<T>(0, 0), up = mk<T>(0, 0);
+          if (c - k >= 0) lw = ld(x + i - k * lo);
+          else if (a.pbc) lw = ld(x + i + (N - k) * lo);
+          if (c + k < N) up = ld(x + i + k * lo);
+          else if (a.pbc) up = ld(x + i + (k - N) * lo);
+          v = v + cmulr(lw + cmulr(up, (T)a.df), (T)cf[o2 - k]);
+        }
+        D = D + cmulr(v, (T)hd);
+        continue;
+      }
+      const long long lrep = i / N;
       if (a.pbc) {
         long long step = lo;
         for (int j = o2 - 1; j >= 0; --j) {

@@ -259,6 +259,16 @@ void fd_weights2(int order, double *cf) {
   cf[o2] = (double)(-2.0L * center);
 }
 
+void fd_weights1(int order, double *cf) {
+  const int o2 = order / 2;
+  long double ratio = 1;
+  for (int k = 1; k <= o2; ++k) {
+    ratio = ratio * (long double)(o2 + 1 - k) / (long double)(o2 + k);
+    cf[o2 - k] = (double)((k & 1 ? -1.0L : 1.0L) * ratio / (long double)k);
+  }
+  cf[o2] = 0.0;
+}
+
 std::vector<int> find_peaks(const std::vector<double> &data, double tol, int width) {
   std::vector<int> peaks;
   const size_t n = data.size();

@@ -62,6 +62,10 @@ std::vector<int> find_peaks(const std::vector<double> &data, double tol, int wid
 // w_0 = -2 sum_k 1/k^2 (Fornberg, Math. Comp. 51 (1988) 699-706), evaluated
 // in long double and rounded once.
 void fd_weights2(int order, double *cf);
+// The same layout for the first derivative: cf[o2 - k] is the weight of the
+// lower neighbour at distance k (the upper one takes -cf), -w_k with
+// w_k = (-1)^(k+1) (o2!)^2 / (k (o2 - k)! (o2 + k)!), and cf[o2] = 0.
+void fd_weights1(int order, double *cf);
 
 }  // namespace host
 }  // namespace qdg

@@ -225,9 +225,12 @@ struct CombArgs {
 // energy of every state by central finite differences over all dimensions,
 // with QDng's neighbour rule (qdg_fdkin.cu), written to out (state stride npts).
 static const int kMaxFdHalf = 25;  // order 50 (HOFD_MAXORDER, HOFD.h:17)
+// mode 1: OGridHOFD (HOFD.h:372-433), each dimension's lines with zero or
+// periodic ends, df = -1 for the first derivative.
 template <typename T>
 struct FdArgs {
-  int nd, S, o2, pbc;
+  int nd, S, o2, pbc, mode;
+  double df;
   long long npts;
   int n[4];
   long long lo[4];                 // stride of each dimension

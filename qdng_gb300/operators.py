@@ -5,6 +5,7 @@ attributes, and flatten the tree into the qdg_hplan_desc the C ABI takes:
 
 * ``GridNablaSq(mass=[...], method, order, pbc)`` -- src/qdlib/OGridNablaSq.cpp:28-58, Diff.cpp:149-200
 * ``GridGMat(dims, gmat, G, Gdef, coup)`` -- src/qdlib/OGridGMat.cpp:142-386 (G-matrix kinetic energy)
+* ``GridHOFD(deriv, order, dim, pbc, mass)`` -- src/qdlib/OGridHOFD.cpp:32-128 (finite differences)
 * ``GridPotential(values)``     -- src/qdlib/OGridPotential.cpp:26-109 (setzero/offset/scale)
 * ``GridDipole(mu, laser)``     -- src/qdlib/OGridDipole.cpp:18-60, Laser.cpp:125-128
 * ``GridNAC([f_0, ...], mass, sign)`` -- src/qdlib/OGridNAC.cpp:26-148 (first-derivative coupling)
@@ -135,6 +136,47 @@ class GridNablaSq(Operator):
             t.mass[i] = m
         t.fd_order = self.order
         t.flags = 1 if self.pbc else 0
+        return [t]
+
+
+class GridHOFD(Operator):
+    """OGridHOFD (src/qdlib/OGridHOFD.cpp:32-128): central finite differences
+    of even ``order`` (2..50) along each dimension (``dim`` = -1) or one
+    dimension, first (``deriv=1``) or second (``deriv=2``) derivative, zero
+    boundaries or periodic ones (``pbc``).  With ``mass`` the factor is
+    -1/(2 m) of the last dimension's mass for every dimension (as the
+    reference assigns it), else 1.  Defaults as the reference's: deriv 1,
+    order 2, all dimensions."""
+
+    def __init__(self, deriv=1, order=2, dim=-1, pbc=False, mass=None):
+        self.deriv, self.order, self.dim, self.pbc = int(deriv), int(order), int(dim), bool(pbc)
+        # HOFD::_CheckSetup (HOFD.h:82-89)
+        if self.order > 50 or self.order % 2 != 0 or self.order < 2:
+            raise EParamProblem("Invalid order of FD derivative", self.order)
+        if self.deriv not in (1, 2):
+            raise EParamProblem("Invalid FD derivative", self.deriv)
+        self.mass = None if mass is None else [float(m) for m in np.atleast_1d(mass)]
+        if self.mass is not None:
+            if len(self.mass) < 1:
+                raise EParamProblem("HOFD operator needs at least one mass defintion")
+            if any(m == 0 for m in self.mass):
+                raise EParamProblem("Zero mass defined")
+
+    def terms(self, row, col, group, ctx):
+        if row != col:
+            raise EIncompatible("GridHOFD must sit on the diagonal")
+        nd = ctx.grid.ndims
+        if self.dim >= nd or self.dim < -1:
+            raise EParamProblem("Invalid number of active dimension", self.dim)
+        if self.mass is not None and len(self.mass) < nd:
+            raise EIncompatible("GridHOFD: fewer masses than dimensions")
+        t = abi.HTerm()
+        t.kind, t.row, t.col, t.grid, t.laser, t.group = abi.TERM_HOFD, row, col, -1, self.dim, group
+        t.fd_order = self.order
+        t.flags = (1 if self.pbc else 0) | (2 if self.deriv == 1 else 0) | (4 if self.mass is not None else 0)
+        if self.mass is not None:
+            for i in range(nd):
+                t.mass[i] = self.mass[i]
         return [t]
 
 

@@ -30,6 +30,7 @@
 #include "qdlib/OGobbler.h"
 #include "qdlib/OGridDipole.h"
 #include "qdlib/OGridGMat.h"
+#include "qdlib/OGridHOFD.h"
 #include "qdlib/OGridNAC.h"
 #include "qdlib/OGridNablaSq.h"
 #include "qdlib/OGridPotential.h"
@@ -148,6 +149,27 @@ class OGPUProp : public OPropagator {
       t.grid = add_grid(static_cast<dVec &>(*Gb));
       t.laser = nip ? 1 : 0;
       t.mass[0] = gain;
+    } else if (OGridHOFD *Hf = dynamic_cast<OGridHOFD *>(O)) {
+      // deriv, order, dim, pbc and mass as OGridHOFD::Init reads them
+      // (OGridHOFD.cpp:32-95; defaults deriv 1, order 2, all dimensions)
+      ParamContainer &hp = Hf->Params();
+      int deriv = 1, order = 2, dim = -1;
+      bool pbc;
+      if (hp.isPresent("deriv")) hp.GetValue("deriv", deriv);
+      if (hp.isPresent("order")) hp.GetValue("order", order);
+      if (hp.isPresent("dim")) hp.GetValue("dim", dim);
+      hp.GetValue("pbc", pbc, false);
+      t.kind = QDG_TERM_HOFD;
+      t.fd_order = order;
+      t.laser = dim;
+      t.flags = (pbc ? 1 : 0) | (deriv == 1 ? 2 : 0);
+      if (deriv != 1 && deriv != 2) throw EParamProblem("Invalid FD derivative", deriv);
+      if (hp.isPresent("mass")) {
+        vector<double> m;
+        hp.GetArray("mass", m);
+        t.flags |= 4;
+        for (size_t d = 0; d < m.size() && d < QDG_MAX_DIMS; d++) t.mass[d] = m[d];
+      }
     } else if (OGridGMat *Gm = dynamic_cast<OGridGMat *>(O)) {
       // OGridGMat keeps its elements private: read them the way its
       // Init(ParamContainer&) does (OGridGMat.cpp:142-248), lower triangle row by row

@@ -1,7 +1,8 @@
 """The kinetic operators without a k-space table on the device: OGridNablaSq
-with method="HOFD" (finite differences, QDng's neighbour rule) and OGridGMat
-(the G-matrix), against the oracle, which reproduces QDng's TGP-Expec-HOFD
-and TGP-Gmat goldens (tests/test_oracle_golden.py)."""
+with method="HOFD" (finite differences, QDng's neighbour rule), OGridHOFD
+(finite differences along each dimension) and OGridGMat (the G-matrix),
+against the oracle, which reproduces QDng's TGP-Expec-HOFD and TGP-Gmat
+goldens (tests/test_oracle_golden.py)."""
 import numpy as np
 import pytest
 
@@ -156,3 +157,34 @@ def test_kinetic_forms_rejected(eng):
         eng.Plan(op.HPlan(g, op.Sum([hofd, op.GridNablaSq([100.0])])), "fp64")
     with pytest.raises(Exception):
         op.GridNablaSq([100.0], method="HOFD", order=7)
+
+
+@pytest.mark.parametrize("shape,deriv,dim,pbc,mass", [
+    ((64,), 1, -1, False, None), ((64,), 2, -1, True, [500.0]), ((32, 24), 2, -1, False, [300.0, 900.0]),
+    ((32, 24), 1, 1, True, None), ((16, 12, 10), 2, 2, False, [100.0, 200.0, 400.0])],
+    ids=["1d-d1", "1d-d2-pbc", "2d-d2-mass", "2d-d1-dim1-pbc", "3d-d2-dim2"])
+def test_gridhofd_h_apply(eng, shape, deriv, dim, pbc, mass):
+    """OGridHOFD: each dimension's (or one dimension's) lines with zero or
+    periodic ends, first or second derivative, the mass factor of the last
+    dimension; H psi and the energy range against the oracle."""
+    g = op.GridSystem(list(shape), [-4.0, -3.0, -2.5][:len(shape)], [4.0, 3.5, 3.0][:len(shape)])
+    Q = g.mesh()
+    hp = op.HPlan(g, op.Sum([op.GridHOFD(deriv=deriv, order=8, dim=dim, pbc=pbc, mass=mass),
+                             op.GridPotential(0.02 * sum(q ** 2 for q in Q))]))
+    psi = _packet(g) + 0.05 * np.random.default_rng(4).normal(size=g.npts)
+    r, a, b = _h_parity(eng, hp, psi)
+    assert r <= 1e-13, r
+    assert abs(a[0] - b[0]) <= 1e-14 * abs(b[0]) and abs(a[1] - b[1]) <= 1e-14 * max(1.0, abs(b[1]))
+
+
+def test_gridhofd_propagation(eng):
+    """A two-dimensional packet under GridHOFD (second derivative, masses)
+    plus a potential: Chebyshev and SIL steps against the oracle."""
+    g = op.GridSystem([32, 24], [-4.0, -3.0], [4.0, 3.5])
+    X, Y = g.mesh()
+    hp = op.HPlan(g, op.Sum([op.GridHOFD(deriv=2, order=8, mass=[900.0, 900.0]),
+                             op.GridPotential(0.01 * (X ** 2 + Y ** 2))]))
+    psi = _packet(g)
+    _assert_parity(hp, *_run_both(eng, hp, psi, dict(name="Cheby", params="", dt=5.0), 20))
+    _assert_parity(hp, *_run_both(eng, hp, psi, dict(name="SIL", params="order=12", dt=5.0), 10),
+                   rtol=1e-11, check_terms=False)

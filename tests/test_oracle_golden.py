@@ -297,3 +297,43 @@ def test_lanczos_eigen_driver(fixtures, golden):
     gold = [float(t) for _, t in golden["tge_imag"][:6]]
     assert abs(er[0] - gold[0]) < 1.5e-7
     np.testing.assert_allclose(er[:6], gold, rtol=2e-3)
+
+
+@pytest.mark.parametrize("pbc", [False, True])
+def test_gridhofd_derivatives(pbc):
+    """OGridHOFD on a periodic function: first and second derivatives of
+    order 8 agree with the analytic ones away from the ends (everywhere with
+    pbc); the zero boundary drops the neighbours beyond the ends."""
+    n = 64
+    L = 2 * np.pi
+    g = op.GridSystem([n], [0.0], [L * (n - 1) / n])  # dx = L / n: sin(3 x) is periodic on the grid
+    x = g.axes()[0]
+    f = np.sin(3 * x).astype(np.complex128)
+    inner = slice(8, n - 8) if not pbc else slice(0, n)
+    for deriv, want in [(1, 3 * np.cos(3 * x)), (2, -9 * np.sin(3 * x))]:
+        S = O.System(op.HPlan(g, op.GridHOFD(deriv=deriv, order=8, pbc=pbc)))
+        got = S.h_apply(f).real
+        assert np.abs(got[inner] - want[inner]).max() < 1e-6, (deriv, np.abs(got[inner] - want[inner]).max())
+    # zero boundary: the first point's second derivative lacks the neighbours below
+    S = O.System(op.HPlan(g, op.GridHOFD(deriv=2, order=2, pbc=pbc)))
+    e = np.zeros(n, complex)
+    e[n - 1] = 1.0
+    col = S.h_apply(e).real * g.dx[0] ** 2
+    assert col[0] == (1.0 if pbc else 0.0) and col[n - 2] == 1.0 and col[n - 1] == -2.0
+
+
+def test_gridhofd_mass_factor_and_erange():
+    """With masses the factor is -1/(2 m) of the last dimension for both
+    dimensions (OGridHOFD.cpp:74-91); Emax follows the per-dimension masses
+    (OGridHOFD.cpp:97-111)."""
+    g = op.GridSystem([32, 24], [-3.0, -2.0], [3.0, 2.0])
+    rng = np.random.default_rng(2)
+    psi = rng.normal(size=g.npts) + 1j * rng.normal(size=g.npts)
+    a = O.System(op.HPlan(g, op.GridHOFD(deriv=2, order=4, mass=[100.0, 400.0]))).h_apply(psi)
+    b = O.System(op.HPlan(g, op.GridHOFD(deriv=2, order=4))).h_apply(psi)
+    assert np.allclose(a, b * (-1.0 / 800.0), rtol=1e-13, atol=0)
+    emax, emin = O.System(op.HPlan(g, op.GridHOFD(deriv=2, order=4, mass=[100.0, 400.0]))).erange()
+    dx = g.dx
+    assert abs(emax - np.pi ** 2 / 2 * (1 / (100 * dx[0] ** 2) + 1 / (400 * dx[1] ** 2))) < 1e-12 * abs(emax)
+    emax, emin = O.System(op.HPlan(g, op.GridHOFD(deriv=1, order=4, dim=1))).erange()
+    assert emax == 1j * np.pi / dx[0] and emin == -1j * np.pi / dx[0]
