@@ -81,7 +81,11 @@ struct FFT1 {
     long Ns = 1;
     int rmax = 1;
     for (int R : radix) rmax = std::max(rmax, R);
-    std::vector<cd> v(rmax), y(rmax);  /* any prime factor: a direct R-point DFT */
+    /* any prime factor is a direct R-point DFT; radices above 64 take heap buffers */
+    cd vs[64], ys[64];
+    std::vector<cd> vh, yh;
+    if (rmax > 64) { vh.resize(rmax); yh.resize(rmax); }
+    cd *v = rmax > 64 ? vh.data() : vs, *y = rmax > 64 ? yh.data() : ys;
     for (int R : radix) {
       long M = n / R;
       long step = n / (Ns * R);
