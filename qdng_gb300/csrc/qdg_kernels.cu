@@ -954,7 +954,7 @@ __device__ __forceinline__ void dots_terms(int S, long long npts, double *partia
   }
 }
 
-// <a|b> finished into the Lanczos scalars (dots_if + ks_finish)
+// <a|b> finished into the Lanczos scalars (alpha, beta or |psi|)
 template <typename T, typename U>
 __global__ void dots_ks_kernel(const cplx<T> *a, const cplx<U> *b, int S, long long npts, double *partials,
                                KsFinish f, double *ks, int *done, unsigned int *ticket) {
@@ -965,7 +965,7 @@ __global__ void dots_ks_kernel(const cplx<T> *a, const cplx<U> *b, int S, long l
   if (threadIdx.x == 0) *ticket = 0;
 }
 // y -= alpha x1 (rounded to T), y -= beta x2, then |y|^2 finished as beta
-// (two ks_lincomb launches + dots_if + ks_finish)
+// with the error estimate
 template <typename T>
 __global__ void ks_lincomb2_dot_kernel(cplx<T> *y, const cplx<T> *x1, int i1, const cplx<T> *x2, int i2, int S,
                                        long long npts, double *partials, KsFinish f, double *ks, int *done,
@@ -984,8 +984,8 @@ __global__ void ks_lincomb2_dot_kernel(cplx<T> *y, const cplx<T> *x1, int i1, co
   ks_finish_body(partials, f, ks, done);
   if (threadIdx.x == 0) *ticket = 0;
 }
-// y /= ks[idx] (ks_lincomb without x), then done[0] |= done[1] in the last
-// block (ks_commit) once every block has read done[0]
+// y /= ks[idx], then done[0] |= done[1] in the last block, once every block
+// has read done[0]
 template <typename T>
 __global__ void ks_scale_commit_kernel(cplx<T> *y, const double *ks, int idx, long long n, int *done,
                                        unsigned int *ticket) {
@@ -1001,7 +1001,7 @@ __global__ void ks_scale_commit_kernel(cplx<T> *y, const double *ks, int idx, lo
     *ticket = 0;
   }
 }
-// <a|b> finished into the Arnoldi scalars (dots_if / dots_lt + ka_finish)
+// <a|b> finished into the Arnoldi scalars (KA_LAST: skipped for j >= order)
 template <typename T, typename U>
 __global__ void dots_ka_kernel(const cplx<T> *a, const cplx<U> *b, int S, long long npts, double *partials,
                                KaArgs ka, int op, int j, int col, double *ks, int *ia, int *done,
@@ -1014,8 +1014,7 @@ __global__ void dots_ka_kernel(const cplx<T> *a, const cplx<U> *b, int S, long l
   if (threadIdx.x == 0) *ticket = 0;
 }
 // one modified Gram-Schmidt step y -= H[jc][col] x, then the next dot
-// product <a|y> (a = nullptr: <y|y>) finished as op (ka_lincomb + dots_if +
-// ka_finish)
+// product <a|y> (a = nullptr: <y|y>) finished as op
 template <typename T>
 __global__ void ka_lincomb_dot_kernel(cplx<T> *y, const cplx<T> *x, const cplx<T> *a, int jc, int S,
                                       long long npts, double *partials, KaArgs ka, int op, int j, int col, double *ks,
@@ -1034,8 +1033,8 @@ __global__ void ka_lincomb_dot_kernel(cplx<T> *y, const cplx<T> *x, const cplx<T
   ka_finish_body(partials, ka, op, j, col, ks, ia, done);
   if (threadIdx.x == 0) *ticket = 0;
 }
-// q = buf / H[it][it-1] (ks_lincomb without x, then ka_commit's copy), and
-// in the last block ia[0] = it + 1, done[0] |= done[1] (ka_order)
+// q = buf / H[it][it-1], and in the last block ia[0] = it + 1,
+// done[0] |= done[1]
 template <typename T>
 __global__ void ka_scale_commit_kernel(cplx<T> *q, const cplx<T> *buf, const double *ks, int idx, long long n, int it,
                                        int *ia, int *done, unsigned int *ticket) {
