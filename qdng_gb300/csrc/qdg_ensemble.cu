@@ -776,13 +776,18 @@ qdg_status build(qdg_ensemble *e, const qdg_ensemble_member *mem, const std::map
     if (!x.potential) return efail(QDG_EINVAL, "ensemble member without a potential");
     m.nd = x.grid.ndims;
     m.npts = 1;
+    bool generic = false;  // a line length with a prime factor above 5
     double dx[2], dk[2], Tmax = 0;
     for (int d = 0; d < m.nd; ++d) {
       const int N = x.grid.n[d];
       if (N < 2 || !(x.grid.xmax[d] > x.grid.xmin[d])) return efail(QDG_EINVAL, "invalid member grid");
       if (!(x.mass[d] > 0)) return efail(QDG_EINVAL, "Zero mass defined");
-      if (!qdg::schedule_radix(qdg::SCHED_ENSEMBLE, N, e->precision, m.rp[d]))
-        return efail(QDG_EUNSUPPORTED, "grid size must be 2^a 3^b 5^c");
+      if (!qdg::schedule_radix(qdg::SCHED_ENSEMBLE, N, e->precision, m.rp[d])) {
+        // other prime factors: direct-DFT stages, which the line-batch path
+        // (fft_lines) takes; such members stay off the resident 1-D path
+        if (!qdg::any_radix(N, m.rp[d])) return efail(QDG_EUNSUPPORTED, "grid size has more than 16 prime factors");
+        generic = true;
+      }
       m.n[d] = N;
       m.npts *= N;
       dx[d] = (x.grid.xmax[d] - x.grid.xmin[d]) / double(N - 1);
@@ -810,7 +815,7 @@ qdg_status build(qdg_ensemble *e, const qdg_ensemble_member *mem, const std::map
       m.lmax[d] = (int)std::max(1, std::min(64, 4096 / N));
       smem = std::max(smem, ((size_t)N + 2 * qdg::line_buf_elems(N, m.lmax[d])) * sizeof(cplx<T>));
     }
-    if (m.nd == 1) {
+    if (m.nd == 1 && !generic) {
       const size_t fsm = qdg::ens_fast_smem<T>(m.n[0]);
       if (fsm <= 216 * 1024) {
         m.fast = 1;

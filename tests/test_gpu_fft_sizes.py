@@ -8,6 +8,7 @@ import pytest
 
 from oracle import oracle as O
 from qdng_gb300 import operators as op
+from tests import cases
 from tests.test_gpu_parity import _assert_parity, _run_both
 
 pytestmark = pytest.mark.gpu
@@ -73,3 +74,34 @@ def test_prime_lengths_mixed(eng):
     hp, psi = _system((28, 21), 2)
     obs_o, _, x, obs_g, _, xg = _run_both(eng, hp, psi, dict(name="Cheby", params="", dt=5.0), 20, precision="mixed")
     assert np.abs(obs_g[:, 0] - obs_o[:, 0]).max() <= 1e-5
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_ensemble_members_of_prime_lengths(eng, precision):
+    """Ensemble members whose lines have prime factors above 5 (1-D 97 and
+    154 points, 2-D 21 x 14) next to a 256-point member, in one launch:
+    binary64 against each member's oracle propagation to 1e-12, the mixed
+    form to 1e-5."""
+    from oracle import oracle as O
+    from tests.test_gpu_parity import rel
+    rng = np.random.default_rng(13)
+    ens = [cases.cfg4_member(rng, 1, n, nt=4) for n in (97, 154, 256)]
+    m2 = cases.cfg4_member(rng, 2, 14, nt=4)
+    g = op.GridSystem([21, 14], [1.0, -3.0], [10.0, 3.0])
+    X, Y = g.mesh()
+    p = m2["params"]
+    psi = np.exp(-(X - p["re"] - 0.1) ** 2 / 0.02 - Y ** 2 / 2.0).astype(np.complex128).reshape(-1)
+    ens.append(dict(grid=g, mass=[1728.0, 1728.0],
+                    V=(p["D"] * (1 - np.exp(-p["a"] * (X - p["re"]))) ** 2 + 0.005 * Y ** 2).reshape(-1),
+                    mu=(X * np.exp(-X / 4)).reshape(-1), laser=m2["laser"],
+                    psi=psi / np.sqrt((np.abs(psi) ** 2).sum() * np.prod(g.dx))))
+    E = eng.Ensemble(ens, dt=10.0, precision=precision)
+    E.upload([m["psi"] for m in ens])
+    E.run(0, 2)
+    out = E.download()
+    for i, m in enumerate(ens):
+        Pm = O.Propagator(O.System(cases.member_hplan(m)), "Cheby", "", dt=10.0)
+        x = m["psi"].copy()
+        Pm.apply(x, 0)
+        Pm.apply(x, 1)
+        assert rel(out[i], x) < (1e-12 if precision == "fp64" else 1e-5), (m["grid"].n, rel(out[i], x))
