@@ -24,6 +24,7 @@
 
 #include "../../include/qdg.h"
 #include "qdg_kernels.cuh"
+#include "qdg_schedule.h"
 
 namespace qdg {
 // The shared scratch of qdg_h_apply_noalloc (see the file comment).
@@ -105,7 +106,9 @@ bool radix_plan_na(int n, qdg::RadixPlan &rp) {
   if (m % 2 == 0) { rp.radix[rp.nstages++] = 2; m /= 2; }
   while (m % 3 == 0) { rp.radix[rp.nstages++] = 3; m /= 3; }
   while (m % 5 == 0) { rp.radix[rp.nstages++] = 5; m /= 5; }
-  return m == 1 && rp.nstages <= 16;
+  if (m == 1) return rp.nstages <= 16;
+  // other prime factors: direct-DFT stages of the line passes' transforms
+  return qdg::any_radix(n, rp);
 }
 
 }  // namespace
@@ -134,7 +137,7 @@ qdg_status qdg_h_apply_noalloc(const qdg_hplan_desc *desc, const double *psi_in,
   qdg::RadixPlan rp[QDG_MAX_DIMS];
   for (int d = 0; d < g.ndims; ++d) {
     if (g.n[d] < 2 || !(g.xmax[d] > g.xmin[d])) return na_fail(QDG_EINVAL, "invalid grid");
-    if (!radix_plan_na(g.n[d], rp[d])) return na_fail(QDG_EUNSUPPORTED, "grid size must be 2^a 3^b 5^c");
+    if (!radix_plan_na(g.n[d], rp[d])) return na_fail(QDG_EUNSUPPORTED, "grid size has more than 16 prime factors");
     stride[d] = npts;
     npts *= g.n[d];
     t.n[d] = g.n[d];

@@ -45,6 +45,13 @@ def _case_3d():
     return op.HPlan(g, op.Sum([op.GridNablaSq([1836.0, 900.0, 2000.0]), op.GridPotential(V)]))
 
 
+def _case_prime_lengths():
+    """Lines of 28 and 21 points (prime factors 7 and 3, 7): direct-DFT stages."""
+    g = op.GridSystem([28, 21], [-4.0, -3.0], [4.0, 3.5])
+    X, Y = g.mesh()
+    return op.HPlan(g, op.Sum([op.GridNablaSq([900.0, 1200.0]), op.GridPotential(0.02 * (X ** 2 + Y ** 2))]))
+
+
 def _case_three_states(nonhermitian=False):
     """Three states with off-diagonal potentials and a dipole coupling; with
     nonhermitian=True the (j, i) elements are not mirrored."""
@@ -84,8 +91,8 @@ def _noalloc_apply(lib, hp, psi, step, torch):
 
 
 @pytest.mark.parametrize("builder", [_case_2d, _case_1d, _case_3d, _case_three_states,
-                                     lambda: _case_three_states(nonhermitian=True)],
-                         ids=["2d", "1d", "3d", "three-states", "three-states-nonhermitian"])
+                                     lambda: _case_three_states(nonhermitian=True), _case_prime_lengths],
+                         ids=["2d", "1d", "3d", "three-states", "three-states-nonhermitian", "prime-lengths"])
 def test_noalloc_matches_plan_h_apply(builder):
     torch = pytest.importorskip("torch")
     from qdng_gb300 import build, engine
