@@ -442,6 +442,31 @@ def engine_arm(args, world, rank, local):
         print(json.dumps(line))
 
 
+def ensemble_timeline_report(ens, se, blk):
+    """Per member class (dimensions, points) of the timed run: members, time
+    on their block (min, max) and the latest end, in ms from the launch's
+    first start; then the makespan and the busy time per block (stderr)."""
+    import collections
+
+    import numpy as np
+    t0 = se[:, 0].min()
+    dur = (se[:, 1] - se[:, 0]) / 1e6
+    end = (se[:, 1] - t0) / 1e6
+    cls = collections.defaultdict(list)
+    for i, m in enumerate(ens):
+        cls[(m["grid"].ndims, m["grid"].npts)].append(i)
+    for k in sorted(cls):
+        ix = cls[k]
+        print("timeline class %dD %7d pts: %3d members, on-block %.1f-%.1f ms, last end %.1f ms"
+              % (k[0], k[1], len(ix), dur[ix].min(), dur[ix].max(), end[ix].max()), file=sys.stderr)
+    busy = collections.defaultdict(float)
+    for i in range(len(ens)):
+        busy[int(blk[i])] += dur[i]
+    b = np.array(sorted(busy.values()))
+    print("timeline makespan %.1f ms; busy per block min %.1f median %.1f max %.1f ms over %d blocks"
+          % (end.max(), b.min(), np.median(b), b.max(), len(b)), file=sys.stderr)
+
+
 def ensemble_arm(args, world, rank, local):
     """Ensemble of 512 laser-driven members, one persistent launch per
     call; wavepackets/s = members x (steps / 5000) / time."""
@@ -470,6 +495,8 @@ def ensemble_arm(args, world, rank, local):
         terms = E.run(args.warmup, args.steps)
         dt_s = time.perf_counter() - t0
     launches = engine.kernel_launches() - l0
+    if args.timeline and rank == 0:
+        ensemble_timeline_report(ens, *E.timeline())
     clocks = clk.summary()
     dt_max = reduce_max(dt_s, world)
     total_members = args.members
@@ -620,6 +647,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="cfg2", choices=list(WORKLOADS) + ["ensemble"])
     ap.add_argument("--members", type=int, default=512)
+    ap.add_argument("--timeline", action="store_true",
+                    help="ensemble: per member class times of the timed run, on stderr")
     ap.add_argument("--plain-baseline", action="store_true",
                     help="ensemble: also run the members one at a time through the plain binary64 plan API")
     args = ap.parse_args()

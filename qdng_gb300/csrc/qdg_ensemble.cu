@@ -101,6 +101,7 @@ struct EnsArgs {
   int *status;            // per member: 2 = non-finite norm
   dfloat *dfr, *dfi;      // mixed form: psi in double-float during a step (members off the resident path)
   unsigned long long *tl; // per member: start, end (GPU clock, ns) and block of the last run
+  int block0;             // number of this launch's first block in the timeline
 };
 
 __device__ __forceinline__ unsigned long long ens_clock() {
@@ -598,8 +599,20 @@ __device__ void ens_step_df(const EnsArgs<float> &a, const EnsMember &m, float f
   terms += used;
 }
 
+// Threads per block.  Members on the resident 1-D path run 256 threads (a
+// 4096-point line is 256 radix-16 items per stage; 512 threads measured 40%
+// slower there).  The FP32 form's line-batch members wait on shared memory
+// and block barriers and run 25% faster with 512 threads, so the mixed
+// ensemble runs them in a second launch beside the first.  The binary64 form
+// is bound by its FP64 work and keeps 256 threads with more registers each.
 template <typename T>
-__global__ void __launch_bounds__(256) ensemble_kernel(EnsArgs<T> a) {
+struct EnsBlock {
+  static constexpr int threads = 256;
+  static constexpr int wide = sizeof(T) == sizeof(float) ? 512 : 256;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(EnsBlock<T>::wide) ensemble_kernel(EnsArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double red[32];
   __shared__ double tot_s;
@@ -612,7 +625,7 @@ __global__ void __launch_bounds__(256) ensemble_kernel(EnsArgs<T> a) {
     if (cur >= a.n) return;
     const int mi = a.order[cur];
     const EnsMember m = a.m[mi];
-    if (threadIdx.x == 0) { a.tl[3 * mi] = ens_clock(); a.tl[3 * mi + 2] = blockIdx.x; }
+    if (threadIdx.x == 0) { a.tl[3 * mi] = ens_clock(); a.tl[3 * mi + 2] = a.block0 + blockIdx.x; }
     long long terms = 0;
     int status = 0;
     for (int k = 0; k < a.nsteps; ++k) {
@@ -670,12 +683,12 @@ __global__ void __launch_bounds__(256) ensemble_kernel(EnsArgs<T> a) {
 }
 
 template <typename T>
-static int ensemble_occupancy(size_t smem) {
+static int ensemble_occupancy(size_t smem, int threads) {
   void *k = (void *)ensemble_kernel<T>;
   if (smem > 48 * 1024 && cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return 0;
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, 256, smem) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, threads, smem) != cudaSuccess) return 0;
   return nb;
 }
 
@@ -704,7 +717,12 @@ struct qdg_ensemble {
   double *d_lasers = nullptr, *d_coef = nullptr;
   size_t smem = 0;
   int grid = 1;
-  cudaStream_t stream = nullptr;
+  // mixed form: order[0, nA) are the resident 1-D members (launch A, 256
+  // threads, `grid` blocks), order[nA, n) the others (launch B beside it on
+  // stream2, wide blocks, gridB blocks); otherwise one launch over all
+  int nA = 0, gridB = 0;
+  cudaStream_t stream = nullptr, stream2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 
 namespace {
@@ -750,12 +768,21 @@ void free_ensemble(qdg_ensemble *e) {
   for (void *p : ps)
     if (p) cudaFree(p);
   if (e->stream) cudaStreamDestroy(e->stream);
+  if (e->stream2) cudaStreamDestroy(e->stream2);
+  if (e->ev_fork) cudaEventDestroy(e->ev_fork);
+  if (e->ev_join) cudaEventDestroy(e->ev_join);
   delete e;
 }
 
 // Time per point and term of a member off the resident path relative to one
 // on it (one block each, measured on GB300 over the workload's sizes).
 constexpr double kOffResidentCost = 2.0;
+// Time per point and term of a line-batch member in a wide (512-thread)
+// block relative to a resident member, for the split of the SMs between the
+// two launches of the mixed form (measured on GB300 over the workload's
+// sizes: 0.26-0.41 ns per point, log2 point and term resident, 0.33-0.41 in
+// wide blocks).
+constexpr double kOffResidentWideCost = 1.1;
 
 template <typename T>
 qdg_status build(qdg_ensemble *e, const qdg_ensemble_member *mem, const std::map<std::string, std::string> &params) {
@@ -896,20 +923,56 @@ qdg_status build(qdg_ensemble *e, const qdg_ensemble_member *mem, const std::map
   }
   ECK(cudaMalloc(&e->d_P0, sizeof(cplx<T>) * pts));
   ECK(cudaMalloc(&e->d_P1, sizeof(cplx<T>) * pts));
-  ECK(cudaMalloc(&e->d_queue, sizeof(int)));
+  ECK(cudaMalloc(&e->d_queue, 2 * sizeof(int)));
   ECK(cudaMalloc(&e->d_status, sizeof(int) * n));
   ECK(cudaMemset(e->d_status, 0, sizeof(int) * n));
   ECK(cudaMalloc(&e->d_terms, sizeof(long long) * n));
   ECK(cudaMalloc(&e->d_tl, sizeof(unsigned long long) * 3 * n));
   ECK(cudaMemset(e->d_tl, 0, sizeof(unsigned long long) * 3 * n));
   ECK(cudaMemset(e->d_terms, 0, sizeof(long long) * n));
-  const int occ = qdg::ensemble_occupancy<T>(smem);
+  const int occ = qdg::ensemble_occupancy<T>(smem, qdg::EnsBlock<T>::threads);
   if (occ <= 0) return efail(QDG_EUNSUPPORTED, "ensemble kernel cannot be resident");
   int dev = 0, sms = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   e->grid = std::max(1, std::min(n, occ * sms));
+  e->nA = n;
   ECK(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+  if (qdg::EnsBlock<T>::wide != qdg::EnsBlock<T>::threads) {
+    // resident 1-D members first, then the others, each group in LPT order
+    std::vector<int> grouped = e->order;
+    const auto mid = std::stable_partition(grouped.begin(), grouped.end(), [&](int i) { return e->hm[i].fast != 0; });
+    const int nA = (int)(mid - grouped.begin());
+    const int occB = qdg::ensemble_occupancy<T>(smem, qdg::EnsBlock<T>::wide);
+    // Two launches only where every block holds an SM alone (then the blocks
+    // of the two launches cannot crowd each other out of SMs), with the SMs
+    // split so that the groups' estimated loads per block match.
+    if (nA > 0 && nA < n && occ == 1 && occB == 1 && sms > 1) {
+      double costA = 0, costB = 0;
+      for (int j = 0; j < n; ++j) {
+        const int i = grouped[j];
+        if (j < nA) costA += cost[i];
+        else costB += cost[i] / kOffResidentCost * kOffResidentWideCost;
+      }
+      int best = 1;
+      double best_t = 0;
+      for (int g = 1; g < sms; ++g) {
+        const double t = std::max(costA / g, costB / (sms - g));
+        if (g == 1 || t < best_t) { best = g; best_t = t; }
+      }
+      e->order = grouped;
+      e->nA = nA;
+      e->grid = std::min(nA, best);
+      e->gridB = std::min(n - nA, sms - best);
+      ECK(cudaStreamCreateWithFlags(&e->stream2, cudaStreamNonBlocking));
+      ECK(cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming));
+      ECK(cudaEventCreateWithFlags(&e->ev_join, cudaEventDisableTiming));
+    } else if (nA == 0 && occB > 0) {  // line-batch members only: one wide launch
+      e->nA = 0;
+      e->gridB = std::max(1, std::min(n, occB * sms));
+    }
+    ECK(cudaMemcpy(e->d_order, e->order.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+  }
   return QDG_OK;
 }
 
@@ -940,12 +1003,36 @@ qdg_status run(qdg_ensemble *e, long long step0, int nsteps) {
   a.dfr = reinterpret_cast<qdg::dfloat *>(e->d_dfr);
   a.tl = e->d_tl;
   a.dfi = reinterpret_cast<qdg::dfloat *>(e->d_dfi);
-  ECK(cudaMemsetAsync(e->d_queue, 0, sizeof(int), e->stream));
+  ECK(cudaMemsetAsync(e->d_queue, 0, 2 * sizeof(int), e->stream));
   void *k = (void *)qdg::ensemble_kernel<T>;
   if (e->smem > 48 * 1024) ECK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smem));
   void *args[] = {(void *)&a};
-  qdg::add_launches(1);
-  ECK(cudaLaunchKernel(k, dim3(e->grid), dim3(256), args, e->smem, e->stream));
+  const bool two = e->nA > 0 && e->nA < e->n;
+  if (e->nA < e->n) {
+    // launch B (members off the resident path, wide blocks); issued first so
+    // that its blocks take their SMs before launch A's
+    cudaStream_t sb = two ? e->stream2 : e->stream;
+    if (two) {
+      ECK(cudaEventRecord(e->ev_fork, e->stream));
+      ECK(cudaStreamWaitEvent(sb, e->ev_fork, 0));
+    }
+    a.order = e->d_order + e->nA;
+    a.n = e->n - e->nA;
+    a.queue = e->d_queue + 1;
+    a.block0 = two ? e->grid : 0;
+    qdg::add_launches(1);
+    ECK(cudaLaunchKernel(k, dim3(e->gridB), dim3(qdg::EnsBlock<T>::wide), args, e->smem, sb));
+    if (two) ECK(cudaEventRecord(e->ev_join, sb));
+  }
+  if (e->nA > 0) {
+    a.order = e->d_order;
+    a.n = e->nA;
+    a.queue = e->d_queue;
+    a.block0 = 0;
+    qdg::add_launches(1);
+    ECK(cudaLaunchKernel(k, dim3(e->grid), dim3(qdg::EnsBlock<T>::threads), args, e->smem, e->stream));
+  }
+  if (two) ECK(cudaStreamWaitEvent(e->stream, e->ev_join, 0));
   return QDG_OK;
 }
 
