@@ -146,6 +146,33 @@ def test_cfg4_member_size_classes(eng):
         assert err_psi < 1e-12 and err_ac < 1e-12, (m["grid"].n, err_psi, err_ac)
 
 
+def test_cfg4_member_size_classes_mixed_two_launches(eng):
+    """The same size classes in the mixed form, which runs the resident 1-D
+    members and the line-batch members as two launches side by side (the
+    4096-point member's resident line holds its SM alone): one step, two
+    kernel launches, each member within 1e-4 of its own oracle propagation
+    (the FP32 recurrence error grows with the series length, ~3000 terms
+    at 4096 points)."""
+    rng = np.random.default_rng(21)
+    ens = [cases.cfg4_member(rng, 1, n, nt=4) for n in cases.ENS_1D_SIZES]
+    ens += [cases.cfg4_member(rng, 2, n, nt=4) for n in cases.ENS_2D_SIDES]
+    E = eng.Ensemble(ens, dt=10.0, precision="mixed")
+    E.upload([m["psi"] for m in ens])
+    l0 = eng.kernel_launches()
+    E.run(0, 1)
+    assert eng.kernel_launches() - l0 == 2
+    out = E.download()
+    for i, m in enumerate(ens):
+        Pm = O.Propagator(O.System(cases.member_hplan(m)), "Cheby", "", dt=10.0)
+        x = m["psi"].copy()
+        Pm.apply(x, 0)
+        assert E.info(i)["order"] == Pm.info()["order"]
+        p0 = m["psi"]
+        err_psi = rel(out[i], x)
+        err_ac = abs(np.vdot(p0, out[i]) - np.vdot(p0, x)) / abs(np.vdot(p0, x))
+        assert err_psi < 1e-4 and err_ac < 1e-4, (m["grid"].n, err_psi, err_ac)
+
+
 def _horizon(eng, hp, psi, run, params):
     plan = eng.Plan(hp, "fp64")
     fwd = eng.Propagator(plan, run["name"], params, dt=run["dt"])
